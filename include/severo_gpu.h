@@ -1,0 +1,276 @@
+/*
+ * severo_gpu.h -- C ABI of libseverogpu.so, the GB300 (sm_103a) implementation of
+ * Severo.jl's embedding hot path:
+ *
+ *   normalize_cells -> scale_features (implicit centre / scale / clip)
+ *   -> irlba PCA over the CenteredMatrix products -> nearest_neighbours
+ *   -> shared_nearest_neighbours / jaccard_index
+ *
+ * Every entry point is plain C: pointers, sizes and enums, no C++ or torch types.
+ * All functions except the four FindNeighbours* compatibility symbols return an
+ * int status (SV_OK = 0, negative on failure) and never throw or abort; the
+ * message of the most recent failure on the calling thread is available through
+ * sv_last_error().  Host pointers passed in are read (or written) before the call
+ * returns; device-resident results live in opaque handles owned by the caller
+ * and released with the matching *_free function.
+ *
+ * Matrix orientation follows Severo.jl: count / data matrices are cells x genes
+ * (src/Severo.jl:26-32), handed over as Julia SparseMatrixCSC arrays (one column
+ * per gene; row indices are cells).  Dense host matrices are column-major, as in
+ * Julia.  Neighbour indices at the boundary are 1-based Int32, as returned by the
+ * native FindNeighbours* routines (src/neighbours.jl:22,37-39).
+ *
+ * A context owns one CUDA stream on one device.  Handles created from a context
+ * are used with that context only, and one context is not re-entrant: calls on
+ * the same context must not overlap in time.  Different contexts are independent.
+ */
+#ifndef SEVERO_GPU_H
+#define SEVERO_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------- */
+#define SV_OK               0
+#define SV_ERR_ARG         -1   /* invalid argument (size, pointer, enum, index range) */
+#define SV_ERR_OOM         -2   /* device or pinned-host allocation failed               */
+#define SV_ERR_CUDA        -3   /* a CUDA runtime error                                   */
+#define SV_ERR_NOCONV      -4   /* irlba did not converge within maxit restarts           */
+#define SV_ERR_UNSUPPORTED -5   /* a size or combination this build does not handle       */
+#define SV_ERR_STATE       -6   /* handle used with the wrong context or in a bad state   */
+#define SV_ERR_DEVICE      -7   /* a kernel reported a bounds / iteration-limit failure   */
+
+/* ---- element types ---------------------------------------------------------- */
+#define SV_I32   1
+#define SV_I64   2
+#define SV_F32   3
+#define SV_F64   4
+#define SV_BF16  5   /* storage type of the mixed-precision form (values only) */
+
+/* ---- normalisation methods (src/normalize.jl:45-51) ------------------------- */
+#define SV_LOGNORMALIZE   0
+#define SV_RELATIVECOUNTS 1
+
+/* ---- kNN metric and distance-kernel precision ------------------------------ */
+#define SV_EUCLIDEAN 0
+#define SV_COSINE    1
+#define SV_KNN_FP32  0   /* FP32 CUDA-core distance tiles                           */
+#define SV_KNN_BF16  1   /* BF16 tcgen05 distance tiles, FP32 accumulation in TMEM  */
+
+typedef struct sv_context  sv_context;
+typedef struct sv_counts   sv_counts;    /* device CSC + CSR copies of a count matrix  */
+typedef struct sv_data     sv_data;      /* normalised values over both copies         */
+typedef struct sv_centered sv_centered;  /* implicit CenteredMatrix over a feature set */
+typedef struct sv_embed    sv_embed;     /* device-resident PCA result                 */
+typedef struct sv_knn      sv_knn;       /* device-resident neighbour lists            */
+typedef struct sv_graph    sv_graph;     /* device-resident SNN graph (CSC)            */
+
+/* ---- context, errors, diagnostics ----------------------------------------- */
+int  sv_version(void);                                   /* 100 * major + minor */
+int  sv_last_error(char* buf, size_t len);               /* copies the message, returns its length */
+int  sv_context_create(int device, sv_context** out);
+int  sv_context_destroy(sv_context* ctx);
+int  sv_synchronize(sv_context* ctx);
+/* Pin (page-lock) caller memory so that uploads run at full link speed. */
+int  sv_host_register(void* ptr, size_t bytes);
+int  sv_host_unregister(void* ptr);
+int  sv_host_alloc(void** ptr, size_t bytes);            /* pinned host allocation */
+int  sv_host_free(void* ptr);
+/* Device time between two marks on the context stream (CUDA events). */
+int  sv_mark(sv_context* ctx, int slot);                 /* slot 0..15 */
+int  sv_elapsed_ms(sv_context* ctx, int slot_a, int slot_b, double* ms);
+/* Number of kernels this library launched on the context since creation. */
+int  sv_launch_count(sv_context* ctx, int64_t* count);
+/* Per-kernel timing with CUDA events around each launch (off by default). */
+int  sv_profile_enable(sv_context* ctx, int enable);
+int  sv_profile_reset(sv_context* ctx);
+/* Sum of device time (ms) and number of launches of kernels whose name contains
+ * `name_substring`.  Synchronises the context. */
+int  sv_profile_query(sv_context* ctx, const char* name_substring, double* total_ms, int64_t* launches);
+/* Writes "name launches total_ms" lines for every kernel seen into buf. */
+int  sv_profile_report(sv_context* ctx, char* buf, size_t len);
+int  sv_device_memory(sv_context* ctx, size_t* free_bytes, size_t* total_bytes);
+
+/* ---- count matrix ------------------------------------------------------------
+ * sv_counts_upload_csc replaces holding the CountMatrix of src/Severo.jl:26-27
+ * in host memory: it copies a cells x genes SparseMatrixCSC (colptr, rowval,
+ * nzval; idx_type SV_I32 or SV_I64; val_type SV_I32 or SV_I64; index_base 0 or 1)
+ * to the device and builds the cell-major (CSR) copy there.  Row indices must
+ * be strictly increasing within each column (Julia's invariant); this is
+ * checked on the device and reported as SV_ERR_ARG. */
+int sv_counts_upload_csc(sv_context* ctx, int64_t n_cells, int64_t n_genes, int64_t nnz,
+                         const void* colptr, const void* rowval, const void* nzval,
+                         int idx_type, int val_type, int index_base, sv_counts** out);
+/* Synthetic negative-binomial counts generated on the device (benchmarks).
+ * Cells x genes; mean depth * s_c * mu_g * exp(lfc[cluster(c), g]); variance
+ * mean + dispersion * mean^2.  mu_g (n_genes), s_c (n_cells), cluster ids
+ * (n_cells, may be NULL) and lfc (n_clusters x n_genes row-major, may be NULL)
+ * are host arrays. Counter-based hashing of (seed, cell, gene) makes the CSC and
+ * CSR copies identical entry for entry. */
+int sv_counts_generate(sv_context* ctx, int64_t n_cells, int64_t n_genes,
+                       const float* mu_g, const float* s_c, const int32_t* cluster,
+                       const float* lfc, int32_t n_clusters, double depth,
+                       double dispersion, uint64_t seed, sv_counts** out);
+int sv_counts_info(const sv_counts* c, int64_t* n_cells, int64_t* n_genes, int64_t* nnz);
+/* Copies the CSC arrays back (0-based int64 colptr, int32 rowval, int32 counts). */
+int sv_counts_download_csc(sv_context* ctx, const sv_counts* c, int64_t* colptr,
+                           int32_t* rowval, int32_t* counts);
+/* Copies the CSR arrays back (0-based int64 rowptr, int32 colidx, int32 counts). */
+int sv_counts_download_csr(sv_context* ctx, const sv_counts* c, int64_t* rowptr,
+                           int32_t* colidx, int32_t* counts);
+int sv_counts_free(sv_counts* c);
+
+/* ---- normalize_cells (src/normalize.jl:17-55,76-79) -------------------------
+ * method SV_LOGNORMALIZE or SV_RELATIVECOUNTS; value dtype SV_F64 (the
+ * reference default), SV_F32 or SV_BF16 (values computed in FP32 and stored
+ * rounded to BF16).  b = (scale_factor * a) / s_cell in dtype (normalize.jl:27),
+ * then log1p for SV_LOGNORMALIZE (normalize.jl:36).  Both the CSC and the CSR
+ * copy receive values; the sparsity pattern is the counts'. */
+int sv_normalize_cells(sv_context* ctx, const sv_counts* counts, int method,
+                       double scale_factor, int dtype, sv_data** out);
+/* Copies the CSC values (in the data's dtype; BF16 as uint16 bit patterns). */
+int sv_data_download_csc(sv_context* ctx, const sv_data* d, void* nzval);
+int sv_data_download_csr(sv_context* ctx, const sv_data* d, void* nzval);
+/* Per-cell totals s_c (normalize.jl:24), int64. */
+int sv_data_cell_totals(sv_context* ctx, const sv_data* d, int64_t* totals);
+int sv_data_free(sv_data* d);
+
+/* ---- scale_features (src/scaling.jl:199-217,335-357) ------------------------
+ * features: 1-based gene indices (nfeatures of them, no duplicates), or NULL
+ * for all genes (src/scaling.jl:338-340).  Per feature, FP64 mean and unbiased
+ * variance with the implicit zeros (scaling.jl:18-34); mu = mean/std
+ * (scaling.jl:207); the represented matrix is
+ *     Xs[c, f] = min(a[c, f] / std_f, scale_max + mu_f) - mu_f   (a != 0)
+ *     Xs[c, f] = -mu_f                                            (a == 0)
+ * (scaling.jl:209-212,219-233).  Nothing is densified: the products below apply
+ * the scaling, clip and centring on the fly. scale_max may be +Inf. */
+int sv_scale_features(sv_context* ctx, const sv_data* data, const int64_t* features,
+                      int64_t nfeatures, double scale_max, sv_centered** out);
+/* CenteredMatrix(A, mu) (src/scaling.jl:224-232) for an arbitrary sparse A
+ * (n_rows x n_cols CSC, 0-based int64 colptr / rowval, FP64 values stored as
+ * dtype SV_F64 or SV_F32) and centring vector mu (n_cols): the represented
+ * matrix is A - 1 mu^T (no scaling, no clip).  Used by the reference's
+ * CenteredMatrix and irlba tests (test/test_scaling.jl:70-113,
+ * test/test_irlba.jl:65-115). */
+int sv_centered_create(sv_context* ctx, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                       const int64_t* colptr, const int64_t* rowval, const double* nzval,
+                       const double* mu, int dtype, sv_centered** out);
+int sv_centered_info(const sv_centered* s, int64_t* n_cells, int64_t* n_features, int64_t* nnz);
+/* mu (= mean/std, the reference's S.mu), mean and std per feature (FP64). */
+int sv_centered_stats(sv_context* ctx, const sv_centered* s, double* mu, double* mean, double* std);
+/* y = alpha * op(Xs) * x + beta * y  (src/scaling.jl:245-272 mul! family).
+ * trans 'N': x is n_features x ncols, y is n_cells x ncols;
+ * trans 'T': x is n_cells x ncols, y is n_features x ncols.  Host FP64,
+ * column-major with leading dimensions ldx / ldy. */
+int sv_centered_mul(sv_context* ctx, const sv_centered* s, char trans, int64_t ncols,
+                    double alpha, const double* x, int64_t ldx, double beta,
+                    double* y, int64_t ldy);
+int sv_centered_free(sv_centered* s);
+
+/* ---- irlba (src/irlba.jl:47-99) ---------------------------------------------
+ * Truncated SVD of the implicit matrix, all Lanczos vectors in HBM.
+ * nu singular triplets; work = Lanczos basis size (the reference passes nu + 7
+ * clamped to [nu + 1, min(m, n)], irlba.jl:50-58; pass 0 for that default);
+ * maxit restarts; tol: converged when every ||Xs^T u_i - s_i v_i|| is below
+ * tol * s_max; init: start vector on the feature side (length n_features,
+ * irlba.jl:62-64); seed: for the random vectors drawn on an invariant subspace.
+ * Outputs (host, column-major FP64, any may be NULL): s (nu), U (n_cells x nu),
+ * V (n_features x nu).  iters / nmatvec report the restarts and products used.
+ * Returns SV_ERR_NOCONV if maxit is reached (the reference raises
+ * "convergence failed", irlba.jl:73); outputs then hold the last iterate. */
+int sv_irlba(sv_context* ctx, const sv_centered* s, int64_t nu, int64_t work, int64_t maxit,
+             double tol, const double* init, uint64_t seed, double* s_out, double* U,
+             double* V, int64_t* iters, int64_t* nmatvec);
+
+/* pca / embedding with algorithm = :irlba (src/embedding.jl:46-94,202-212):
+ * runs sv_irlba and keeps coordinates Z = U diag(s) (n_cells x npcs) on the
+ * device for kNN.  Host outputs (NULL to skip): Z (n_cells x npcs, column-major
+ * FP64), stdev = s / sqrt(max(1, n_cells - 1)) (npcs), loadings = V
+ * (n_features x npcs). */
+int sv_pca(sv_context* ctx, const sv_centered* s, int64_t npcs, int64_t maxit, double tol,
+           const double* init, uint64_t seed, sv_embed** out, double* Z, double* stdev,
+           double* loadings, int64_t* iters, int64_t* nmatvec);
+int sv_embed_info(const sv_embed* e, int64_t* n_cells, int64_t* npcs);
+int sv_embed_free(sv_embed* e);
+
+/* Drop-in for the native `irlba` symbol that src/irlba.jl:66-71 calls:
+ *   int irlba(BlasInt m, BlasInt n, BlasInt nu, BlasInt work, BlasInt maxit,
+ *             BlasInt restart, double tol, double* init, double* s, double* U,
+ *             double* V, randv, matmul, void* data)
+ * with BlasInt = int64_t (ILP64, deps/build.jl:17-57).  The matrix is only known
+ * through the caller's callback matmul(y, trans, x, temp, data) ('T' = 84:
+ * y = A' x, x in R^m, y in R^n; otherwise y = A x), invoked on the calling
+ * thread with host FP64 vectors; reorthogonalisation, the restart SVD and all
+ * basis updates run on the device (context 0 of device 0, created on first use).
+ * randv(y, n, data) fills y with standard normals for restarts on an invariant
+ * subspace.  restart > 0 (warm restart) is accepted and treated as a cold start,
+ * which the reference's own test marks as broken (test/test_irlba.jl:60-62).
+ * Returns 0 on convergence, 1 when maxit is reached, < 0 on errors. */
+typedef void (*sv_randv_fn)(double* y, int n, void* data);
+typedef void (*sv_matmul_fn)(double* y, char trans, double* x, double* temp, void* data);
+int irlba(int64_t m, int64_t n, int64_t nu, int64_t work, int64_t maxit, int64_t restart,
+          double tol, double* init, double* s, double* U, double* V,
+          sv_randv_fn randv, sv_matmul_fn matmul, void* data);
+
+/* ---- nearest neighbours (src/neighbours.jl:19-86) ---------------------------
+ * Exact k-nearest neighbours of the n points (rows) of X (n x d, column-major,
+ * leading dimension ldX >= n; dtype SV_F32 or SV_F64; host memory).
+ * include_self != 0 puts each point first in its own list; otherwise it is
+ * excluded.  precision SV_KNN_FP32 or SV_KNN_BF16 (candidates from BF16
+ * tensor-core distances, then an FP32 exact re-rank of the best 2k).
+ * Outputs (host, NULL to skip): nn_index (n x k column-major, 1-based Int32,
+ * ascending distance, ties by index) and distances (n x k column-major, in
+ * dtype: Euclidean distance, or 1 - cosine similarity for SV_COSINE). */
+int sv_knn_host(sv_context* ctx, const void* X, int dtype, int64_t n, int64_t d, int64_t ldX,
+                int64_t k, int metric, int include_self, int precision,
+                int32_t* nn_index, void* distances, sv_knn** out);
+/* Same, on the device-resident PCA coordinates (dims 1..ndims of the embedding). */
+int sv_knn_embed(sv_context* ctx, const sv_embed* e, int64_t ndims, int64_t k, int metric,
+                 int include_self, int precision, int32_t* nn_index, double* distances,
+                 sv_knn** out);
+int sv_knn_info(const sv_knn* k, int64_t* n, int64_t* kk);
+int sv_knn_free(sv_knn* k);
+
+/* Drop-ins for the native libcell symbols of src/neighbours.jl:37-72 (the Julia
+ * side declares every X / distances pointer as Ptr{Float64}; the element type is
+ * the one in the name).  The search is exact, so ntables and seed are accepted
+ * and ignored.  void return as in the reference: failures leave nn_index
+ * filled with 0 and are reported through sv_last_error(). */
+void FindNeighboursEuclidean32(const float* X, int n, int d, int ldX, int k, int ntables,
+                               int include_self, int seed, int32_t* nn_index, float* distances);
+void FindNeighboursEuclidean64(const double* X, int n, int d, int ldX, int k, int ntables,
+                               int include_self, int seed, int32_t* nn_index, double* distances);
+void FindNeighboursCosine32(const float* X, int n, int d, int ldX, int k, int ntables,
+                            int include_self, int seed, int32_t* nn_index, float* distances);
+void FindNeighboursCosine64(const double* X, int n, int d, int ldX, int k, int ntables,
+                            int include_self, int seed, int32_t* nn_index, double* distances);
+
+/* ---- shared nearest neighbours (src/neighbours.jl:76-108,127-155,272-278) ----
+ * Builds the kNN graph of src/neighbours.jl:79 (column j holds the neighbours
+ * of cell j), counts c_ij = |N(i) & N(j)| in integers, weights
+ * w = c / (k + (k - c)) in dtype (SV_F32 or SV_F64) with k = k_param, or, when
+ * k_param < 0, k = |N(j)| of the column (the diag variant, neighbours.jl:96-108),
+ * and keeps w > prune (prune converted to dtype; droptol!, neighbours.jl:92).
+ * The result is an n x n CSC with sorted rows, bit-identical to the reference's
+ * given the same neighbour lists.
+ * sv_snn_host takes nn_index as the caller holds it (n x k column-major, 1-based
+ * Int32); sv_snn_knn takes a device-resident kNN result. */
+int sv_snn_host(sv_context* ctx, const int32_t* nn_index, int64_t n, int64_t k,
+                int64_t k_param, double prune, int dtype, sv_graph** out);
+int sv_snn_knn(sv_context* ctx, const sv_knn* knn, int64_t k_param, double prune, int dtype,
+               sv_graph** out);
+int sv_graph_info(const sv_graph* g, int64_t* n, int64_t* nnz);
+/* Copies the graph out as a Julia SparseMatrixCSC: colptr (n + 1) and rowval
+ * (nnz) as 1-based Int64, nzval (nnz) in the graph's dtype.  Any may be NULL. */
+int sv_graph_download(sv_context* ctx, const sv_graph* g, int64_t* colptr, int64_t* rowval,
+                      void* nzval);
+int sv_graph_free(sv_graph* g);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SEVERO_GPU_H */

@@ -1,0 +1,519 @@
+"""CPU oracle for the Severo.jl embedding hot path -- TEST INFRASTRUCTURE ONLY.
+
+This module is the checker.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` may import it; the product path (the CUDA
+library and its Python mirror in ``severo.jl_gb300``) never calls into it.
+
+It restates, in FP64 numpy/scipy (and FP32 where the reference computes in
+FP32), the algorithms of the Severo.jl files below.  Each function cites the
+reference file:line it follows (paths relative to the Severo.jl project).
+
+Parity status: the reference is Julia and cannot be executed on this machine
+(no Julia toolchain; its native ``libcell`` is a binary-only dependency that is
+not available).  The restatement is pinned against every literal fixture the
+reference's own tests hold for this path (test/test_input.jl:45-101,
+test/test_scaling.jl:20-131, test/test_irlba.jl:24-116, test/test_nn.jl:21-96)
+through the committed fixtures in ``tests/golden``; irlba, kNN and SNN have no
+stored expected outputs in the reference, so they are pinned by the reference
+tests' properties (singular values vs LAPACK, residual bound, brute-force
+neighbour sets) and, for SNN, by hand-computed graphs.
+"""
+from __future__ import annotations
+
+import math
+import numpy as np
+import scipy.sparse as sp
+
+# ---------------------------------------------------------------------------
+# normalisation -- src/normalize.jl
+# ---------------------------------------------------------------------------
+
+
+def _as_csc(X):
+    X = sp.csc_matrix(X)
+    X.sort_indices()
+    return X
+
+
+def row_norm(A, scale_factor=1.0, dtype=np.float64):
+    """src/normalize.jl:17-32.  ``b = (sf * a) / s_cell`` evaluated in ``dtype``.
+
+    ``s`` is the integer per-cell (row) total (normalize.jl:24); the product
+    ``scale_factor * a`` is formed first, then divided (normalize.jl:27).
+    The sparsity pattern (colptr/rowval) is unchanged.
+    """
+    A = _as_csc(A)
+    dt = np.dtype(dtype)
+    s = np.asarray(A.sum(axis=1, dtype=np.int64)).ravel()          # normalize.jl:24
+    sf = dt.type(scale_factor)
+    rows = A.indices
+    num = (sf * A.data.astype(dt)).astype(dt)                          # sf * a in dtype
+    den = s[rows].astype(dt)
+    vals = (num / den).astype(dt)                                      # normalize.jl:27
+    B = sp.csc_matrix((vals, A.indices.copy(), A.indptr.copy()), shape=A.shape)
+    return B, s
+
+
+def log_norm(A, scale_factor=1.0, dtype=np.float64):
+    """src/normalize.jl:34-38: row_norm then ``log1p`` on the stored values."""
+    B, s = row_norm(A, scale_factor, dtype)
+    B.data = np.log1p(B.data).astype(np.dtype(dtype))
+    return B, s
+
+
+def normalize_cells(X, method="lognormalize", scale_factor=1.0, dtype=np.float64):
+    """src/normalize.jl:40-55 (method dispatch; Symbol or String; unknown -> error)."""
+    if method == "lognormalize":
+        f = log_norm
+    elif method == "relativecounts":
+        f = row_norm
+    else:
+        raise ValueError(f"unknown normalization method: {method}")
+    return f(X, scale_factor, dtype)[0]
+
+
+def round_bf16(x):
+    """Round-to-nearest-even FP32 -> BF16, returned as FP32 (storage rounding of the
+    mixed form; BF16 is not a reference dtype)."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    u = x.view(np.uint32).astype(np.uint64)
+    lsb = (u >> 16) & 1
+    r = ((u + 0x7FFF + lsb) >> 16) << 16
+    nan = np.isnan(x)
+    out = r.astype(np.uint32).view(np.float32).copy()
+    out[nan] = np.nan
+    return out
+
+
+# ---------------------------------------------------------------------------
+# scaling -- src/scaling.jl
+# ---------------------------------------------------------------------------
+
+
+def mean_var_column(vals, n, acc=np.float64):
+    """src/scaling.jl:18-34.  Welford over the stored values of one sparse column,
+    started from ``count = n - nnz`` with ``mu = s = 0`` (the state after the
+    implicit zeros); variance ``s / (n - 1)``.  Pure-Python loop: small cases."""
+    T = np.dtype(acc).type
+    count = n - len(vals)
+    mu = T(0)
+    s = T(0)
+    for v in vals:
+        v = T(v)
+        count += 1
+        delta = T(v - mu)
+        mu = T(mu + delta / T(count))
+        s = T(s + delta * T(v - mu))
+    return mu, T(s / T(n - 1))
+
+
+def mean_var(A, acc=np.float64):
+    """Vectorised FP64 per-column mean / unbiased variance with implicit zeros.
+
+    Mathematically the quantity of src/scaling.jl:18-34,132-142; computed here by
+    the shifted two-pass formula in FP64 (exact to a few ulps of the Welford
+    result, which is what the tests compare against)."""
+    A = _as_csc(A)
+    n, d = A.shape
+    T = np.dtype(acc)
+    data = A.data.astype(np.float64)
+    nnz_col = np.diff(A.indptr)
+    sums = np.add.reduceat(data, A.indptr[:-1]) if data.size else np.zeros(d)
+    sums = np.where(nnz_col > 0, sums, 0.0)
+    mu = sums / n
+    col = np.repeat(np.arange(d), nnz_col)
+    dev = data - mu[col]
+    m2 = np.bincount(col, weights=dev * dev, minlength=d) + (n - nnz_col) * mu * mu
+    var = m2 / (n - 1)
+    return mu.astype(T), var.astype(T)
+
+
+def mean_var_grouped(x_idx, x_val, n, lbls, nlabels, acc=np.float64):
+    """src/scaling.jl:46-88: grouped Welford over a sparse vector (1-based labels)."""
+    T = np.dtype(acc).type
+    mu = np.zeros(nlabels, dtype=acc)
+    var = np.zeros(nlabels, dtype=acc)
+    cnt = np.zeros(nlabels, dtype=np.int64)
+    nz = np.zeros(nlabels, dtype=np.int64)
+    prev = 1
+    for idx, v in zip(x_idx, x_val):
+        while prev < idx:
+            nz[lbls[prev - 1] - 1] += 1
+            prev += 1
+        k = lbls[idx - 1] - 1
+        cnt[k] += 1
+        delta = T(v) - mu[k]
+        mu[k] += delta / cnt[k]
+        var[k] += delta * (T(v) - mu[k])
+        prev = idx + 1
+    while prev <= n:
+        nz[lbls[prev - 1] - 1] += 1
+        prev += 1
+    for k in range(nlabels):
+        delta = mu[k]
+        mu[k] *= cnt[k] / (nz[k] + cnt[k])
+        var[k] += nz[k] * (mu[k] * delta)
+        cnt[k] += nz[k]
+    var = var / (cnt - 1)
+    return mu, var, cnt
+
+
+def scale_data(A, scale_max=np.inf, dtype=np.float64):
+    """src/scaling.jl:199-217.  Per column: ``mu_i = mean/std``; stored values
+    ``min(a/std, scale_max + mu_i)`` (upper clip only; zeros are never clipped)."""
+    A = _as_csc(A)
+    dt = np.dtype(dtype)
+    mean, var = mean_var(A, np.float64 if dt == np.float64 else np.float64)
+    mean = mean.astype(dt)
+    std = np.sqrt(var.astype(dt)).astype(dt)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        mu = (mean / std).astype(dt)                                    # scaling.jl:207
+        clip = (dt.type(scale_max) + mu).astype(dt)                      # scaling.jl:209
+        col = np.repeat(np.arange(A.shape[1]), np.diff(A.indptr))
+        v = (A.data.astype(dt) / std[col]).astype(dt)                    # scaling.jl:211
+        b = np.where(v > clip[col], clip[col], v).astype(dt)             # scaling.jl:212
+    B = sp.csc_matrix((b, A.indices.copy(), A.indptr.copy()), shape=A.shape)
+    return B, mu, mean, std
+
+
+class CenteredMatrix:
+    """src/scaling.jl:219-243: the lazily centred matrix ``A - 1 mu^T``."""
+
+    def __init__(self, A, mu):
+        self.A = A
+        self.mu = np.asarray(mu)
+        assert A.shape[1] == self.mu.shape[0]                          # scaling.jl:226
+
+    @property
+    def shape(self):
+        return self.A.shape
+
+    def dense(self):
+        """src/scaling.jl:298-303 convert(Matrix, C)."""
+        A = self.A.toarray() if sp.issparse(self.A) else np.asarray(self.A)
+        return A.astype(np.float64) - self.mu[None, :]
+
+    def mul(self, v, alpha=1.0, beta=0.0, y=None):
+        """src/scaling.jl:245-250 (vector) / 259-264 (matrix): y = a*(A v - (mu.v)) + b*y."""
+        v = np.asarray(v, dtype=np.float64)
+        Av = self.A @ v
+        out = alpha * (Av - np.tensordot(self.mu, v, axes=(0, 0)))
+        if y is not None and beta != 0:
+            out = out + beta * y
+        return out
+
+    def rmul(self, u, alpha=1.0, beta=0.0, y=None):
+        """src/scaling.jl:252-257 (vector) / 266-272 (matrix): y = a*(A^T u - mu sum(u)) + b*y."""
+        u = np.asarray(u, dtype=np.float64)
+        Atu = self.A.T @ u
+        su = u.sum(axis=0)
+        out = alpha * (Atu - np.multiply.outer(self.mu, su))
+        if y is not None and beta != 0:
+            out = out + beta * y
+        return out
+
+
+def scale_features(X, scale_max=np.inf, dtype=np.float64, features=None):
+    """src/scaling.jl:335-357: optional column subset (1-based feature indices),
+    then scale_data; returns the CenteredMatrix plus the per-feature stats."""
+    X = _as_csc(X)
+    if features is not None:
+        X = X[:, np.asarray(features, dtype=np.int64) - 1]
+        X = _as_csc(X)
+    B, mu, mean, std = scale_data(X, scale_max, dtype)
+    return CenteredMatrix(B, mu), mean, std
+
+
+# ---------------------------------------------------------------------------
+# irlba -- src/irlba.jl (wrapper) + the native routine restated from
+# Baglama & Reichel, "Augmented implicitly restarted Lanczos bidiagonalization
+# methods", SIAM J. Sci. Comput. 27 (2005) 19-42.
+# ---------------------------------------------------------------------------
+
+
+def irlba_work_size(m, n, nu):
+    """src/irlba.jl:49-58: m_b = nu + 7, at least nu + 1, at most min(m, n)."""
+    m_b = nu + 7
+    if m_b < nu:
+        m_b = nu + 1
+    if m_b > min(m, n):
+        m_b = min(m, n)
+    return m_b
+
+
+def _cgs2(x, Q):
+    """Classical Gram-Schmidt, twice: x <- x - Q (Q^T x), applied two times."""
+    if Q.shape[1] == 0:
+        return x
+    for _ in range(2):
+        x = x - Q @ (Q.T @ x)
+    return x
+
+
+def restart_keep(nu, work, nconv):
+    """Number of Ritz vectors kept at a restart: nu (at most work - 1), so each
+    cycle adds work - nu new Lanczos steps."""
+    return max(1, min(nu, work - 1))
+
+
+def irlba(matvec, rmatvec, m, n, nu, work=None, maxit=1000, tol=1e-5, init=None,
+          rng=None, breakdown_tol=None):
+    """Augmented implicitly restarted Lanczos bidiagonalisation (FP64).
+
+    ``matvec(x)`` = A x (x in R^n, result in R^m); ``rmatvec(y)`` = A^T y.
+    Defaults follow src/irlba.jl:47-64 (work = nu + 7 clamped, tol 1e-5,
+    maxit 1000, start vector ``init`` on the n side).  Returns
+    (U (m x nu), s (nu), V (n x nu), info, iters, nmatvec), info = 0 when all
+    nu residuals ||A^T u_i - s_i v_i|| are below tol * max singular value.
+    """
+    if work is None:
+        work = irlba_work_size(m, n, nu)
+    rng = np.random.default_rng(0) if rng is None else rng
+    if init is None:
+        init = rng.standard_normal(n)
+    eps_b = np.sqrt(np.finfo(np.float64).eps) if breakdown_tol is None else breakdown_tol
+    V = np.zeros((n, work))
+    W = np.zeros((m, work))
+    B = np.zeros((work, work))
+    V[:, 0] = init / np.linalg.norm(init)
+    k = 0
+    smax = 0.0
+    nmv = 0
+    it = 0
+    info = 1
+    F = None
+    P = sig = Qt = None
+    while it < maxit:
+        j = k
+        w = matvec(V[:, j]); nmv += 1
+        w = _cgs2(w, W[:, :j])
+        S = np.linalg.norm(w)
+        if S < eps_b * max(smax, 1.0):
+            w = _cgs2(rng.standard_normal(m), W[:, :j]); w /= np.linalg.norm(w); S = 0.0
+        else:
+            w = w / S
+        W[:, j] = w
+        while True:
+            F = rmatvec(W[:, j]) - S * V[:, j]; nmv += 1
+            F = _cgs2(F, V[:, :j + 1])
+            if j + 1 < work:
+                R = np.linalg.norm(F)
+                if R < eps_b * max(smax, 1.0):
+                    F = _cgs2(rng.standard_normal(n), V[:, :j + 1]); F /= np.linalg.norm(F); R = 0.0
+                else:
+                    F = F / R
+                V[:, j + 1] = F
+                B[j, j] = S
+                B[j, j + 1] = R
+                w = matvec(V[:, j + 1]) - R * W[:, j]; nmv += 1
+                w = _cgs2(w, W[:, :j + 1])
+                S = np.linalg.norm(w)
+                if S < eps_b * max(smax, 1.0):
+                    w = _cgs2(rng.standard_normal(m), W[:, :j + 1]); w /= np.linalg.norm(w); S = 0.0
+                else:
+                    w = w / S
+                W[:, j + 1] = w
+                j += 1
+            else:
+                B[j, j] = S
+                break
+        P, sig, Qt = np.linalg.svd(B)
+        RF = np.linalg.norm(F)
+        smax = max(smax, sig[0])
+        res = RF * P[work - 1, :nu]
+        conv = np.abs(res) < tol * smax
+        nconv = int(conv.sum())
+        it += 1
+        if nconv >= nu or RF < eps_b * smax:
+            info = 0
+            break
+        k = restart_keep(nu, work, nconv)
+        Fh = F / RF
+        V[:, :k] = V @ Qt.T[:, :k]
+        W[:, :k] = W @ P[:, :k]
+        V[:, k] = Fh
+        B = np.zeros((work, work))
+        B[np.arange(k), np.arange(k)] = sig[:k]
+        B[:k, k] = RF * P[work - 1, :k]
+    U = W @ P[:, :nu]
+    Vo = V @ Qt.T[:, :nu]
+    return U, sig[:nu].copy(), Vo, info, it, nmv
+
+
+def pca_from_svd(U, s, V, m):
+    """src/embedding.jl:67-73: Z = U diag(s), stdev = s / sqrt(max(1, m-1)), loadings = V."""
+    Z = U * s[None, :]
+    stdev = s / math.sqrt(max(1, m - 1))
+    return Z, stdev, V
+
+
+def svd_flip(U, V, u_based=True):
+    """src/utils.jl:215-228: sign convention used by the reference tests."""
+    M = U if u_based else V
+    idx = np.argmax(np.abs(M), axis=0)
+    signs = np.sign(M[idx, np.arange(M.shape[1])])
+    return U * signs, V * signs
+
+
+def principal_angles(A, B):
+    """Principal angles (radians) between the column spaces of A and B."""
+    qa, _ = np.linalg.qr(A)
+    qb, _ = np.linalg.qr(B)
+    c = np.linalg.svd(qa.T @ qb, compute_uv=False)
+    c = np.clip(c, -1.0, 1.0)
+    return np.arccos(c)
+
+
+# ---------------------------------------------------------------------------
+# neighbours -- src/neighbours.jl
+# ---------------------------------------------------------------------------
+
+
+def knn_exact(X, k, include_self=True, metric="euclidean", block=2048):
+    """Exact FP64 brute-force kNN (the ground truth for the reference's ANN,
+    src/neighbours.jl:19-74; test/test_nn.jl:31-35 uses the same brute force).
+
+    Returns (idx (n x k, 0-based, ascending distance, ties by index),
+    dist (n x k, metric distance)).  include_self=True puts the point itself
+    first; include_self=False excludes it.
+    """
+    X = np.asarray(X, dtype=np.float64)
+    n = X.shape[0]
+    if metric == "cosine":
+        nr = np.linalg.norm(X, axis=1, keepdims=True)
+        X = X / np.where(nr > 0, nr, 1.0)
+    sq = np.einsum("ij,ij->i", X, X)
+    idx_out = np.empty((n, k), dtype=np.int64)
+    d_out = np.empty((n, k), dtype=np.float64)
+    for s in range(0, n, block):
+        e = min(n, s + block)
+        D = sq[s:e, None] + sq[None, :] - 2.0 * (X[s:e] @ X.T)
+        np.maximum(D, 0.0, out=D)
+        rows = np.arange(e - s)
+        D[rows, np.arange(s, e)] = -1.0           # self sorts first
+        kk = k if include_self else k + 1
+        part = np.argpartition(D, kk - 1, axis=1)[:, :kk] if kk < n else np.tile(np.arange(n), (e - s, 1))
+        pd = np.take_along_axis(D, part, axis=1)
+        order = np.lexsort((part, pd), axis=1)
+        part = np.take_along_axis(part, order, axis=1)
+        if include_self:
+            sel = part[:, :k]
+        else:
+            sel = part[:, 1:k + 1]
+        idx_out[s:e] = sel
+        # exact distances recomputed by differences
+        diff = X[s:e, None, :] - X[sel]
+        d2 = np.einsum("ijk,ijk->ij", diff, diff)
+        d_out[s:e] = d2 / 2.0 if metric == "cosine" else np.sqrt(d2)
+    return idx_out, d_out
+
+
+def knn_graph(nn_index_1based, n):
+    """src/neighbours.jl:79: sparse(vec(nn_index'), repeat(1:n, inner=k), trues(n*k)).
+    Column j holds the neighbour rows of cell j (Bool, duplicates OR-ed)."""
+    nn = np.asarray(nn_index_1based, dtype=np.int64)
+    k = nn.shape[1]
+    rows = nn.reshape(-1) - 1
+    cols = np.repeat(np.arange(n), k)
+    G = sp.csc_matrix((np.ones(rows.size, dtype=np.int64), (rows, cols)), shape=(n, n))
+    G.sum_duplicates()
+    G.data[:] = 1
+    G.sort_indices()
+    return G
+
+
+def jaccard_index(G, k=None, prune=1.0 / 15.0, dtype=np.float64):
+    """src/neighbours.jl:88-108.
+
+    ``snn = nn' * nn`` as integer counts c_ij = |N(i) & N(j)| (Bool x Bool
+    accumulates to Int), converted to ``dtype``; weight ``x / (k + (k - x))``
+    (variant with k, :88-94) or with k = diag(snn)[j] per column (:96-108);
+    then ``droptol!(snn, prune)`` keeps |w| > prune.  Rows sorted per column.
+    """
+    dt = np.dtype(dtype)
+    G = sp.csc_matrix(G, dtype=np.int64)
+    C = (G.T @ G).tocsc()
+    C.sort_indices()
+    x = C.data.astype(dt)
+    if k is not None:
+        kk = dt.type(k)
+        w = (x / (kk + (kk - x))).astype(dt)
+    else:
+        diag = C.diagonal().astype(dt)
+        col = np.repeat(np.arange(C.shape[1]), np.diff(C.indptr))
+        kc = diag[col]
+        w = (x / (kc + (kc - x))).astype(dt)
+    pr = dt.type(prune)
+    keep = np.abs(w) > pr
+    col = np.repeat(np.arange(C.shape[1]), np.diff(C.indptr))
+    rows = C.indices[keep]
+    cols = col[keep]
+    vals = w[keep]
+    counts = np.bincount(cols, minlength=C.shape[1])
+    indptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    return sp.csc_matrix((vals, rows, indptr), shape=C.shape)
+
+
+def shared_nearest_neighbours(X, k, prune=1.0 / 15.0, include_self=True, dtype=None):
+    """src/neighbours.jl:272-278 with exact neighbours."""
+    X = np.asarray(X)
+    dt = X.dtype if dtype is None else np.dtype(dtype)
+    idx, _ = knn_exact(X, k, include_self)
+    G = knn_graph(idx + 1, X.shape[0])
+    return jaccard_index(G, k, prune, dt)
+
+
+# ---------------------------------------------------------------------------
+# synthetic count generator (numpy; small configurations)
+# ---------------------------------------------------------------------------
+
+
+def synth_counts(n_cells, n_genes, mu_mean=-1.0, mu_sd=1.5, depth=1.0, size_sd=0.3,
+                 dispersion=0.2, seed=0, n_clusters=0, lfc_sd=0.8, lfc_frac=0.05,
+                 dtype=np.int32):
+    """Cells x genes CSC of NegBinomial counts (mean depth*s_c*mu_g*fc, var mu + phi mu^2).
+
+    mu_g ~ LogNormal(mu_mean, mu_sd), s_c ~ LogNormal(0, size_sd); optional
+    latent clusters with log-fold-changes ~ N(0, lfc_sd) on lfc_frac of genes.
+    """
+    rng = np.random.default_rng(seed)
+    mu_g = rng.lognormal(mu_mean, mu_sd, n_genes)
+    s_c = rng.lognormal(0.0, size_sd, n_cells)
+    r = 1.0 / dispersion
+    cols = []
+    if n_clusters > 0:
+        cl = rng.integers(0, n_clusters, n_cells)
+        lfc = np.zeros((n_clusters, n_genes))
+        for c in range(n_clusters):
+            sel = rng.random(n_genes) < lfc_frac
+            lfc[c, sel] = rng.normal(0.0, lfc_sd, sel.sum())
+    rows_all, cols_all, vals_all = [], [], []
+    chunk = max(1, int(2e7 // max(1, n_cells)))
+    for g0 in range(0, n_genes, chunk):
+        g1 = min(n_genes, g0 + chunk)
+        mean = depth * s_c[:, None] * mu_g[None, g0:g1]
+        if n_clusters > 0:
+            mean = mean * np.exp(lfc[cl][:, g0:g1])
+        p = r / (r + mean)
+        x = rng.negative_binomial(r, p)
+        ri, ci = np.nonzero(x)
+        rows_all.append(ri)
+        cols_all.append(ci + g0)
+        vals_all.append(x[ri, ci])
+    rows = np.concatenate(rows_all)
+    cols_ = np.concatenate(cols_all)
+    vals = np.concatenate(vals_all).astype(dtype)
+    X = sp.csc_matrix((vals, (rows, cols_)), shape=(n_cells, n_genes))
+    X.sort_indices()
+    X.indices = X.indices.astype(np.int64)
+    X.indptr = X.indptr.astype(np.int64)
+    return X
+
+
+def top_variable_genes(Xn, nfeat):
+    """Stand-in HVF selection: the nfeat genes with the largest variance of the
+    normalised data (1-based, ascending).  The reference's vst selection
+    (src/variablefeatures.jl) is not on the measured path; its indices are an input."""
+    _, var = mean_var(Xn)
+    order = np.argsort(-var, kind="stable")[:nfeat]
+    return np.sort(order) + 1

@@ -1,0 +1,560 @@
+"""severo.jl_gb300 -- GB300 (sm_103a) implementation of Severo.jl's embedding hot path.
+
+Python host mirror of the reference's Julia interface for the path, over the C
+ABI of libseverogpu.so (include/severo_gpu.h):
+
+    normalize_cells      src/normalize.jl:40-55,76-79
+    scale_features       src/scaling.jl:335-357   -> CenteredMatrix (implicit)
+    CenteredMatrix.mul   src/scaling.jl:245-272   (mul! family)
+    irlba                src/irlba.jl:47-99
+    pca / embedding      src/embedding.jl:46-94,202-212
+    ann                  src/neighbours.jl:19-74
+    nearest_neighbours   src/neighbours.jl:76-86,177-248
+    jaccard_index        src/neighbours.jl:88-155
+    shared_nearest_neighbours  src/neighbours.jl:272-349
+
+Matrices follow Severo's orientation: cells x genes, held as scipy CSC (the
+SparseMatrixCSC layout); dense matrices column-major semantics, neighbour
+indices 1-based Int32.  Every compute call runs on the GPU; there is no CPU
+fallback and importing the package fails loudly if the library is not built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib as L
+from ._lib import (ConvergenceError, SeveroGPUError, SV_BF16, SV_COSINE, SV_EUCLIDEAN, SV_F32,
+                   SV_F64, SV_I32, SV_I64, SV_KNN_BF16, SV_KNN_FP32, SV_LOGNORMALIZE,
+                   SV_RELATIVECOUNTS)
+
+__all__ = [
+    "Context", "CountMatrix", "DataMatrix", "CenteredMatrix", "LinearEmbedding",
+    "normalize_cells", "scale_features", "irlba", "irlba_callback", "pca", "embedding", "ann",
+    "nearest_neighbours", "jaccard_index", "shared_nearest_neighbours", "SeveroGPUError",
+    "ConvergenceError", "default_context",
+]
+
+_DTYPES = {"float64": SV_F64, "float32": SV_F32, "bfloat16": SV_BF16,
+           np.float64: SV_F64, np.float32: SV_F32}
+
+
+def _dtype_code(dtype):
+    if isinstance(dtype, str):
+        return _DTYPES[dtype]
+    return _DTYPES[np.dtype(dtype).type]
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class Context:
+    """One CUDA stream on one device (sv_context)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = L.load()
+        h = C.c_void_p()
+        L.check(self.lib.sv_context_create(device, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sv_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        L.check(self.lib.sv_synchronize(self.h))
+
+    def mark(self, slot):
+        L.check(self.lib.sv_mark(self.h, slot))
+
+    def elapsed_ms(self, a, b):
+        v = C.c_double()
+        L.check(self.lib.sv_elapsed_ms(self.h, a, b, C.byref(v)))
+        return v.value
+
+    def launches(self):
+        v = C.c_int64()
+        L.check(self.lib.sv_launch_count(self.h, C.byref(v)))
+        return v.value
+
+    def profile(self, enable=True):
+        L.check(self.lib.sv_profile_enable(self.h, 1 if enable else 0))
+
+    def profile_reset(self):
+        L.check(self.lib.sv_profile_reset(self.h))
+
+    def profile_query(self, name=""):
+        ms = C.c_double()
+        n = C.c_int64()
+        L.check(self.lib.sv_profile_query(self.h, name.encode(), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def profile_report(self):
+        n = self.lib.sv_profile_report(self.h, None, 0)
+        buf = C.create_string_buffer(max(1, n + 1))
+        self.lib.sv_profile_report(self.h, buf, len(buf))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, cnt, ms = line.split()
+            out[name] = (int(cnt), float(ms))
+        return out
+
+    def memory(self):
+        f = C.c_size_t()
+        t = C.c_size_t()
+        L.check(self.lib.sv_device_memory(self.h, C.byref(f), C.byref(t)))
+        return f.value, t.value
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class _Handle:
+    _free = None
+
+    def __init__(self, ctx, h):
+        self.ctx = ctx
+        self.h = h
+
+    def __del__(self):
+        try:
+            if self.h is not None and self._free:
+                getattr(self.ctx.lib, self._free)(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+class CountMatrix(_Handle):
+    """Device-resident count matrix (CSC + CSR copies), cells x genes."""
+    _free = "sv_counts_free"
+
+    @classmethod
+    def from_csc(cls, X, ctx: Context | None = None):
+        ctx = ctx or default_context()
+        X = sp.csc_matrix(X)
+        if not X.has_sorted_indices:
+            X = X.sorted_indices()
+        if not np.issubdtype(X.dtype, np.integer):
+            raise TypeError("counts must be integers (CountMatrix, src/Severo.jl:26)")
+        # one index type for colptr and rowval: Int32 while nnz fits, else Int64
+        it = SV_I32 if X.nnz < 2**31 - 1 else SV_I64
+        idt = np.int32 if it == SV_I32 else np.int64
+        colptr = np.ascontiguousarray(X.indptr, dtype=idt)
+        rowval = np.ascontiguousarray(X.indices, dtype=idt)
+        vt = SV_I64 if X.dtype.itemsize == 8 else SV_I32
+        vals = np.ascontiguousarray(X.data, dtype=np.int64 if vt == SV_I64 else np.int32)
+        h = C.c_void_p()
+        L.check(ctx.lib.sv_counts_upload_csc(ctx.h, X.shape[0], X.shape[1], X.nnz, _ptr(colptr),
+                                              _ptr(rowval), _ptr(vals), it, vt, 0, C.byref(h)))
+        return cls(ctx, h)
+
+    @classmethod
+    def upload(cls, colptr, rowval, nzval, shape, index_base=0, ctx: Context | None = None):
+        """Upload raw CSC arrays (Julia SparseMatrixCSC layout; 1-based when index_base=1)."""
+        ctx = ctx or default_context()
+        colptr = np.ascontiguousarray(colptr)
+        rowval = np.ascontiguousarray(rowval)
+        nzval = np.ascontiguousarray(nzval)
+        if colptr.dtype != rowval.dtype:
+            raise TypeError("colptr and rowval must share an index type")
+        it = SV_I64 if colptr.dtype.itemsize == 8 else SV_I32
+        vt = SV_I64 if nzval.dtype.itemsize == 8 else SV_I32
+        h = C.c_void_p()
+        L.check(ctx.lib.sv_counts_upload_csc(ctx.h, shape[0], shape[1], len(rowval), _ptr(colptr),
+                                              _ptr(rowval), _ptr(nzval), it, vt, index_base,
+                                              C.byref(h)))
+        return cls(ctx, h)
+
+    @classmethod
+    def generate(cls, n_cells, n_genes, mu_g, s_c, cluster=None, lfc=None, depth=1.0,
+                 dispersion=0.2, seed=0, ctx: Context | None = None):
+        ctx = ctx or default_context()
+        mu_g = np.ascontiguousarray(mu_g, dtype=np.float32)
+        s_c = np.ascontiguousarray(s_c, dtype=np.float32)
+        ncl = 0
+        if cluster is not None:
+            cluster = np.ascontiguousarray(cluster, dtype=np.int32)
+            lfc = np.ascontiguousarray(lfc, dtype=np.float32)
+            ncl = lfc.shape[0]
+        h = C.c_void_p()
+        L.check(ctx.lib.sv_counts_generate(ctx.h, n_cells, n_genes, _ptr(mu_g), _ptr(s_c),
+                                            _ptr(cluster), _ptr(lfc), ncl, depth, dispersion, seed,
+                                            C.byref(h)))
+        return cls(ctx, h)
+
+    @property
+    def shape(self):
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        L.check(self.ctx.lib.sv_counts_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value
+
+    @property
+    def nnz(self):
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        L.check(self.ctx.lib.sv_counts_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return c.value
+
+    def to_csc(self):
+        m, n = self.shape
+        cp = np.empty(n + 1, np.int64)
+        rv = np.empty(self.nnz, np.int32)
+        cv = np.empty(self.nnz, np.int32)
+        L.check(self.ctx.lib.sv_counts_download_csc(self.ctx.h, self.h, _ptr(cp), _ptr(rv), _ptr(cv)))
+        return sp.csc_matrix((cv, rv, cp), shape=(m, n))
+
+    def to_csr(self):
+        m, n = self.shape
+        rp = np.empty(m + 1, np.int64)
+        ci = np.empty(self.nnz, np.int32)
+        cv = np.empty(self.nnz, np.int32)
+        L.check(self.ctx.lib.sv_counts_download_csr(self.ctx.h, self.h, _ptr(rp), _ptr(ci), _ptr(cv)))
+        return sp.csr_matrix((cv, ci, rp), shape=(m, n))
+
+
+class DataMatrix(_Handle):
+    """Normalised values on the device (both copies; the counts' pattern)."""
+    _free = "sv_data_free"
+
+    def __init__(self, ctx, h, counts, dtype):
+        super().__init__(ctx, h)
+        self.counts = counts
+        self.dtype = dtype
+
+    @property
+    def shape(self):
+        return self.counts.shape
+
+    def _host_dtype(self):
+        return {SV_F64: np.float64, SV_F32: np.float32, SV_BF16: np.uint16}[self.dtype]
+
+    def _decode(self, v):
+        if self.dtype == SV_BF16:
+            return (v.astype(np.uint32) << 16).view(np.float32)
+        return v
+
+    def values_csc(self):
+        v = np.empty(self.counts.nnz, self._host_dtype())
+        L.check(self.ctx.lib.sv_data_download_csc(self.ctx.h, self.h, _ptr(v)))
+        return self._decode(v)
+
+    def values_csr(self):
+        v = np.empty(self.counts.nnz, self._host_dtype())
+        L.check(self.ctx.lib.sv_data_download_csr(self.ctx.h, self.h, _ptr(v)))
+        return self._decode(v)
+
+    def cell_totals(self):
+        t = np.empty(self.shape[0], np.int64)
+        L.check(self.ctx.lib.sv_data_cell_totals(self.ctx.h, self.h, _ptr(t)))
+        return t
+
+    def to_csc(self):
+        c = self.counts.to_csc()
+        return sp.csc_matrix((self.values_csc(), c.indices, c.indptr), shape=c.shape)
+
+
+def normalize_cells(X, method="lognormalize", scale_factor=1.0, dtype="float64",
+                    ctx: Context | None = None) -> DataMatrix:
+    """src/normalize.jl:40-55: ``:lognormalize`` or ``:relativecounts`` (Symbol or
+    String); unknown methods raise.  X: CountMatrix or an integer scipy CSC."""
+    method = str(method).lstrip(":")
+    if method == "lognormalize":
+        mcode = SV_LOGNORMALIZE
+    elif method == "relativecounts":
+        mcode = SV_RELATIVECOUNTS
+    else:
+        raise ValueError(f"unknown normalization method: {method}")   # normalize.jl:50
+    if not isinstance(X, CountMatrix):
+        X = CountMatrix.from_csc(X, ctx)
+    ctx = X.ctx
+    dt = _dtype_code(dtype)
+    h = C.c_void_p()
+    L.check(ctx.lib.sv_normalize_cells(ctx.h, X.h, mcode, float(scale_factor), dt, C.byref(h)))
+    return DataMatrix(ctx, h, X, dt)
+
+
+class CenteredMatrix(_Handle):
+    """src/scaling.jl:219-243: implicit ``min(A/std, scale_max + mu) - 1 mu^T``."""
+    _free = "sv_centered_free"
+
+    def __init__(self, ctx, h, data):
+        super().__init__(ctx, h)
+        self.data = data
+
+    @classmethod
+    def from_sparse(cls, A, mu, dtype="float64", ctx: Context | None = None):
+        """CenteredMatrix(A, mu) (src/scaling.jl:224-232) for any sparse A."""
+        ctx = ctx or default_context()
+        A = sp.csc_matrix(A, dtype=np.float64)
+        A.sort_indices()
+        mu = np.ascontiguousarray(mu, dtype=np.float64)
+        if mu.shape[0] != A.shape[1]:
+            raise ValueError("length(mu) must equal size(A, 2)")   # scaling.jl:226
+        cp = np.ascontiguousarray(A.indptr, dtype=np.int64)
+        rv = np.ascontiguousarray(A.indices, dtype=np.int64)
+        vv = np.ascontiguousarray(A.data, dtype=np.float64)
+        h = C.c_void_p()
+        L.check(ctx.lib.sv_centered_create(ctx.h, A.shape[0], A.shape[1], A.nnz, _ptr(cp), _ptr(rv),
+                                            _ptr(vv), _ptr(mu), _dtype_code(dtype), C.byref(h)))
+        return cls(ctx, h, None)
+
+    @property
+    def shape(self):
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        L.check(self.ctx.lib.sv_centered_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value
+
+    @property
+    def nnz(self):
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        L.check(self.ctx.lib.sv_centered_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return c.value
+
+    def stats(self):
+        nf = self.shape[1]
+        mu, mean, std = (np.empty(nf) for _ in range(3))
+        L.check(self.ctx.lib.sv_centered_stats(self.ctx.h, self.h, _ptr(mu), _ptr(mean), _ptr(std)))
+        return mu, mean, std
+
+    @property
+    def mu(self):
+        return self.stats()[0]
+
+    def _mul(self, trans, x, alpha, beta, y):
+        m, n = self.shape
+        x = np.asarray(x, dtype=np.float64)
+        vec = x.ndim == 1
+        X2 = np.asfortranarray(x.reshape(x.shape[0], -1))
+        ny = m if trans == b"N" else n
+        if X2.shape[0] != (n if trans == b"N" else m):
+            raise ValueError("dimension mismatch")
+        if y is None:
+            Y = np.zeros((ny, X2.shape[1]), order="F")
+            beta = 0.0
+        else:
+            Y = np.asfortranarray(np.asarray(y, dtype=np.float64).reshape(ny, -1)).copy(order="F")
+        L.check(self.ctx.lib.sv_centered_mul(self.ctx.h, self.h, trans, X2.shape[1], float(alpha),
+                                              _ptr(X2), X2.shape[0], float(beta), _ptr(Y), ny))
+        return Y[:, 0] if vec else Y
+
+    def mul(self, v, alpha=1.0, beta=0.0, y=None):
+        """y = alpha * C v + beta * y   (scaling.jl:245-250, 259-264)."""
+        return self._mul(b"N", v, alpha, beta, y)
+
+    def rmul(self, u, alpha=1.0, beta=0.0, y=None):
+        """y = alpha * C' u + beta * y  (scaling.jl:252-257, 266-272)."""
+        return self._mul(b"T", u, alpha, beta, y)
+
+
+def scale_features(X: DataMatrix, scale_max=np.inf, features=None) -> CenteredMatrix:
+    """src/scaling.jl:347-357 (features: 1-based gene indices or None)."""
+    ctx = X.ctx
+    h = C.c_void_p()
+    if features is not None:
+        f = np.ascontiguousarray(features, dtype=np.int64)
+        L.check(ctx.lib.sv_scale_features(ctx.h, X.h, _ptr(f), len(f), float(scale_max), C.byref(h)))
+    else:
+        L.check(ctx.lib.sv_scale_features(ctx.h, X.h, None, 0, float(scale_max), C.byref(h)))
+    return CenteredMatrix(ctx, h, X)
+
+
+def irlba(S: CenteredMatrix, nu, tol=1e-5, maxit=1000, work=0, init=None, seed=0,
+          return_info=False):
+    """src/irlba.jl:78-85 on the device matrix; returns (U, s, V)."""
+    ctx = S.ctx
+    m, n = S.shape
+    if init is None:
+        init = np.random.default_rng(seed).standard_normal(n)
+    init = np.ascontiguousarray(init, dtype=np.float64)
+    U = np.zeros((m, nu), order="F")
+    V = np.zeros((n, nu), order="F")
+    s = np.zeros(nu)
+    it, nmv = C.c_int64(), C.c_int64()
+    L.check(ctx.lib.sv_irlba(ctx.h, S.h, nu, work, maxit, tol, _ptr(init), seed, _ptr(s), _ptr(U),
+                             _ptr(V), C.byref(it), C.byref(nmv)))
+    if return_info:
+        return U, s, V, {"iters": it.value, "nmatvec": nmv.value}
+    return U, s, V
+
+
+def irlba_callback(matvec, rmatvec, m, n, nu, tol=1e-5, maxit=1000, work=0, init=None, seed=0):
+    """The native `irlba` symbol (src/irlba.jl:66-71) driven by host callbacks
+    (the reference's matmul protocol: trans 'T' -> A'x, else Ax)."""
+    lib = L.load()
+    if init is None:
+        init = np.random.default_rng(seed).standard_normal(n)
+    init = np.ascontiguousarray(init, dtype=np.float64)
+    U = np.zeros((m, nu), order="F")
+    V = np.zeros((n, nu), order="F")
+    s = np.zeros(nu)
+
+    def _mm(yp, trans, xp, tp, data):
+        if trans == b"T":
+            x = np.ctypeslib.as_array(xp, shape=(m,))
+            y = np.ctypeslib.as_array(yp, shape=(n,))
+            y[:] = rmatvec(x)
+        else:
+            x = np.ctypeslib.as_array(xp, shape=(n,))
+            y = np.ctypeslib.as_array(yp, shape=(m,))
+            y[:] = matvec(x)
+
+    def _rv(yp, k, data):
+        np.ctypeslib.as_array(yp, shape=(k,))[:] = np.random.default_rng(seed).standard_normal(k)
+
+    mm = L.MATMUL(_mm)
+    rv = L.RANDV(_rv)
+    info = lib.irlba(m, n, nu, work, maxit, 0, tol, _ptr(init), _ptr(s), _ptr(U), _ptr(V), rv, mm,
+                     None)
+    if info < 0:
+        L.check(info)
+    if info != 0:
+        raise ConvergenceError(L.SV_ERR_NOCONV, "convergence failed")   # irlba.jl:73
+    return U, s, V
+
+
+@dataclass
+class LinearEmbedding:
+    """src/embedding.jl:20-25 (coordinates cells x PCs, stdev, basis genes x PCs)."""
+    coordinates: np.ndarray
+    stdev: np.ndarray
+    basis: np.ndarray
+    handle: object = None
+    info: dict = None
+
+
+class _Embed(_Handle):
+    _free = "sv_embed_free"
+
+
+def pca(S: CenteredMatrix, npcs, tol=1e-5, maxit=1000, init=None, seed=0, download=True):
+    """src/embedding.jl:46-94 with algorithm=:irlba: Z = U diag(s), stdev, loadings."""
+    ctx = S.ctx
+    m, n = S.shape
+    k = min(m, n, npcs)
+    if init is None:
+        init = np.random.default_rng(seed).standard_normal(n)
+    init = np.ascontiguousarray(init, dtype=np.float64)
+    Z = np.zeros((m, k), order="F") if download else None
+    stdev = np.zeros(k)
+    load = np.zeros((n, k), order="F")
+    h = C.c_void_p()
+    it, nmv = C.c_int64(), C.c_int64()
+    L.check(ctx.lib.sv_pca(ctx.h, S.h, npcs, maxit, tol, _ptr(init), seed, C.byref(h), _ptr(Z),
+                           _ptr(stdev), _ptr(load), C.byref(it), C.byref(nmv)))
+    return LinearEmbedding(Z, stdev, load, _Embed(ctx, h), {"iters": it.value, "nmatvec": nmv.value})
+
+
+def embedding(S, npcs, method="pca", algorithm="irlba", **kw):
+    """src/embedding.jl:202-212 for method=:pca (the path this library implements)."""
+    if str(method).lstrip(":") != "pca" or str(algorithm).lstrip(":") != "irlba":
+        raise ValueError("only method=:pca with algorithm=:irlba runs on this path")
+    return pca(S, npcs, **kw)
+
+
+class KNN(_Handle):
+    _free = "sv_knn_free"
+
+
+_METRICS = {"euclidean": SV_EUCLIDEAN, "cosine": SV_COSINE}
+_PREC = {"fp32": SV_KNN_FP32, "bf16": SV_KNN_BF16}
+
+
+def ann(X, k, metric="euclidean", include_self=True, precision="fp32", ctx: Context | None = None,
+        keep=False):
+    """src/neighbours.jl:19-30: (nn_index n x k Int32 1-based, distances n x k)."""
+    ctx = ctx or default_context()
+    if isinstance(X, LinearEmbedding):
+        n = X.coordinates.shape[0] if X.coordinates is not None else None
+        h = C.c_void_p()
+        e = X.handle.h
+        a, b = C.c_int64(), C.c_int64()
+        L.check(ctx.lib.sv_embed_info(e, C.byref(a), C.byref(b)))
+        n = a.value
+        idx = np.zeros((n, k), dtype=np.int32, order="F")
+        dist = np.zeros((n, k), dtype=np.float64, order="F")
+        L.check(ctx.lib.sv_knn_embed(ctx.h, e, 0, k, _METRICS[metric], int(include_self),
+                                      _PREC[precision], _ptr(idx), _ptr(dist), C.byref(h)))
+        return (idx, dist, KNN(ctx, h)) if keep else (idx, dist)
+    X = np.asarray(X)
+    dt = np.float32 if X.dtype == np.float32 else np.float64
+    Xf = np.asfortranarray(X, dtype=dt)
+    n, d = Xf.shape
+    idx = np.zeros((n, k), dtype=np.int32, order="F")
+    dist = np.zeros((n, k), dtype=dt, order="F")
+    h = C.c_void_p()
+    L.check(ctx.lib.sv_knn_host(ctx.h, _ptr(Xf), SV_F32 if dt == np.float32 else SV_F64, n, d, n, k,
+                                 _METRICS[metric], int(include_self), _PREC[precision], _ptr(idx),
+                                 _ptr(dist), C.byref(h)))
+    return (idx, dist, KNN(ctx, h)) if keep else (idx, dist)
+
+
+def nearest_neighbours(X, k, metric="euclidean", include_self=True, dims=None, precision="fp32",
+                       ctx: Context | None = None):
+    """src/neighbours.jl:76-86,177-248: Bool n x n CSC, column j = neighbours of j."""
+    if dims is not None and not isinstance(X, LinearEmbedding):
+        X = np.asarray(X)[:, dims]
+    idx, _ = ann(X, k, metric, include_self, precision, ctx)
+    n = idx.shape[0]
+    rows = idx.reshape(-1) - 1
+    cols = np.repeat(np.arange(n), k)
+    G = sp.csc_matrix((np.ones(rows.size, dtype=bool), (rows, cols)), shape=(n, n))
+    G.sort_indices()
+    return G
+
+
+class Graph(_Handle):
+    _free = "sv_graph_free"
+
+    def to_csc(self, dtype):
+        n, nnz = C.c_int64(), C.c_int64()
+        L.check(self.ctx.lib.sv_graph_info(self.h, C.byref(n), C.byref(nnz)))
+        cp = np.empty(n.value + 1, np.int64)
+        rv = np.empty(nnz.value, np.int64)
+        vv = np.empty(nnz.value, dtype)
+        L.check(self.ctx.lib.sv_graph_download(self.ctx.h, self.h, _ptr(cp), _ptr(rv), _ptr(vv)))
+        return sp.csc_matrix((vv, rv - 1, cp - 1), shape=(n.value, n.value))
+
+
+def jaccard_index(nn_index, k=None, prune=1.0 / 15.0, dtype=np.float64, ctx: Context | None = None):
+    """src/neighbours.jl:127-155 from neighbour lists (n x k, 1-based Int32);
+    k=None selects the diag variant (:96-108)."""
+    ctx = ctx or default_context()
+    nn = np.asfortranarray(nn_index, dtype=np.int32)
+    n, kk = nn.shape
+    dt = _dtype_code(dtype)
+    h = C.c_void_p()
+    L.check(ctx.lib.sv_snn_host(ctx.h, _ptr(nn), n, kk, -1 if k is None else int(k), float(prune), dt,
+                                 C.byref(h)))
+    return Graph(ctx, h).to_csc(np.float64 if dt == SV_F64 else np.float32)
+
+
+def shared_nearest_neighbours(X, k, prune=1.0 / 15.0, metric="euclidean", include_self=True,
+                              precision="fp32", ctx: Context | None = None):
+    """src/neighbours.jl:272-278: kNN then Jaccard weights in the coordinates' type."""
+    ctx = ctx or default_context()
+    if isinstance(X, LinearEmbedding):
+        dt = np.float64
+    else:
+        dt = np.float32 if np.asarray(X).dtype == np.float32 else np.float64
+    _, _, knn = ann(X, k, metric, include_self, precision, ctx, keep=True)
+    h = C.c_void_p()
+    L.check(ctx.lib.sv_snn_knn(ctx.h, knn.h, int(k), float(prune), _dtype_code(dt), C.byref(h)))
+    return Graph(ctx, h).to_csc(dt)

@@ -1,0 +1,546 @@
+// Count matrix on the device: upload of a Julia SparseMatrixCSC (cells x genes),
+// the cell-major (CSR) copy built on the device, and the synthetic generator.
+//
+// Layout in HBM (both copies resident, as the embedding path reads both):
+//   CSC  colptr int64[n_genes+1], rowidx int32[nnz], count int32[nnz]   (gene-major)
+//   CSR  rowptr int64[n_cells+1], colidx int32[nnz], count int32[nnz]   (cell-major)
+// Indices are 0-based on the device; rows are sorted within columns and columns
+// within rows.
+#include "sv_internal.cuh"
+
+namespace {
+
+// ---- conversion of the uploaded arrays --------------------------------------
+template <typename T>
+__global__ void k_colptr_to_i64(const T* __restrict__ in, int64_t* __restrict__ out, int64_t n,
+                                int64_t base) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (int64_t)in[i] - base;
+}
+
+template <typename T>
+__global__ void k_idx_to_i32(const T* __restrict__ in, int32_t* __restrict__ out, int64_t n,
+                             int64_t base, int64_t limit, int* status) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t v = (int64_t)in[i] - base;
+    if (v < 0 || v >= limit) {
+      sv_flag(status, SV_STATUS_OOB);
+      v = 0;
+    }
+    out[i] = (int32_t)v;
+  }
+}
+
+// Checks the CSC invariants (rows in range, strictly increasing per column) and
+// counts entries per row for the transpose.  One warp per column.
+__global__ void k_csc_check_hist(const int64_t* __restrict__ colptr,
+                                 const int32_t* __restrict__ rowidx, int64_t n_genes,
+                                 int64_t n_cells, int64_t nnz, unsigned long long* __restrict__ row_cnt,
+                                 int* status) {
+  int lane = threadIdx.x & 31;
+  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = warp; c < n_genes; c += nwarps) {
+    int64_t s = colptr[c], e = colptr[c + 1];
+    if (s < 0 || e < s || e > nnz) {
+      if (lane == 0) sv_flag(status, SV_STATUS_OOB);
+      continue;
+    }
+    for (int64_t i = s + lane; i < e; i += 32) {
+      int32_t r = rowidx[i];
+      if (r < 0 || r >= n_cells) {
+        sv_flag(status, SV_STATUS_OOB);
+        continue;
+      }
+      if (i + 1 < e && rowidx[i + 1] <= r) sv_flag(status, SV_STATUS_UNSORTED);
+      atomicAdd(&row_cnt[r], 1ull);
+    }
+  }
+}
+
+__global__ void k_u64_to_i64(const unsigned long long* in, int64_t* out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (int64_t)in[i];
+}
+
+// Scatter of CSC entries into their CSR rows (slot order within a row is
+// arbitrary here and fixed by the per-row sort below).
+__global__ void k_csc_scatter(const int64_t* __restrict__ colptr, const int32_t* __restrict__ rowidx,
+                              const int32_t* __restrict__ cnt, int64_t n_genes,
+                              unsigned long long* __restrict__ cursor, int32_t* __restrict__ out_col,
+                              int32_t* __restrict__ out_cnt) {
+  int lane = threadIdx.x & 31;
+  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = warp; c < n_genes; c += nwarps) {
+    int64_t s = colptr[c], e = colptr[c + 1];
+    for (int64_t i = s + lane; i < e; i += 32) {
+      int32_t r = rowidx[i];
+      unsigned long long pos = atomicAdd(&cursor[r], 1ull);
+      out_col[pos] = (int32_t)c;
+      out_cnt[pos] = cnt[i];
+    }
+  }
+}
+
+// Bitonic sort of `n2` (power of two) 64-bit keys held in `buf` by the whole block.
+__device__ void block_bitonic_u64(unsigned long long* buf, int n2) {
+  for (int k = 2; k <= n2; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+        int ixj = i ^ j;
+        if (ixj > i) {
+          unsigned long long a = buf[i], b = buf[ixj];
+          bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            buf[i] = b;
+            buf[ixj] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Sorts each CSR row by column.  Rows that fit `cap` keys are sorted in shared
+// memory; longer rows are appended to `long_rows` for the global-memory pass.
+__global__ void k_sort_rows_smem(const int64_t* __restrict__ rowptr, int64_t n_rows,
+                                 int32_t* __restrict__ col, int32_t* __restrict__ cnt, int cap,
+                                 int64_t* __restrict__ long_rows,
+                                 unsigned long long* __restrict__ n_long) {
+  extern __shared__ unsigned long long skeys[];
+  for (int64_t r = blockIdx.x; r < n_rows; r += gridDim.x) {
+    int64_t s = rowptr[r], e = rowptr[r + 1];
+    int L = e - s < (int64_t)cap + 1 ? (int)(e - s) : cap + 1;
+    if (L <= 1) continue;
+    if (L > cap) {
+      if (threadIdx.x == 0) long_rows[atomicAdd(n_long, 1ull)] = r;
+      continue;
+    }
+    int n2 = 1;
+    while (n2 < L) n2 <<= 1;
+    for (int i = threadIdx.x; i < n2; i += blockDim.x)
+      skeys[i] = i < L ? ((unsigned long long)(uint32_t)col[s + i] << 32) | (uint32_t)cnt[s + i]
+                       : ~0ull;
+    __syncthreads();
+    block_bitonic_u64(skeys, n2);
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+      unsigned long long kv = skeys[i];
+      col[s + i] = (int32_t)(kv >> 32);
+      cnt[s + i] = (int32_t)(kv & 0xffffffffu);
+    }
+    __syncthreads();
+  }
+}
+
+// Long rows: the same bitonic network on a global scratch buffer, one block per row.
+__global__ void k_sort_rows_global(const int64_t* __restrict__ rowptr,
+                                   const int64_t* __restrict__ long_rows, int64_t n_long,
+                                   int32_t* __restrict__ col, int32_t* __restrict__ cnt,
+                                   unsigned long long* __restrict__ scratch, int64_t scratch_per_block) {
+  unsigned long long* buf = scratch + blockIdx.x * scratch_per_block;
+  for (int64_t t = blockIdx.x; t < n_long; t += gridDim.x) {
+    int64_t r = long_rows[t];
+    int64_t s = rowptr[r], e = rowptr[r + 1];
+    int L = (int)(e - s);
+    int n2 = 1;
+    while (n2 < L) n2 <<= 1;
+    for (int i = threadIdx.x; i < n2; i += blockDim.x)
+      buf[i] = i < L ? ((unsigned long long)(uint32_t)col[s + i] << 32) | (uint32_t)cnt[s + i] : ~0ull;
+    __syncthreads();
+    block_bitonic_u64(buf, n2);
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+      unsigned long long kv = buf[i];
+      col[s + i] = (int32_t)(kv >> 32);
+      cnt[s + i] = (int32_t)(kv & 0xffffffffu);
+    }
+    __syncthreads();
+  }
+}
+
+// ---- synthetic negative-binomial generator -----------------------------------
+struct GenParams {
+  const float* mu_g;     // n_genes, already multiplied by the depth factor
+  const float* s_c;      // n_cells
+  const int32_t* cl;     // n_cells or null
+  const float* fold;     // n_clusters x n_genes (exp of the log fold change) or null
+  int64_t n_cells, n_genes;
+  float phi, inv_phi;
+  unsigned long long seed;
+};
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// One count for (cell, gene).  Not inlined so that every kernel that samples
+// runs the identical instruction sequence and the CSC and CSR copies agree.
+__device__ __noinline__ int nb_sample(const GenParams p, int64_t cell, int64_t gene) {
+  float mean = p.mu_g[gene] * p.s_c[cell];
+  if (p.fold) mean *= p.fold[(int64_t)p.cl[cell] * p.n_genes + gene];
+  unsigned long long h =
+      mix64(p.seed ^ mix64((unsigned long long)cell * 0x9E3779B97F4A7C15ull + (unsigned long long)gene));
+  float u = ((float)(h >> 40) + 0.5f) * (1.0f / 16777216.0f);
+  // P(X = 0) = (1 + phi*mean)^(-1/phi); inversion of the NB cdf from 0 upwards
+  float lp = log1pf(p.phi * mean);
+  float pk = expf(-p.inv_phi * lp);
+  if (u < pk) return 0;
+  float ratio = (p.phi * mean) / (1.0f + p.phi * mean);
+  float cum = pk;
+  int k = 0;
+  while (u >= cum && k < 1000000) {
+    pk *= ((float)k + p.inv_phi) / (float)(k + 1) * ratio;
+    k++;
+    cum += pk;
+    if (pk < 1e-30f && cum < u) {  // tail underflow: stop at the current count
+      break;
+    }
+  }
+  return k;
+}
+
+// Pass 1 (cells): non-zeros per cell.  One warp per cell, lanes over genes.
+__global__ void k_gen_row_counts(const GenParams p, int64_t* __restrict__ row_nnz) {
+  int lane = threadIdx.x & 31;
+  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = warp; c < p.n_cells; c += nwarps) {
+    int64_t cntv = 0;
+    for (int64_t g = lane; g < p.n_genes; g += 32) cntv += nb_sample(p, c, g) > 0;
+    cntv = sv_warp_sum(cntv);
+    if (lane == 0) row_nnz[c] = cntv;
+  }
+}
+
+// Pass 1 (genes): non-zeros per gene.  One block per gene, threads over cells.
+__global__ void k_gen_col_counts(const GenParams p, int64_t* __restrict__ col_nnz) {
+  __shared__ int64_t red[32];
+  for (int64_t g = blockIdx.x; g < p.n_genes; g += gridDim.x) {
+    int64_t cntv = 0;
+    for (int64_t c = threadIdx.x; c < p.n_cells; c += blockDim.x) cntv += nb_sample(p, c, g) > 0;
+    cntv = sv_warp_sum(cntv);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = cntv;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      int64_t v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0;
+      v = sv_warp_sum(v);
+      if (threadIdx.x == 0) col_nnz[g] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// Pass 2 (cells): write the CSR rows in gene order (warp ballot compaction).
+__global__ void k_gen_write_csr(const GenParams p, const int64_t* __restrict__ rowptr,
+                                int32_t* __restrict__ colidx, int32_t* __restrict__ cnt) {
+  int lane = threadIdx.x & 31;
+  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = warp; c < p.n_cells; c += nwarps) {
+    int64_t pos = rowptr[c];
+    for (int64_t g0 = 0; g0 < p.n_genes; g0 += 32) {
+      int64_t g = g0 + lane;
+      int v = g < p.n_genes ? nb_sample(p, c, g) : 0;
+      unsigned m = __ballot_sync(0xffffffffu, v > 0);
+      if (v > 0) {
+        int off = __popc(m & ((1u << lane) - 1));
+        colidx[pos + off] = (int32_t)g;
+        cnt[pos + off] = v;
+      }
+      pos += __popc(m);
+    }
+  }
+}
+
+// Pass 2 (genes): write the CSC columns in cell order (block-wide compaction).
+__global__ void k_gen_write_csc(const GenParams p, const int64_t* __restrict__ colptr,
+                                int32_t* __restrict__ rowidx, int32_t* __restrict__ cnt) {
+  __shared__ int wsum[32];
+  __shared__ int64_t base_s;
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int64_t g = blockIdx.x; g < p.n_genes; g += gridDim.x) {
+    if (threadIdx.x == 0) base_s = colptr[g];
+    __syncthreads();
+    for (int64_t c0 = 0; c0 < p.n_cells; c0 += blockDim.x) {
+      int64_t c = c0 + threadIdx.x;
+      int v = c < p.n_cells ? nb_sample(p, c, g) : 0;
+      unsigned m = __ballot_sync(0xffffffffu, v > 0);
+      if (lane == 0) wsum[wid] = __popc(m);
+      __syncthreads();
+      int before = 0, tot = 0;
+      for (int w = 0; w < nw; ++w) {
+        int x = wsum[w];
+        if (w < wid) before += x;
+        tot += x;
+      }
+      int64_t b = base_s;
+      if (v > 0) {
+        int64_t pos = b + before + __popc(m & ((1u << lane) - 1));
+        rowidx[pos] = (int32_t)c;
+        cnt[pos] = v;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) base_s = b + tot;
+      __syncthreads();
+    }
+  }
+}
+
+template <typename T>
+void upload_idx(sv_context* ctx, const void* host, int64_t n, int64_t base, int64_t limit,
+                int32_t* dst) {
+  if (n == 0) return;
+  DevBuf<T> tmp(n);
+  sv_h2d(ctx, tmp.get(), host, n * sizeof(T));
+  sv_launch(ctx, "counts_convert_idx", k_idx_to_i32<T>, dim3(sv_grid_for(ctx, n, 256)), dim3(256),
+            0, (const T*)tmp.get(), dst, n, base, limit, ctx->d_status);
+  sv_sync(ctx);
+}
+
+}  // namespace
+
+// Builds the CSR copy from the CSC copy already on the device.
+static void build_csr_from_csc(sv_context* ctx, sv_counts* c) {
+  DevBuf<unsigned long long> rcnt(c->n_cells + 1);
+  sv_memset(ctx, rcnt.get(), 0, (c->n_cells + 1) * sizeof(unsigned long long));
+  sv_launch(ctx, "counts_check_hist", k_csc_check_hist, dim3(sv_grid_for(ctx, c->n_genes * 32, 256)),
+            dim3(256), 0, (const int64_t*)c->csc_colptr.get(), (const int32_t*)c->csc_rowidx.get(),
+            c->n_genes, c->n_cells, c->nnz, rcnt.get(), ctx->d_status);
+  sv_check_device_status(ctx, "sv_counts_upload_csc");
+  c->csr_rowptr.alloc(c->n_cells + 1);
+  DevBuf<int64_t> rc64(c->n_cells + 1);
+  sv_launch(ctx, "counts_u64_to_i64", k_u64_to_i64, dim3(sv_grid_for(ctx, c->n_cells, 256)), dim3(256),
+            0, (const unsigned long long*)rcnt.get(), rc64.get(), c->n_cells);
+  sv_scan_i64(ctx, rc64.get(), c->csr_rowptr.get(), c->n_cells);
+  // cursors start at the row offsets
+  sv_launch(ctx, "counts_u64_to_i64", k_colptr_to_i64<int64_t>, dim3(sv_grid_for(ctx, c->n_cells, 256)),
+            dim3(256), 0, (const int64_t*)c->csr_rowptr.get(), (int64_t*)rcnt.get(), c->n_cells,
+            (int64_t)0);
+  c->csr_colidx.alloc(c->nnz);
+  c->csr_count.alloc(c->nnz);
+  sv_launch(ctx, "counts_scatter", k_csc_scatter, dim3(sv_grid_for(ctx, c->n_genes * 32, 256)),
+            dim3(256), 0, (const int64_t*)c->csc_colptr.get(), (const int32_t*)c->csc_rowidx.get(),
+            (const int32_t*)c->csc_count.get(), c->n_genes, rcnt.get(), c->csr_colidx.get(),
+            c->csr_count.get());
+  // per-row sort
+  const int cap = 8192;
+  DevBuf<int64_t> long_rows(c->n_cells + 1);
+  DevBuf<unsigned long long> n_long(1);
+  sv_memset(ctx, n_long.get(), 0, sizeof(unsigned long long));
+  SV_CUDA(cudaFuncSetAttribute(k_sort_rows_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               cap * 8));
+  sv_launch(ctx, "counts_sort_rows", k_sort_rows_smem, dim3(sv_grid_for(ctx, c->n_cells, 1, 16)),
+            dim3(256), (size_t)cap * 8, (const int64_t*)c->csr_rowptr.get(), c->n_cells,
+            c->csr_colidx.get(), c->csr_count.get(), cap, long_rows.get(), n_long.get());
+  int64_t nl = sv_read_i64(ctx, (const int64_t*)n_long.get());
+  if (nl > 0) {
+    // longest row bounds the scratch per block
+    std::vector<int64_t> rp(c->n_cells + 1);
+    sv_d2h(ctx, rp.data(), c->csr_rowptr.get(), (c->n_cells + 1) * sizeof(int64_t));
+    int64_t maxlen = 0;
+    for (int64_t r = 0; r < c->n_cells; ++r) maxlen = std::max(maxlen, rp[r + 1] - rp[r]);
+    int64_t n2 = 1;
+    while (n2 < maxlen) n2 <<= 1;
+    int blocks = (int)std::min<int64_t>(nl, (int64_t)ctx->num_sms * 2);
+    DevBuf<unsigned long long> scratch((size_t)blocks * n2);
+    sv_launch(ctx, "counts_sort_rows_long", k_sort_rows_global, dim3(blocks), dim3(1024), 0,
+              (const int64_t*)c->csr_rowptr.get(), (const int64_t*)long_rows.get(), nl,
+              c->csr_colidx.get(), c->csr_count.get(), scratch.get(), n2);
+    sv_sync(ctx);
+  }
+  sv_sync(ctx);
+}
+
+SV_API int sv_counts_upload_csc(sv_context* ctx, int64_t n_cells, int64_t n_genes, int64_t nnz,
+                                const void* colptr, const void* rowval, const void* nzval,
+                                int idx_type, int val_type, int index_base, sv_counts** out) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(out, "out is null");
+  SV_REQUIRE(n_cells >= 1 && n_genes >= 1 && nnz >= 0, "bad sizes");
+  SV_REQUIRE(n_cells < (1ll << 31) && n_genes < (1ll << 31), "dimension exceeds Int32 indices");
+  SV_REQUIRE(idx_type == SV_I32 || idx_type == SV_I64, "idx_type must be SV_I32 or SV_I64");
+  SV_REQUIRE(val_type == SV_I32 || val_type == SV_I64, "val_type must be SV_I32 or SV_I64");
+  SV_REQUIRE(index_base == 0 || index_base == 1, "index_base must be 0 or 1");
+  SV_REQUIRE(colptr && (nnz == 0 || (rowval && nzval)), "null array");
+  auto* c = new sv_counts();
+  try {
+    c->ctx = ctx;
+    c->n_cells = n_cells;
+    c->n_genes = n_genes;
+    c->nnz = nnz;
+    c->csc_colptr.alloc(n_genes + 1);
+    {
+      size_t es = idx_type == SV_I32 ? 4 : 8;
+      DevBuf<unsigned char> tmp((n_genes + 1) * es);
+      sv_h2d(ctx, tmp.get(), colptr, (n_genes + 1) * es);
+      if (idx_type == SV_I32)
+        sv_launch(ctx, "counts_colptr", k_colptr_to_i64<int32_t>, dim3(sv_grid_for(ctx, n_genes + 1, 256)),
+                  dim3(256), 0, (const int32_t*)tmp.get(), c->csc_colptr.get(), n_genes + 1,
+                  (int64_t)index_base);
+      else
+        sv_launch(ctx, "counts_colptr", k_colptr_to_i64<int64_t>, dim3(sv_grid_for(ctx, n_genes + 1, 256)),
+                  dim3(256), 0, (const int64_t*)tmp.get(), c->csc_colptr.get(), n_genes + 1,
+                  (int64_t)index_base);
+      int64_t first = sv_read_i64(ctx, c->csc_colptr.get());
+      int64_t last = sv_read_i64(ctx, c->csc_colptr.get() + n_genes);
+      SV_REQUIRE(first == 0 && last == nnz, "colptr[0] must equal index_base and colptr[end] nnz+base");
+    }
+    c->csc_rowidx.alloc(nnz);
+    c->csc_count.alloc(nnz);
+    if (idx_type == SV_I32 && index_base == 0) {
+      sv_h2d(ctx, c->csc_rowidx.get(), rowval, nnz * 4);
+    } else if (idx_type == SV_I32) {
+      upload_idx<int32_t>(ctx, rowval, nnz, index_base, n_cells, c->csc_rowidx.get());
+    } else {
+      upload_idx<int64_t>(ctx, rowval, nnz, index_base, n_cells, c->csc_rowidx.get());
+    }
+    if (val_type == SV_I32) {
+      sv_h2d(ctx, c->csc_count.get(), nzval, nnz * 4);
+    } else {
+      upload_idx<int64_t>(ctx, nzval, nnz, 0, (1ll << 31) - 1, c->csc_count.get());
+    }
+    sv_check_device_status(ctx, "sv_counts_upload_csc");
+    build_csr_from_csc(ctx, c);
+  } catch (...) {
+    delete c;
+    throw;
+  }
+  *out = c;
+  SV_CATCH
+}
+
+// Pattern-only upload used by sv_centered_create: "counts" hold the CSC position
+// of each entry, so that after the transpose the CSR copy carries, per entry, the
+// index of its value in the CSC order.
+sv_counts* sv_counts_upload_positions(sv_context* ctx, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                                      const int64_t* colptr, const int64_t* rowval) {
+  std::vector<int32_t> pos(std::max<int64_t>(1, nnz));
+  for (int64_t i = 0; i < nnz; ++i) pos[i] = (int32_t)i;
+  sv_counts* c = nullptr;
+  int st = sv_counts_upload_csc(ctx, n_rows, n_cols, nnz, colptr, rowval, pos.data(), SV_I64, SV_I32,
+                                0, &c);
+  if (st != SV_OK) sv_throw(st, "pattern upload failed");
+  return c;
+}
+
+SV_API int sv_counts_generate(sv_context* ctx, int64_t n_cells, int64_t n_genes, const float* mu_g,
+                              const float* s_c, const int32_t* cluster, const float* lfc,
+                              int32_t n_clusters, double depth, double dispersion, uint64_t seed,
+                              sv_counts** out) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(out && mu_g && s_c, "null argument");
+  SV_REQUIRE(n_cells >= 1 && n_genes >= 1 && n_cells < (1ll << 31) && n_genes < (1ll << 31),
+             "bad sizes");
+  SV_REQUIRE(dispersion > 0, "dispersion must be > 0");
+  SV_REQUIRE((n_clusters > 0) == (cluster != nullptr && lfc != nullptr),
+             "cluster and lfc must both be given with n_clusters > 0");
+  std::vector<float> mu_h(n_genes);
+  for (int64_t g = 0; g < n_genes; ++g) mu_h[g] = (float)(mu_g[g] * depth);
+  DevBuf<float> d_mu(n_genes), d_s(n_cells), d_fold;
+  DevBuf<int32_t> d_cl;
+  sv_h2d(ctx, d_mu.get(), mu_h.data(), n_genes * 4);
+  sv_h2d(ctx, d_s.get(), s_c, n_cells * 4);
+  GenParams p{};
+  p.mu_g = d_mu.get();
+  p.s_c = d_s.get();
+  if (n_clusters > 0) {
+    std::vector<float> fold((size_t)n_clusters * n_genes);
+    for (size_t i = 0; i < fold.size(); ++i) fold[i] = expf(lfc[i]);
+    for (int64_t i = 0; i < n_cells; ++i)
+      SV_REQUIRE(cluster[i] >= 0 && cluster[i] < n_clusters, "cluster id out of range");
+    d_fold.alloc(fold.size());
+    d_cl.alloc(n_cells);
+    sv_h2d(ctx, d_fold.get(), fold.data(), fold.size() * 4);
+    sv_h2d(ctx, d_cl.get(), cluster, n_cells * 4);
+    p.fold = d_fold.get();
+    p.cl = d_cl.get();
+  }
+  p.n_cells = n_cells;
+  p.n_genes = n_genes;
+  p.phi = (float)dispersion;
+  p.inv_phi = (float)(1.0 / dispersion);
+  p.seed = seed;
+  auto* c = new sv_counts();
+  try {
+    c->ctx = ctx;
+    c->n_cells = n_cells;
+    c->n_genes = n_genes;
+    DevBuf<int64_t> rn(n_cells + 1), cn(n_genes + 1);
+    sv_launch(ctx, "gen_row_counts", k_gen_row_counts, dim3(sv_grid_for(ctx, n_cells * 32, 256, 16)),
+              dim3(256), 0, p, rn.get());
+    sv_launch(ctx, "gen_col_counts", k_gen_col_counts, dim3(sv_grid_for(ctx, n_genes, 1, 8)),
+              dim3(1024), 0, p, cn.get());
+    c->csr_rowptr.alloc(n_cells + 1);
+    c->csc_colptr.alloc(n_genes + 1);
+    sv_scan_i64(ctx, rn.get(), c->csr_rowptr.get(), n_cells);
+    sv_scan_i64(ctx, cn.get(), c->csc_colptr.get(), n_genes);
+    int64_t nnz_r = sv_read_i64(ctx, c->csr_rowptr.get() + n_cells);
+    int64_t nnz_c = sv_read_i64(ctx, c->csc_colptr.get() + n_genes);
+    if (nnz_r != nnz_c)
+      sv_throw(SV_ERR_DEVICE, "generator: row and column totals disagree (%lld vs %lld)",
+               (long long)nnz_r, (long long)nnz_c);
+    c->nnz = nnz_r;
+    c->csr_colidx.alloc(c->nnz);
+    c->csr_count.alloc(c->nnz);
+    c->csc_rowidx.alloc(c->nnz);
+    c->csc_count.alloc(c->nnz);
+    sv_launch(ctx, "gen_write_csr", k_gen_write_csr, dim3(sv_grid_for(ctx, n_cells * 32, 256, 16)),
+              dim3(256), 0, p, (const int64_t*)c->csr_rowptr.get(), c->csr_colidx.get(),
+              c->csr_count.get());
+    sv_launch(ctx, "gen_write_csc", k_gen_write_csc, dim3(sv_grid_for(ctx, n_genes, 1, 8)), dim3(1024),
+              0, p, (const int64_t*)c->csc_colptr.get(), c->csc_rowidx.get(), c->csc_count.get());
+    sv_sync(ctx);
+  } catch (...) {
+    delete c;
+    throw;
+  }
+  *out = c;
+  SV_CATCH
+}
+
+SV_API int sv_counts_info(const sv_counts* c, int64_t* n_cells, int64_t* n_genes, int64_t* nnz) {
+  SV_TRY
+  SV_REQUIRE(c, "null handle");
+  if (n_cells) *n_cells = c->n_cells;
+  if (n_genes) *n_genes = c->n_genes;
+  if (nnz) *nnz = c->nnz;
+  SV_CATCH
+}
+
+SV_API int sv_counts_download_csc(sv_context* ctx, const sv_counts* c, int64_t* colptr,
+                                  int32_t* rowval, int32_t* counts) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(c && c->ctx == ctx, "handle does not belong to this context");
+  if (colptr) sv_d2h(ctx, colptr, c->csc_colptr.get(), (c->n_genes + 1) * 8);
+  if (rowval) sv_d2h(ctx, rowval, c->csc_rowidx.get(), c->nnz * 4);
+  if (counts) sv_d2h(ctx, counts, c->csc_count.get(), c->nnz * 4);
+  SV_CATCH
+}
+
+SV_API int sv_counts_download_csr(sv_context* ctx, const sv_counts* c, int64_t* rowptr,
+                                  int32_t* colidx, int32_t* counts) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(c && c->ctx == ctx, "handle does not belong to this context");
+  if (rowptr) sv_d2h(ctx, rowptr, c->csr_rowptr.get(), (c->n_cells + 1) * 8);
+  if (colidx) sv_d2h(ctx, colidx, c->csr_colidx.get(), c->nnz * 4);
+  if (counts) sv_d2h(ctx, counts, c->csr_count.get(), c->nnz * 4);
+  SV_CATCH
+}
+
+SV_API int sv_counts_free(sv_counts* c) {
+  if (c) {
+    if (c->ctx) cudaSetDevice(c->ctx->device);
+    delete c;
+  }
+  return SV_OK;
+}

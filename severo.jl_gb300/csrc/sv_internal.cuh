@@ -1,0 +1,277 @@
+// Internal definitions shared by the translation units of libseverogpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+#include <string>
+#include <vector>
+#include <map>
+#include <mutex>
+#include <algorithm>
+
+#include "../../include/severo_gpu.h"
+
+#define SV_API extern "C" __attribute__((visibility("default")))
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+void sv_set_error(const char* fmt, ...);
+
+struct SvError {
+  int code;
+};
+
+#define SV_TRY try {
+#define SV_CATCH                       \
+  }                                    \
+  catch (const SvError& e) {           \
+    return e.code;                     \
+  }                                    \
+  catch (...) {                        \
+    sv_set_error("unexpected C++ exception"); \
+    return SV_ERR_CUDA;                \
+  }                                    \
+  return SV_OK;
+
+[[noreturn]] void sv_throw(int code, const char* fmt, ...);
+
+#define SV_REQUIRE(cond, ...)                          \
+  do {                                                 \
+    if (!(cond)) sv_throw(SV_ERR_ARG, __VA_ARGS__);    \
+  } while (0)
+
+#define SV_CUDA(call)                                                          \
+  do {                                                                         \
+    cudaError_t _e = (call);                                                   \
+    if (_e != cudaSuccess) {                                                   \
+      if (_e == cudaErrorMemoryAllocation) {                                   \
+        cudaGetLastError();                                                    \
+        sv_throw(SV_ERR_OOM, "%s:%d %s: %s", __FILE__, __LINE__, #call,        \
+                 cudaGetErrorString(_e));                                      \
+      }                                                                        \
+      sv_throw(SV_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,         \
+               cudaGetErrorString(_e));                                        \
+    }                                                                          \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct SvTimedLaunch {
+  std::string name;
+  cudaEvent_t a, b;
+};
+
+struct sv_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+  bool profiling = false;
+  std::vector<SvTimedLaunch> pending;             // events not yet harvested
+  std::map<std::string, std::pair<double, int64_t>> prof;  // name -> (ms, count)
+  std::vector<cudaEvent_t> event_pool;
+  cudaEvent_t marks[16] = {};
+  // device status word written by kernels that detect a bounds / limit failure
+  int* d_status = nullptr;
+  // small pinned staging buffer for scalar read-backs
+  void* h_stage = nullptr;
+  size_t h_stage_bytes = 0;
+};
+
+void sv_ctx_check(sv_context* ctx);
+cudaEvent_t sv_ctx_event(sv_context* ctx);
+void sv_ctx_harvest(sv_context* ctx);
+void* sv_ctx_stage(sv_context* ctx, size_t bytes);
+void sv_check_device_status(sv_context* ctx, const char* where);
+
+// Launch a kernel on the context stream; counts launches and, when profiling
+// is on, brackets it with events.
+template <typename Kern, typename... Args>
+inline void sv_launch(sv_context* ctx, const char* name, Kern kernel, dim3 grid, dim3 block,
+                      size_t smem, Args... args) {
+  if (grid.x == 0 || grid.y == 0 || grid.z == 0) return;
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (ctx->profiling) {
+    a = sv_ctx_event(ctx);
+    b = sv_ctx_event(ctx);
+    SV_CUDA(cudaEventRecord(a, ctx->stream));
+  }
+  kernel<<<grid, block, smem, ctx->stream>>>(args...);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) sv_throw(SV_ERR_CUDA, "launch of %s failed: %s", name, cudaGetErrorString(e));
+  ctx->launches++;
+  if (ctx->profiling) {
+    SV_CUDA(cudaEventRecord(b, ctx->stream));
+    ctx->pending.push_back({name, a, b});
+  }
+}
+
+// ---------------------------------------------------------------------------
+// device memory
+// ---------------------------------------------------------------------------
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  explicit DevBuf(size_t count) { alloc(count); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    n = count;
+    // pad so that 16-byte vector loads past the logical end stay inside the allocation
+    size_t bytes = (count * sizeof(T) + 64 + 255) & ~size_t(255);
+    cudaError_t e = cudaMalloc((void**)&p, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      n = 0;
+      sv_throw(SV_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    }
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  T* get() const { return p; }
+};
+
+// ---------------------------------------------------------------------------
+// handles
+// ---------------------------------------------------------------------------
+struct sv_counts {
+  sv_context* ctx = nullptr;
+  int64_t n_cells = 0, n_genes = 0, nnz = 0;
+  DevBuf<int64_t> csc_colptr;   // n_genes + 1
+  DevBuf<int32_t> csc_rowidx;   // nnz
+  DevBuf<int32_t> csc_count;    // nnz
+  DevBuf<int64_t> csr_rowptr;   // n_cells + 1
+  DevBuf<int32_t> csr_colidx;   // nnz
+  DevBuf<int32_t> csr_count;    // nnz
+};
+
+struct sv_data {
+  sv_context* ctx = nullptr;
+  const sv_counts* counts = nullptr;
+  int dtype = SV_F64;
+  int method = SV_LOGNORMALIZE;
+  double scale_factor = 1.0;
+  DevBuf<unsigned char> csc_val;   // nnz * elem
+  DevBuf<unsigned char> csr_val;   // nnz * elem
+  DevBuf<int64_t> totals;          // n_cells
+};
+
+struct sv_centered {
+  sv_context* ctx = nullptr;
+  const sv_data* data = nullptr;
+  int64_t n_cells = 0, nf = 0, nnz_h = 0;
+  int dtype = SV_F64;          // value storage type
+  double scale_max = 0;
+  DevBuf<int32_t> feat_gene;   // nf: 0-based gene index of each feature
+  DevBuf<int64_t> feat_start;  // nf: CSC range of the feature
+  DevBuf<int64_t> feat_end;
+  DevBuf<double> mean, std_, mu;      // nf (FP64)
+  DevBuf<float> inv_std_f, clip_f;    // nf (FP32 form of the scale / clip)
+  DevBuf<double> inv_std_d, clip_d;   // nf (FP64 form, for FP64 data)
+  // chunk table of the CSC (X^T u) product
+  int64_t n_chunks = 0;
+  DevBuf<int32_t> chunk_feat;
+  DevBuf<int64_t> chunk_start, chunk_end;
+  DevBuf<int64_t> feat_chunk_off;     // nf + 1
+  DevBuf<double> chunk_partial;       // n_chunks * block_cols
+  int64_t partial_cols = 0;
+  // cell-major copy of the feature subset (X v product)
+  DevBuf<int64_t> h_rowptr;           // n_cells + 1
+  DevBuf<uint16_t> h_col16;           // nnz_h when nf <= 65536
+  DevBuf<int32_t> h_col32;            // nnz_h otherwise
+  DevBuf<unsigned char> h_val;        // nnz_h * elem
+  // scratch for the product prologues
+  DevBuf<float> u_f32;                // n_cells
+  DevBuf<double> red_partial;         // reduction partials
+  DevBuf<double> scal;                // small device scalars
+  // set when the matrix was built by sv_centered_create (owned here)
+  sv_counts* own_counts = nullptr;
+  sv_data* own_data = nullptr;
+};
+
+struct sv_embed {
+  sv_context* ctx = nullptr;
+  int64_t n_cells = 0, npcs = 0, nf = 0;
+  DevBuf<double> Z;        // n_cells x npcs column-major (U diag(s))
+  DevBuf<double> s;        // npcs
+};
+
+struct sv_knn {
+  sv_context* ctx = nullptr;
+  int64_t n = 0, k = 0;
+  DevBuf<int32_t> idx;     // n x k row-major, 0-based
+  DevBuf<float> dist;      // n x k row-major, metric distance
+};
+
+struct sv_graph {
+  sv_context* ctx = nullptr;
+  int64_t n = 0, nnz = 0;
+  int dtype = SV_F64;
+  DevBuf<int64_t> colptr;          // n + 1, 0-based
+  DevBuf<int32_t> rowidx;          // nnz, 0-based
+  DevBuf<unsigned char> val;       // nnz * elem
+};
+
+inline size_t sv_elem_size(int dtype) {
+  switch (dtype) {
+    case SV_I32: return 4;
+    case SV_I64: return 8;
+    case SV_F32: return 4;
+    case SV_F64: return 8;
+    case SV_BF16: return 2;
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// shared device helpers
+// ---------------------------------------------------------------------------
+#define SV_STATUS_OOB 1
+#define SV_STATUS_UNSORTED 2
+#define SV_STATUS_LIMIT 4
+
+__device__ __forceinline__ void sv_flag(int* status, int bit) { atomicOr(status, bit); }
+
+template <typename T>
+__device__ __forceinline__ T sv_warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ float sv_load_val(const float* p, int64_t i) { return p[i]; }
+__device__ __forceinline__ float sv_load_val(const __nv_bfloat16* p, int64_t i) {
+  return __bfloat162float(p[i]);
+}
+__device__ __forceinline__ double sv_load_val(const double* p, int64_t i) { return p[i]; }
+
+// ---------------------------------------------------------------------------
+// host helpers implemented in sv_core.cu
+// ---------------------------------------------------------------------------
+// out[0..n] = exclusive scan of in[0..n-1]; out[n] = total.  in may equal out
+// only if the caller does not need in afterwards.
+void sv_scan_i64(sv_context* ctx, const int64_t* in, int64_t* out, int64_t n);
+int64_t sv_read_i64(sv_context* ctx, const int64_t* dptr);
+void sv_memset(sv_context* ctx, void* p, int v, size_t bytes);
+void sv_h2d(sv_context* ctx, void* dst, const void* src, size_t bytes);
+void sv_d2h(sv_context* ctx, void* dst, const void* src, size_t bytes);
+void sv_sync(sv_context* ctx);
+int sv_grid_for(sv_context* ctx, int64_t work_items, int per_block, int max_per_sm = 8);

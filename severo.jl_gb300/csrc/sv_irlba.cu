@@ -1,0 +1,707 @@
+// irlba on the device: augmented implicitly restarted Lanczos bidiagonalisation
+// (Baglama & Reichel, SIAM J. Sci. Comput. 27 (2005)), the routine that
+// src/irlba.jl:47-76 reaches through the native `irlba` symbol.
+//
+//   A V_j = W_j B_j,  A^T W_j = V_j B_j^T + f e_j^T      (A = Xs, m x n)
+//
+// Both Lanczos bases live in HBM in FP64, column-major: W (m x work, the cell
+// side, 1.3M x 57 doubles at the atlas size) and V (n x work, the feature side).
+// Every new vector is reorthogonalised against its basis by classical
+// Gram-Schmidt applied twice (CGS2) in FP64.  After `work` steps the small
+// matrix B (work x work, upper triangular) is decomposed by a one-block FP64
+// one-sided Jacobi SVD; the nu leading Ritz vectors are kept (thick restart):
+//   V <- [V Q_k, f/|f|],  W <- W P_k,  B <- [diag(s_k) rho; 0 ...],
+//   rho_i = |f| P[work-1, i]
+// and convergence is declared when every |rho_i| < tol * max singular value
+// (the residual ||A^T u_i - s_i v_i||).  The host reads back 2*work+2 doubles
+// per restart; everything else stays on the device.
+#include "sv_internal.cuh"
+#include <math.h>
+
+void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const double* x, double* y,
+                       double alpha, double beta, const double* csub, const double* z);
+
+namespace {
+
+constexpr int RED_BLOCKS = 256;    // blocks of the tall reductions
+constexpr int MAX_WORK = 96;       // largest Lanczos basis the Jacobi kernel holds in smem
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  v = sv_warp_sum(v);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0;
+  if (wid == 0) {
+    r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+    r = sv_warp_sum(r);
+  }
+  return r;  // valid in thread 0
+}
+
+// c[j] = Q[:, j] . x  (j < ncols), per-block partials, the last block to finish
+// sums them in block order (deterministic) and writes c.
+__global__ void __launch_bounds__(256) k_dots(const double* __restrict__ Q, int64_t ld, int ncols,
+                                              const double* __restrict__ x, int64_t len,
+                                              double* __restrict__ part, double* __restrict__ c,
+                                              unsigned int* __restrict__ counter) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  int64_t seg = (len + gridDim.x - 1) / gridDim.x;
+  int64_t r0 = (int64_t)blockIdx.x * seg, r1 = min(len, r0 + seg);
+  for (int j = 0; j < ncols; ++j) {
+    const double* q = Q + (int64_t)j * ld;
+    double acc = 0;
+    for (int64_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) acc += q[i] * x[i];
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[(int64_t)blockIdx.x * ncols + j] = acc;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    for (int j = threadIdx.x; j < ncols; j += blockDim.x) {
+      double s = 0;
+      for (unsigned b = 0; b < gridDim.x; ++b) s += part[(int64_t)b * ncols + j];
+      c[j] = s;
+    }
+    if (threadIdx.x == 0) *counter = 0;
+  }
+}
+
+// x -= Q[:, :ncols] c ; optionally nrm = ||x|| (after the update).
+__global__ void __launch_bounds__(256) k_update_norm(double* __restrict__ x, int64_t len,
+                                                     const double* __restrict__ Q, int64_t ld,
+                                                     int ncols, const double* __restrict__ c,
+                                                     double* __restrict__ part,
+                                                     double* __restrict__ nrm,
+                                                     unsigned int* __restrict__ counter) {
+  __shared__ double sh[32];
+  __shared__ double cs[MAX_WORK];
+  __shared__ bool last;
+  for (int j = threadIdx.x; j < ncols; j += blockDim.x) cs[j] = c[j];
+  __syncthreads();
+  double acc = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v = x[i];
+    for (int j = 0; j < ncols; ++j) v -= Q[(int64_t)j * ld + i] * cs[j];
+    if (ncols) x[i] = v;
+    acc += v * v;
+  }
+  if (!nrm) return;
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    if (threadIdx.x == 0) {
+      double s = 0;
+      for (unsigned b = 0; b < gridDim.x; ++b) s += part[b];
+      *nrm = sqrt(s);
+      *counter = 0;
+    }
+  }
+}
+
+__device__ __forceinline__ unsigned long long mixbits(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double normal_at(unsigned long long seed, unsigned long long tag, int64_t i) {
+  unsigned long long h1 = mixbits(seed ^ mixbits(tag * 0x9E3779B97F4A7C15ull + (unsigned long long)i));
+  unsigned long long h2 = mixbits(h1 + 0x632BE59BD9B4E019ull);
+  double u1 = ((double)(h1 >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+  double u2 = ((double)(h2 >> 11)) * (1.0 / 9007199254740992.0);
+  return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);    // Box-Muller
+}
+
+// out = in / *nrm and the B entry := *nrm; when *nrm < thresh the Krylov space is
+// (numerically) invariant: out := a random vector, B entry and *nrm := 0, flag set
+// for k_fix, which orthonormalises it against the basis.
+__global__ void k_scal(double* __restrict__ out, const double* __restrict__ in, int64_t len,
+                       double* __restrict__ nrm, double thresh, double* __restrict__ bentry,
+                       int* __restrict__ flag, unsigned long long seed, unsigned long long tag) {
+  double s = *nrm;
+  bool brk = !(s >= thresh);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = brk ? normal_at(seed, tag, i) : in[i] / s;
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (bentry) *bentry = brk ? 0.0 : s;
+    if (brk) {
+      *flag = 1;
+    }
+  }
+}
+
+// second half of the breakdown branch: zero the norm slot once all blocks of
+// k_scal have read it (separate launch)
+__global__ void k_scal_post(double* nrm, const int* flag) {
+  if (*flag) *nrm = 0.0;
+}
+
+// One block: if *flag, x <- CGS2(x, Q[:, :ncols]) normalised; clears the flag.
+__global__ void k_fix(double* __restrict__ x, int64_t len, const double* __restrict__ Q, int64_t ld,
+                      int ncols, int* __restrict__ flag) {
+  __shared__ double sh[32];
+  __shared__ double cs[MAX_WORK];
+  __shared__ double tot;
+  if (*flag == 0) return;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int j = 0; j < ncols; ++j) {
+      double acc = 0;
+      for (int64_t i = threadIdx.x; i < len; i += blockDim.x) acc += Q[(int64_t)j * ld + i] * x[i];
+      acc = block_sum(acc, sh);
+      if (threadIdx.x == 0) cs[j] = acc;
+    }
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
+      double v = x[i];
+      for (int j = 0; j < ncols; ++j) v -= Q[(int64_t)j * ld + i] * cs[j];
+      x[i] = v;
+    }
+    __syncthreads();
+  }
+  double acc = 0;
+  for (int64_t i = threadIdx.x; i < len; i += blockDim.x) acc += x[i] * x[i];
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) tot = sqrt(acc);
+  __syncthreads();
+  double s = tot;
+  for (int64_t i = threadIdx.x; i < len; i += blockDim.x) x[i] = x[i] / s;
+  __syncthreads();
+  if (threadIdx.x == 0) *flag = 0;
+}
+
+// One-sided (Hestenes) Jacobi SVD of B (m x m, row-major) in FP64, one block.
+// Columns of A = B are orthogonalised by plane rotations J accumulated in Qm;
+// then s_i = |A e_i|, P_i = A e_i / s_i, sorted by descending s.
+// Outputs: P (m x m col-major), s (m), Q (m x m col-major), summary =
+// [s (m), P[m-1, :] (m), rf, sweeps].
+__global__ void k_jacobi_svd(const double* __restrict__ B, int m, double* __restrict__ Pout,
+                             double* __restrict__ sout, double* __restrict__ Qout,
+                             double* __restrict__ summary, const double* __restrict__ rf,
+                             int max_sweeps, int* __restrict__ status) {
+  extern __shared__ double sm[];
+  double* A = sm;              // m*m, column c at A[c*m]
+  double* J = sm + m * m;      // m*m
+  __shared__ int rotated;
+  __shared__ int order[MAX_WORK];
+  __shared__ double nrm[MAX_WORK];
+  int tid = threadIdx.x;
+  for (int idx = tid; idx < m * m; idx += blockDim.x) {
+    int r = idx % m, c = idx / m;
+    A[idx] = B[r * m + c];
+    J[idx] = r == c ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  int mp = (m + 1) & ~1;   // even number of slots (one dummy when m is odd)
+  int npairs = mp / 2;
+  int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    if (tid == 0) rotated = 0;
+    __syncthreads();
+    for (int round = 0; round < mp - 1; ++round) {
+      for (int pi = wid; pi < npairs; pi += nw) {
+        // circle method: slot 0 fixed, slots 1..mp-1 rotate by `round`
+        int a = pi == 0 ? 0 : 1 + (pi - 1 + round) % (mp - 1);
+        int b = 1 + (mp - 2 - pi + round) % (mp - 1);
+        if (a >= m || b >= m) continue;
+        int p = min(a, b), q = max(a, b);
+        double* ap = A + p * m;
+        double* aq = A + q * m;
+        double al = 0, be = 0, ga = 0;
+        for (int r = lane; r < m; r += 32) {
+          double x = ap[r], y = aq[r];
+          al += x * x;
+          be += y * y;
+          ga += x * y;
+        }
+        al = sv_warp_sum(al);
+        be = sv_warp_sum(be);
+        ga = sv_warp_sum(ga);
+        if (fabs(ga) > 1e-15 * sqrt(al * be) && ga != 0.0) {
+          double zeta = (be - al) / (2.0 * ga);
+          double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + hypot(1.0, zeta));
+          double cth = 1.0 / sqrt(1.0 + t * t);
+          double sth = cth * t;
+          for (int r = lane; r < m; r += 32) {
+            double x = ap[r], y = aq[r];
+            ap[r] = cth * x - sth * y;
+            aq[r] = sth * x + cth * y;
+          }
+          double* jp = J + p * m;
+          double* jq = J + q * m;
+          for (int r = lane; r < m; r += 32) {
+            double x = jp[r], y = jq[r];
+            jp[r] = cth * x - sth * y;
+            jq[r] = sth * x + cth * y;
+          }
+          if (lane == 0) rotated = 1;
+        }
+      }
+      __syncthreads();
+    }
+    if (!rotated) break;
+    __syncthreads();
+  }
+  if (sweep >= max_sweeps && tid == 0) atomicOr(status, SV_STATUS_LIMIT);
+  // singular values and ordering
+  for (int c = wid; c < m; c += nw) {
+    double s = 0;
+    for (int r = lane; r < m; r += 32) s += A[c * m + r] * A[c * m + r];
+    s = sv_warp_sum(s);
+    if (lane == 0) nrm[c] = sqrt(s);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    // stable insertion sort, descending
+    for (int i = 0; i < m; ++i) order[i] = i;
+    for (int i = 1; i < m; ++i) {
+      int v = order[i];
+      int t = i - 1;
+      while (t >= 0 && nrm[order[t]] < nrm[v]) {
+        order[t + 1] = order[t];
+        --t;
+      }
+      order[t + 1] = v;
+    }
+  }
+  __syncthreads();
+  for (int idx = tid; idx < m * m; idx += blockDim.x) {
+    int r = idx % m, i = idx / m;
+    int c = order[i];
+    double s = nrm[c];
+    Pout[i * m + r] = s > 0 ? A[c * m + r] / s : (r == i ? 1.0 : 0.0);
+    Qout[i * m + r] = J[c * m + r];
+  }
+  for (int i = tid; i < m; i += blockDim.x) {
+    sout[i] = nrm[order[i]];
+    summary[i] = nrm[order[i]];
+    double s = nrm[order[i]];
+    summary[m + i] = s > 0 ? A[order[i] * m + (m - 1)] / s : 0.0;
+  }
+  if (tid == 0) {
+    summary[2 * m] = rf ? *rf : 0.0;
+    summary[2 * m + 1] = (double)sweep;
+  }
+}
+
+// Out[:, c] = sum_r In[:, r] * M[r + c*nin]  for c < nout   (tall x small, FP64)
+template <int KB>
+__global__ void __launch_bounds__(256) k_rotate(const double* __restrict__ In, int64_t ld_in,
+                                                int64_t len, int nin, const double* __restrict__ M,
+                                                int nout, double* __restrict__ Out, int64_t ld_out) {
+  extern __shared__ double Ms[];
+  for (int i = threadIdx.x; i < nin * nout; i += blockDim.x) Ms[i] = M[i];
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    for (int c0 = 0; c0 < nout; c0 += KB) {
+      double acc[KB];
+#pragma unroll
+      for (int t = 0; t < KB; ++t) acc[t] = 0;
+      for (int r = 0; r < nin; ++r) {
+        double w = In[(int64_t)r * ld_in + i];
+#pragma unroll
+        for (int t = 0; t < KB; ++t)
+          if (c0 + t < nout) acc[t] += w * Ms[r + (c0 + t) * nin];
+      }
+#pragma unroll
+      for (int t = 0; t < KB; ++t)
+        if (c0 + t < nout) Out[(int64_t)(c0 + t) * ld_out + i] = acc[t];
+    }
+  }
+}
+
+// V[:, k] = F / rf and B reset for the next cycle.
+__global__ void k_restart_tail(double* __restrict__ vk, const double* __restrict__ F, int64_t n,
+                               const double* __restrict__ summary, int m, int k,
+                               double* __restrict__ B) {
+  double rf = summary[2 * m];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    vk[i] = F[i] / rf;
+  if (blockIdx.x == 0) {
+    for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
+      int r = idx / m, c = idx % m;
+      double v = 0;
+      if (r < k && c == r) v = summary[r];
+      if (r < k && c == k) v = rf * summary[m + r];
+      B[idx] = v;
+    }
+  }
+}
+
+__global__ void k_axpy_sub(double* __restrict__ y, const double* __restrict__ z,
+                           const double* __restrict__ cs, int64_t len) {
+  double c = *cs;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] -= c * z[i];
+}
+
+__global__ void k_scale_cols(double* __restrict__ X, int64_t len, int ncols,
+                             const double* __restrict__ s) {
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < len * ncols;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int c = (int)(idx / len);
+    X[idx] *= s[c];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// operator abstraction: the implicit matrix on the device, or host callbacks
+// ---------------------------------------------------------------------------
+struct Op {
+  virtual ~Op() {}
+  // y = A x - (csub ? *csub : 0) * z        (x in R^n, y in R^m)
+  virtual void N(const double* x, double* y, const double* csub, const double* z) = 0;
+  // y = A^T x - (csub ? *csub : 0) * z      (x in R^m, y in R^n)
+  virtual void T(const double* x, double* y, const double* csub, const double* z) = 0;
+};
+
+struct CenteredOp : Op {
+  sv_context* ctx;
+  const sv_centered* S;
+  CenteredOp(sv_context* c, const sv_centered* s) : ctx(c), S(s) {}
+  void N(const double* x, double* y, const double* csub, const double* z) override {
+    sv_centered_apply(ctx, S, 'N', x, y, 1.0, 0.0, csub, z);
+  }
+  void T(const double* x, double* y, const double* csub, const double* z) override {
+    sv_centered_apply(ctx, S, 'T', x, y, 1.0, 0.0, csub, z);
+  }
+};
+
+struct CallbackOp : Op {
+  sv_context* ctx;
+  int64_t m, n;
+  sv_matmul_fn mm;
+  void* data;
+  std::vector<double> hx, hy, tmp;
+  CallbackOp(sv_context* c, int64_t m_, int64_t n_, sv_matmul_fn f, void* d)
+      : ctx(c), m(m_), n(n_), mm(f), data(d), hx(std::max(m_, n_)), hy(std::max(m_, n_)),
+        tmp(std::max(m_, n_)) {}
+  void run(char trans, const double* x, int64_t lx, double* y, int64_t ly, const double* csub,
+           const double* z) {
+    sv_d2h(ctx, hx.data(), x, lx * 8);
+    mm(hy.data(), trans, hx.data(), tmp.data(), data);
+    sv_h2d(ctx, y, hy.data(), ly * 8);
+    if (csub)
+      sv_launch(ctx, "irlba_axpy", k_axpy_sub, dim3(sv_grid_for(ctx, ly, 256, 4)), dim3(256), 0, y, z,
+                csub, ly);
+  }
+  void N(const double* x, double* y, const double* csub, const double* z) override {
+    run('N', x, n, y, m, csub, z);
+  }
+  void T(const double* x, double* y, const double* csub, const double* z) override {
+    run('T', x, m, y, n, csub, z);
+  }
+};
+
+struct IrlbaResult {
+  int info = 1;
+  int64_t iters = 0, nmatvec = 0;
+};
+
+// The Lanczos driver.  m = rows of A (the W side), n = columns (the V side).
+struct Lanczos {
+  sv_context* ctx;
+  Op* op;
+  int64_t m, n;
+  int nu, work;
+  DevBuf<double> V, W, Vt, Wt, F, B, P, Q, sig, summary, scal, part, cvec;
+  DevBuf<unsigned int> counter;
+  DevBuf<int> flag;
+  std::vector<double> hsum;
+
+  Lanczos(sv_context* c, Op* o, int64_t m_, int64_t n_, int nu_, int work_)
+      : ctx(c), op(o), m(m_), n(n_), nu(nu_), work(work_) {
+    V.alloc(n * work);
+    Vt.alloc(n * work);
+    W.alloc(m * work);
+    Wt.alloc(m * work);
+    F.alloc(n);
+    B.alloc(work * work);
+    P.alloc(work * work);
+    Q.alloc(work * work);
+    sig.alloc(work);
+    summary.alloc(2 * work + 2);
+    scal.alloc(8);
+    part.alloc((size_t)RED_BLOCKS * (work + 1));
+    cvec.alloc(work + 1);
+    counter.alloc(4);
+    flag.alloc(4);
+    sv_memset(ctx, counter.get(), 0, 16);
+    sv_memset(ctx, flag.get(), 0, 16);
+    sv_memset(ctx, B.get(), 0, work * work * 8);
+    hsum.resize(2 * work + 2);
+    SV_CUDA(cudaFuncSetAttribute(k_jacobi_svd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 2 * MAX_WORK * MAX_WORK * 8));
+    SV_CUDA(cudaFuncSetAttribute(k_rotate<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 MAX_WORK * MAX_WORK * 8));
+  }
+
+  int red_grid(int64_t len) { return (int)std::min<int64_t>(RED_BLOCKS, std::max<int64_t>(1, (len + 1023) / 1024)); }
+
+  // x <- CGS2(x, Qb[:, :ncols]); *nrm = ||x||
+  void orth_norm(double* x, int64_t len, const double* Qb, int ncols, double* nrm) {
+    int g = red_grid(len);
+    for (int pass = 0; pass < 2 && ncols > 0; ++pass) {
+      sv_launch(ctx, "irlba_dots", k_dots, dim3(g), dim3(256), 0, Qb, len, ncols, (const double*)x, len,
+                part.get(), cvec.get(), counter.get());
+      sv_launch(ctx, "irlba_update", k_update_norm, dim3(g), dim3(256), 0, x, len, Qb, len, ncols,
+                (const double*)cvec.get(), part.get(), pass == 1 ? nrm : (double*)nullptr,
+                counter.get());
+    }
+    if (ncols == 0)
+      sv_launch(ctx, "irlba_update", k_update_norm, dim3(g), dim3(256), 0, x, len, Qb, len, 0,
+                (const double*)cvec.get(), part.get(), nrm, counter.get());
+  }
+
+  void scal_fix(double* out, const double* in, int64_t len, double* nrm, double thresh,
+                double* bentry, const double* basis, int ncols, uint64_t seed, uint64_t tag) {
+    sv_launch(ctx, "irlba_scal", k_scal, dim3(sv_grid_for(ctx, len, 256, 4)), dim3(256), 0, out, in,
+              len, nrm, thresh, bentry, flag.get(), (unsigned long long)seed,
+              (unsigned long long)tag);
+    sv_launch(ctx, "irlba_scal_post", k_scal_post, dim3(1), dim3(1), 0, nrm, (const int*)flag.get());
+    sv_launch(ctx, "irlba_fix", k_fix, dim3(1), dim3(1024), 0, out, len, basis, len, ncols, flag.get());
+  }
+
+  void rotate(const double* In, int64_t len, const double* M, int nout, double* Out) {
+    sv_launch(ctx, "irlba_rotate", k_rotate<16>, dim3(sv_grid_for(ctx, len, 256, 8)), dim3(256),
+              (size_t)work * nout * 8, In, len, len, work, M, nout, Out, len);
+  }
+
+  IrlbaResult run(const double* init_host, int maxit, double tol, uint64_t seed) {
+    IrlbaResult res;
+    double* s0 = scal.get();       // S (W-side norm)
+    double* s1 = scal.get() + 1;   // R (V-side norm)
+    sv_h2d(ctx, F.get(), init_host, n * 8);
+    orth_norm(F.get(), n, V.get(), 0, s1);
+    const double eps_b = sqrt(2.220446049250313e-16);
+    scal_fix(V.get(), F.get(), n, s1, 1e-300, nullptr, V.get(), 0, seed, 0);
+    int k = 0;
+    double smax = 0;
+    uint64_t tag = 1;
+    int it = 0;
+    for (; it < maxit; ++it) {
+      double thresh = eps_b * std::max(smax, 1.0);
+      int j = k;
+      double* Vj = V.get() + (int64_t)j * n;
+      double* Wj = W.get() + (int64_t)j * m;
+      op->N(Vj, Wj, nullptr, nullptr);
+      res.nmatvec++;
+      orth_norm(Wj, m, W.get(), j, s0);
+      scal_fix(Wj, Wj, m, s0, thresh, B.get() + (int64_t)j * work + j, W.get(), j, seed, tag++);
+      while (true) {
+        Vj = V.get() + (int64_t)j * n;
+        Wj = W.get() + (int64_t)j * m;
+        op->T(Wj, F.get(), s0, Vj);
+        res.nmatvec++;
+        orth_norm(F.get(), n, V.get(), j + 1, s1);
+        if (j + 1 < work) {
+          double* Vn = V.get() + (int64_t)(j + 1) * n;
+          double* Wn = W.get() + (int64_t)(j + 1) * m;
+          scal_fix(Vn, F.get(), n, s1, thresh, B.get() + (int64_t)j * work + j + 1, V.get(), j + 1,
+                   seed, tag++);
+          op->N(Vn, Wn, s1, Wj);
+          res.nmatvec++;
+          orth_norm(Wn, m, W.get(), j + 1, s0);
+          scal_fix(Wn, Wn, m, s0, thresh, B.get() + (int64_t)(j + 1) * work + j + 1, W.get(), j + 1,
+                   seed, tag++);
+          ++j;
+        } else {
+          break;
+        }
+      }
+      sv_launch(ctx, "irlba_svd", k_jacobi_svd, dim3(1), dim3(1024), (size_t)2 * work * work * 8,
+                (const double*)B.get(), work, P.get(), sig.get(), Q.get(), summary.get(),
+                (const double*)s1, 60, ctx->d_status);
+      sv_d2h(ctx, hsum.data(), summary.get(), (2 * work + 2) * 8);
+      double rf = hsum[2 * work];
+      smax = std::max(smax, hsum[0]);
+      int nconv = 0;
+      for (int i = 0; i < nu; ++i)
+        if (fabs(rf * hsum[work + i]) < tol * smax) ++nconv;
+      res.iters = it + 1;
+      if (nconv >= nu || rf < eps_b * smax) {
+        res.info = 0;
+        break;
+      }
+      if (it + 1 >= maxit) break;   // keep P, Q consistent with the bases
+      k = std::min(nu, work - 1);
+      // thick restart
+      rotate(V.get(), n, Q.get(), k, Vt.get());
+      rotate(W.get(), m, P.get(), k, Wt.get());
+      std::swap(V, Vt);
+      std::swap(W, Wt);
+      sv_launch(ctx, "irlba_restart", k_restart_tail, dim3(sv_grid_for(ctx, n, 256, 4)), dim3(256), 0,
+                V.get() + (int64_t)k * n, (const double*)F.get(), n, (const double*)summary.get(),
+                work, k, B.get());
+    }
+    if (it >= maxit) res.iters = maxit;
+    sv_check_device_status(ctx, "irlba");
+    return res;
+  }
+
+  // U = W P[:, :nu] -> Wt ; Vout = V Q[:, :nu] -> Vt
+  void finish() {
+    rotate(W.get(), m, P.get(), nu, Wt.get());
+    rotate(V.get(), n, Q.get(), nu, Vt.get());
+  }
+};
+
+int default_work(int64_t m, int64_t n, int64_t nu) {
+  // src/irlba.jl:50-58
+  int64_t mb = nu + 7;
+  if (mb < nu) mb = nu + 1;
+  if (mb > std::min(m, n)) mb = std::min(m, n);
+  return (int)mb;
+}
+
+}  // namespace
+
+static int irlba_core(sv_context* ctx, Op* op, int64_t m, int64_t n, int64_t nu, int64_t work,
+                      int64_t maxit, double tol, const double* init, uint64_t seed, double* s_out,
+                      double* U, double* V, int64_t* iters, int64_t* nmatvec, sv_embed* emb) {
+  SV_REQUIRE(nu >= 1 && nu <= std::min(m, n), "nu must be in 1..min(m, n)");
+  if (work <= 0) work = default_work(m, n, nu);
+  SV_REQUIRE(work > nu || work == std::min(m, n), "work must exceed nu (or equal min(m, n))");
+  SV_REQUIRE(work <= std::min(m, n), "work exceeds min(m, n)");
+  if (work > MAX_WORK) sv_throw(SV_ERR_UNSUPPORTED, "work %lld exceeds %d", (long long)work, MAX_WORK);
+  SV_REQUIRE(maxit >= 1, "maxit must be >= 1");
+  SV_REQUIRE(init != nullptr, "init (length n) is required");
+  Lanczos L(ctx, op, m, n, (int)nu, (int)work);
+  IrlbaResult r = L.run(init, (int)maxit, tol, seed);
+  L.finish();
+  if (s_out) sv_d2h(ctx, s_out, L.sig.get(), nu * 8);
+  if (U) sv_d2h(ctx, U, L.Wt.get(), m * nu * 8);
+  if (V) sv_d2h(ctx, V, L.Vt.get(), n * nu * 8);
+  if (emb) {
+    emb->Z.alloc(m * nu);
+    emb->s.alloc(nu);
+    SV_CUDA(cudaMemcpyAsync(emb->Z.get(), L.Wt.get(), m * nu * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    SV_CUDA(cudaMemcpyAsync(emb->s.get(), L.sig.get(), nu * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    sv_launch(ctx, "pca_scale", k_scale_cols, dim3(sv_grid_for(ctx, m * nu, 256, 8)), dim3(256), 0,
+              emb->Z.get(), m, (int)nu, (const double*)emb->s.get());
+    sv_sync(ctx);
+  }
+  if (iters) *iters = r.iters;
+  if (nmatvec) *nmatvec = r.nmatvec;
+  return r.info;
+}
+
+SV_API int sv_irlba(sv_context* ctx, const sv_centered* s, int64_t nu, int64_t work, int64_t maxit,
+                    double tol, const double* init, uint64_t seed, double* s_out, double* U,
+                    double* V, int64_t* iters, int64_t* nmatvec) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(s && s->ctx == ctx, "bad centered handle");
+  CenteredOp op(ctx, s);
+  int info = irlba_core(ctx, &op, s->n_cells, s->nf, nu, work, maxit, tol, init, seed, s_out, U, V,
+                        iters, nmatvec, nullptr);
+  if (info != 0) {
+    sv_set_error("convergence failed");   // src/irlba.jl:73
+    return SV_ERR_NOCONV;
+  }
+  SV_CATCH
+}
+
+SV_API int sv_pca(sv_context* ctx, const sv_centered* s, int64_t npcs, int64_t maxit, double tol,
+                  const double* init, uint64_t seed, sv_embed** out, double* Z, double* stdev,
+                  double* loadings, int64_t* iters, int64_t* nmatvec) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(s && s->ctx == ctx, "bad centered handle");
+  SV_REQUIRE(npcs >= 1, "npcs must be >= 1");
+  int64_t k = std::min(std::min(s->n_cells, s->nf), npcs);   // embedding.jl:48
+  if (k > 0.5 * std::min(s->n_cells, s->nf))
+    sv_throw(SV_ERR_UNSUPPORTED,
+             "npcs > 0.5 min(m, n): the reference switches to a dense svd (embedding.jl:50-53)");
+  CenteredOp op(ctx, s);
+  auto* e = new sv_embed();
+  try {
+    e->ctx = ctx;
+    e->n_cells = s->n_cells;
+    e->npcs = k;
+    e->nf = s->nf;
+    std::vector<double> sv(k);
+    int info = irlba_core(ctx, &op, s->n_cells, s->nf, k, 0, maxit, tol, init, seed, sv.data(),
+                          nullptr, loadings, iters, nmatvec, e);
+    if (info != 0) {
+      delete e;
+      sv_set_error("convergence failed");
+      return SV_ERR_NOCONV;
+    }
+    if (Z) sv_d2h(ctx, Z, e->Z.get(), s->n_cells * k * 8);
+    if (stdev)
+      for (int64_t i = 0; i < k; ++i)
+        stdev[i] = sv[i] / sqrt((double)std::max<int64_t>(1, s->n_cells - 1));   // embedding.jl:68
+  } catch (...) {
+    delete e;
+    throw;
+  }
+  if (out) *out = e;
+  else delete e;
+  SV_CATCH
+}
+
+SV_API int sv_embed_info(const sv_embed* e, int64_t* n_cells, int64_t* npcs) {
+  SV_TRY
+  SV_REQUIRE(e, "null handle");
+  if (n_cells) *n_cells = e->n_cells;
+  if (npcs) *npcs = e->npcs;
+  SV_CATCH
+}
+
+SV_API int sv_embed_free(sv_embed* e) {
+  if (e) {
+    if (e->ctx) cudaSetDevice(e->ctx->device);
+    delete e;
+  }
+  return SV_OK;
+}
+
+// ---- drop-in for the native `irlba` symbol --------------------------------------
+static sv_context* g_default_ctx = nullptr;
+static std::mutex g_default_mu;
+
+sv_context* sv_default_context() {
+  std::lock_guard<std::mutex> lk(g_default_mu);
+  if (!g_default_ctx) {
+    sv_context* c = nullptr;
+    int st = sv_context_create(0, &c);
+    if (st != SV_OK) sv_throw(st, "could not create the default context");
+    g_default_ctx = c;
+  }
+  return g_default_ctx;
+}
+
+SV_API int irlba(int64_t m, int64_t n, int64_t nu, int64_t work, int64_t maxit, int64_t restart,
+                 double tol, double* init, double* s, double* U, double* V, sv_randv_fn randv,
+                 sv_matmul_fn matmul, void* data) {
+  (void)restart;
+  (void)randv;
+  SV_TRY
+  SV_REQUIRE(matmul != nullptr, "matmul callback is required");
+  SV_REQUIRE(m >= 1 && n >= 1, "bad sizes");
+  sv_context* ctx = sv_default_context();
+  sv_ctx_check(ctx);
+  CallbackOp op(ctx, m, n, matmul, data);
+  int info = irlba_core(ctx, &op, m, n, nu, work, maxit, tol, init, 0x5EEDull, s, U, V, nullptr,
+                        nullptr, nullptr);
+  return info == 0 ? 0 : 1;
+  SV_CATCH
+}

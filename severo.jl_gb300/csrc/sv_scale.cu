@@ -1,0 +1,733 @@
+// scale_features and the CenteredMatrix products (src/scaling.jl:18-44,199-357).
+//
+// Nothing is densified and no scaled copy is written: the products read the
+// normalised values and apply, per element,
+//     b = min(a * inv_std_f, clip_f)        clip_f = scale_max + mean_f/std_f
+// and the centring as a rank-1 correction:
+//     Xs v   = B v  - (mu . v) 1                 (scaling.jl:245-250)
+//     Xs^T u = B^T u - (sum u) mu                (scaling.jl:252-257)
+//
+// Layout in HBM:
+//   * the feature (HVF) subset of the CSC copy is a view: per feature its
+//     [start, end) range in the full CSC arrays; X^T u walks those ranges in
+//     fixed-size chunks (a chunk table built once), one warp per chunk;
+//   * X v uses a cell-major copy of the subset (CSR_h): rowptr int64, feature
+//     index uint16 (int32 when there are more than 65536 features), value in the
+//     data's storage type.  One warp per cell; the per-feature (inv*x, clip*x)
+//     pairs are staged in shared memory.
+// Algorithmic bytes per product: CSR_h nnz_h*(idx + v) + 8*(n_cells+1) +
+// 8*n_cells (y) ; CSC nnz_h*(4 + v) + 4*n_cells (u, FP32) + chunk table.
+#include "sv_internal.cuh"
+
+namespace {
+
+constexpr int64_t CHUNK = 4096;   // non-zeros per warp task in the X^T u product
+
+// ---- per-feature moments (FP64) ---------------------------------------------
+// Mean and unbiased variance of each feature column including its implicit
+// zeros (scaling.jl:18-34): per-thread Welford over the stored values, merged
+// across the block with the pairwise (Chan) update, then merged with the group
+// of n - nnz zeros, which is the state Welford starts from in the reference.
+template <typename ValT>
+__global__ void k_moments(const ValT* __restrict__ val, const int64_t* __restrict__ fstart,
+                          const int64_t* __restrict__ fend, int64_t nf, int64_t n_cells,
+                          double scale_max, double* __restrict__ mean_o, double* __restrict__ std_o,
+                          double* __restrict__ mu_o, float* __restrict__ inv_f,
+                          float* __restrict__ clip_f, double* __restrict__ inv_d,
+                          double* __restrict__ clip_d) {
+  __shared__ double sh_n[32], sh_m[32], sh_s[32];
+  for (int64_t f = blockIdx.x; f < nf; f += gridDim.x) {
+    int64_t s = fstart[f], e = fend[f];
+    double n = 0, m = 0, M2 = 0;
+    for (int64_t i = s + threadIdx.x; i < e; i += blockDim.x) {
+      double v = (double)sv_load_val(val, i);
+      n += 1;
+      double d = v - m;
+      m += d / n;
+      M2 += d * (v - m);
+    }
+    // warp merge
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      double n2 = __shfl_xor_sync(0xffffffffu, n, o);
+      double m2 = __shfl_xor_sync(0xffffffffu, m, o);
+      double M22 = __shfl_xor_sync(0xffffffffu, M2, o);
+      double nt = n + n2;
+      if (nt > 0) {
+        double d = m2 - m;
+        m = m + d * (n2 / nt);
+        M2 = M2 + M22 + d * d * (n * n2 / nt);
+      }
+      n = nt;
+    }
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+      sh_n[wid] = n;
+      sh_m[wid] = m;
+      sh_s[wid] = M2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double N = 0, Mn = 0, S = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        double n2 = sh_n[w], m2 = sh_m[w], s2 = sh_s[w];
+        double nt = N + n2;
+        if (nt > 0) {
+          double d = m2 - Mn;
+          Mn = Mn + d * (n2 / nt);
+          S = S + s2 + d * d * (N * n2 / nt);
+        }
+        N = nt;
+      }
+      // merge the implicit zeros (count n_cells - nnz, mean 0, M2 0)
+      double nz = (double)(n_cells - (e - s));
+      double nt = N + nz;
+      double d = -Mn;
+      double meanv = Mn + d * (nz / nt);
+      double M2t = S + d * d * (N * nz / nt);
+      double var = M2t / (double)(n_cells - 1);
+      double sd = sqrt(var);
+      double mu = meanv / sd;                       // scaling.jl:207
+      mean_o[f] = meanv;
+      std_o[f] = sd;
+      mu_o[f] = mu;
+      inv_d[f] = sd;                                // FP64 path divides by std
+      clip_d[f] = scale_max + mu;                   // scaling.jl:209
+      inv_f[f] = (float)(1.0 / sd);
+      clip_f[f] = (float)(scale_max + mu);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_feat_ranges(const int32_t* __restrict__ fgene, const int64_t* __restrict__ colptr,
+                              int64_t nf, int64_t* __restrict__ fs, int64_t* __restrict__ fe,
+                              int32_t* __restrict__ gene_map) {
+  for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < nf;
+       f += (int64_t)gridDim.x * blockDim.x) {
+    int32_t g = fgene[f];
+    fs[f] = colptr[g];
+    fe[f] = colptr[g + 1];
+    gene_map[g] = (int32_t)f;
+  }
+}
+
+// ---- CSR_h construction ------------------------------------------------------
+__global__ void k_hsub_count(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                             int64_t n_rows, const int32_t* __restrict__ gene_map,
+                             int64_t* __restrict__ cnt) {
+  int lane = threadIdx.x & 31;
+  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n_rows; r += nwarps) {
+    int64_t s = rowptr[r], e = rowptr[r + 1];
+    int64_t c = 0;
+    for (int64_t i = s + lane; i < e; i += 32) c += __ldg(gene_map + col[i]) >= 0;
+    c = sv_warp_sum(c);
+    if (lane == 0) cnt[r] = c;
+  }
+}
+
+template <typename ValT, typename IdxT>
+__global__ void k_hsub_write(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                             const ValT* __restrict__ val, int64_t n_rows,
+                             const int32_t* __restrict__ gene_map, const int64_t* __restrict__ hrowptr,
+                             IdxT* __restrict__ hcol, ValT* __restrict__ hval) {
+  int lane = threadIdx.x & 31;
+  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n_rows; r += nwarps) {
+    int64_t s = rowptr[r], e = rowptr[r + 1];
+    int64_t pos = hrowptr[r];
+    for (int64_t i0 = s; i0 < e; i0 += 32) {
+      int64_t i = i0 + lane;
+      int32_t f = i < e ? __ldg(gene_map + col[i]) : -1;
+      unsigned m = __ballot_sync(0xffffffffu, f >= 0);
+      if (f >= 0) {
+        int64_t p = pos + __popc(m & ((1u << lane) - 1));
+        hcol[p] = (IdxT)f;
+        hval[p] = val[i];
+      }
+      pos += __popc(m);
+    }
+  }
+}
+
+// ---- vector loads of 4 consecutive elements (allocation padded) -------------
+__device__ __forceinline__ void ld4(const uint16_t* p, int64_t g, int (&o)[4]) {
+  uint2 w = __ldg((const uint2*)(p + g));
+  o[0] = w.x & 0xffff;
+  o[1] = w.x >> 16;
+  o[2] = w.y & 0xffff;
+  o[3] = w.y >> 16;
+}
+__device__ __forceinline__ void ld4(const int32_t* p, int64_t g, int (&o)[4]) {
+  int4 w = __ldg((const int4*)(p + g));
+  o[0] = w.x;
+  o[1] = w.y;
+  o[2] = w.z;
+  o[3] = w.w;
+}
+__device__ __forceinline__ void ld4v(const __nv_bfloat16* p, int64_t g, float (&o)[4]) {
+  uint2 w = __ldg((const uint2*)(p + g));
+  o[0] = __uint_as_float(w.x << 16);
+  o[1] = __uint_as_float(w.x & 0xffff0000u);
+  o[2] = __uint_as_float(w.y << 16);
+  o[3] = __uint_as_float(w.y & 0xffff0000u);
+}
+__device__ __forceinline__ void ld4v(const float* p, int64_t g, float (&o)[4]) {
+  float4 w = __ldg((const float4*)(p + g));
+  o[0] = w.x;
+  o[1] = w.y;
+  o[2] = w.z;
+  o[3] = w.w;
+}
+__device__ __forceinline__ void ld4v(const double* p, int64_t g, double (&o)[4]) {
+  double2 a = __ldg((const double2*)(p + g));
+  double2 b = __ldg((const double2*)(p + g + 2));
+  o[0] = a.x;
+  o[1] = a.y;
+  o[2] = b.x;
+  o[3] = b.y;
+}
+
+template <typename ValT>
+struct AccOf {
+  typedef float type;
+};
+template <>
+struct AccOf<double> {
+  typedef double type;
+};
+
+// ---- X v over CSR_h ------------------------------------------------------------
+// y = alpha * (B x - (mu . x)) + beta * y - (csub ? *csub : 0) * z
+// Per-feature table in shared memory.  FP32 form: (P, Q) = (inv*x, clip*x); the
+// product term is min(a*P, Q) for x >= 0 and max(a*P, Q) for x < 0 (= min(a*inv,
+// clip)*x).  FP64 form: (std, clip, x) with the reference's a/std division.
+template <typename ValT, typename IdxT>
+__global__ void __launch_bounds__(256) k_spmv_csr(
+    const int64_t* __restrict__ rowptr, const IdxT* __restrict__ hcol, const ValT* __restrict__ hval,
+    int64_t n_rows, int64_t nf, const double* __restrict__ x, const float* __restrict__ inv_f,
+    const float* __restrict__ clip_f, const double* __restrict__ std_d,
+    const double* __restrict__ clip_d, const double* __restrict__ mu, double alpha, double beta,
+    double* __restrict__ y, const double* __restrict__ csub, const double* __restrict__ z) {
+  typedef typename AccOf<ValT>::type AccT;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[32];
+  // stage the table and compute mu . x (same value in every block)
+  double mux = 0;
+  if constexpr (sizeof(AccT) == 4) {
+    float2* tab = (float2*)smem_raw;
+    for (int64_t f = threadIdx.x; f < nf; f += blockDim.x) {
+      double xf = x[f];
+      float xs = (float)xf;
+      float P = inv_f[f] * xs;
+      float Q = xs == 0.f ? 0.f : clip_f[f] * xs;
+      tab[f] = make_float2(P, Q);
+      mux += mu[f] * xf;
+    }
+  } else {
+    double* tab = (double*)smem_raw;
+    for (int64_t f = threadIdx.x; f < nf; f += blockDim.x) {
+      double xf = x[f];
+      tab[3 * f] = std_d[f];
+      tab[3 * f + 1] = clip_d[f];
+      tab[3 * f + 2] = xf;
+      mux += mu[f] * xf;
+    }
+  }
+  mux = sv_warp_sum(mux);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mux;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    v = sv_warp_sum(v);
+    if (threadIdx.x == 0) red[0] = v;
+  }
+  __syncthreads();
+  mux = red[0];
+  double cs = csub ? *csub : 0.0;
+
+  int lane = threadIdx.x & 31;
+  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n_rows; r += nwarps) {
+    int64_t s = rowptr[r], e = rowptr[r + 1];
+    int64_t a0 = s & ~3ll;
+    AccT acc = 0;
+    for (int64_t g = a0 + 4 * lane; g < e; g += 128) {
+      int ci[4];
+      AccT av[4];
+      ld4(hcol, g, ci);
+      ld4v(hval, g, av);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        if (g + t >= s && g + t < e) {
+          if constexpr (sizeof(AccT) == 4) {
+            float2 pq = ((const float2*)smem_raw)[ci[t]];
+            float rr = av[t] * pq.x;
+            acc += pq.x >= 0.f ? fminf(rr, pq.y) : fmaxf(rr, pq.y);
+          } else {
+            const double* tab = (const double*)smem_raw;
+            double v = av[t] / tab[3 * ci[t]];          // scaling.jl:211
+            double c = tab[3 * ci[t] + 1];
+            acc += (v > c ? c : v) * tab[3 * ci[t] + 2];  // scaling.jl:212
+          }
+        }
+      }
+    }
+    acc = sv_warp_sum(acc);
+    if (lane == 0) {
+      double out = alpha * ((double)acc - mux);
+      if (beta != 0.0) out += beta * y[r];
+      if (z) out -= cs * z[r];
+      y[r] = out;
+    }
+  }
+}
+
+// ---- X^T u over the CSC feature ranges ---------------------------------------
+// Prologue: u -> FP32 copy and per-block partial sums of u (FP64).
+__global__ void k_u_prep(const double* __restrict__ u, int64_t n, float* __restrict__ uf,
+                         double* __restrict__ part) {
+  __shared__ double red[32];
+  double s = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v = u[i];
+    if (uf) uf[i] = (float)v;
+    s += v;
+  }
+  s = sv_warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    v = sv_warp_sum(v);
+    if (threadIdx.x == 0) part[blockIdx.x] = v;
+  }
+}
+
+template <typename ValT>
+__global__ void __launch_bounds__(256) k_spmv_csc_chunks(
+    const int32_t* __restrict__ rowidx, const ValT* __restrict__ val,
+    const int32_t* __restrict__ chunk_feat, const int64_t* __restrict__ cstart,
+    const int64_t* __restrict__ cend, int64_t nchunks, const float* __restrict__ inv_f,
+    const float* __restrict__ clip_f, const double* __restrict__ std_d,
+    const double* __restrict__ clip_d, const float* __restrict__ uf, const double* __restrict__ ud,
+    double* __restrict__ partial) {
+  typedef typename AccOf<ValT>::type AccT;
+  int lane = threadIdx.x & 31;
+  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = warp; c < nchunks; c += nwarps) {
+    int32_t f = chunk_feat[c];
+    int64_t s = cstart[c], e = cend[c];
+    int64_t a0 = s & ~3ll;
+    AccT acc = 0;
+    if constexpr (sizeof(AccT) == 4) {
+      float inv = inv_f[f], clip = clip_f[f];
+      for (int64_t g = a0 + 4 * lane; g < e; g += 128) {
+        int ri[4];
+        float av[4];
+        ld4(rowidx, g, ri);
+        ld4v(val, g, av);
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+          if (g + t >= s && g + t < e) acc += fminf(av[t] * inv, clip) * __ldg(uf + ri[t]);
+      }
+    } else {
+      double sd = std_d[f], clip = clip_d[f];
+      for (int64_t g = a0 + 4 * lane; g < e; g += 128) {
+        int ri[4];
+        double av[4];
+        ld4(rowidx, g, ri);
+        ld4v(val, g, av);
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+          if (g + t >= s && g + t < e) {
+            double v = av[t] / sd;
+            acc += (v > clip ? clip : v) * __ldg(ud + ri[t]);
+          }
+      }
+    }
+    acc = sv_warp_sum(acc);
+    if (lane == 0) partial[c] = (double)acc;
+  }
+}
+
+// y_f = alpha * (sum of the feature's chunk partials - mu_f * sum(u)) + beta*y_f - csub*z_f
+__global__ void k_spmv_csc_finish(const double* __restrict__ partial,
+                                  const int64_t* __restrict__ foff, int64_t nf,
+                                  const double* __restrict__ mu, const double* __restrict__ upart,
+                                  int nupart, double alpha, double beta, double* __restrict__ y,
+                                  const double* __restrict__ csub, const double* __restrict__ z) {
+  __shared__ double su_s;
+  if (threadIdx.x < 32) {
+    double v = 0;
+    for (int i = threadIdx.x; i < nupart; i += 32) v += upart[i];
+    v = sv_warp_sum(v);
+    if (threadIdx.x == 0) su_s = v;
+  }
+  __syncthreads();
+  double su = su_s;
+  double cs = csub ? *csub : 0.0;
+  for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < nf;
+       f += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0;
+    for (int64_t c = foff[f]; c < foff[f + 1]; ++c) acc += partial[c];
+    double out = alpha * (acc - mu[f] * su);
+    if (beta != 0.0) out += beta * y[f];
+    if (z) out -= cs * z[f];
+    y[f] = out;
+  }
+}
+
+constexpr int UPREP_BLOCKS = 304;
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// internal product entry points (device vectors), used by irlba too
+// ---------------------------------------------------------------------------
+void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const double* x, double* y,
+                       double alpha, double beta, const double* csub, const double* z) {
+  if (trans == 'N') {
+    size_t smem = S->dtype == SV_F64 ? (size_t)S->nf * 24 : (size_t)S->nf * 8;
+    int grid = sv_grid_for(ctx, S->n_cells * 32, 256, 8);
+    const double* sd = S->inv_std_d.get();
+#define LAUNCH_CSR(VT, IT, COL)                                                                   \
+  sv_launch(ctx, "spmv_csr_h", k_spmv_csr<VT, IT>, dim3(grid), dim3(256), smem,                   \
+            (const int64_t*)S->h_rowptr.get(), (const IT*)COL, (const VT*)S->h_val.get(),          \
+            S->n_cells, S->nf, x, (const float*)S->inv_std_f.get(), (const float*)S->clip_f.get(), \
+            sd, (const double*)S->clip_d.get(), (const double*)S->mu.get(), alpha, beta, y, csub, z)
+    bool small = S->nf <= 65536;
+    switch (S->dtype) {
+      case SV_F64:
+        if (small) LAUNCH_CSR(double, uint16_t, S->h_col16.get());
+        else LAUNCH_CSR(double, int32_t, S->h_col32.get());
+        break;
+      case SV_F32:
+        if (small) LAUNCH_CSR(float, uint16_t, S->h_col16.get());
+        else LAUNCH_CSR(float, int32_t, S->h_col32.get());
+        break;
+      default:
+        if (small) LAUNCH_CSR(__nv_bfloat16, uint16_t, S->h_col16.get());
+        else LAUNCH_CSR(__nv_bfloat16, int32_t, S->h_col32.get());
+        break;
+    }
+#undef LAUNCH_CSR
+  } else {
+    sv_centered* Sm = const_cast<sv_centered*>(S);
+    bool f64 = S->dtype == SV_F64;
+    sv_launch(ctx, "spmv_csc_uprep", k_u_prep, dim3(UPREP_BLOCKS), dim3(256), 0, x, S->n_cells,
+              f64 ? (float*)nullptr : Sm->u_f32.get(), Sm->red_partial.get());
+    int grid = sv_grid_for(ctx, S->n_chunks * 32, 256, 8);
+    const sv_data* D = S->data;
+    const int32_t* rowidx = D->counts->csc_rowidx.get();
+#define LAUNCH_CSC(VT)                                                                            \
+  sv_launch(ctx, "spmv_csc_chunks", k_spmv_csc_chunks<VT>, dim3(grid), dim3(256), 0, rowidx,      \
+            (const VT*)D->csc_val.get(), (const int32_t*)S->chunk_feat.get(),                     \
+            (const int64_t*)S->chunk_start.get(), (const int64_t*)S->chunk_end.get(), S->n_chunks, \
+            (const float*)S->inv_std_f.get(), (const float*)S->clip_f.get(),                      \
+            (const double*)S->inv_std_d.get(), (const double*)S->clip_d.get(),                    \
+            (const float*)Sm->u_f32.get(), x, Sm->chunk_partial.get())
+    switch (S->dtype) {
+      case SV_F64: LAUNCH_CSC(double); break;
+      case SV_F32: LAUNCH_CSC(float); break;
+      default: LAUNCH_CSC(__nv_bfloat16); break;
+    }
+#undef LAUNCH_CSC
+    sv_launch(ctx, "spmv_csc_finish", k_spmv_csc_finish, dim3(sv_grid_for(ctx, S->nf, 256, 4)),
+              dim3(256), 0, (const double*)S->chunk_partial.get(),
+              (const int64_t*)S->feat_chunk_off.get(), S->nf, (const double*)S->mu.get(),
+              (const double*)Sm->red_partial.get(), UPREP_BLOCKS, alpha, beta, y, csub, z);
+  }
+}
+
+// Builds the implicit matrix over the features `fg` (0-based genes) of `data`.
+// mu_given == nullptr: per-feature moments (scale_features).  Otherwise the
+// CenteredMatrix(A, mu) constructor of src/scaling.jl:224-232: std = 1, no clip.
+static sv_centered* make_centered(sv_context* ctx, const sv_data* data, const std::vector<int32_t>& fg,
+                                  double scale_max, const double* mu_given) {
+  const sv_counts* C = data->counts;
+  int64_t nf = (int64_t)fg.size();
+  size_t smem_need = data->dtype == SV_F64 ? (size_t)nf * 24 : (size_t)nf * 8;
+  if (smem_need > 200 * 1024)
+    sv_throw(SV_ERR_UNSUPPORTED, "%lld features exceed the shared-memory feature table",
+             (long long)nf);
+  auto* S = new sv_centered();
+  try {
+    S->ctx = ctx;
+    S->data = data;
+    S->n_cells = C->n_cells;
+    S->nf = nf;
+    S->dtype = data->dtype;
+    S->scale_max = scale_max;
+    S->feat_gene.alloc(nf);
+    S->feat_start.alloc(nf);
+    S->feat_end.alloc(nf);
+    sv_h2d(ctx, S->feat_gene.get(), fg.data(), nf * 4);
+    DevBuf<int32_t> gene_map(C->n_genes);
+    sv_memset(ctx, gene_map.get(), 0xff, C->n_genes * 4);
+    sv_launch(ctx, "scale_feat_ranges", k_feat_ranges, dim3(sv_grid_for(ctx, nf, 256)), dim3(256), 0,
+              (const int32_t*)S->feat_gene.get(), (const int64_t*)C->csc_colptr.get(), nf,
+              S->feat_start.get(), S->feat_end.get(), gene_map.get());
+    // moments
+    S->mean.alloc(nf);
+    S->std_.alloc(nf);
+    S->mu.alloc(nf);
+    S->inv_std_f.alloc(nf);
+    S->clip_f.alloc(nf);
+    S->inv_std_d.alloc(nf);
+    S->clip_d.alloc(nf);
+#define LAUNCH_MOM(VT)                                                                          \
+  sv_launch(ctx, "scale_moments", k_moments<VT>, dim3(sv_grid_for(ctx, nf, 1, 16)), dim3(256), 0, \
+            (const VT*)data->csc_val.get(), (const int64_t*)S->feat_start.get(),                 \
+            (const int64_t*)S->feat_end.get(), nf, C->n_cells, scale_max, S->mean.get(),         \
+            S->std_.get(), S->mu.get(), S->inv_std_f.get(), S->clip_f.get(), S->inv_std_d.get(), \
+            S->clip_d.get())
+    if (!mu_given) {
+      switch (data->dtype) {
+        case SV_F64: LAUNCH_MOM(double); break;
+        case SV_F32: LAUNCH_MOM(float); break;
+        default: LAUNCH_MOM(__nv_bfloat16); break;
+      }
+    } else {
+      std::vector<double> one(nf, 1.0), inf(nf, INFINITY);
+      std::vector<float> onef(nf, 1.0f), inff(nf, INFINITY);
+      sv_h2d(ctx, S->mu.get(), mu_given, nf * 8);
+      sv_h2d(ctx, S->mean.get(), mu_given, nf * 8);
+      sv_h2d(ctx, S->std_.get(), one.data(), nf * 8);
+      sv_h2d(ctx, S->inv_std_d.get(), one.data(), nf * 8);
+      sv_h2d(ctx, S->clip_d.get(), inf.data(), nf * 8);
+      sv_h2d(ctx, S->inv_std_f.get(), onef.data(), nf * 4);
+      sv_h2d(ctx, S->clip_f.get(), inff.data(), nf * 4);
+      sv_sync(ctx);
+    }
+#undef LAUNCH_MOM
+    // chunk table of the CSC product (built on the host from the nf ranges)
+    std::vector<int64_t> hs(nf), he(nf);
+    sv_d2h(ctx, hs.data(), S->feat_start.get(), nf * 8);
+    sv_d2h(ctx, he.data(), S->feat_end.get(), nf * 8);
+    std::vector<int32_t> cf;
+    std::vector<int64_t> cs, ce, foff(nf + 1);
+    int64_t nnz_h = 0;
+    for (int64_t f = 0; f < nf; ++f) {
+      foff[f] = (int64_t)cf.size();
+      int64_t s = hs[f], e = he[f];
+      nnz_h += e - s;
+      if (e == s) continue;
+      // chunk boundaries on multiples of 4 elements (16-byte aligned vector loads)
+      int64_t b = s;
+      while (b < e) {
+        int64_t nb = ((b + CHUNK) & ~3ll);
+        if (nb > e || e - nb < CHUNK / 4) nb = e;
+        cf.push_back((int32_t)f);
+        cs.push_back(b);
+        ce.push_back(nb);
+        b = nb;
+      }
+    }
+    foff[nf] = (int64_t)cf.size();
+    S->nnz_h = nnz_h;
+    S->n_chunks = (int64_t)cf.size();
+    S->chunk_feat.alloc(std::max<int64_t>(1, S->n_chunks));
+    S->chunk_start.alloc(std::max<int64_t>(1, S->n_chunks));
+    S->chunk_end.alloc(std::max<int64_t>(1, S->n_chunks));
+    S->chunk_partial.alloc(std::max<int64_t>(1, S->n_chunks));
+    S->feat_chunk_off.alloc(nf + 1);
+    sv_h2d(ctx, S->chunk_feat.get(), cf.data(), S->n_chunks * 4);
+    sv_h2d(ctx, S->chunk_start.get(), cs.data(), S->n_chunks * 8);
+    sv_h2d(ctx, S->chunk_end.get(), ce.data(), S->n_chunks * 8);
+    sv_h2d(ctx, S->feat_chunk_off.get(), foff.data(), (nf + 1) * 8);
+    // cell-major copy of the subset
+    DevBuf<int64_t> rc(C->n_cells + 1);
+    sv_launch(ctx, "scale_hsub_count", k_hsub_count, dim3(sv_grid_for(ctx, C->n_cells * 32, 256, 8)),
+              dim3(256), 0, (const int64_t*)C->csr_rowptr.get(), (const int32_t*)C->csr_colidx.get(),
+              C->n_cells, (const int32_t*)gene_map.get(), rc.get());
+    S->h_rowptr.alloc(C->n_cells + 1);
+    sv_scan_i64(ctx, rc.get(), S->h_rowptr.get(), C->n_cells);
+    int64_t tot = sv_read_i64(ctx, S->h_rowptr.get() + C->n_cells);
+    if (tot != nnz_h)
+      sv_throw(SV_ERR_DEVICE, "subset sizes disagree between copies (%lld vs %lld)", (long long)tot,
+               (long long)nnz_h);
+    size_t es = sv_elem_size(data->dtype);
+    S->h_val.alloc(std::max<int64_t>(1, nnz_h) * es);
+    bool small = nf <= 65536;
+    if (small) S->h_col16.alloc(std::max<int64_t>(1, nnz_h));
+    else S->h_col32.alloc(std::max<int64_t>(1, nnz_h));
+    int gridw = sv_grid_for(ctx, C->n_cells * 32, 256, 8);
+#define LAUNCH_HW(VT, IT, COL)                                                                  \
+  sv_launch(ctx, "scale_hsub_write", k_hsub_write<VT, IT>, dim3(gridw), dim3(256), 0,           \
+            (const int64_t*)C->csr_rowptr.get(), (const int32_t*)C->csr_colidx.get(),            \
+            (const VT*)data->csr_val.get(), C->n_cells, (const int32_t*)gene_map.get(),          \
+            (const int64_t*)S->h_rowptr.get(), (IT*)COL, (VT*)S->h_val.get())
+    switch (data->dtype) {
+      case SV_F64:
+        if (small) LAUNCH_HW(double, uint16_t, S->h_col16.get());
+        else LAUNCH_HW(double, int32_t, S->h_col32.get());
+        break;
+      case SV_F32:
+        if (small) LAUNCH_HW(float, uint16_t, S->h_col16.get());
+        else LAUNCH_HW(float, int32_t, S->h_col32.get());
+        break;
+      default:
+        if (small) LAUNCH_HW(uint16_t, uint16_t, S->h_col16.get());
+        else LAUNCH_HW(uint16_t, int32_t, S->h_col32.get());
+        break;
+    }
+#undef LAUNCH_HW
+    S->u_f32.alloc(C->n_cells);
+    S->red_partial.alloc(UPREP_BLOCKS);
+    S->scal.alloc(64);
+    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<double, uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<double, int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<float, uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<float, int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<__nv_bfloat16, uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<__nv_bfloat16, int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    sv_sync(ctx);
+  } catch (...) {
+    delete S;
+    throw;
+  }
+  return S;
+}
+
+SV_API int sv_scale_features(sv_context* ctx, const sv_data* data, const int64_t* features,
+                             int64_t nfeatures, double scale_max, sv_centered** out) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(out && data, "null argument");
+  SV_REQUIRE(data->ctx == ctx, "data handle belongs to another context");
+  const sv_counts* C = data->counts;
+  SV_REQUIRE(C->n_cells >= 2, "need at least two cells for a variance");
+  int64_t nf = features ? nfeatures : C->n_genes;
+  SV_REQUIRE(nf >= 1, "no features");
+  std::vector<int32_t> fg(nf);
+  {
+    std::vector<char> seen(C->n_genes, 0);
+    for (int64_t f = 0; f < nf; ++f) {
+      int64_t g = features ? features[f] - 1 : f;
+      SV_REQUIRE(g >= 0 && g < C->n_genes, "feature %lld out of range 1..%lld",
+                 (long long)(g + 1), (long long)C->n_genes);
+      SV_REQUIRE(!seen[g], "duplicate feature %lld", (long long)(g + 1));
+      seen[g] = 1;
+      fg[f] = (int32_t)g;
+    }
+  }
+  *out = make_centered(ctx, data, fg, scale_max, nullptr);
+  SV_CATCH
+}
+
+sv_counts* sv_counts_upload_positions(sv_context* ctx, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                                      const int64_t* colptr, const int64_t* rowval);
+
+namespace {
+template <typename T>
+__global__ void k_gather_vals(const double* __restrict__ src, const int32_t* __restrict__ pos,
+                              int64_t nnz, T* __restrict__ dst_csr, T* __restrict__ dst_csc) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    dst_csr[e] = (T)src[pos[e]];
+    dst_csc[e] = (T)src[e];
+  }
+}
+}  // namespace
+
+SV_API int sv_centered_create(sv_context* ctx, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                              const int64_t* colptr, const int64_t* rowval, const double* nzval,
+                              const double* mu, int dtype, sv_centered** out) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(out && colptr && mu && (nnz == 0 || (rowval && nzval)), "null argument");
+  SV_REQUIRE(dtype == SV_F64 || dtype == SV_F32, "dtype must be F64 or F32");
+  SV_REQUIRE(nnz < (1ll << 31), "nnz must fit Int32 positions");
+  sv_counts* C = sv_counts_upload_positions(ctx, n_rows, n_cols, nnz, colptr, rowval);
+  sv_data* D = nullptr;
+  try {
+    D = new sv_data();
+    D->ctx = ctx;
+    D->counts = C;
+    D->dtype = dtype;
+    size_t es = sv_elem_size(dtype);
+    D->csc_val.alloc(std::max<int64_t>(1, nnz) * es);
+    D->csr_val.alloc(std::max<int64_t>(1, nnz) * es);
+    DevBuf<double> src(std::max<int64_t>(1, nnz));
+    sv_h2d(ctx, src.get(), nzval, nnz * 8);
+    if (dtype == SV_F64)
+      sv_launch(ctx, "centered_gather", k_gather_vals<double>, dim3(sv_grid_for(ctx, nnz, 256, 8)),
+                dim3(256), 0, (const double*)src.get(), (const int32_t*)C->csr_count.get(), nnz,
+                (double*)D->csr_val.get(), (double*)D->csc_val.get());
+    else
+      sv_launch(ctx, "centered_gather", k_gather_vals<float>, dim3(sv_grid_for(ctx, nnz, 256, 8)),
+                dim3(256), 0, (const double*)src.get(), (const int32_t*)C->csr_count.get(), nnz,
+                (float*)D->csr_val.get(), (float*)D->csc_val.get());
+    std::vector<int32_t> fg(n_cols);
+    for (int64_t f = 0; f < n_cols; ++f) fg[f] = (int32_t)f;
+    sv_centered* S = make_centered(ctx, D, fg, INFINITY, mu);
+    S->own_counts = C;
+    S->own_data = D;
+    *out = S;
+  } catch (...) {
+    delete D;
+    delete C;
+    throw;
+  }
+  SV_CATCH
+}
+
+SV_API int sv_centered_info(const sv_centered* s, int64_t* n_cells, int64_t* nf, int64_t* nnz) {
+  SV_TRY
+  SV_REQUIRE(s, "null handle");
+  if (n_cells) *n_cells = s->n_cells;
+  if (nf) *nf = s->nf;
+  if (nnz) *nnz = s->nnz_h;
+  SV_CATCH
+}
+
+SV_API int sv_centered_stats(sv_context* ctx, const sv_centered* s, double* mu, double* mean,
+                             double* sd) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(s && s->ctx == ctx, "bad handle");
+  if (mu) sv_d2h(ctx, mu, s->mu.get(), s->nf * 8);
+  if (mean) sv_d2h(ctx, mean, s->mean.get(), s->nf * 8);
+  if (sd) sv_d2h(ctx, sd, s->std_.get(), s->nf * 8);
+  SV_CATCH
+}
+
+SV_API int sv_centered_mul(sv_context* ctx, const sv_centered* s, char trans, int64_t ncols,
+                           double alpha, const double* x, int64_t ldx, double beta, double* y,
+                           int64_t ldy) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(s && s->ctx == ctx, "bad handle");
+  SV_REQUIRE(trans == 'N' || trans == 'T', "trans must be 'N' or 'T'");
+  SV_REQUIRE(ncols >= 0 && x && y, "bad arguments");
+  int64_t nx = trans == 'N' ? s->nf : s->n_cells;
+  int64_t ny = trans == 'N' ? s->n_cells : s->nf;
+  SV_REQUIRE(ldx >= nx && ldy >= ny, "leading dimension too small");
+  DevBuf<double> dx(nx), dy(ny);
+  for (int64_t j = 0; j < ncols; ++j) {
+    sv_h2d(ctx, dx.get(), x + j * ldx, nx * 8);
+    if (beta != 0.0) sv_h2d(ctx, dy.get(), y + j * ldy, ny * 8);
+    sv_centered_apply(ctx, s, trans, dx.get(), dy.get(), alpha, beta, nullptr, nullptr);
+    sv_d2h(ctx, y + j * ldy, dy.get(), ny * 8);
+  }
+  SV_CATCH
+}
+
+SV_API int sv_centered_free(sv_centered* s) {
+  if (s) {
+    if (s->ctx) cudaSetDevice(s->ctx->device);
+    sv_data* d = s->own_data;
+    sv_counts* c = s->own_counts;
+    delete s;
+    delete d;
+    delete c;
+  }
+  return SV_OK;
+}
