@@ -1,0 +1,520 @@
+#!/usr/bin/env python
+"""Benchmark of the embedding hot path: normalize_cells (both copies) ->
+scale_features (3,000 features, implicit centre/scale/clip) -> irlba PCA (50)
+-> kNN (20), on one GB300, with counts already resident in HBM.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload atlas|plain|small] [--cells N]
+
+Prints one JSON line (rank 0).  Workload "atlas": 1,300,000 cells x 27,998
+genes, ~2,000 non-zeros per cell, 40 latent clusters, values stored in BF16
+with FP32 product accumulation and FP64 Lanczos reorthogonalisation/restart.
+The plain-FP32 form of the same pipeline is timed on the same data for the
+mixed-vs-FP32 ratio.  Data: seeded synthetic negative-binomial counts (no
+public dataset is read).  --impl reference times the CPU oracle (the
+restatement of the reference's CPU path) on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = ("cells/s norm→PCA50→kNN20 @1.3M: mixed vs FP32 on GB300 (σ err≤1e-4); "
+          "SpMM HBM%")
+
+WORKLOADS = {
+    # 1.3M-cell atlas, mixed precision (the configuration the metric is quoted on)
+    "atlas": dict(n_cells=1_300_000, n_genes=27_998, mu_mean=-1.2, mu_sd=1.6, nnz_per_cell=2000,
+                  n_clusters=40, n_hvf=3000, npcs=50, k=20, dtype="bfloat16", knn="bf16"),
+    # 100k cells x 33,538 genes, plain FP32
+    "plain": dict(n_cells=100_000, n_genes=33_538, mu_mean=-1.2, mu_sd=1.6, nnz_per_cell=2500,
+                  n_clusters=0, n_hvf=3000, npcs=50, k=20, dtype="float32", knn="fp32"),
+    # the CPU-runnable reference case
+    "small": dict(n_cells=2_000, n_genes=20_000, mu_mean=-1.0, mu_sd=1.5, nnz_per_cell=1000,
+                  n_clusters=0, n_hvf=2000, npcs=50, k=20, dtype="float64", knn="fp32"),
+}
+SEED = 20261203
+SCALE_FACTOR = 1e4
+SCALE_MAX = 10.0
+DISPERSION = 0.2
+CPU_SAMPLE_CELLS = 6000
+
+
+# ---------------------------------------------------------------------------
+# synthetic parameters
+# ---------------------------------------------------------------------------
+def gen_params(w, n_cells, seed):
+    rng = np.random.default_rng(seed)
+    g = w["n_genes"]
+    mu_g = rng.lognormal(w["mu_mean"], w["mu_sd"], g)
+    s_c = rng.lognormal(0.0, 0.3, n_cells)
+    cl = lfc = None
+    if w["n_clusters"]:
+        cl = rng.integers(0, w["n_clusters"], n_cells).astype(np.int32)
+        lfc = np.zeros((w["n_clusters"], g), dtype=np.float32)
+        for c in range(w["n_clusters"]):
+            sel = rng.random(g) < 0.05
+            lfc[c, sel] = rng.normal(0.0, 0.8, sel.sum())
+    return mu_g, s_c, cl, lfc
+
+
+def calibrate_depth(mu_g, s_c, cl, lfc, target, phi=DISPERSION, sample=256, seed=1):
+    """Depth factor D with E[non-zeros per cell] = target under the NB model."""
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(len(s_c), min(sample, len(s_c)), replace=False)
+    base = s_c[idx, None] * mu_g[None, :]
+    if cl is not None:
+        base = base * np.exp(lfc[cl[idx]])
+
+    def nnz(D):
+        m = D * base
+        return float(np.mean(np.sum(1.0 - (1.0 + phi * m) ** (-1.0 / phi), axis=1)))
+
+    lo, hi = 1e-4, 1e3
+    for _ in range(36):
+        mid = math.sqrt(lo * hi)
+        if nnz(mid) < target:
+            lo = mid
+        else:
+            hi = mid
+    return math.sqrt(lo * hi)
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (replicas: one independent pipeline per GPU)
+# ---------------------------------------------------------------------------
+def dist_setup(n_gpus):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1:
+        import torch.distributed as td
+        td.init_process_group("gloo")
+        return td, td.get_rank(), ws, int(os.environ.get("LOCAL_RANK", "0"))
+    return None, 0, 1, 0
+
+
+def barrier(td):
+    if td is not None:
+        td.barrier()
+
+
+def allmax(td, x):
+    if td is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# the GPU pipeline
+# ---------------------------------------------------------------------------
+def run_pipeline(sv, ctx, counts, hvf, w, init, form, marks=False):
+    """One step: normalise -> scale -> PCA -> kNN on device-resident counts.
+    form: (value dtype, knn precision).  Returns (embedding, knn handle)."""
+    dtype, knn = form
+    if marks:
+        ctx.mark(1)
+    d = sv.normalize_cells(counts, scale_factor=SCALE_FACTOR, dtype=dtype, ctx=ctx)
+    if marks:
+        ctx.mark(2)
+    S = sv.scale_features(d, scale_max=SCALE_MAX, features=hvf)
+    if marks:
+        ctx.mark(3)
+    em = sv.pca(S, w["npcs"], tol=1e-5, init=init, download=False)
+    if marks:
+        ctx.mark(4)
+    _, _, kh = sv.ann(em, w["k"], precision=knn, ctx=ctx, keep=True, download=False)
+    if marks:
+        ctx.mark(5)
+    return d, S, em, kh
+
+
+def timed_steps(sv, ctx, td, counts, hvf, w, init, form, steps, warmup, with_stages=False):
+    for _ in range(warmup):
+        run_pipeline(sv, ctx, counts, hvf, w, init, form)
+    ctx.sync()
+    barrier(td)
+    stages = {"normalize": 0.0, "scale": 0.0, "pca": 0.0, "knn": 0.0}
+    l0 = ctx.launches()
+    t0 = time.perf_counter()
+    ctx.mark(0)
+    info = None
+    for _ in range(steps):
+        d, S, em, kh = run_pipeline(sv, ctx, counts, hvf, w, init, form, marks=with_stages)
+        if with_stages:
+            ctx.sync()
+            stages["normalize"] += ctx.elapsed_ms(1, 2)
+            stages["scale"] += ctx.elapsed_ms(2, 3)
+            stages["pca"] += ctx.elapsed_ms(3, 4)
+            stages["knn"] += ctx.elapsed_ms(4, 5)
+        info = em.info
+        del d, S, em, kh
+    ctx.mark(6)
+    ctx.sync()
+    wall = time.perf_counter() - t0
+    dev_ms = ctx.elapsed_ms(0, 6)
+    launches = ctx.launches() - l0
+    barrier(td)
+    return {"dev_ms": dev_ms, "wall_s": wall, "launches": launches,
+            "stages_ms": {k: v / steps for k, v in stages.items()} if with_stages else None,
+            "irlba": info}
+
+
+def e2e_steps(sv, ctx, td, host, shape, hvf, w, init, form, steps):
+    """The same pipeline through the public API with host buffers: upload of the
+    CSC counts (pinned host memory) and download of Z, nn_index and distances."""
+    colptr, rowval, nzval = host
+    n = shape[0]
+    h2d = colptr.nbytes + rowval.nbytes + nzval.nbytes
+    d2h = 0
+    ctx.sync()
+    barrier(td)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        counts = sv.CountMatrix.upload(colptr, rowval, nzval, shape, 0, ctx)
+        d = sv.normalize_cells(counts, scale_factor=SCALE_FACTOR, dtype=form[0], ctx=ctx)
+        S = sv.scale_features(d, scale_max=SCALE_MAX, features=hvf)
+        em = sv.pca(S, w["npcs"], tol=1e-5, init=init, download=True)
+        idx, dist = sv.ann(em, w["k"], precision=form[1], ctx=ctx)
+        d2h = (em.coordinates.nbytes + em.stdev.nbytes + em.basis.nbytes + idx.nbytes + dist.nbytes)
+        del counts, d, S, em
+    ctx.sync()
+    dt = time.perf_counter() - t0
+    barrier(td)
+    return dt, h2d, d2h
+
+
+def pinned_copy(sv, arr):
+    """Copies a numpy array into pinned host memory (sv_host_alloc)."""
+    import ctypes as C
+    lib = sv._lib.load()
+    p = C.c_void_p()
+    sv._lib.check(lib.sv_host_alloc(C.byref(p), max(1, arr.nbytes)))
+    buf = (C.c_byte * max(1, arr.nbytes)).from_address(p.value)
+    out = np.frombuffer(buf, dtype=arr.dtype, count=arr.size)
+    out[:] = arr
+    return out, p
+
+
+def profile_step(sv, ctx, counts, hvf, w, init, form):
+    """One extra step with per-kernel CUDA events (outside the timed steps)."""
+    ctx.profile_reset()
+    ctx.profile(True)
+    run_pipeline(sv, ctx, counts, hvf, w, init, form)
+    ctx.sync()
+    rep = ctx.profile_report()
+    ctx.profile(False)
+    return rep
+
+
+def roofline(rep, S_nnz, n_cells, n_hvf, dtype, peaks):
+    """Roofline of the dominant HBM-bound kernel pair (the implicit SpMV)."""
+    v = {"bfloat16": 2, "float32": 4, "float64": 8}[dtype]
+    idx = 2 if n_hvf <= 65536 else 4
+    # bytes per launch (the algorithmic traffic)
+    csr = S_nnz * (idx + v) + 8 * (n_cells + 1) + 8 * n_cells
+    csc = S_nnz * (4 + v) + 4 * n_cells
+    out = {}
+    for name, b in (("spmv_csr_h", csr), ("spmv_csc_chunks", csc)):
+        if name in rep:
+            cnt, ms = rep[name]
+            avg = ms / cnt / 1e3
+            out[name] = {"bytes": b, "avg_ms": avg * 1e3, "gbs": b / avg / 1e9, "launches": cnt}
+    return out
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle restatement of the reference's CPU path)
+# ---------------------------------------------------------------------------
+def cpu_pipeline(w, n_sample, seed, D):
+    from oracle import severo_oracle as O
+    X = O.synth_counts(n_sample, w["n_genes"], w["mu_mean"], w["mu_sd"], depth=D, seed=seed,
+                       n_clusters=w["n_clusters"], dispersion=DISPERSION)
+    t = {}
+    t0 = time.perf_counter()
+    Xn = O.normalize_cells(X, scale_factor=SCALE_FACTOR, dtype=np.float64)   # reference default dtype
+    t["normalize"] = time.perf_counter() - t0
+    hvf = O.top_variable_genes(Xn, w["n_hvf"])                                   # precomputed input
+    t0 = time.perf_counter()
+    S, _, _ = O.scale_features(Xn, SCALE_MAX, np.float64, hvf)
+    t["scale"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    m, n = S.shape
+    init = np.random.default_rng(seed).standard_normal(n)
+    U, s, V, info, it, nmv = O.irlba(S.mul, S.rmul, m, n, w["npcs"], tol=1e-5, init=init)
+    Z = U * s
+    t["pca"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.knn_exact(Z, w["k"])
+    t["knn"] = time.perf_counter() - t0
+    return t, X.nnz
+
+
+def cpu_extrapolate(t, n_sample, n_full):
+    r = n_full / n_sample
+    total = (t["normalize"] + t["scale"] + t["pca"]) * r + t["knn"] * r * r
+    return n_full / total
+
+
+# ---------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="atlas", choices=sorted(WORKLOADS))
+    ap.add_argument("--cells", type=int, default=0, help="override the cell count (smaller runs)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    w = dict(WORKLOADS[args.workload])
+    if args.cells:
+        w["n_cells"] = args.cells
+    td, rank, world, local = dist_setup(args.gpus)
+
+    if args.impl == "reference":
+        return reference_arm(args, w, td, rank, world)
+
+    import __graft_entry__ as ge
+    ge._build_module().build()
+    sv = ge.load_package()
+    ctx = sv.Context(local)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+
+    # ---- data (untimed): generated on the device ------------------------------
+    n = w["n_cells"]
+    mu_g, s_c, cl, lfc = gen_params(w, n, SEED + rank)
+    D = calibrate_depth(mu_g, s_c, cl, lfc, w["nnz_per_cell"])
+    t0 = time.perf_counter()
+    counts = sv.CountMatrix.generate(n, w["n_genes"], mu_g, s_c, cl, lfc, depth=D,
+                                     dispersion=DISPERSION, seed=SEED + rank, ctx=ctx)
+    gen_s = time.perf_counter() - t0
+    nnz = counts.nnz
+    # HVF indices: a precomputed input (the reference selects them with vst,
+    # src/variablefeatures.jl); stand-in: the most variable normalised genes
+    d0 = sv.normalize_cells(counts, scale_factor=SCALE_FACTOR, dtype=w["dtype"], ctx=ctx)
+    _, var = d0.gene_moments()
+    hvf = np.sort(np.argsort(-var, kind="stable")[: w["n_hvf"]]) + 1
+    del d0
+    init = np.random.default_rng(SEED).standard_normal(w["n_hvf"])
+    form = (w["dtype"], w["knn"])
+    if form[1] == "bf16" and not knn_tc_available(sv, ctx):
+        form = (form[0], "fp32")
+
+    # ---- timed: device-resident -----------------------------------------------
+    clk = ClockSampler(local)
+    clk.start()
+    res = timed_steps(sv, ctx, td, counts, hvf, w, init, form, args.steps, args.warmup)
+    clocks = clk.stop()
+    dev_ms = allmax(td, res["dev_ms"])
+    ms_per_step = dev_ms / args.steps
+    value = world * n * args.steps / (dev_ms / 1e3)
+
+    # per-stage times (one extra pass with stage marks), per-kernel profile
+    st = timed_steps(sv, ctx, None, counts, hvf, w, init, form, 1, 0, with_stages=True)
+    rep = profile_step(sv, ctx, counts, hvf, w, init, form)
+    S = sv.scale_features(sv.normalize_cells(counts, scale_factor=SCALE_FACTOR, dtype=w["dtype"],
+                                             ctx=ctx), scale_max=SCALE_MAX, features=hvf)
+    nnz_h = S.nnz
+    del S
+    rl = roofline(rep, nnz_h, n, w["n_hvf"], w["dtype"], peaks)
+    top = sorted(rep.items(), key=lambda kv: -kv[1][1])[:8]
+
+    # ---- plain FP32 form on the same data -----------------------------------
+    fp32 = None
+    if not args.no_fp32 and w["dtype"] != "float32":
+        k32 = max(1, min(args.steps, 2))
+        r32 = timed_steps(sv, ctx, td, counts, hvf, w, init, ("float32", "fp32"), k32, 1)
+        ms32 = allmax(td, r32["dev_ms"]) / k32
+        fp32 = {"value": world * n / (ms32 / 1e3), "ms_per_step": ms32, "steps": k32}
+
+    # ---- e2e through the C ABI with host buffers ------------------------------
+    e2e = None
+    if not args.no_e2e:
+        A = counts.to_csc()
+        host = []
+        keep = []
+        for arr in (A.indptr.astype(np.int64), A.indices.astype(np.int32), A.data.astype(np.int32)):
+            a, p = pinned_copy(sv, arr)
+            host.append(a)
+            keep.append(p)
+        del A
+        ke = max(1, min(args.steps, 3))
+        e2e_steps(sv, ctx, td, host, (n, w["n_genes"]), hvf, w, init, form, 1)   # warm-up
+        dt, h2d, d2h = e2e_steps(sv, ctx, td, host, (n, w["n_genes"]), hvf, w, init, form, ke)
+        dt = allmax(td, dt)
+        e2e = {"value": world * n * ke / dt, "unit": "cells/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": ke}
+        lib = sv._lib.load()
+        for p in keep:
+            lib.sv_host_free(p)
+
+    # ---- CPU baseline (rank 0, N = 1): oracle on a bounded sample -------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        ns = min(CPU_SAMPLE_CELLS, n)
+        t, _ = cpu_pipeline(w, ns, SEED, D)
+        cpu = {"value": cpu_extrapolate(t, ns, n), "unit": "cells/s", "cores": os.cpu_count(),
+               "kind": "port",
+               "sample": (f"oracle pipeline on {ns} cells of the same generator, FP64, scipy "
+                          f"single-thread SpMV + BLAS kNN; stage times "
+                          + ", ".join(f"{k} {v:.2f}s" for k, v in t.items())
+                          + f"; extrapolated to {n} cells (linear stages x n, kNN x n^2)")}
+
+    if rank == 0:
+        dom = max(rl.items(), key=lambda kv: kv[1]["avg_ms"] * kv[1]["launches"]) if rl else None
+        roof = None
+        if dom:
+            name, r = dom
+            roof = {"kernel": name, "bound": "hbm", "achieved": round(r["gbs"], 1),
+                    "peak": hbm_peak, "unit": "GB/s", "frac": round(r["gbs"] / hbm_peak, 4),
+                    "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
+                    "bytes_per_launch": r["bytes"], "avg_launch_ms": round(r["avg_ms"], 4)}
+        out = {
+            "metric": METRIC, "value": round(value, 1), "unit": "cells/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"bfloat16": "bf16", "float32": "f32", "float64": "f64"}[w["dtype"]],
+            "data": "synthetic: seeded negative-binomial counts generated on the device (no dataset)",
+            "config": {"workload": f"{args.workload}: {n} cells x {w['n_genes']} genes, "
+                                   f"{nnz / n:.0f} nnz/cell, {w['n_hvf']} features, PCA {w['npcs']}, "
+                                   f"kNN {w['k']}",
+                       "n_cells": n, "n_genes": w["n_genes"], "nnz": nnz, "nnz_features": nnz_h,
+                       "depth_factor": round(D, 5), "n_clusters": w["n_clusters"],
+                       "value_dtype": w["dtype"], "knn_kernel": form[1],
+                       "irlba": res["irlba"], "parallelism": f"replicas x{world}",
+                       "l2": "inputs (tens of GB) exceed L2; no flush needed"},
+            "stages_ms": st["stages_ms"],
+            "kernels_ms": {k: {"launches": c, "ms": round(ms, 3)} for k, (c, ms) in top},
+            "spmv": rl,
+            "roofline": roof,
+            "e2e": e2e,
+            "plain_fp32": fp32,
+            "mixed_vs_fp32": round(fp32["ms_per_step"] / ms_per_step, 3) if fp32 else None,
+            "cpu_baseline": cpu,
+            "gpu_launches": res["launches"],
+            "clocks": clocks,
+            "generate_s": round(gen_s, 2),
+        }
+        print(json.dumps(out), flush=True)
+    if td is not None:
+        td.destroy_process_group()
+
+
+def knn_tc_available(sv, ctx):
+    try:
+        X = np.random.default_rng(0).standard_normal((256, 16))
+        sv.ann(X, 4, precision="bf16", ctx=ctx)
+        return True
+    except sv.SeveroGPUError:
+        return False
+
+
+def reference_arm(args, w, td, rank, world):
+    """The reference's CPU path (restated by the oracle) on a bounded sample per
+    step, on the host cores.  Rank 0 alone works under torchrun."""
+    if rank != 0:
+        if td is not None:
+            td.destroy_process_group()
+        return
+    n = w["n_cells"]
+    ns = min(CPU_SAMPLE_CELLS, n)
+    mu_g, s_c, cl, lfc = gen_params(w, ns, SEED)
+    D = calibrate_depth(mu_g, s_c, cl, lfc, w["nnz_per_cell"])
+    for _ in range(args.warmup):
+        cpu_pipeline(w, min(ns, 1000), SEED, D)
+    vals = []
+    t_all = time.perf_counter()
+    for s in range(args.steps):
+        t, _ = cpu_pipeline(w, ns, SEED + s, D)
+        vals.append(cpu_extrapolate(t, ns, n))
+    wall = time.perf_counter() - t_all
+    value = float(np.median(vals))
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": "cells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * n / value, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded negative-binomial counts (numpy), bounded sample per step",
+        "config": {"workload": f"{args.workload}: {n} cells x {w['n_genes']} genes",
+                   "n_cells": n, "sample_cells": ns},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(value, 3), "unit": "cells/s", "cores": os.cpu_count(),
+                         "kind": "port",
+                         "sample": f"{ns}-cell sample per step, extrapolated to {n} cells "
+                                   f"(linear stages x n, kNN x n^2); wall {wall:.1f}s"},
+        "e2e": {"value": round(value, 3), "unit": "cells/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    if td is not None:
+        td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

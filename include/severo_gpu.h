@@ -98,13 +98,14 @@ int  sv_device_memory(sv_context* ctx, size_t* free_bytes, size_t* total_bytes);
 /* ---- count matrix ------------------------------------------------------------
  * sv_counts_upload_csc replaces holding the CountMatrix of src/Severo.jl:26-27
  * in host memory: it copies a cells x genes SparseMatrixCSC (colptr, rowval,
- * nzval; idx_type SV_I32 or SV_I64; val_type SV_I32 or SV_I64; index_base 0 or 1)
- * to the device and builds the cell-major (CSR) copy there.  Row indices must
- * be strictly increasing within each column (Julia's invariant); this is
- * checked on the device and reported as SV_ERR_ARG. */
+ * nzval, each SV_I32 or SV_I64 as declared by its *_type; index_base 0 or 1, 1
+ * for Julia's arrays) to the device and builds the cell-major (CSR) copy there.
+ * Row indices must be strictly increasing within each column (Julia's
+ * invariant); this is checked on the device and reported as SV_ERR_ARG. */
 int sv_counts_upload_csc(sv_context* ctx, int64_t n_cells, int64_t n_genes, int64_t nnz,
-                         const void* colptr, const void* rowval, const void* nzval,
-                         int idx_type, int val_type, int index_base, sv_counts** out);
+                         const void* colptr, int colptr_type, const void* rowval,
+                         int rowval_type, const void* nzval, int val_type, int index_base,
+                         sv_counts** out);
 /* Synthetic negative-binomial counts generated on the device (benchmarks).
  * Cells x genes; mean depth * s_c * mu_g * exp(lfc[cluster(c), g]); variance
  * mean + dispersion * mean^2.  mu_g (n_genes), s_c (n_cells), cluster ids
@@ -159,6 +160,10 @@ int sv_scale_features(sv_context* ctx, const sv_data* data, const int64_t* featu
 int sv_centered_create(sv_context* ctx, int64_t n_rows, int64_t n_cols, int64_t nnz,
                        const int64_t* colptr, const int64_t* rowval, const double* nzval,
                        const double* mu, int dtype, sv_centered** out);
+/* Per-gene mean and unbiased variance over all genes of a data matrix, with the
+ * implicit zeros (the statistics of src/scaling.jl:132-142 on every column); the
+ * input of highly-variable-feature selection (src/variablefeatures.jl). */
+int sv_gene_moments(sv_context* ctx, const sv_data* data, double* mean, double* var);
 int sv_centered_info(const sv_centered* s, int64_t* n_cells, int64_t* n_features, int64_t* nnz);
 /* mu (= mean/std, the reference's S.mu), mean and std per feature (FP64). */
 int sv_centered_stats(sv_context* ctx, const sv_centered* s, double* mu, double* mean, double* std);

@@ -155,33 +155,28 @@ class CountMatrix(_Handle):
             X = X.sorted_indices()
         if not np.issubdtype(X.dtype, np.integer):
             raise TypeError("counts must be integers (CountMatrix, src/Severo.jl:26)")
-        # one index type for colptr and rowval: Int32 while nnz fits, else Int64
-        it = SV_I32 if X.nnz < 2**31 - 1 else SV_I64
-        idt = np.int32 if it == SV_I32 else np.int64
-        colptr = np.ascontiguousarray(X.indptr, dtype=idt)
-        rowval = np.ascontiguousarray(X.indices, dtype=idt)
-        vt = SV_I64 if X.dtype.itemsize == 8 else SV_I32
-        vals = np.ascontiguousarray(X.data, dtype=np.int64 if vt == SV_I64 else np.int32)
-        h = C.c_void_p()
-        L.check(ctx.lib.sv_counts_upload_csc(ctx.h, X.shape[0], X.shape[1], X.nnz, _ptr(colptr),
-                                              _ptr(rowval), _ptr(vals), it, vt, 0, C.byref(h)))
-        return cls(ctx, h)
+        colptr = np.ascontiguousarray(X.indptr, dtype=np.int64)
+        rowval = np.ascontiguousarray(X.indices, dtype=np.int32)
+        vals = np.ascontiguousarray(X.data, dtype=np.int64 if X.dtype.itemsize == 8 else np.int32)
+        return cls.upload(colptr, rowval, vals, X.shape, 0, ctx)
 
     @classmethod
     def upload(cls, colptr, rowval, nzval, shape, index_base=0, ctx: Context | None = None):
-        """Upload raw CSC arrays (Julia SparseMatrixCSC layout; 1-based when index_base=1)."""
+        """Upload raw CSC arrays (Julia SparseMatrixCSC layout; 1-based when index_base=1).
+        Each array may be Int32 or Int64; they are read from host memory (pinned
+        memory gives full link speed)."""
         ctx = ctx or default_context()
         colptr = np.ascontiguousarray(colptr)
         rowval = np.ascontiguousarray(rowval)
         nzval = np.ascontiguousarray(nzval)
-        if colptr.dtype != rowval.dtype:
-            raise TypeError("colptr and rowval must share an index type")
-        it = SV_I64 if colptr.dtype.itemsize == 8 else SV_I32
-        vt = SV_I64 if nzval.dtype.itemsize == 8 else SV_I32
+        code = lambda a: SV_I64 if a.dtype.itemsize == 8 else SV_I32
+        for a in (colptr, rowval, nzval):
+            if not np.issubdtype(a.dtype, np.integer) or a.dtype.itemsize not in (4, 8):
+                raise TypeError("colptr, rowval and counts must be Int32 or Int64")
         h = C.c_void_p()
         L.check(ctx.lib.sv_counts_upload_csc(ctx.h, shape[0], shape[1], len(rowval), _ptr(colptr),
-                                              _ptr(rowval), _ptr(nzval), it, vt, index_base,
-                                              C.byref(h)))
+                                              code(colptr), _ptr(rowval), code(rowval), _ptr(nzval),
+                                              code(nzval), index_base, C.byref(h)))
         return cls(ctx, h)
 
     @classmethod
@@ -260,6 +255,14 @@ class DataMatrix(_Handle):
         v = np.empty(self.counts.nnz, self._host_dtype())
         L.check(self.ctx.lib.sv_data_download_csr(self.ctx.h, self.h, _ptr(v)))
         return self._decode(v)
+
+    def gene_moments(self):
+        """Per-gene mean and variance (implicit zeros included) on the device."""
+        n = self.shape[1]
+        mean = np.empty(n)
+        var = np.empty(n)
+        L.check(self.ctx.lib.sv_gene_moments(self.ctx.h, self.h, _ptr(mean), _ptr(var)))
+        return mean, var
 
     def cell_totals(self):
         t = np.empty(self.shape[0], np.int64)
@@ -478,18 +481,19 @@ _PREC = {"fp32": SV_KNN_FP32, "bf16": SV_KNN_BF16}
 
 
 def ann(X, k, metric="euclidean", include_self=True, precision="fp32", ctx: Context | None = None,
-        keep=False):
-    """src/neighbours.jl:19-30: (nn_index n x k Int32 1-based, distances n x k)."""
+        keep=False, download=True):
+    """src/neighbours.jl:19-30: (nn_index n x k Int32 1-based, distances n x k).
+    X may be a LinearEmbedding whose coordinates are still on the device;
+    download=False leaves the lists on the device (returned handle only)."""
     ctx = ctx or default_context()
     if isinstance(X, LinearEmbedding):
-        n = X.coordinates.shape[0] if X.coordinates is not None else None
         h = C.c_void_p()
         e = X.handle.h
         a, b = C.c_int64(), C.c_int64()
         L.check(ctx.lib.sv_embed_info(e, C.byref(a), C.byref(b)))
         n = a.value
-        idx = np.zeros((n, k), dtype=np.int32, order="F")
-        dist = np.zeros((n, k), dtype=np.float64, order="F")
+        idx = np.zeros((n, k), dtype=np.int32, order="F") if download else None
+        dist = np.zeros((n, k), dtype=np.float64, order="F") if download else None
         L.check(ctx.lib.sv_knn_embed(ctx.h, e, 0, k, _METRICS[metric], int(include_self),
                                       _PREC[precision], _ptr(idx), _ptr(dist), C.byref(h)))
         return (idx, dist, KNN(ctx, h)) if keep else (idx, dist)

@@ -71,7 +71,7 @@ SIGNATURES = {
     "sv_profile_query": (i32, [vp, C.c_char_p, P(dbl), P(i64)]),
     "sv_profile_report": (i32, [vp, C.c_char_p, C.c_size_t]),
     "sv_device_memory": (i32, [vp, P(C.c_size_t), P(C.c_size_t)]),
-    "sv_counts_upload_csc": (i32, [vp, i64, i64, i64, vp, vp, vp, i32, i32, i32, P(vp)]),
+    "sv_counts_upload_csc": (i32, [vp, i64, i64, i64, vp, i32, vp, i32, vp, i32, i32, P(vp)]),
     "sv_counts_generate": (i32, [vp, i64, i64, vp, vp, vp, vp, C.c_int32, dbl, dbl, C.c_uint64, P(vp)]),
     "sv_counts_info": (i32, [vp, P(i64), P(i64), P(i64)]),
     "sv_counts_download_csc": (i32, [vp, vp, vp, vp, vp]),
@@ -84,6 +84,7 @@ SIGNATURES = {
     "sv_data_free": (i32, [vp]),
     "sv_scale_features": (i32, [vp, vp, vp, i64, dbl, P(vp)]),
     "sv_centered_create": (i32, [vp, i64, i64, i64, vp, vp, vp, vp, i32, P(vp)]),
+    "sv_gene_moments": (i32, [vp, vp, vp, vp]),
     "sv_centered_info": (i32, [vp, P(i64), P(i64), P(i64)]),
     "sv_centered_stats": (i32, [vp, vp, vp, vp, vp]),
     "sv_centered_mul": (i32, [vp, vp, C.c_char, i64, dbl, vp, i64, dbl, vp, i64]),

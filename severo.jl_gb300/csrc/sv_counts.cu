@@ -358,14 +358,17 @@ static void build_csr_from_csc(sv_context* ctx, sv_counts* c) {
 }
 
 SV_API int sv_counts_upload_csc(sv_context* ctx, int64_t n_cells, int64_t n_genes, int64_t nnz,
-                                const void* colptr, const void* rowval, const void* nzval,
-                                int idx_type, int val_type, int index_base, sv_counts** out) {
+                                const void* colptr, int colptr_type, const void* rowval,
+                                int idx_type, const void* nzval, int val_type, int index_base,
+                                sv_counts** out) {
   SV_TRY
   sv_ctx_check(ctx);
   SV_REQUIRE(out, "out is null");
   SV_REQUIRE(n_cells >= 1 && n_genes >= 1 && nnz >= 0, "bad sizes");
   SV_REQUIRE(n_cells < (1ll << 31) && n_genes < (1ll << 31), "dimension exceeds Int32 indices");
-  SV_REQUIRE(idx_type == SV_I32 || idx_type == SV_I64, "idx_type must be SV_I32 or SV_I64");
+  SV_REQUIRE(colptr_type == SV_I32 || colptr_type == SV_I64, "colptr_type must be SV_I32 or SV_I64");
+  SV_REQUIRE(colptr_type == SV_I64 || nnz < (1ll << 31), "nnz >= 2^31 needs Int64 colptr");
+  SV_REQUIRE(idx_type == SV_I32 || idx_type == SV_I64, "rowval_type must be SV_I32 or SV_I64");
   SV_REQUIRE(val_type == SV_I32 || val_type == SV_I64, "val_type must be SV_I32 or SV_I64");
   SV_REQUIRE(index_base == 0 || index_base == 1, "index_base must be 0 or 1");
   SV_REQUIRE(colptr && (nnz == 0 || (rowval && nzval)), "null array");
@@ -377,10 +380,10 @@ SV_API int sv_counts_upload_csc(sv_context* ctx, int64_t n_cells, int64_t n_gene
     c->nnz = nnz;
     c->csc_colptr.alloc(n_genes + 1);
     {
-      size_t es = idx_type == SV_I32 ? 4 : 8;
+      size_t es = colptr_type == SV_I32 ? 4 : 8;
       DevBuf<unsigned char> tmp((n_genes + 1) * es);
       sv_h2d(ctx, tmp.get(), colptr, (n_genes + 1) * es);
-      if (idx_type == SV_I32)
+      if (colptr_type == SV_I32)
         sv_launch(ctx, "counts_colptr", k_colptr_to_i64<int32_t>, dim3(sv_grid_for(ctx, n_genes + 1, 256)),
                   dim3(256), 0, (const int32_t*)tmp.get(), c->csc_colptr.get(), n_genes + 1,
                   (int64_t)index_base);
@@ -424,8 +427,8 @@ sv_counts* sv_counts_upload_positions(sv_context* ctx, int64_t n_rows, int64_t n
   std::vector<int32_t> pos(std::max<int64_t>(1, nnz));
   for (int64_t i = 0; i < nnz; ++i) pos[i] = (int32_t)i;
   sv_counts* c = nullptr;
-  int st = sv_counts_upload_csc(ctx, n_rows, n_cols, nnz, colptr, rowval, pos.data(), SV_I64, SV_I32,
-                                0, &c);
+  int st = sv_counts_upload_csc(ctx, n_rows, n_cols, nnz, colptr, SV_I64, rowval, SV_I64, pos.data(),
+                                SV_I32, 0, &c);
   if (st != SV_OK) sv_throw(st, "pattern upload failed");
   return c;
 }

@@ -679,6 +679,39 @@ SV_API int sv_centered_create(sv_context* ctx, int64_t n_rows, int64_t n_cols, i
   SV_CATCH
 }
 
+SV_API int sv_gene_moments(sv_context* ctx, const sv_data* data, double* mean, double* var) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(data && data->ctx == ctx && (mean || var), "bad argument");
+  const sv_counts* C = data->counts;
+  SV_REQUIRE(C->n_cells >= 2, "need at least two cells for a variance");
+  int64_t ng = C->n_genes;
+  DevBuf<int64_t> fs(ng), fe(ng);
+  DevBuf<double> m(ng), sd(ng), mu(ng), invd(ng), clipd(ng);
+  DevBuf<float> invf(ng), clipf(ng);
+  SV_CUDA(cudaMemcpyAsync(fs.get(), C->csc_colptr.get(), ng * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+  SV_CUDA(cudaMemcpyAsync(fe.get(), C->csc_colptr.get() + 1, ng * 8, cudaMemcpyDeviceToDevice,
+                          ctx->stream));
+#define LAUNCH_MOM(VT)                                                                           \
+  sv_launch(ctx, "gene_moments", k_moments<VT>, dim3(sv_grid_for(ctx, ng, 1, 16)), dim3(256), 0, \
+            (const VT*)data->csc_val.get(), (const int64_t*)fs.get(), (const int64_t*)fe.get(), ng, \
+            C->n_cells, (double)INFINITY, m.get(), sd.get(), mu.get(), invf.get(), clipf.get(),   \
+            invd.get(), clipd.get())
+  switch (data->dtype) {
+    case SV_F64: LAUNCH_MOM(double); break;
+    case SV_F32: LAUNCH_MOM(float); break;
+    default: LAUNCH_MOM(__nv_bfloat16); break;
+  }
+#undef LAUNCH_MOM
+  if (mean) sv_d2h(ctx, mean, m.get(), ng * 8);
+  if (var) {
+    std::vector<double> s(ng);
+    sv_d2h(ctx, s.data(), sd.get(), ng * 8);
+    for (int64_t g = 0; g < ng; ++g) var[g] = s[g] * s[g];
+  }
+  SV_CATCH
+}
+
 SV_API int sv_centered_info(const sv_centered* s, int64_t* n_cells, int64_t* nf, int64_t* nnz) {
   SV_TRY
   SV_REQUIRE(s, "null handle");
