@@ -331,6 +331,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload])
     if args.cells:
@@ -393,6 +394,11 @@ def main():
         r32 = timed_steps(sv, ctx, td, counts, hvf, w, init, ("float32", "fp32"), k32, 1)
         ms32 = allmax(td, r32["dev_ms"]) / k32
         fp32 = {"value": world * n / (ms32 / 1e3), "ms_per_step": ms32, "steps": k32}
+
+    # ---- accuracy against FP64 (untimed, rank 0) -------------------------------
+    acc = None
+    if rank == 0 and not args.no_accuracy:
+        acc = accuracy(sv, ctx, counts, hvf, w, init, form)
 
     # ---- e2e through the C ABI with host buffers ------------------------------
     e2e = None
@@ -458,6 +464,7 @@ def main():
             "plain_fp32": fp32,
             "mixed_vs_fp32": round(fp32["ms_per_step"] / ms_per_step, 3) if fp32 else None,
             "cpu_baseline": cpu,
+            "accuracy": acc,
             "gpu_launches": res["launches"],
             "clocks": clocks,
             "generate_s": round(gen_s, 2),
@@ -465,6 +472,48 @@ def main():
         print(json.dumps(out), flush=True)
     if td is not None:
         td.destroy_process_group()
+
+
+def accuracy(sv, ctx, counts, hvf, w, init, form, n_queries=1000):
+    """Errors of the measured form against the same pipeline in FP64: relative
+    error of the singular values, largest principal angle of the PC (loading)
+    subspace, and kNN recall@k against exact FP64 neighbours (brute force on the
+    host, for a sample of query cells, over the measured form's coordinates)."""
+    from oracle import severo_oracle as O
+    out = {}
+    d = sv.normalize_cells(counts, scale_factor=SCALE_FACTOR, dtype=form[0], ctx=ctx)
+    S = sv.scale_features(d, scale_max=SCALE_MAX, features=hvf)
+    em = sv.pca(S, w["npcs"], tol=1e-5, init=init, download=True)
+    idx, _ = sv.ann(em, w["k"], precision=form[1], ctx=ctx)
+    del d, S
+    d64 = sv.normalize_cells(counts, scale_factor=SCALE_FACTOR, dtype="float64", ctx=ctx)
+    S64 = sv.scale_features(d64, scale_max=SCALE_MAX, features=hvf)
+    em64 = sv.pca(S64, w["npcs"], tol=1e-8, init=init, download=False)
+    del d64, S64
+    s = em.stdev
+    s64 = em64.stdev
+    out["sigma_rel_err_max"] = float(np.max(np.abs(s - s64) / s64))
+    ang = O.principal_angles(em.basis, em64.basis)
+    out["pc_subspace_angle_max_rad"] = float(ang.max())
+    out["sigma_gap_last"] = float(s64[-2] / s64[-1] - 1)
+    k10 = min(10, w["npcs"])
+    out["pc1_10_angle_max_rad"] = float(O.principal_angles(em.basis[:, :k10], em64.basis[:, :k10]).max())
+    Z = np.ascontiguousarray(em.coordinates)
+    n = Z.shape[0]
+    q = np.random.default_rng(7).choice(n, min(n_queries, n), replace=False)
+    sq = np.einsum("ij,ij->i", Z, Z)
+    hits = 0
+    for b in range(0, len(q), 250):
+        qq = q[b:b + 250]
+        D = sq[qq, None] + sq[None, :] - 2.0 * (Z[qq] @ Z.T)
+        D[np.arange(len(qq)), qq] = -1.0
+        part = np.argpartition(D, w["k"] - 1, axis=1)[:, :w["k"]]
+        for r, i in enumerate(qq):
+            hits += len(set(part[r]) & set(idx[i] - 1))
+    out["knn_recall"] = hits / (len(q) * w["k"])
+    out["knn_recall_queries"] = int(len(q))
+    out["reference"] = "same pipeline in FP64 on the device (normalised values FP64, FP64 products)"
+    return out
 
 
 def knn_tc_available(sv, ctx):

@@ -58,6 +58,7 @@ __global__ void __launch_bounds__(KNN_THREADS) k_knn_fp32(const float* __restric
                                                           int32_t* __restrict__ cand) {
   __shared__ __align__(16) float tile[KNN_TILE * DP];
   __shared__ float tsq[KNN_TILE];
+  __shared__ float kslot[KNN_THREADS][9];
   int64_t qi = (int64_t)blockIdx.x * KNN_THREADS + threadIdx.x;
   bool active = qi < n;
   float q[DP];
@@ -90,31 +91,48 @@ __global__ void __launch_bounds__(KNN_THREADS) k_knn_fp32(const float* __restric
     }
     for (int r = threadIdx.x; r < KNN_TILE; r += KNN_THREADS) tsq[r] = p0 + r < n ? sq[p0 + r] : FLT_MAX;
     __syncthreads();
-    int lim = n - p0 < KNN_TILE ? (int)(n - p0) : KNN_TILE;
-    for (int r = 0; r < lim; ++r) {
-      const float4* pr = (const float4*)(tile + r * DP);
-      float acc = tsq[r];
+    // 8 candidates at a time: 8 independent FMA chains; padded rows have key FLT_MAX
+#pragma unroll 1
+    for (int r0 = 0; r0 < KNN_TILE; r0 += 8) {
+      float acc[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) acc[u] = tsq[r0 + u];
 #pragma unroll
       for (int c = 0; c < DP; c += 4) {
-        float4 v = pr[c / 4];
-        acc = fmaf(q[c], v.x, acc);
-        acc = fmaf(q[c + 1], v.y, acc);
-        acc = fmaf(q[c + 2], v.z, acc);
-        acc = fmaf(q[c + 3], v.w, acc);
-      }
-      int pid = (int)(p0 + r);
-      if (acc < best[K2 - 1] && pid != qi) {
-        float cd = acc;
-        int ci = pid;
 #pragma unroll
-        for (int t = 0; t < K2; ++t) {
-          if (cd < best[t]) {
-            float td = best[t];
-            int ti = bidx[t];
-            best[t] = cd;
-            bidx[t] = ci;
-            cd = td;
-            ci = ti;
+        for (int u = 0; u < 8; ++u) {
+          float4 v = ((const float4*)(tile + (r0 + u) * DP))[c / 4];
+          acc[u] = fmaf(q[c], v.x, acc[u]);
+          acc[u] = fmaf(q[c + 1], v.y, acc[u]);
+          acc[u] = fmaf(q[c + 2], v.z, acc[u]);
+          acc[u] = fmaf(q[c + 3], v.w, acc[u]);
+        }
+      }
+      float thr = best[K2 - 1];
+      uint32_t m = 0;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) m |= (acc[u] < thr ? 1u : 0u) << u;
+      if (m) {
+        float* slot = kslot[threadIdx.x];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) slot[u] = acc[u];
+        while (m) {
+          int u = __ffs(m) - 1;
+          m &= m - 1;
+          int pid = (int)(p0 + r0 + u);
+          float cd = slot[u];
+          if (pid == qi || !(cd < best[K2 - 1])) continue;
+          int ci = pid;
+#pragma unroll
+          for (int t = 0; t < K2; ++t) {
+            if (cd < best[t]) {
+              float td = best[t];
+              int ti = bidx[t];
+              best[t] = cd;
+              bidx[t] = ci;
+              cd = td;
+              ci = ti;
+            }
           }
         }
       }
@@ -141,7 +159,7 @@ __global__ void k_rerank(const float* __restrict__ X, int64_t n, const int32_t* 
     for (int t = lane; t < K2; t += 32) {
       int c = cand[qi * K2 + t];
       unsigned long long key = ~0ull;
-      if (c >= 0) {
+      if (c >= 0 && c != qi) {
         const float* p = X + (int64_t)c * DP;
         float s = 0.f;
 #pragma unroll 8
@@ -149,7 +167,6 @@ __global__ void k_rerank(const float* __restrict__ X, int64_t n, const int32_t* 
           float df = q[j] - p[j];
           s = fmaf(df, df, s);
         }
-        if (include_self && c == qi) s = -1.0f;   // the point itself sorts first
         // order-preserving bit pattern of a float (all finite here)
         unsigned int b = __float_as_uint(s);
         b = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
@@ -175,15 +192,21 @@ __global__ void k_rerank(const float* __restrict__ X, int64_t n, const int32_t* 
         __syncwarp();
       }
     }
-    for (int t = lane; t < k; t += 32) {
+    // the point itself first when include_self (distance 0), then the others
+    int off = include_self ? 1 : 0;
+    if (include_self && lane == 0) {
+      out_idx[qi * k] = (int32_t)qi;
+      out_dist[qi * k] = 0.f;
+    }
+    for (int t = lane; t + off < k; t += 32) {
       unsigned long long key = keys[t];
       int c = (int)(key & 0xffffffffu);
       unsigned int b = (unsigned int)(key >> 32);
       b = (b & 0x80000000u) ? (b & 0x7fffffffu) : ~b;
       float s = __uint_as_float(b);
       if (s < 0.f) s = 0.f;
-      out_idx[qi * k + t] = key == ~0ull ? -1 : c;
-      out_dist[qi * k + t] = cosine ? 0.5f * s : sqrtf(s);
+      out_idx[qi * k + t + off] = key == ~0ull ? -1 : c;
+      out_dist[qi * k + t + off] = cosine ? 0.5f * s : sqrtf(s);
     }
     __syncwarp();
   }
@@ -224,7 +247,8 @@ __global__ void k_to_host_layout(const int32_t* __restrict__ idx, const float* _
 // Core: X32 row-major [n][dp] FP32 with norms -> knn handle (row-major, 0-based).
 static void knn_core(sv_context* ctx, const float* X32, const float* sq, int64_t n, int dp, int k,
                      int include_self, int cosine, int precision, sv_knn* out) {
-  int K2 = 2 * k <= 32 ? 32 : 64;
+  // candidates per query: at least 2k; the tensor-core stage always keeps 64
+  int K2 = (2 * k <= 32 && precision != SV_KNN_BF16) ? 32 : 64;
   if (2 * k > 64) sv_throw(SV_ERR_UNSUPPORTED, "k = %d exceeds the supported maximum of 32", k);
   DevBuf<int32_t> cand((size_t)n * K2);
   bool done = false;

@@ -1,9 +1,413 @@
-// BF16 tensor-core (tcgen05) distance tiles for the kNN candidate stage.
+// BF16 tensor-core (tcgen05) candidate stage of the exact kNN.
+//
+// Distances in the GEMM form key(q, p) = |p|^2 - 2 q.p over BF16-rounded
+// coordinates (K padded to 64 = one 128-byte swizzle row), FP32 accumulation in
+// tensor memory.  One CTA per block of 128 queries streams every point tile of
+// 256 points:
+//   warp 0      TMA producer (one thread): the query tile once, point tiles into
+//               a 4-stage ring (cp.async.bulk.tensor, 128B swizzle, mbarriers);
+//   warp 1      MMA issuer (one thread): 4 x tcgen05.mma.kind::f16 (K = 16 each)
+//               per tile into one of two 256-column TMEM accumulators;
+//   warps 2..9  epilogue: tcgen05.ld of their lane quarter (= 32 queries) and
+//               column half (128 points), key = |p|^2 - 2 acc, and a register
+//               top-32 per (query, half).
+// The 64 candidates per query then go through the exact FP32 re-rank
+// (sv_knn.cu).  Every mbarrier wait is bounded: on a timeout the kernel records
+// an error, drains its own outstanding copies and MMAs (bounded as well),
+// releases its tensor memory and returns.
 #include "sv_internal.cuh"
+#include <cuda.h>
+#include <float.h>
 
-int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq, int64_t n, int d,
+namespace {
+
+constexpr int BM = 128;            // queries per CTA (MMA M)
+constexpr int BN = 256;            // points per tile (MMA N)
+constexpr int BK = 64;             // padded dimension (BF16 elements, 128 bytes)
+constexpr int STAGES = 4;
+constexpr int EPI_WARPS = 8;
+constexpr int THREADS = (2 + EPI_WARPS) * 32;
+constexpr int KH = 32;             // candidates kept per (query, column half)
+constexpr long long TIMEOUT = 4000000000ll;   // cycles (~2 s) per wait
+
+struct __align__(1024) Smem {
+  __nv_bfloat16 A[BM * BK];              // 16 KB
+  __nv_bfloat16 B[STAGES][BN * BK];      // 4 x 32 KB
+  float keys[EPI_WARPS * 32][33];        // per-epilogue-thread key slot (padded: no bank conflicts)
+  unsigned long long full[STAGES];
+  unsigned long long empty[STAGES];
+  unsigned long long tfull[2];
+  unsigned long long tempty[2];
+  unsigned long long abar;
+  unsigned long long drain;
+  uint32_t tmem_base;
+  int err;
+};
+
+__device__ __forceinline__ uint32_t su32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned long long* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(su32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait.  Returns false when the CTA is aborting (timeout here or elsewhere).
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, uint32_t parity, int* err) {
+  if (mbar_try(b, parity)) return true;
+  long long t0 = clock64();
+  while (!mbar_try(b, parity)) {
+    if (*(volatile int*)err) return false;
+    if (clock64() - t0 > TIMEOUT) {
+      atomicOr(err, 1);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          su32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(su32(bar))
+      : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;                  // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;        // stride byte offset
+  d |= (uint64_t)1 << 46;                  // descriptor version (sm_100 family)
+  d |= (uint64_t)2 << 61;                  // 128-byte swizzle
+  return d;
+}
+
+// instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = 256
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(IDESC), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(unsigned long long* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   su32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_knn_tc(const __grid_constant__ CUtensorMap tmapA, const __grid_constant__ CUtensorMap tmapB,
+             const float* __restrict__ sqpad, int64_t n, int ntiles, int32_t* __restrict__ cand,
+             int* __restrict__ status) {
+  extern __shared__ unsigned char smem_raw[];
+  Smem* s = (Smem*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int64_t q0 = (int64_t)blockIdx.x * BM;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < STAGES; ++i) {
+      mbar_init(&s->full[i], 1);
+      mbar_init(&s->empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&s->tfull[i], 1);
+      mbar_init(&s->tempty[i], EPI_WARPS);
+    }
+    mbar_init(&s->abar, 1);
+    mbar_init(&s->drain, 1);
+    s->err = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     su32(&s->tmem_base)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  uint32_t tmem = s->tmem_base;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int issued = 0;
+      mbar_expect_tx(&s->abar, BM * BK * 2);
+      tma_load_2d(s->A, &tmapA, 0, (int)q0, &s->abar);
+      for (int t = 0; t < ntiles; ++t) {
+        int st = t % STAGES;
+        uint32_t ph = (t / STAGES) & 1;
+        if (!mbar_wait(&s->empty[st], ph ^ 1, &s->err)) break;
+        mbar_expect_tx(&s->full[st], BN * BK * 2);
+        tma_load_2d(s->B[st], &tmapB, 0, t * BN, &s->full[st]);
+        issued = t + 1;
+      }
+      // drain: every issued copy has landed before the CTA may exit
+      {
+        long long t0 = clock64();
+        while (!mbar_try(&s->abar, 0) && clock64() - t0 < TIMEOUT) {
+        }
+      }
+      for (int t = issued - STAGES < 0 ? 0 : issued - STAGES; t < issued; ++t) {
+        int st = t % STAGES;
+        uint32_t ph = (t / STAGES) & 1;
+        long long t0 = clock64();
+        while (!mbar_try(&s->full[st], ph) && clock64() - t0 < TIMEOUT) {
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      bool ok = mbar_wait(&s->abar, 0, &s->err);
+      uint32_t a_base = su32(s->A);
+      int t = 0;
+      for (; ok && t < ntiles; ++t) {
+        int st = t % STAGES;
+        uint32_t ph = (t / STAGES) & 1;
+        int ab = t & 1;
+        uint32_t aph = (t >> 1) & 1;
+        if (!mbar_wait(&s->tempty[ab], aph ^ 1, &s->err)) break;
+        if (!mbar_wait(&s->full[st], ph, &s->err)) break;
+        fence_after();
+        uint32_t b_base = su32(s->B[st]);
+        uint32_t d = tmem + (uint32_t)(ab * BN);
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; ++kk)
+          mma_bf16(d, sw128_desc(a_base + kk * 32), sw128_desc(b_base + kk * 32), kk > 0 ? 1u : 0u);
+        mma_commit(&s->empty[st]);
+        mma_commit(&s->tfull[ab]);
+      }
+      // all MMAs issued by this thread complete before the drain barrier fires
+      mma_commit(&s->drain);
+      long long t0 = clock64();
+      while (!mbar_try(&s->drain, 0) && clock64() - t0 < TIMEOUT) {
+      }
+    }
+  } else {
+    // ---------------- epilogue ----------------
+    int ew = warp - 2;
+    int quarter = warp & 3;            // TMEM lane quarter this warp may access
+    int half = ew >> 2;                // column half: warps 2..5 -> 0, 6..9 -> 1
+    int row = quarter * 32 + lane;
+    int64_t q = q0 + row;
+    float best[KH];
+    int bidx[KH];
+#pragma unroll
+    for (int i = 0; i < KH; ++i) {
+      best[i] = FLT_MAX;
+      bidx[i] = -1;
+    }
+    uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
+    for (int t = 0; t < ntiles; ++t) {
+      int ab = t & 1;
+      uint32_t aph = (t >> 1) & 1;
+      bool ok = mbar_wait(&s->tfull[ab], aph, &s->err);
+      if (!__all_sync(0xffffffffu, ok)) break;   // warp-uniform: the TMEM loads are .aligned
+      fence_after();
+      int j0 = t * BN + half * (BN / 2);
+      uint32_t tbase = tmem + lane_off + (uint32_t)(ab * BN + half * (BN / 2));
+#pragma unroll 1
+      for (int c = 0; c < BN / 2 / 32; ++c) {
+        float acc[32];
+        float pn[32];
+        const float4* np = (const float4*)(sqpad + j0 + c * 32);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          float4 v = __ldg(np + i);
+          pn[4 * i] = v.x;
+          pn[4 * i + 1] = v.y;
+          pn[4 * i + 2] = v.z;
+          pn[4 * i + 3] = v.w;
+        }
+        __syncwarp();
+        tmem_ld32(tbase + c * 32, acc);
+        if (c == BN / 2 / 32 - 1) {
+          // accumulator values are in registers: release the buffer to the MMA warp
+          fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&s->tempty[ab]);
+        }
+        // cheap pass: keys and the mask of those below the current threshold
+        float thr = best[KH - 1];
+        uint32_t m = 0;
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          acc[i] = fmaf(-2.0f, acc[i], pn[i]);
+          m |= (acc[i] < thr ? 1u : 0u) << i;
+        }
+        if (m) {
+          // rare: park the keys in this thread's shared slot and insert one by one
+          // (one copy of the insertion code keeps the loop small in the I-cache)
+          float* slot = s->keys[threadIdx.x - 64];
+#pragma unroll
+          for (int i = 0; i < 32; ++i) slot[i] = acc[i];
+          int cbase = j0 + c * 32;
+          while (m) {
+            int i = __ffs(m) - 1;
+            m &= m - 1;
+            float cd = slot[i];
+            if (!(cd < best[KH - 1])) continue;
+            int ci = cbase + i;
+#pragma unroll
+            for (int u = 0; u < KH; ++u) {
+              if (cd < best[u]) {
+                float tf = best[u];
+                int ti = bidx[u];
+                best[u] = cd;
+                bidx[u] = ci;
+                cd = tf;
+                ci = ti;
+              }
+            }
+          }
+        }
+      }
+    }
+    if (q < n) {
+      int32_t* o = cand + q * (2 * KH) + half * KH;
+#pragma unroll
+      for (int i = 0; i < KH; ++i) o[i] = (bidx[i] >= 0 && bidx[i] < n) ? bidx[i] : -1;
+    }
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512)
+                 : "memory");
+  }
+  if (threadIdx.x == 0 && s->err) atomicOr(status, SV_STATUS_LIMIT);
+}
+
+// FP32 row-major [n][dp] -> BF16 row-major [n][64] (zero padded) and the FP32 squared
+// norms of the rounded rows, padded with FLT_MAX up to npad.
+__global__ void k_pack_bf16(const float* __restrict__ X, int64_t n, int dp, int64_t npad,
+                            __nv_bfloat16* __restrict__ Xb, float* __restrict__ sq) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npad;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (i >= n) {
+      sq[i] = FLT_MAX;
+      continue;
+    }
+    float s = 0.f;
+    for (int c = 0; c < BK; ++c) {
+      float v = c < dp ? X[i * dp + c] : 0.f;
+      __nv_bfloat16 b = __float2bfloat16_rn(v);
+      Xb[i * BK + c] = b;
+      float r = __bfloat162float(b);
+      s = fmaf(r, r, s);
+    }
+    sq[i] = s;
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    SV_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p)
+      sv_throw(SV_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available from the driver");
+    fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+}  // namespace
+
+int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unused, int64_t n, int dp,
                          int K2, int include_self, int32_t* cand) {
-  (void)ctx; (void)X32; (void)sq; (void)n; (void)d; (void)K2; (void)include_self; (void)cand;
-  sv_set_error("the BF16 tensor-core kNN path is not built yet");
-  return SV_ERR_UNSUPPORTED;
+  (void)sq_unused;
+  (void)include_self;   // the re-rank places or removes the point itself
+  try {
+    if (dp > BK) sv_throw(SV_ERR_UNSUPPORTED, "tensor-core kNN handles up to %d dimensions", BK);
+    if (K2 != 2 * KH) sv_throw(SV_ERR_UNSUPPORTED, "tensor-core kNN keeps %d candidates", 2 * KH);
+    if (n >= (1ll << 31) - BN) sv_throw(SV_ERR_UNSUPPORTED, "too many points");
+    int ntiles = (int)((n + BN - 1) / BN);
+    int64_t npad = (int64_t)ntiles * BN;
+    DevBuf<__nv_bfloat16> Xb((size_t)n * BK);
+    DevBuf<float> sq(npad);
+    sv_launch(ctx, "knn_pack_bf16", k_pack_bf16, dim3(sv_grid_for(ctx, npad, 256, 8)), dim3(256), 0, X32,
+              n, dp, npad, Xb.get(), sq.get());
+    // the same row-major BF16 matrix seen with two box heights: 128 query rows
+    // and 256 point rows, 64 elements (128 bytes, one swizzle row) wide
+    CUtensorMap tmapA, tmapB;
+    cuuint64_t gdim[2] = {(cuuint64_t)BK, (cuuint64_t)n};
+    cuuint64_t gstride[1] = {(cuuint64_t)BK * 2};
+    cuuint32_t boxA[2] = {(cuuint32_t)BK, (cuuint32_t)BM};
+    cuuint32_t boxB[2] = {(cuuint32_t)BK, (cuuint32_t)BN};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode_fn()(&tmapA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, Xb.get(), gdim, gstride,
+                             boxA, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) sv_throw(SV_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    r = encode_fn()(&tmapB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, Xb.get(), gdim, gstride, boxB, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) sv_throw(SV_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    size_t smem = sizeof(Smem) + 1024;
+    SV_CUDA(cudaFuncSetAttribute(k_knn_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int nblocks = (int)((n + BM - 1) / BM);
+    sv_launch(ctx, "knn_tc_tiles", k_knn_tc, dim3(nblocks), dim3(THREADS), smem, tmapA, tmapB,
+              (const float*)sq.get(), n, ntiles, cand, ctx->d_status);
+    sv_check_device_status(ctx, "tensor-core kNN");
+  } catch (const SvError& e) {
+    return e.code;
+  }
+  return SV_OK;
 }

@@ -91,7 +91,7 @@ __global__ void k_moments(const ValT* __restrict__ val, const int64_t* __restric
       mean_o[f] = meanv;
       std_o[f] = sd;
       mu_o[f] = mu;
-      inv_d[f] = sd;                                // FP64 path divides by std
+      inv_d[f] = 1.0 / sd;                          // a * (1/std): within 1 ulp of a/std
       clip_d[f] = scale_max + mu;                   // scaling.jl:209
       inv_f[f] = (float)(1.0 / sd);
       clip_f[f] = (float)(scale_max + mu);
@@ -204,7 +204,8 @@ struct AccOf<double> {
 // y = alpha * (B x - (mu . x)) + beta * y - (csub ? *csub : 0) * z
 // Per-feature table in shared memory.  FP32 form: (P, Q) = (inv*x, clip*x); the
 // product term is min(a*P, Q) for x >= 0 and max(a*P, Q) for x < 0 (= min(a*inv,
-// clip)*x).  FP64 form: (std, clip, x) with the reference's a/std division.
+// clip)*x).  FP64 form: (1/std, clip, x); a * (1/std) is within one ulp of the
+// reference's a/std (FP64 division is slow on this part).
 template <typename ValT, typename IdxT>
 __global__ void __launch_bounds__(256) k_spmv_csr(
     const int64_t* __restrict__ rowptr, const IdxT* __restrict__ hcol, const ValT* __restrict__ hval,
@@ -270,7 +271,7 @@ __global__ void __launch_bounds__(256) k_spmv_csr(
             acc += pq.x >= 0.f ? fminf(rr, pq.y) : fmaxf(rr, pq.y);
           } else {
             const double* tab = (const double*)smem_raw;
-            double v = av[t] / tab[3 * ci[t]];          // scaling.jl:211
+            double v = av[t] * tab[3 * ci[t]];          // scaling.jl:211 (times 1/std)
             double c = tab[3 * ci[t] + 1];
             acc += (v > c ? c : v) * tab[3 * ci[t] + 2];  // scaling.jl:212
           }
@@ -347,7 +348,7 @@ __global__ void __launch_bounds__(256) k_spmv_csc_chunks(
 #pragma unroll
         for (int t = 0; t < 4; ++t)
           if (g + t >= s && g + t < e) {
-            double v = av[t] / sd;
+            double v = av[t] * sd;   // sd holds 1/std
             acc += (v > clip ? clip : v) * __ldg(ud + ri[t]);
           }
       }

@@ -94,6 +94,37 @@ def test_findneighbours_dropins(sv, O, name, dt):
     assert _check_sets(idx, X, k, True, metric, O=O) == 0
 
 
+def _recall(idx1, X, k, include_self, metric, O):
+    ridx, _ = O.knn_exact(X, k, include_self, metric)
+    hits = sum(len(set(a - 1) & set(b)) for a, b in zip(idx1, ridx))
+    return hits / ridx.size
+
+
+@pytest.mark.parametrize("n,d,k", [(100, 10, 4), (300, 50, 20), (1000, 50, 20), (4099, 37, 30),
+                                   (2600, 64, 16)])
+def test_knn_bf16_tensor_cores(sv, ctx, O, n, d, k):
+    """BF16 tcgen05 candidates + FP32 exact re-rank: recall against FP64 exact."""
+    rng = np.random.default_rng(n + d)
+    means = rng.normal(0, 4, (20, d))
+    X = means[rng.integers(0, 20, n)] + rng.standard_normal((n, d)) / np.sqrt(np.arange(1, d + 1))
+    X = X.astype(np.float32)
+    idx, dist = sv.ann(X, k, precision="bf16", ctx=ctx)
+    assert np.all(idx[:, 0] == np.arange(1, n + 1))
+    assert _recall(idx, X, k, True, "euclidean", O) >= 0.999
+    # results agree with the FP32 path except for near-ties
+    assert _check_sets(idx, X, k, True, "euclidean", tie_rtol=1e-4, O=O) <= 0.001 * n * k
+
+
+def test_knn_bf16_exclude_self_and_cosine(sv, ctx, O):
+    rng = np.random.default_rng(9)
+    X = rng.standard_normal((1500, 24)).astype(np.float32)
+    idx, _ = sv.ann(X, 10, include_self=False, precision="bf16", ctx=ctx)
+    assert not np.any(idx == np.arange(1, 1501)[:, None])
+    assert _recall(idx, X, 10, False, "euclidean", O) >= 0.999
+    idx, _ = sv.ann(X, 10, metric="cosine", precision="bf16", ctx=ctx)
+    assert _recall(idx, X, 10, True, "cosine", O) >= 0.999
+
+
 def test_knn_bad_k(sv, ctx):
     with pytest.raises(sv.SeveroGPUError):
         sv.ann(np.zeros((5, 3)), 6, ctx=ctx)
