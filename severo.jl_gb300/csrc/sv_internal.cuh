@@ -202,6 +202,8 @@ struct sv_centered {
   DevBuf<float> u_f32;                // n_cells
   DevBuf<double> red_partial;         // reduction partials
   DevBuf<double> scal;                // small device scalars
+  int t_blocks = 0;                   // > 0: X^T u over CSR_h with this many blocks
+  DevBuf<unsigned char> t_partial;    // t_blocks x nf partial sums
   // set when the matrix was built by sv_centered_create (owned here)
   sv_counts* own_counts = nullptr;
   sv_data* own_data = nullptr;

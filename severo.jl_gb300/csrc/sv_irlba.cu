@@ -4,12 +4,19 @@
 //
 //   A V_j = W_j B_j,  A^T W_j = V_j B_j^T + f e_j^T      (A = Xs, m x n)
 //
-// Both Lanczos bases live in HBM in FP64, column-major: W (m x work, the cell
-// side, 1.3M x 57 doubles at the atlas size) and V (n x work, the feature side).
+// Both Lanczos bases live in HBM, column-major: W (m x work, the cell side,
+// 1.3M x 57 at the atlas size) and V (n x work, the feature side).  They are held
+// in double-float form -- each value as an unevaluated sum hi + lo of two FP32
+// numbers (about 48 significand bits) -- and all basis arithmetic runs on the
+// FP32 pipe with exact two-product / two-sum steps: GB300 executes FP64 at
+// 1/57 of its FP32 rate, and the reorthogonalisation and restart rotation are
+// the only O(m * work) arithmetic of the method.  Reductions across blocks,
+// the norms, the small matrix B and its SVD are FP64.
+//
 // Every new vector is reorthogonalised against its basis by classical
-// Gram-Schmidt applied twice (CGS2) in FP64.  After `work` steps the small
-// matrix B (work x work, upper triangular) is decomposed by a one-block FP64
-// one-sided Jacobi SVD; the nu leading Ritz vectors are kept (thick restart):
+// Gram-Schmidt applied twice (CGS2).  After `work` steps B (work x work, upper
+// triangular) is decomposed by a one-block FP64 one-sided Jacobi SVD; the nu
+// leading Ritz vectors are kept (thick restart):
 //   V <- [V Q_k, f/|f|],  W <- W P_k,  B <- [diag(s_k) rho; 0 ...],
 //   rho_i = |f| P[work-1, i]
 // and convergence is declared when every |rho_i| < tol * max singular value
@@ -23,8 +30,41 @@ void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const 
 
 namespace {
 
-constexpr int RED_BLOCKS = 256;    // blocks of the tall reductions
+constexpr int RED_BLOCKS = 608;    // blocks of the tall reductions (4 per SM)
 constexpr int MAX_WORK = 96;       // largest Lanczos basis the Jacobi kernel holds in smem
+constexpr int JB = 8;              // basis columns per pass of the dot-product kernel
+
+// ---- double-float arithmetic --------------------------------------------------
+__device__ __forceinline__ void df_split(double x, float& h, float& l) {
+  h = (float)x;
+  l = (float)(x - (double)h);
+}
+__device__ __forceinline__ double df_val(float h, float l) { return (double)h + (double)l; }
+
+// s += a * b: exact product of the high parts (FMA), first-order cross terms,
+// two-sum accumulation of the high part
+__device__ __forceinline__ void df_fma(float& sh, float& sl, float ah, float al, float bh, float bl) {
+  float p = ah * bh;
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, e);
+  e = fmaf(al, bh, e);
+  float t = sh + p;
+  float v = t - sh;
+  float err = (sh - (t - v)) + (p - v);
+  sh = t;
+  sl += err + e;
+}
+
+// (xh, xl) - (sh, sl), renormalised
+__device__ __forceinline__ void df_sub(float& xh, float& xl, float sh, float sl) {
+  float t = xh - sh;
+  float v = t - xh;
+  float err = (xh - (t - v)) + (-sh - v);
+  float lo = err + xl - sl;
+  float h = t + lo;
+  xl = lo - (h - t);
+  xh = h;
+}
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
   v = sv_warp_sum(v);
@@ -40,29 +80,56 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return r;  // valid in thread 0
 }
 
-// c[j] = Q[:, j] . x  (j < ncols), per-block partials, the last block to finish
-// sums them in block order (deterministic) and writes c.
-__global__ void __launch_bounds__(256) k_dots(const double* __restrict__ Q, int64_t ld, int ncols,
-                                              const double* __restrict__ x, int64_t len,
-                                              double* __restrict__ part, double* __restrict__ c,
-                                              unsigned int* __restrict__ counter) {
-  __shared__ double sh[32];
-  __shared__ bool last;
-  int64_t seg = (len + gridDim.x - 1) / gridDim.x;
-  int64_t r0 = (int64_t)blockIdx.x * seg, r1 = min(len, r0 + seg);
-  for (int j = 0; j < ncols; ++j) {
-    const double* q = Q + (int64_t)j * ld;
-    double acc = 0;
-    for (int64_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) acc += q[i] * x[i];
-    acc = block_sum(acc, sh);
-    if (threadIdx.x == 0) part[(int64_t)blockIdx.x * ncols + j] = acc;
-  }
+// last-block pattern: every block has written its partials; the last one to
+// arrive sums them in block order (deterministic) and resets the counter
+__device__ __forceinline__ bool last_block(unsigned int* counter, bool* flag_smem) {
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  if (threadIdx.x == 0) *flag_smem = atomicAdd(counter, 1u) == gridDim.x - 1;
   __syncthreads();
-  if (last) {
-    __threadfence();
+  if (*flag_smem) __threadfence();
+  return *flag_smem;
+}
+
+// c[j] = Q[:, j] . x  (j < ncols): Q and x double-float; per-block FP64 partials.
+// Block of 8 warps over a contiguous row segment; warp w owns the columns
+// j = w, w + 8, ... (at most NJ of them), lanes walk 32 consecutive rows, so every
+// basis element is read once with coalesced loads and each warp reduces its
+// columns across lanes once at the end.
+constexpr int NJ = (MAX_WORK + 7) / 8;
+__global__ void __launch_bounds__(256) k_dots_df(const float* __restrict__ Qh,
+                                                 const float* __restrict__ Ql, int64_t ld,
+                                                 int ncols, const float* __restrict__ xh,
+                                                 const float* __restrict__ xl, int64_t len,
+                                                 double* __restrict__ part, double* __restrict__ c,
+                                                 unsigned int* __restrict__ counter) {
+  __shared__ bool last;
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int64_t seg = (len + gridDim.x - 1) / gridDim.x;
+  int64_t r0 = (int64_t)blockIdx.x * seg, r1 = min(len, r0 + seg);
+  float ah[NJ], al[NJ];
+#pragma unroll
+  for (int t = 0; t < NJ; ++t) ah[t] = al[t] = 0.f;
+  for (int64_t i = r0 + lane; i < r1; i += 32) {
+    float bh = xh[i], bl = xl[i];
+#pragma unroll
+    for (int t = 0; t < NJ; ++t) {
+      int j = w + 8 * t;
+      if (j < ncols) {
+        int64_t o = (int64_t)j * ld + i;
+        df_fma(ah[t], al[t], Qh[o], Ql[o], bh, bl);
+      }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < NJ; ++t) {
+    int j = w + 8 * t;
+    if (j < ncols) {
+      double v = sv_warp_sum(df_val(ah[t], al[t]));
+      if (lane == 0) part[(int64_t)blockIdx.x * ncols + j] = v;
+    }
+  }
+  if (last_block(counter, &last)) {
     for (int j = threadIdx.x; j < ncols; j += blockDim.x) {
       double s = 0;
       for (unsigned b = 0; b < gridDim.x; ++b) s += part[(int64_t)b * ncols + j];
@@ -72,35 +139,43 @@ __global__ void __launch_bounds__(256) k_dots(const double* __restrict__ Q, int6
   }
 }
 
-// x -= Q[:, :ncols] c ; optionally nrm = ||x|| (after the update).
-__global__ void __launch_bounds__(256) k_update_norm(double* __restrict__ x, int64_t len,
-                                                     const double* __restrict__ Q, int64_t ld,
-                                                     int ncols, const double* __restrict__ c,
-                                                     double* __restrict__ part,
-                                                     double* __restrict__ nrm,
-                                                     unsigned int* __restrict__ counter) {
+// x -= Q[:, :ncols] c (double-float); optionally *nrm = ||x|| afterwards.
+__global__ void __launch_bounds__(256) k_update_df(float* __restrict__ xh, float* __restrict__ xl,
+                                                   int64_t len, const float* __restrict__ Qh,
+                                                   const float* __restrict__ Ql, int64_t ld,
+                                                   int ncols, const double* __restrict__ c,
+                                                   double* __restrict__ part,
+                                                   double* __restrict__ nrm,
+                                                   unsigned int* __restrict__ counter) {
   __shared__ double sh[32];
-  __shared__ double cs[MAX_WORK];
+  __shared__ float chs[MAX_WORK], cls[MAX_WORK];
   __shared__ bool last;
-  for (int j = threadIdx.x; j < ncols; j += blockDim.x) cs[j] = c[j];
+  for (int j = threadIdx.x; j < ncols; j += blockDim.x) df_split(c[j], chs[j], cls[j]);
   __syncthreads();
   double acc = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
        i += (int64_t)gridDim.x * blockDim.x) {
-    double v = x[i];
-    for (int j = 0; j < ncols; ++j) v -= Q[(int64_t)j * ld + i] * cs[j];
-    if (ncols) x[i] = v;
-    acc += v * v;
+    float h = xh[i], l = xl[i];
+    if (ncols) {
+      float sh_ = 0.f, sl_ = 0.f;
+#pragma unroll 8
+      for (int j = 0; j < ncols; ++j) {
+        int64_t o = (int64_t)j * ld + i;
+        df_fma(sh_, sl_, Qh[o], Ql[o], chs[j], cls[j]);
+      }
+      df_sub(h, l, sh_, sl_);
+      xh[i] = h;
+      xl[i] = l;
+    }
+    if (nrm) {
+      double v = df_val(h, l);
+      acc += v * v;
+    }
   }
   if (!nrm) return;
   acc = block_sum(acc, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (last) {
-    __threadfence();
+  if (last_block(counter, &last)) {
     if (threadIdx.x == 0) {
       double s = 0;
       for (unsigned b = 0; b < gridDim.x; ++b) s += part[b];
@@ -108,6 +183,14 @@ __global__ void __launch_bounds__(256) k_update_norm(double* __restrict__ x, int
       *counter = 0;
     }
   }
+}
+
+// FP64 vector -> double-float working vector
+__global__ void k_to_df(const double* __restrict__ y, int64_t len, float* __restrict__ xh,
+                        float* __restrict__ xl) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    df_split(y[i], xh[i], xl[i]);
 }
 
 __device__ __forceinline__ unsigned long long mixbits(unsigned long long z) {
@@ -124,35 +207,46 @@ __device__ __forceinline__ double normal_at(unsigned long long seed, unsigned lo
   return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);    // Box-Muller
 }
 
-// out = in / *nrm and the B entry := *nrm; when *nrm < thresh the Krylov space is
-// (numerically) invariant: out := a random vector, B entry and *nrm := 0, flag set
-// for k_fix, which orthonormalises it against the basis.
-__global__ void k_scal(double* __restrict__ out, const double* __restrict__ in, int64_t len,
-                       double* __restrict__ nrm, double thresh, double* __restrict__ bentry,
-                       int* __restrict__ flag, unsigned long long seed, unsigned long long tag) {
+// Basis column := x / *nrm (double-float) and cur := the same in FP64; the B
+// entry := *nrm.  When *nrm < thresh the Krylov space is (numerically)
+// invariant: cur := a random vector, B entry := 0, flag set for k_fix_df, which
+// orthonormalises cur against the basis and writes the column.
+__global__ void k_scal_df(const float* __restrict__ xh, const float* __restrict__ xl, int64_t len,
+                          const double* __restrict__ nrm, double thresh, float* __restrict__ colh,
+                          float* __restrict__ coll, double* __restrict__ cur,
+                          double* __restrict__ bentry, int* __restrict__ flag,
+                          unsigned long long seed, unsigned long long tag) {
   double s = *nrm;
   bool brk = !(s >= thresh);
+  double inv = brk ? 0.0 : 1.0 / s;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
-       i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = brk ? normal_at(seed, tag, i) : in[i] / s;
-  __syncthreads();
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (brk) {
+      cur[i] = normal_at(seed, tag, i);
+    } else {
+      double v = df_val(xh[i], xl[i]) * inv;
+      cur[i] = v;
+      df_split(v, colh[i], coll[i]);
+    }
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     if (bentry) *bentry = brk ? 0.0 : s;
-    if (brk) {
-      *flag = 1;
-    }
+    if (brk) *flag = 1;
   }
 }
 
-// second half of the breakdown branch: zero the norm slot once all blocks of
-// k_scal have read it (separate launch)
+// zero the norm slot (the sub-diagonal scalar the next product uses) when a
+// breakdown was flagged; separate launch so every k_scal_df block has read it
 __global__ void k_scal_post(double* nrm, const int* flag) {
   if (*flag) *nrm = 0.0;
 }
 
-// One block: if *flag, x <- CGS2(x, Q[:, :ncols]) normalised; clears the flag.
-__global__ void k_fix(double* __restrict__ x, int64_t len, const double* __restrict__ Q, int64_t ld,
-                      int ncols, int* __restrict__ flag) {
+// One block: if *flag, cur <- CGS2(cur, Q[:, :ncols]) normalised (FP64
+// arithmetic on the double-float basis), written to the basis column as well;
+// clears the flag.  Runs only on a breakdown.
+__global__ void k_fix_df(double* __restrict__ cur, int64_t len, const float* __restrict__ Qh,
+                         const float* __restrict__ Ql, int64_t ld, int ncols, float* __restrict__ colh,
+                         float* __restrict__ coll, int* __restrict__ flag) {
   __shared__ double sh[32];
   __shared__ double cs[MAX_WORK];
   __shared__ double tot;
@@ -160,27 +254,137 @@ __global__ void k_fix(double* __restrict__ x, int64_t len, const double* __restr
   for (int pass = 0; pass < 2; ++pass) {
     for (int j = 0; j < ncols; ++j) {
       double acc = 0;
-      for (int64_t i = threadIdx.x; i < len; i += blockDim.x) acc += Q[(int64_t)j * ld + i] * x[i];
+      for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
+        int64_t o = (int64_t)j * ld + i;
+        acc += df_val(Qh[o], Ql[o]) * cur[i];
+      }
       acc = block_sum(acc, sh);
       if (threadIdx.x == 0) cs[j] = acc;
     }
     __syncthreads();
     for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
-      double v = x[i];
-      for (int j = 0; j < ncols; ++j) v -= Q[(int64_t)j * ld + i] * cs[j];
-      x[i] = v;
+      double v = cur[i];
+      for (int j = 0; j < ncols; ++j) {
+        int64_t o = (int64_t)j * ld + i;
+        v -= df_val(Qh[o], Ql[o]) * cs[j];
+      }
+      cur[i] = v;
     }
     __syncthreads();
   }
   double acc = 0;
-  for (int64_t i = threadIdx.x; i < len; i += blockDim.x) acc += x[i] * x[i];
+  for (int64_t i = threadIdx.x; i < len; i += blockDim.x) acc += cur[i] * cur[i];
   acc = block_sum(acc, sh);
   if (threadIdx.x == 0) tot = sqrt(acc);
   __syncthreads();
   double s = tot;
-  for (int64_t i = threadIdx.x; i < len; i += blockDim.x) x[i] = x[i] / s;
+  for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
+    double v = cur[i] / s;
+    cur[i] = v;
+    df_split(v, colh[i], coll[i]);
+  }
   __syncthreads();
   if (threadIdx.x == 0) *flag = 0;
+}
+
+// The whole feature-side step in one block (the feature side is short: a few
+// thousand entries): x = F (FP64 in, double-float working copy in xh/xl); CGS2
+// against V[:, :ncols]; *nrm = |x|; when write_col >= 0 the column write_col :=
+// x/|x| (double-float, FP64 copy in cur) and *bentry = |x|, or on a breakdown
+// (|x| < thresh) a random vector orthonormalised against V[:, :ncols] with
+// *bentry = *nrm = 0.  write_col < 0 (last step of a cycle) leaves the residual
+// in xh/xl.
+__device__ void vside_cgs2(float* __restrict__ xh, float* __restrict__ xl, int64_t len,
+                           const float* __restrict__ Vh, const float* __restrict__ Vl, int ncols,
+                           double* c, float* ch, float* cl) {
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int pass = 0; pass < 2 && ncols > 0; ++pass) {
+    for (int j = w; j < ncols; j += nw) {
+      float ah = 0.f, al = 0.f;
+      const float* qh = Vh + (int64_t)j * len;
+      const float* ql = Vl + (int64_t)j * len;
+      for (int64_t i = lane; i < len; i += 32) df_fma(ah, al, qh[i], ql[i], xh[i], xl[i]);
+      double v = sv_warp_sum(df_val(ah, al));
+      if (lane == 0) c[j] = v;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < ncols; j += blockDim.x) df_split(c[j], ch[j], cl[j]);
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
+      float sh_ = 0.f, sl_ = 0.f;
+      for (int j = 0; j < ncols; ++j) {
+        int64_t o = (int64_t)j * len + i;
+        df_fma(sh_, sl_, Vh[o], Vl[o], ch[j], cl[j]);
+      }
+      float h = xh[i], l = xl[i];
+      df_sub(h, l, sh_, sl_);
+      xh[i] = h;
+      xl[i] = l;
+    }
+    __syncthreads();
+  }
+}
+
+__device__ double vside_norm(const float* __restrict__ xh, const float* __restrict__ xl, int64_t len,
+                             double* sh, double* tot) {
+  double acc = 0;
+  for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
+    double v = df_val(xh[i], xl[i]);
+    acc += v * v;
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) *tot = sqrt(acc);
+  __syncthreads();
+  return *tot;
+}
+
+__global__ void __launch_bounds__(1024) k_vside(const double* __restrict__ F, int64_t len,
+                                                float* __restrict__ Vh, float* __restrict__ Vl,
+                                                int ncols, int write_col, double* __restrict__ nrm,
+                                                double thresh, double* __restrict__ bentry,
+                                                double* __restrict__ cur, float* __restrict__ xh,
+                                                float* __restrict__ xl, unsigned long long seed,
+                                                unsigned long long tag) {
+  __shared__ double c[MAX_WORK];
+  __shared__ float ch[MAX_WORK], cl[MAX_WORK];
+  __shared__ double sh[32];
+  __shared__ double tot;
+  for (int64_t i = threadIdx.x; i < len; i += blockDim.x) df_split(F[i], xh[i], xl[i]);
+  __syncthreads();
+  vside_cgs2(xh, xl, len, Vh, Vl, ncols, c, ch, cl);
+  double s = vside_norm(xh, xl, len, sh, &tot);
+  if (write_col < 0) {
+    if (threadIdx.x == 0) *nrm = s;
+    return;
+  }
+  bool brk = !(s >= thresh);
+  if (brk) {
+    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) df_split(normal_at(seed, tag, i), xh[i], xl[i]);
+    __syncthreads();
+    vside_cgs2(xh, xl, len, Vh, Vl, ncols, c, ch, cl);
+    double r = vside_norm(xh, xl, len, sh, &tot);
+    double inv = 1.0 / r;
+    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
+      double v = df_val(xh[i], xl[i]) * inv;
+      cur[i] = v;
+      df_split(v, Vh[(int64_t)write_col * len + i], Vl[(int64_t)write_col * len + i]);
+    }
+    if (threadIdx.x == 0) {
+      *nrm = 0.0;
+      if (bentry) *bentry = 0.0;
+    }
+  } else {
+    double inv = 1.0 / s;
+    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
+      double v = df_val(xh[i], xl[i]) * inv;
+      cur[i] = v;
+      df_split(v, Vh[(int64_t)write_col * len + i], Vl[(int64_t)write_col * len + i]);
+    }
+    if (threadIdx.x == 0) {
+      *nrm = s;
+      if (bentry) *bentry = s;
+    }
+  }
 }
 
 // One-sided (Hestenes) Jacobi SVD of B (m x m, row-major) in FP64, one block.
@@ -298,41 +502,63 @@ __global__ void k_jacobi_svd(const double* __restrict__ B, int m, double* __rest
   }
 }
 
-// Out[:, c] = sum_r In[:, r] * M[r + c*nin]  for c < nout   (tall x small, FP64)
+// Out[:, c] = sum_r In[:, r] * M[r + c*nin] for c < nout (tall x small), In
+// double-float; Out double-float (outh/outl) or FP64 (outd).
 template <int KB>
-__global__ void __launch_bounds__(256) k_rotate(const double* __restrict__ In, int64_t ld_in,
-                                                int64_t len, int nin, const double* __restrict__ M,
-                                                int nout, double* __restrict__ Out, int64_t ld_out) {
-  extern __shared__ double Ms[];
-  for (int i = threadIdx.x; i < nin * nout; i += blockDim.x) Ms[i] = M[i];
+__global__ void __launch_bounds__(256) k_rotate_df(const float* __restrict__ Inh,
+                                                   const float* __restrict__ Inl, int64_t ld_in,
+                                                   int64_t len, int nin, const double* __restrict__ M,
+                                                   int nout, float* __restrict__ outh,
+                                                   float* __restrict__ outl, double* __restrict__ outd,
+                                                   int64_t ld_out) {
+  extern __shared__ float Ms[];   // nin*nout pairs (hi, lo)
+  for (int i = threadIdx.x; i < nin * nout; i += blockDim.x) df_split(M[i], Ms[2 * i], Ms[2 * i + 1]);
   __syncthreads();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
        i += (int64_t)gridDim.x * blockDim.x) {
     for (int c0 = 0; c0 < nout; c0 += KB) {
-      double acc[KB];
+      float ah[KB], al[KB];
 #pragma unroll
-      for (int t = 0; t < KB; ++t) acc[t] = 0;
+      for (int t = 0; t < KB; ++t) ah[t] = al[t] = 0.f;
       for (int r = 0; r < nin; ++r) {
-        double w = In[(int64_t)r * ld_in + i];
+        int64_t o = (int64_t)r * ld_in + i;
+        float wh = Inh[o], wl = Inl[o];
 #pragma unroll
         for (int t = 0; t < KB; ++t)
-          if (c0 + t < nout) acc[t] += w * Ms[r + (c0 + t) * nin];
+          if (c0 + t < nout) {
+            int mi = 2 * (r + (c0 + t) * nin);
+            df_fma(ah[t], al[t], wh, wl, Ms[mi], Ms[mi + 1]);
+          }
       }
 #pragma unroll
       for (int t = 0; t < KB; ++t)
-        if (c0 + t < nout) Out[(int64_t)(c0 + t) * ld_out + i] = acc[t];
+        if (c0 + t < nout) {
+          int64_t o = (int64_t)(c0 + t) * ld_out + i;
+          if (outd) {
+            outd[o] = df_val(ah[t], al[t]);
+          } else {
+            // renormalise the pair
+            float h = ah[t] + al[t];
+            outh[o] = h;
+            outl[o] = al[t] - (h - ah[t]);
+          }
+        }
     }
   }
 }
 
-// V[:, k] = F / rf and B reset for the next cycle.
-__global__ void k_restart_tail(double* __restrict__ vk, const double* __restrict__ F, int64_t n,
+// V[:, k] = F / rf (double-float column + FP64 current vector) and B reset.
+__global__ void k_restart_tail(float* __restrict__ vkh, float* __restrict__ vkl,
+                               double* __restrict__ vcur, const double* __restrict__ F, int64_t n,
                                const double* __restrict__ summary, int m, int k,
                                double* __restrict__ B) {
   double rf = summary[2 * m];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    vk[i] = F[i] / rf;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v = F[i] / rf;
+    vcur[i] = v;
+    df_split(v, vkh[i], vkl[i]);
+  }
   if (blockIdx.x == 0) {
     for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
       int r = idx / m, c = idx % m;
@@ -342,6 +568,13 @@ __global__ void k_restart_tail(double* __restrict__ vk, const double* __restrict
       B[idx] = v;
     }
   }
+}
+
+__global__ void k_df_to_fp64(const float* __restrict__ h, const float* __restrict__ l, int64_t len,
+                             double* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = df_val(h[i], l[i]);
 }
 
 __global__ void k_axpy_sub(double* __restrict__ y, const double* __restrict__ z,
@@ -415,23 +648,45 @@ struct IrlbaResult {
   int64_t iters = 0, nmatvec = 0;
 };
 
+// One side of the bidiagonalisation: a double-float basis (len x work), its
+// rotation buffer, the double-float working vector and the FP64 copy of the
+// current basis vector (the input of the next product).
+struct Side {
+  int64_t len = 0;
+  DevBuf<float> h, l, th, tl;   // basis and rotation target
+  DevBuf<float> xh, xl;         // working vector
+  DevBuf<double> cur;           // current basis vector, FP64
+  void alloc(int64_t n, int work) {
+    len = n;
+    h.alloc(n * work);
+    l.alloc(n * work);
+    th.alloc(n * work);
+    tl.alloc(n * work);
+    xh.alloc(n);
+    xl.alloc(n);
+    cur.alloc(n);
+  }
+  float* ch(int j) { return h.get() + (int64_t)j * len; }
+  float* cl(int j) { return l.get() + (int64_t)j * len; }
+};
+
 // The Lanczos driver.  m = rows of A (the W side), n = columns (the V side).
 struct Lanczos {
   sv_context* ctx;
   Op* op;
   int64_t m, n;
   int nu, work;
-  DevBuf<double> V, W, Vt, Wt, F, B, P, Q, sig, summary, scal, part, cvec;
+  Side Ws, Vs;
+  DevBuf<double> ytmp, F, B, P, Q, sig, summary, scal, part, cvec, Ufin, Vfin;
   DevBuf<unsigned int> counter;
   DevBuf<int> flag;
   std::vector<double> hsum;
 
   Lanczos(sv_context* c, Op* o, int64_t m_, int64_t n_, int nu_, int work_)
       : ctx(c), op(o), m(m_), n(n_), nu(nu_), work(work_) {
-    V.alloc(n * work);
-    Vt.alloc(n * work);
-    W.alloc(m * work);
-    Wt.alloc(m * work);
+    Ws.alloc(m, work);
+    Vs.alloc(n, work);
+    ytmp.alloc(std::max(m, n));
     F.alloc(n);
     B.alloc(work * work);
     P.alloc(work * work);
@@ -449,39 +704,69 @@ struct Lanczos {
     hsum.resize(2 * work + 2);
     SV_CUDA(cudaFuncSetAttribute(k_jacobi_svd, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  2 * MAX_WORK * MAX_WORK * 8));
-    SV_CUDA(cudaFuncSetAttribute(k_rotate<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    SV_CUDA(cudaFuncSetAttribute(k_rotate_df<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  MAX_WORK * MAX_WORK * 8));
   }
 
-  int red_grid(int64_t len) { return (int)std::min<int64_t>(RED_BLOCKS, std::max<int64_t>(1, (len + 1023) / 1024)); }
+  int red_grid(int64_t len) {
+    return (int)std::min<int64_t>(RED_BLOCKS, std::max<int64_t>(1, (len + 255) / 256));
+  }
 
-  // x <- CGS2(x, Qb[:, :ncols]); *nrm = ||x||
-  void orth_norm(double* x, int64_t len, const double* Qb, int ncols, double* nrm) {
-    int g = red_grid(len);
+  // working vector <- CGS2(working vector, basis[:, :ncols]); *nrm = its norm
+  void orth_norm(Side& s, int ncols, double* nrm) {
+    int g = red_grid(s.len);
     for (int pass = 0; pass < 2 && ncols > 0; ++pass) {
-      sv_launch(ctx, "irlba_dots", k_dots, dim3(g), dim3(256), 0, Qb, len, ncols, (const double*)x, len,
-                part.get(), cvec.get(), counter.get());
-      sv_launch(ctx, "irlba_update", k_update_norm, dim3(g), dim3(256), 0, x, len, Qb, len, ncols,
+      sv_launch(ctx, "irlba_dots", k_dots_df, dim3(g), dim3(256), 0, (const float*)s.h.get(),
+                (const float*)s.l.get(), s.len, ncols, (const float*)s.xh.get(),
+                (const float*)s.xl.get(), s.len, part.get(), cvec.get(), counter.get());
+      sv_launch(ctx, "irlba_update", k_update_df, dim3(g), dim3(256), 0, s.xh.get(), s.xl.get(), s.len,
+                (const float*)s.h.get(), (const float*)s.l.get(), s.len, ncols,
                 (const double*)cvec.get(), part.get(), pass == 1 ? nrm : (double*)nullptr,
                 counter.get());
     }
     if (ncols == 0)
-      sv_launch(ctx, "irlba_update", k_update_norm, dim3(g), dim3(256), 0, x, len, Qb, len, 0,
+      sv_launch(ctx, "irlba_update", k_update_df, dim3(g), dim3(256), 0, s.xh.get(), s.xl.get(), s.len,
+                (const float*)s.h.get(), (const float*)s.l.get(), s.len, 0,
                 (const double*)cvec.get(), part.get(), nrm, counter.get());
   }
 
-  void scal_fix(double* out, const double* in, int64_t len, double* nrm, double thresh,
-                double* bentry, const double* basis, int ncols, uint64_t seed, uint64_t tag) {
-    sv_launch(ctx, "irlba_scal", k_scal, dim3(sv_grid_for(ctx, len, 256, 4)), dim3(256), 0, out, in,
-              len, nrm, thresh, bentry, flag.get(), (unsigned long long)seed,
+  // basis column j := working vector / *nrm (FP64 copy in cur), breakdown handling
+  void scal_fix(Side& s, int j, double* nrm, double thresh, double* bentry, uint64_t seed,
+                uint64_t tag) {
+    sv_launch(ctx, "irlba_scal", k_scal_df, dim3(sv_grid_for(ctx, s.len, 256, 4)), dim3(256), 0,
+              (const float*)s.xh.get(), (const float*)s.xl.get(), s.len, (const double*)nrm, thresh,
+              s.ch(j), s.cl(j), s.cur.get(), bentry, flag.get(), (unsigned long long)seed,
               (unsigned long long)tag);
     sv_launch(ctx, "irlba_scal_post", k_scal_post, dim3(1), dim3(1), 0, nrm, (const int*)flag.get());
-    sv_launch(ctx, "irlba_fix", k_fix, dim3(1), dim3(1024), 0, out, len, basis, len, ncols, flag.get());
+    sv_launch(ctx, "irlba_fix", k_fix_df, dim3(1), dim3(1024), 0, s.cur.get(), s.len,
+              (const float*)s.h.get(), (const float*)s.l.get(), s.len, j, s.ch(j), s.cl(j),
+              flag.get());
   }
 
-  void rotate(const double* In, int64_t len, const double* M, int nout, double* Out) {
-    sv_launch(ctx, "irlba_rotate", k_rotate<16>, dim3(sv_grid_for(ctx, len, 256, 8)), dim3(256),
-              (size_t)work * nout * 8, In, len, len, work, M, nout, Out, len);
+  // the feature-side step in one launch (see k_vside)
+  void vside(int ncols, int write_col, double* nrm, double thresh, double* bentry, uint64_t seed,
+             uint64_t tag) {
+    if (n > 32768) {   // long feature side: the multi-block kernels
+      to_working(Vs, F.get());
+      orth_norm(Vs, ncols, nrm);
+      if (write_col >= 0) scal_fix(Vs, write_col, nrm, thresh, bentry, seed, tag);
+      return;
+    }
+    sv_launch(ctx, "irlba_vside", k_vside, dim3(1), dim3(1024), 0, (const double*)F.get(), n,
+              Vs.h.get(), Vs.l.get(), ncols, write_col, nrm, thresh, bentry, Vs.cur.get(),
+              Vs.xh.get(), Vs.xl.get(), (unsigned long long)seed, (unsigned long long)tag);
+  }
+
+  void to_working(Side& s, const double* y) {
+    sv_launch(ctx, "irlba_to_df", k_to_df, dim3(sv_grid_for(ctx, s.len, 256, 4)), dim3(256), 0, y,
+              s.len, s.xh.get(), s.xl.get());
+  }
+
+  void rotate(Side& s, const double* M, int nout, double* outd) {
+    sv_launch(ctx, "irlba_rotate", k_rotate_df<16>, dim3(sv_grid_for(ctx, s.len, 256, 8)), dim3(256),
+              (size_t)work * nout * 8, (const float*)s.h.get(), (const float*)s.l.get(), s.len, s.len,
+              work, M, nout, outd ? (float*)nullptr : s.th.get(), outd ? (float*)nullptr : s.tl.get(),
+              outd, s.len);
   }
 
   IrlbaResult run(const double* init_host, int maxit, double tol, uint64_t seed) {
@@ -489,9 +774,8 @@ struct Lanczos {
     double* s0 = scal.get();       // S (W-side norm)
     double* s1 = scal.get() + 1;   // R (V-side norm)
     sv_h2d(ctx, F.get(), init_host, n * 8);
-    orth_norm(F.get(), n, V.get(), 0, s1);
     const double eps_b = sqrt(2.220446049250313e-16);
-    scal_fix(V.get(), F.get(), n, s1, 1e-300, nullptr, V.get(), 0, seed, 0);
+    vside(0, 0, s1, 1e-300, nullptr, seed, 0);
     int k = 0;
     double smax = 0;
     uint64_t tag = 1;
@@ -499,30 +783,27 @@ struct Lanczos {
     for (; it < maxit; ++it) {
       double thresh = eps_b * std::max(smax, 1.0);
       int j = k;
-      double* Vj = V.get() + (int64_t)j * n;
-      double* Wj = W.get() + (int64_t)j * m;
-      op->N(Vj, Wj, nullptr, nullptr);
+      // W[:, j] = A V[:, j]; CGS2 against W[:, :j]
+      op->N(Vs.cur.get(), ytmp.get(), nullptr, nullptr);
       res.nmatvec++;
-      orth_norm(Wj, m, W.get(), j, s0);
-      scal_fix(Wj, Wj, m, s0, thresh, B.get() + (int64_t)j * work + j, W.get(), j, seed, tag++);
+      to_working(Ws, ytmp.get());
+      orth_norm(Ws, j, s0);
+      scal_fix(Ws, j, s0, thresh, B.get() + (int64_t)j * work + j, seed, tag++);
       while (true) {
-        Vj = V.get() + (int64_t)j * n;
-        Wj = W.get() + (int64_t)j * m;
-        op->T(Wj, F.get(), s0, Vj);
+        // F = A^T W[:, j] - S V[:, j]; CGS2 against V[:, :j+1]
+        op->T(Ws.cur.get(), F.get(), s0, Vs.cur.get());
         res.nmatvec++;
-        orth_norm(F.get(), n, V.get(), j + 1, s1);
         if (j + 1 < work) {
-          double* Vn = V.get() + (int64_t)(j + 1) * n;
-          double* Wn = W.get() + (int64_t)(j + 1) * m;
-          scal_fix(Vn, F.get(), n, s1, thresh, B.get() + (int64_t)j * work + j + 1, V.get(), j + 1,
-                   seed, tag++);
-          op->N(Vn, Wn, s1, Wj);
+          vside(j + 1, j + 1, s1, thresh, B.get() + (int64_t)j * work + j + 1, seed, tag++);
+          // W[:, j+1] = A V[:, j+1] - R W[:, j]
+          op->N(Vs.cur.get(), ytmp.get(), s1, Ws.cur.get());
           res.nmatvec++;
-          orth_norm(Wn, m, W.get(), j + 1, s0);
-          scal_fix(Wn, Wn, m, s0, thresh, B.get() + (int64_t)(j + 1) * work + j + 1, W.get(), j + 1,
-                   seed, tag++);
+          to_working(Ws, ytmp.get());
+          orth_norm(Ws, j + 1, s0);
+          scal_fix(Ws, j + 1, s0, thresh, B.get() + (int64_t)(j + 1) * work + j + 1, seed, tag++);
           ++j;
         } else {
+          vside(j + 1, -1, s1, thresh, nullptr, seed, tag++);   // residual f and |f|
           break;
         }
       }
@@ -542,24 +823,36 @@ struct Lanczos {
       }
       if (it + 1 >= maxit) break;   // keep P, Q consistent with the bases
       k = std::min(nu, work - 1);
-      // thick restart
-      rotate(V.get(), n, Q.get(), k, Vt.get());
-      rotate(W.get(), m, P.get(), k, Wt.get());
-      std::swap(V, Vt);
-      std::swap(W, Wt);
+      // thick restart: V <- V Q_k, W <- W P_k, V[:, k] = F/|F|
+      rotate(Vs, Q.get(), k, nullptr);
+      rotate(Ws, P.get(), k, nullptr);
+      std::swap(Vs.h, Vs.th);
+      std::swap(Vs.l, Vs.tl);
+      std::swap(Ws.h, Ws.th);
+      std::swap(Ws.l, Ws.tl);
+      df_residual_to_fp64();
       sv_launch(ctx, "irlba_restart", k_restart_tail, dim3(sv_grid_for(ctx, n, 256, 4)), dim3(256), 0,
-                V.get() + (int64_t)k * n, (const double*)F.get(), n, (const double*)summary.get(),
-                work, k, B.get());
+                Vs.ch(k), Vs.cl(k), Vs.cur.get(), (const double*)F.get(), n,
+                (const double*)summary.get(), work, k, B.get());
     }
     if (it >= maxit) res.iters = maxit;
     sv_check_device_status(ctx, "irlba");
     return res;
   }
 
-  // U = W P[:, :nu] -> Wt ; Vout = V Q[:, :nu] -> Vt
+  // F holds the residual in FP64 only before to_working; the orthogonalised
+  // residual lives in the V-side working vector: bring it back to FP64
+  void df_residual_to_fp64() {
+    sv_launch(ctx, "irlba_f_fp64", k_df_to_fp64, dim3(sv_grid_for(ctx, n, 256, 4)), dim3(256), 0,
+              (const float*)Vs.xh.get(), (const float*)Vs.xl.get(), n, F.get());
+  }
+
+  // U = W P[:, :nu], V = V Q[:, :nu] (FP64)
   void finish() {
-    rotate(W.get(), m, P.get(), nu, Wt.get());
-    rotate(V.get(), n, Q.get(), nu, Vt.get());
+    Ufin.alloc(m * nu);
+    Vfin.alloc(n * nu);
+    rotate(Ws, P.get(), nu, Ufin.get());
+    rotate(Vs, Q.get(), nu, Vfin.get());
   }
 };
 
@@ -587,13 +880,12 @@ static int irlba_core(sv_context* ctx, Op* op, int64_t m, int64_t n, int64_t nu,
   IrlbaResult r = L.run(init, (int)maxit, tol, seed);
   L.finish();
   if (s_out) sv_d2h(ctx, s_out, L.sig.get(), nu * 8);
-  if (U) sv_d2h(ctx, U, L.Wt.get(), m * nu * 8);
-  if (V) sv_d2h(ctx, V, L.Vt.get(), n * nu * 8);
+  if (U) sv_d2h(ctx, U, L.Ufin.get(), m * nu * 8);
+  if (V) sv_d2h(ctx, V, L.Vfin.get(), n * nu * 8);
   if (emb) {
-    emb->Z.alloc(m * nu);
     emb->s.alloc(nu);
-    SV_CUDA(cudaMemcpyAsync(emb->Z.get(), L.Wt.get(), m * nu * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     SV_CUDA(cudaMemcpyAsync(emb->s.get(), L.sig.get(), nu * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    emb->Z = std::move(L.Ufin);
     sv_launch(ctx, "pca_scale", k_scale_cols, dim3(sv_grid_for(ctx, m * nu, 256, 8)), dim3(256), 0,
               emb->Z.get(), m, (int)nu, (const double*)emb->s.get());
     sv_sync(ctx);

@@ -257,23 +257,34 @@ __global__ void __launch_bounds__(256) k_spmv_csr(
     int64_t s = rowptr[r], e = rowptr[r + 1];
     int64_t a0 = s & ~3ll;
     AccT acc = 0;
-    for (int64_t g = a0 + 4 * lane; g < e; g += 128) {
-      int ci[4];
-      AccT av[4];
-      ld4(hcol, g, ci);
-      ld4v(hval, g, av);
+    // two 4-element groups per lane in flight (memory-level parallelism)
+    for (int64_t g = a0 + 4 * lane; g < e; g += 256) {
+      int ci[2][4];
+      AccT av[2][4];
+      bool two = g + 128 < e;
+      ld4(hcol, g, ci[0]);
+      ld4v(hval, g, av[0]);
+      if (two) {
+        ld4(hcol, g + 128, ci[1]);
+        ld4v(hval, g + 128, av[1]);
+      }
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        if (g + t >= s && g + t < e) {
-          if constexpr (sizeof(AccT) == 4) {
-            float2 pq = ((const float2*)smem_raw)[ci[t]];
-            float rr = av[t] * pq.x;
-            acc += pq.x >= 0.f ? fminf(rr, pq.y) : fmaxf(rr, pq.y);
-          } else {
-            const double* tab = (const double*)smem_raw;
-            double v = av[t] * tab[3 * ci[t]];          // scaling.jl:211 (times 1/std)
-            double c = tab[3 * ci[t] + 1];
-            acc += (v > c ? c : v) * tab[3 * ci[t] + 2];  // scaling.jl:212
+      for (int h = 0; h < 2; ++h) {
+        if (h == 1 && !two) break;
+        int64_t gh = g + 128 * h;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          if (gh + t >= s && gh + t < e) {
+            if constexpr (sizeof(AccT) == 4) {
+              float2 pq = ((const float2*)smem_raw)[ci[h][t]];
+              float rr = av[h][t] * pq.x;
+              acc += pq.x >= 0.f ? fminf(rr, pq.y) : fmaxf(rr, pq.y);
+            } else {
+              const double* tab = (const double*)smem_raw;
+              double v = av[h][t] * tab[3 * ci[h][t]];          // scaling.jl:211 (times 1/std)
+              double c = tab[3 * ci[h][t] + 1];
+              acc += (v > c ? c : v) * tab[3 * ci[h][t] + 2];   // scaling.jl:212
+            }
           }
         }
       }
@@ -285,6 +296,117 @@ __global__ void __launch_bounds__(256) k_spmv_csr(
       if (z) out -= cs * z[r];
       y[r] = out;
     }
+  }
+}
+
+// ---- X^T u over CSR_h (warp per cell, shared-memory accumulation) -----------
+// Each block accumulates sum_i min(a_if * inv_f, clip_f) * u_i for its cells into
+// a shared array of nf partial sums (shared atomics), then writes the array to
+// its row of `partial` (blocks x nf) together with its sum of u; the finish
+// kernel adds the block rows in block order (deterministic result).
+template <typename ValT, typename IdxT>
+__global__ void __launch_bounds__(256) k_spmv_csr_t(
+    const int64_t* __restrict__ rowptr, const IdxT* __restrict__ hcol, const ValT* __restrict__ hval,
+    int64_t n_rows, int64_t nf, const double* __restrict__ u, const float* __restrict__ inv_f,
+    const float* __restrict__ clip_f, const double* __restrict__ inv_d,
+    const double* __restrict__ clip_d, void* __restrict__ partial, double* __restrict__ upart) {
+  typedef typename AccOf<ValT>::type AccT;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[32];
+  AccT* accs;
+  if constexpr (sizeof(AccT) == 4) {
+    float2* tab = (float2*)smem_raw;
+    accs = (AccT*)(tab + nf);
+    for (int64_t f = threadIdx.x; f < nf; f += blockDim.x) {
+      tab[f] = make_float2(inv_f[f], clip_f[f]);
+      accs[f] = 0;
+    }
+  } else {
+    double2* tab = (double2*)smem_raw;
+    accs = (AccT*)(tab + nf);
+    for (int64_t f = threadIdx.x; f < nf; f += blockDim.x) {
+      tab[f] = make_double2(inv_d[f], clip_d[f]);
+      accs[f] = 0;
+    }
+  }
+  __syncthreads();
+  int lane = threadIdx.x & 31;
+  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double usum = 0;
+  for (int64_t r = warp; r < n_rows; r += nwarps) {
+    int64_t s = rowptr[r], e = rowptr[r + 1];
+    double ud = u[r];
+    usum += ud;
+    AccT ur = (AccT)ud;
+    int64_t a0 = s & ~3ll;
+    for (int64_t g = a0 + 4 * lane; g < e; g += 256) {
+      int ci[2][4];
+      AccT av[2][4];
+      bool two = g + 128 < e;
+      ld4(hcol, g, ci[0]);
+      ld4v(hval, g, av[0]);
+      if (two) {
+        ld4(hcol, g + 128, ci[1]);
+        ld4v(hval, g + 128, av[1]);
+      }
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (h == 1 && !two) break;
+        int64_t gh = g + 128 * h;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          if (gh + t >= s && gh + t < e) {
+            if constexpr (sizeof(AccT) == 4) {
+              float2 ic = ((const float2*)smem_raw)[ci[h][t]];
+              atomicAdd(&accs[ci[h][t]], fminf(av[h][t] * ic.x, ic.y) * ur);
+            } else {
+              double2 ic = ((const double2*)smem_raw)[ci[h][t]];
+              double v = av[h][t] * ic.x;
+              atomicAdd(&accs[ci[h][t]], (v > ic.y ? ic.y : v) * ur);
+            }
+          }
+        }
+      }
+    }
+  }
+  // lane 0 of each warp holds the rows' u (all lanes accumulated the same values)
+  if (lane != 0) usum = 0;
+  usum = sv_warp_sum(usum);
+  if (lane == 0) red[threadIdx.x >> 5] = usum;
+  __syncthreads();
+  AccT* prow = (AccT*)partial + (int64_t)blockIdx.x * nf;
+  for (int64_t f = threadIdx.x; f < nf; f += blockDim.x) prow[f] = accs[f];
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    upart[blockIdx.x] = t;
+  }
+}
+
+template <typename AccT>
+__global__ void k_spmv_t_finish(const AccT* __restrict__ partial, int nblocks, int64_t nf,
+                                const double* __restrict__ mu, const double* __restrict__ upart,
+                                double alpha, double beta, double* __restrict__ y,
+                                const double* __restrict__ csub, const double* __restrict__ z) {
+  __shared__ double su_s;
+  if (threadIdx.x < 32) {
+    double v = 0;
+    for (int i = threadIdx.x; i < nblocks; i += 32) v += upart[i];
+    v = sv_warp_sum(v);
+    if (threadIdx.x == 0) su_s = v;
+  }
+  __syncthreads();
+  double su = su_s;
+  double cs = csub ? *csub : 0.0;
+  for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < nf;
+       f += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0;
+    for (int b = 0; b < nblocks; ++b) acc += (double)partial[(int64_t)b * nf + f];
+    double out = alpha * (acc - mu[f] * su);
+    if (beta != 0.0) out += beta * y[f];
+    if (z) out -= cs * z[f];
+    y[f] = out;
   }
 }
 
@@ -419,6 +541,43 @@ void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const 
         break;
     }
 #undef LAUNCH_CSR
+  } else if (S->t_blocks > 0) {
+    // warp per cell over CSR_h, shared-memory accumulation per block
+    sv_centered* Sm = const_cast<sv_centered*>(S);
+    bool f64 = S->dtype == SV_F64;
+    size_t smem = (size_t)S->nf * (f64 ? 24 : 12);
+    bool small = S->nf <= 65536;
+#define LAUNCH_CT(VT, IT, COL)                                                                     \
+  sv_launch(ctx, "spmv_csr_t", k_spmv_csr_t<VT, IT>, dim3(S->t_blocks), dim3(256), smem,            \
+            (const int64_t*)S->h_rowptr.get(), (const IT*)COL, (const VT*)S->h_val.get(),            \
+            S->n_cells, S->nf, x, (const float*)S->inv_std_f.get(), (const float*)S->clip_f.get(),   \
+            (const double*)S->inv_std_d.get(), (const double*)S->clip_d.get(),                       \
+            (void*)Sm->t_partial.get(), Sm->red_partial.get())
+    switch (S->dtype) {
+      case SV_F64:
+        if (small) LAUNCH_CT(double, uint16_t, S->h_col16.get());
+        else LAUNCH_CT(double, int32_t, S->h_col32.get());
+        break;
+      case SV_F32:
+        if (small) LAUNCH_CT(float, uint16_t, S->h_col16.get());
+        else LAUNCH_CT(float, int32_t, S->h_col32.get());
+        break;
+      default:
+        if (small) LAUNCH_CT(__nv_bfloat16, uint16_t, S->h_col16.get());
+        else LAUNCH_CT(__nv_bfloat16, int32_t, S->h_col32.get());
+        break;
+    }
+#undef LAUNCH_CT
+    if (f64)
+      sv_launch(ctx, "spmv_t_finish", k_spmv_t_finish<double>, dim3(sv_grid_for(ctx, S->nf, 256, 4)),
+                dim3(256), 0, (const double*)Sm->t_partial.get(), S->t_blocks, S->nf,
+                (const double*)S->mu.get(), (const double*)Sm->red_partial.get(), alpha, beta, y, csub,
+                z);
+    else
+      sv_launch(ctx, "spmv_t_finish", k_spmv_t_finish<float>, dim3(sv_grid_for(ctx, S->nf, 256, 4)),
+                dim3(256), 0, (const float*)Sm->t_partial.get(), S->t_blocks, S->nf,
+                (const double*)S->mu.get(), (const double*)Sm->red_partial.get(), alpha, beta, y, csub,
+                z);
   } else {
     sv_centered* Sm = const_cast<sv_centered*>(S);
     bool f64 = S->dtype == SV_F64;
@@ -581,8 +740,26 @@ static sv_centered* make_centered(sv_context* ctx, const sv_data* data, const st
     }
 #undef LAUNCH_HW
     S->u_f32.alloc(C->n_cells);
-    S->red_partial.alloc(UPREP_BLOCKS);
     S->scal.alloc(64);
+    // X^T u: CSC chunks by default (measured faster on GB300: the CSR_h form is
+    // bound by shared-memory atomics); SV_TPRODUCT=csr selects the warp-per-cell
+    // form over CSR_h when its per-block feature arrays fit in shared memory
+    {
+      size_t tsmem = (size_t)nf * (data->dtype == SV_F64 ? 24 : 12);
+      const char* mode = getenv("SV_TPRODUCT");
+      bool want_csr = mode && strcmp(mode, "csr") == 0;
+      if (want_csr && tsmem <= 200 * 1024) {
+        S->t_blocks = ctx->num_sms * 2;
+        S->t_partial.alloc((size_t)S->t_blocks * nf * (data->dtype == SV_F64 ? 8 : 4));
+        SV_CUDA(cudaFuncSetAttribute(k_spmv_csr_t<double, uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SV_CUDA(cudaFuncSetAttribute(k_spmv_csr_t<double, int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SV_CUDA(cudaFuncSetAttribute(k_spmv_csr_t<float, uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SV_CUDA(cudaFuncSetAttribute(k_spmv_csr_t<float, int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SV_CUDA(cudaFuncSetAttribute(k_spmv_csr_t<__nv_bfloat16, uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SV_CUDA(cudaFuncSetAttribute(k_spmv_csr_t<__nv_bfloat16, int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      }
+      S->red_partial.alloc(std::max<int64_t>(UPREP_BLOCKS, S->t_blocks));
+    }
     SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<double, uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<double, int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<float, uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
