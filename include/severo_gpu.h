@@ -133,6 +133,25 @@ int sv_counts_free(sv_counts* c);
  * copy receive values; the sparsity pattern is the counts'. */
 int sv_normalize_cells(sv_context* ctx, const sv_counts* counts, int method,
                        double scale_factor, int dtype, sv_data** out);
+/* normalize_cells for callers that cannot let this library allocate device
+ * memory.  No counterpart in the reference: it exists for hosts that keep the
+ * device memory budget in their own pool, and for work recorded inside a stream
+ * capture, where cudaMalloc is not permitted and cudaFree synchronises the
+ * device.  Inputs and output are device arrays owned by the caller: a 0-based
+ * cells x genes CSC (colptr int64 [n_genes + 1], rowval and counts int32 [nnz])
+ * and values (FP32 [nnz], CSC order, the same numbers as the SV_F32 form of
+ * sv_normalize_cells).  The per-cell totals live in a file-scope device array
+ * of 2,097,152 entries (16 MiB on every GPU that loads the library, until the
+ * process exits); more cells are rejected with SV_ERR_ARG.  Nothing is
+ * allocated: no cudaMalloc, no cudaFree.  The first call on a device looks up
+ * the array's device address with that device current, so make it before any
+ * stream capture.  Work is queued on `stream` (a cudaStream_t, NULL for the
+ * legacy default stream) and the call returns without waiting.  Every call on a
+ * device shares the array: calls that overlap on the GPU (other streams, other
+ * host threads) race and corrupt each other's totals. */
+int sv_normalize_csc_noalloc(const int64_t* colptr, const int32_t* rowval, const int32_t* counts,
+                             int64_t n_cells, int64_t n_genes, int64_t nnz, int method,
+                             double scale_factor, float* values, void* stream);
 /* Copies the CSC values (in the data's dtype; BF16 as uint16 bit patterns). */
 int sv_data_download_csc(sv_context* ctx, const sv_data* d, void* nzval);
 int sv_data_download_csr(sv_context* ctx, const sv_data* d, void* nzval);

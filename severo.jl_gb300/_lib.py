@@ -78,6 +78,7 @@ SIGNATURES = {
     "sv_counts_download_csr": (i32, [vp, vp, vp, vp, vp]),
     "sv_counts_free": (i32, [vp]),
     "sv_normalize_cells": (i32, [vp, vp, i32, dbl, i32, P(vp)]),
+    "sv_normalize_csc_noalloc": (i32, [vp, vp, vp, i64, i64, i64, i32, dbl, vp, vp]),
     "sv_data_download_csc": (i32, [vp, vp, vp]),
     "sv_data_download_csr": (i32, [vp, vp, vp]),
     "sv_data_cell_totals": (i32, [vp, vp, vp]),

@@ -1,0 +1,83 @@
+// normalize_cells over a device CSC without any allocation by the library.
+//
+// Some callers cannot let a library call cudaMalloc: a host runtime that has
+// already reserved the device memory budget in its own pool (a garbage-collected
+// language runtime handing out device arrays), or code that records work inside
+// a stream capture, where cudaMalloc is not permitted and cudaFree would
+// synchronise the whole device.  This entry point takes the count matrix and the
+// output as device arrays owned by the caller and keeps its only scratch -- the
+// per-cell totals -- in the file-scope array below, sized for at most
+// SV_NOALLOC_MAX_CELLS cells (16 MiB, held by every GPU that loads the library
+// until the process exits).
+#include "sv_internal.cuh"
+
+namespace {
+
+constexpr int64_t SV_NOALLOC_MAX_CELLS = 2097152;
+
+// per-cell totals shared by every call on a device
+static __device__ __align__(256) unsigned long long g_cell_totals[SV_NOALLOC_MAX_CELLS];
+
+std::mutex g_sym_mu;
+unsigned long long* g_sym_ptr[64] = {};   // device address of g_cell_totals, per device
+
+__global__ void k_totals_scatter(const int32_t* __restrict__ rowidx, const int32_t* __restrict__ cnt,
+                                 int64_t nnz, unsigned long long* __restrict__ totals) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnz;
+       i += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&totals[rowidx[i]], (unsigned long long)(long long)cnt[i]);
+}
+
+// b = (sf * a) / s_cell in FP32 (src/normalize.jl:27), log1p for :lognormalize (:36)
+__global__ void k_values_static(const int32_t* __restrict__ rowidx, const int32_t* __restrict__ cnt,
+                                int64_t nnz, const unsigned long long* __restrict__ totals, float sf,
+                                int log, float* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnz;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float v = (sf * (float)cnt[i]) / (float)(long long)totals[rowidx[i]];
+    out[i] = log ? log1pf(v) : v;
+  }
+}
+
+}  // namespace
+
+SV_API int sv_normalize_csc_noalloc(const int64_t* colptr, const int32_t* rowval,
+                                    const int32_t* counts, int64_t n_cells, int64_t n_genes,
+                                    int64_t nnz, int method, double scale_factor, float* values,
+                                    void* stream) {
+  SV_TRY
+  (void)colptr;   // the values depend on the row of each entry only
+  SV_REQUIRE(n_cells >= 1 && n_genes >= 1 && nnz >= 0, "bad sizes");
+  if (n_cells > SV_NOALLOC_MAX_CELLS)
+    sv_throw(SV_ERR_ARG, "sv_normalize_csc_noalloc handles at most %lld cells (got %lld)",
+             (long long)SV_NOALLOC_MAX_CELLS, (long long)n_cells);
+  if (method != SV_LOGNORMALIZE && method != SV_RELATIVECOUNTS)
+    sv_throw(SV_ERR_ARG, "unknown normalization method: %d", method);
+  SV_REQUIRE(nnz == 0 || (rowval && counts && values), "null array");
+  int dev = 0;
+  SV_CUDA(cudaGetDevice(&dev));
+  SV_REQUIRE(dev >= 0 && dev < 64, "device index out of range");
+  unsigned long long* totals = nullptr;
+  {
+    // once per device, with that device current: the device address of the array
+    std::lock_guard<std::mutex> lk(g_sym_mu);
+    if (!g_sym_ptr[dev]) {
+      void* p = nullptr;
+      SV_CUDA(cudaGetSymbolAddress(&p, g_cell_totals));
+      g_sym_ptr[dev] = (unsigned long long*)p;
+    }
+    totals = g_sym_ptr[dev];
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  // the array keeps the previous call's totals: clear the range this call uses
+  SV_CUDA(cudaMemsetAsync(totals, 0, (size_t)n_cells * sizeof(unsigned long long), s));
+  if (nnz > 0) {
+    int blocks = 1216;
+    k_totals_scatter<<<blocks, 256, 0, s>>>(rowval, counts, nnz, totals);
+    SV_CUDA(cudaGetLastError());
+    k_values_static<<<blocks, 256, 0, s>>>(rowval, counts, nnz, totals, (float)scale_factor,
+                                           method == SV_LOGNORMALIZE, values);
+    SV_CUDA(cudaGetLastError());
+  }
+  SV_CATCH
+}
