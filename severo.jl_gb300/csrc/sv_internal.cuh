@@ -202,6 +202,12 @@ struct sv_centered {
   DevBuf<float> u_f32;                // n_cells
   DevBuf<double> red_partial;         // reduction partials
   DevBuf<double> scal;                // small device scalars
+  // row-blocked CSC copy of the subset for X^T u (FP32 / BF16 storage)
+  int64_t rb_rows = 0, n_rb = 0;      // rows per block, number of row blocks
+  DevBuf<int64_t> rb_ptr;             // n_rb * nf + 1 entry offsets, ordered (block, feature)
+  DevBuf<uint16_t> rb_idx;            // local row within the block
+  DevBuf<unsigned char> rb_val;       // value (storage type)
+  DevBuf<float> rb_partial;           // n_rb x nf partial sums
   int t_blocks = 0;                   // > 0: X^T u over CSR_h with this many blocks
   DevBuf<unsigned char> t_partial;    // t_blocks x nf partial sums
   // set when the matrix was built by sv_centered_create (owned here)

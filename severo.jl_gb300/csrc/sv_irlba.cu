@@ -110,14 +110,32 @@ __global__ void __launch_bounds__(256) k_dots_df(const float* __restrict__ Qh,
   float ah[NJ], al[NJ];
 #pragma unroll
   for (int t = 0; t < NJ; ++t) ah[t] = al[t] = 0.f;
-  for (int64_t i = r0 + lane; i < r1; i += 32) {
-    float bh = xh[i], bl = xl[i];
+  // two 32-row groups per iteration: all loads of both groups are issued before
+  // the arithmetic (memory-level parallelism)
+  for (int64_t i = r0 + lane; i < r1; i += 64) {
+    bool two = i + 32 < r1;
+    float bh0 = xh[i], bl0 = xl[i];
+    float bh1 = two ? xh[i + 32] : 0.f, bl1 = two ? xl[i + 32] : 0.f;
+    float q0h[NJ], q0l[NJ], q1h[NJ], q1l[NJ];
 #pragma unroll
     for (int t = 0; t < NJ; ++t) {
       int j = w + 8 * t;
+      int64_t o = (int64_t)j * ld + i;
+      q0h[t] = q0l[t] = q1h[t] = q1l[t] = 0.f;
       if (j < ncols) {
-        int64_t o = (int64_t)j * ld + i;
-        df_fma(ah[t], al[t], Qh[o], Ql[o], bh, bl);
+        q0h[t] = Qh[o];
+        q0l[t] = Ql[o];
+        if (two) {
+          q1h[t] = Qh[o + 32];
+          q1l[t] = Ql[o + 32];
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < NJ; ++t) {
+      if (w + 8 * t < ncols) {
+        df_fma(ah[t], al[t], q0h[t], q0l[t], bh0, bl0);
+        df_fma(ah[t], al[t], q1h[t], q1l[t], bh1, bl1);
       }
     }
   }
@@ -125,15 +143,29 @@ __global__ void __launch_bounds__(256) k_dots_df(const float* __restrict__ Qh,
   for (int t = 0; t < NJ; ++t) {
     int j = w + 8 * t;
     if (j < ncols) {
-      double v = sv_warp_sum(df_val(ah[t], al[t]));
-      if (lane == 0) part[(int64_t)blockIdx.x * ncols + j] = v;
+      // warp reduction in double-float (FP32 shuffles), one FP64 value per warp
+      float h = ah[t], l = al[t];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        float h2 = __shfl_xor_sync(0xffffffffu, h, o);
+        float l2 = __shfl_xor_sync(0xffffffffu, l, o);
+        float s = h + h2;
+        float v = s - h;
+        float err = (h - (s - v)) + (h2 - v);
+        float lo = err + l + l2;
+        h = s + lo;
+        l = lo - (h - s);
+      }
+      if (lane == 0) part[(int64_t)blockIdx.x * ncols + j] = df_val(h, l);
     }
   }
   if (last_block(counter, &last)) {
-    for (int j = threadIdx.x; j < ncols; j += blockDim.x) {
+    // one warp per column, lanes over blocks (block order fixed: deterministic)
+    for (int j = w; j < ncols; j += 8) {
       double s = 0;
-      for (unsigned b = 0; b < gridDim.x; ++b) s += part[(int64_t)b * ncols + j];
-      c[j] = s;
+      for (unsigned b = lane; b < gridDim.x; b += 32) s += part[(int64_t)b * ncols + j];
+      s = sv_warp_sum(s);
+      if (lane == 0) c[j] = s;
     }
     if (threadIdx.x == 0) *counter = 0;
   }
@@ -715,11 +747,13 @@ struct Lanczos {
   // working vector <- CGS2(working vector, basis[:, :ncols]); *nrm = its norm
   void orth_norm(Side& s, int ncols, double* nrm) {
     int g = red_grid(s.len);
+    // the update has no per-block partials besides the norm: more, smaller blocks
+    int gu = (int)std::min<int64_t>(2 * RED_BLOCKS, std::max<int64_t>(1, (s.len + 255) / 256));
     for (int pass = 0; pass < 2 && ncols > 0; ++pass) {
       sv_launch(ctx, "irlba_dots", k_dots_df, dim3(g), dim3(256), 0, (const float*)s.h.get(),
                 (const float*)s.l.get(), s.len, ncols, (const float*)s.xh.get(),
                 (const float*)s.xl.get(), s.len, part.get(), cvec.get(), counter.get());
-      sv_launch(ctx, "irlba_update", k_update_df, dim3(g), dim3(256), 0, s.xh.get(), s.xl.get(), s.len,
+      sv_launch(ctx, "irlba_update", k_update_df, dim3(gu), dim3(256), 0, s.xh.get(), s.xl.get(), s.len,
                 (const float*)s.h.get(), (const float*)s.l.get(), s.len, ncols,
                 (const double*)cvec.get(), part.get(), pass == 1 ? nrm : (double*)nullptr,
                 counter.get());

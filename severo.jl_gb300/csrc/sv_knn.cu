@@ -16,7 +16,7 @@
 #include "sv_internal.cuh"
 #include <float.h>
 
-int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq, int64_t n, int d,
+int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq, int64_t n, int dp, int d,
                          int K2, int include_self, int32_t* cand);
 sv_context* sv_default_context();
 
@@ -245,7 +245,7 @@ __global__ void k_to_host_layout(const int32_t* __restrict__ idx, const float* _
 }  // namespace
 
 // Core: X32 row-major [n][dp] FP32 with norms -> knn handle (row-major, 0-based).
-static void knn_core(sv_context* ctx, const float* X32, const float* sq, int64_t n, int dp, int k,
+static void knn_core(sv_context* ctx, const float* X32, const float* sq, int64_t n, int dp, int d, int k,
                      int include_self, int cosine, int precision, sv_knn* out) {
   // candidates per query: at least 2k; the tensor-core stage always keeps 64
   int K2 = (2 * k <= 32 && precision != SV_KNN_BF16) ? 32 : 64;
@@ -253,7 +253,7 @@ static void knn_core(sv_context* ctx, const float* X32, const float* sq, int64_t
   DevBuf<int32_t> cand((size_t)n * K2);
   bool done = false;
   if (precision == SV_KNN_BF16) {
-    int st = sv_knn_tc_candidates(ctx, X32, sq, n, dp, K2, include_self, cand.get());
+    int st = sv_knn_tc_candidates(ctx, X32, sq, n, dp, d, K2, include_self, cand.get());
     if (st != SV_OK) sv_throw(st, "tensor-core kNN failed");
     done = true;
   }
@@ -329,7 +329,7 @@ SV_API int sv_knn_host(sv_context* ctx, const void* X, int dtype, int64_t n, int
   auto* h = new sv_knn();
   try {
     h->ctx = ctx;
-    knn_core(ctx, X32.get(), sq.get(), n, dp, (int)k, include_self, metric == SV_COSINE, precision, h);
+    knn_core(ctx, X32.get(), sq.get(), n, dp, (int)d, (int)k, include_self, metric == SV_COSINE, precision, h);
     knn_outputs(ctx, h, dtype, nn_index, distances);
   } catch (...) {
     delete h;
@@ -357,7 +357,7 @@ SV_API int sv_knn_embed(sv_context* ctx, const sv_embed* e, int64_t ndims, int64
   auto* h = new sv_knn();
   try {
     h->ctx = ctx;
-    knn_core(ctx, X32.get(), sq.get(), n, dp, (int)k, include_self, metric == SV_COSINE, precision, h);
+    knn_core(ctx, X32.get(), sq.get(), n, dp, (int)ndims, (int)k, include_self, metric == SV_COSINE, precision, h);
     knn_outputs(ctx, h, SV_F64, nn_index, distances);
   } catch (...) {
     delete h;

@@ -141,6 +141,10 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// FOLD: |p|^2 is part of the MMA (see k_pack_fold): the accumulator is
+// D = q.p - |p|^2 / 2 and key = -2 D, so no norm is loaded in the epilogue and a
+// 32-candidate chunk is rejected by one compare of its maximum D.
+template <bool FOLD>
 __global__ void __launch_bounds__(THREADS, 1)
     k_knn_tc(const __grid_constant__ CUtensorMap tmapA, const __grid_constant__ CUtensorMap tmapB,
              const float* __restrict__ sqpad, int64_t n, int ntiles, int32_t* __restrict__ cand,
@@ -259,14 +263,16 @@ __global__ void __launch_bounds__(THREADS, 1)
       for (int c = 0; c < BN / 2 / 32; ++c) {
         float acc[32];
         float pn[32];
-        const float4* np = (const float4*)(sqpad + j0 + c * 32);
+        if constexpr (!FOLD) {
+          const float4* np = (const float4*)(sqpad + j0 + c * 32);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          float4 v = __ldg(np + i);
-          pn[4 * i] = v.x;
-          pn[4 * i + 1] = v.y;
-          pn[4 * i + 2] = v.z;
-          pn[4 * i + 3] = v.w;
+          for (int i = 0; i < 8; ++i) {
+            float4 v = __ldg(np + i);
+            pn[4 * i] = v.x;
+            pn[4 * i + 1] = v.y;
+            pn[4 * i + 2] = v.z;
+            pn[4 * i + 3] = v.w;
+          }
         }
         __syncwarp();
         tmem_ld32(tbase + c * 32, acc);
@@ -276,13 +282,38 @@ __global__ void __launch_bounds__(THREADS, 1)
           __syncwarp();
           if (lane == 0) mbar_arrive(&s->tempty[ab]);
         }
-        // cheap pass: keys and the mask of those below the current threshold
         float thr = best[KH - 1];
         uint32_t m = 0;
+        if constexpr (FOLD) {
+          // columns past the last point read zero rows (TMA fill): never candidates
+          if (j0 + c * 32 + 32 > n) {
 #pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          acc[i] = fmaf(-2.0f, acc[i], pn[i]);
-          m |= (acc[i] < thr ? 1u : 0u) << i;
+            for (int i = 0; i < 32; ++i)
+              if (j0 + c * 32 + i >= n) acc[i] = -FLT_MAX;
+          }
+          // key < thr  <=>  D > -thr/2 (exact: scaling by powers of two)
+          float thrD = -0.5f * thr;
+          float t16[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) t16[i] = fmaxf(acc[2 * i], acc[2 * i + 1]);
+#pragma unroll
+          for (int w2 = 8; w2 >= 1; w2 >>= 1)
+#pragma unroll
+            for (int i = 0; i < w2; ++i) t16[i] = fmaxf(t16[i], t16[i + w2]);
+          if (t16[0] > thrD) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              acc[i] = -2.0f * acc[i];
+              m |= (acc[i] < thr ? 1u : 0u) << i;
+            }
+          }
+        } else {
+          // keys and the mask of those below the current threshold
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            acc[i] = fmaf(-2.0f, acc[i], pn[i]);
+            m |= (acc[i] < thr ? 1u : 0u) << i;
+          }
         }
         if (m) {
           // rare: park the keys in this thread's shared slot and insert one by one
@@ -350,6 +381,37 @@ __global__ void k_pack_bf16(const float* __restrict__ X, int64_t n, int dp, int6
   }
 }
 
+// Operands with |p|^2 folded into the product (d + 3 <= 64): queries carry -1/2 in
+// columns d..d+2, points carry |p|^2 split into three BF16 parts (hi, mid, lo,
+// summing to the FP32 norm of the rounded row to ~2^-24), so that the MMA yields
+// D = q.p - |p|^2/2 and the key |p|^2 - 2 q.p is -2 D.
+__global__ void k_pack_fold(const float* __restrict__ X, int64_t n, int dp, int d,
+                            __nv_bfloat16* __restrict__ Xq, __nv_bfloat16* __restrict__ Xp) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int c = 0; c < BK; ++c) {
+      float v = c < d ? X[i * dp + c] : 0.f;
+      __nv_bfloat16 b = __float2bfloat16_rn(v);
+      Xq[i * BK + c] = b;
+      Xp[i * BK + c] = b;
+      float r = __bfloat162float(b);
+      s = fmaf(r, r, s);
+    }
+    __nv_bfloat16 p1 = __float2bfloat16_rn(s);
+    float r1 = s - __bfloat162float(p1);
+    __nv_bfloat16 p2 = __float2bfloat16_rn(r1);
+    __nv_bfloat16 p3 = __float2bfloat16_rn(r1 - __bfloat162float(p2));
+    __nv_bfloat16 mh = __float2bfloat16_rn(-0.5f);
+    Xq[i * BK + d] = mh;
+    Xq[i * BK + d + 1] = mh;
+    Xq[i * BK + d + 2] = mh;
+    Xp[i * BK + d] = p1;
+    Xp[i * BK + d + 1] = p2;
+    Xp[i * BK + d + 2] = p3;
+  }
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
@@ -371,7 +433,7 @@ EncodeTiledFn encode_fn() {
 }  // namespace
 
 int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unused, int64_t n, int dp,
-                         int K2, int include_self, int32_t* cand) {
+                         int d, int K2, int include_self, int32_t* cand) {
   (void)sq_unused;
   (void)include_self;   // the re-rank places or removes the point itself
   try {
@@ -380,31 +442,44 @@ int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unus
     if (n >= (1ll << 31) - BN) sv_throw(SV_ERR_UNSUPPORTED, "too many points");
     int ntiles = (int)((n + BN - 1) / BN);
     int64_t npad = (int64_t)ntiles * BN;
-    DevBuf<__nv_bfloat16> Xb((size_t)n * BK);
+    bool fold = d + 3 <= BK && !getenv("SV_KNN_NOFOLD");
+    DevBuf<__nv_bfloat16> Xq((size_t)n * BK), Xp;
     DevBuf<float> sq(npad);
-    sv_launch(ctx, "knn_pack_bf16", k_pack_bf16, dim3(sv_grid_for(ctx, npad, 256, 8)), dim3(256), 0, X32,
-              n, dp, npad, Xb.get(), sq.get());
-    // the same row-major BF16 matrix seen with two box heights: 128 query rows
-    // and 256 point rows, 64 elements (128 bytes, one swizzle row) wide
+    if (fold) {
+      Xp.alloc((size_t)n * BK);
+      sv_launch(ctx, "knn_pack_fold", k_pack_fold, dim3(sv_grid_for(ctx, n, 256, 8)), dim3(256), 0, X32,
+                n, dp, d, Xq.get(), Xp.get());
+    } else {
+      sv_launch(ctx, "knn_pack_bf16", k_pack_bf16, dim3(sv_grid_for(ctx, npad, 256, 8)), dim3(256), 0,
+                X32, n, dp, npad, Xq.get(), sq.get());
+    }
+    // row-major BF16 operands, 64 elements (128 bytes, one swizzle row) wide: the
+    // query box is 128 rows, the point box 256 rows
     CUtensorMap tmapA, tmapB;
     cuuint64_t gdim[2] = {(cuuint64_t)BK, (cuuint64_t)n};
     cuuint64_t gstride[1] = {(cuuint64_t)BK * 2};
     cuuint32_t boxA[2] = {(cuuint32_t)BK, (cuuint32_t)BM};
     cuuint32_t boxB[2] = {(cuuint32_t)BK, (cuuint32_t)BN};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = encode_fn()(&tmapA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, Xb.get(), gdim, gstride,
+    CUresult r = encode_fn()(&tmapA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, Xq.get(), gdim, gstride,
                              boxA, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) sv_throw(SV_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
-    r = encode_fn()(&tmapB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, Xb.get(), gdim, gstride, boxB, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+    r = encode_fn()(&tmapB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, fold ? Xp.get() : Xq.get(), gdim,
+                    gstride, boxB, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) sv_throw(SV_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     size_t smem = sizeof(Smem) + 1024;
-    SV_CUDA(cudaFuncSetAttribute(k_knn_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int nblocks = (int)((n + BM - 1) / BM);
-    sv_launch(ctx, "knn_tc_tiles", k_knn_tc, dim3(nblocks), dim3(THREADS), smem, tmapA, tmapB,
-              (const float*)sq.get(), n, ntiles, cand, ctx->d_status);
+    if (fold) {
+      SV_CUDA(cudaFuncSetAttribute(k_knn_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      sv_launch(ctx, "knn_tc_tiles", k_knn_tc<true>, dim3(nblocks), dim3(THREADS), smem, tmapA, tmapB,
+                (const float*)sq.get(), n, ntiles, cand, ctx->d_status);
+    } else {
+      SV_CUDA(cudaFuncSetAttribute(k_knn_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      sv_launch(ctx, "knn_tc_tiles", k_knn_tc<false>, dim3(nblocks), dim3(THREADS), smem, tmapA, tmapB,
+                (const float*)sq.get(), n, ntiles, cand, ctx->d_status);
+    }
     sv_check_device_status(ctx, "tensor-core kNN");
   } catch (const SvError& e) {
     return e.code;

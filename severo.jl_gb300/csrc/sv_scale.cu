@@ -206,48 +206,46 @@ struct AccOf<double> {
 // product term is min(a*P, Q) for x >= 0 and max(a*P, Q) for x < 0 (= min(a*inv,
 // clip)*x).  FP64 form: (1/std, clip, x); a * (1/std) is within one ulp of the
 // reference's a/std (FP64 division is slow on this part).
+// Every block builds the table and mu.x itself from x (a separate one-block
+// kernel preparing the table for all blocks measured no faster).
 template <typename ValT, typename IdxT>
 __global__ void __launch_bounds__(256) k_spmv_csr(
     const int64_t* __restrict__ rowptr, const IdxT* __restrict__ hcol, const ValT* __restrict__ hval,
     int64_t n_rows, int64_t nf, const double* __restrict__ x, const float* __restrict__ inv_f,
-    const float* __restrict__ clip_f, const double* __restrict__ std_d,
+    const float* __restrict__ clip_f, const double* __restrict__ inv_d,
     const double* __restrict__ clip_d, const double* __restrict__ mu, double alpha, double beta,
     double* __restrict__ y, const double* __restrict__ csub, const double* __restrict__ z) {
   typedef typename AccOf<ValT>::type AccT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[32];
-  // stage the table and compute mu . x (same value in every block)
   double mux = 0;
-  if constexpr (sizeof(AccT) == 4) {
-    float2* tab = (float2*)smem_raw;
+  {
     for (int64_t f = threadIdx.x; f < nf; f += blockDim.x) {
       double xf = x[f];
-      float xs = (float)xf;
-      float P = inv_f[f] * xs;
-      float Q = xs == 0.f ? 0.f : clip_f[f] * xs;
-      tab[f] = make_float2(P, Q);
+      if constexpr (sizeof(AccT) == 4) {
+        float xs = (float)xf;
+        float P = inv_f[f] * xs;
+        float Q = xs == 0.f ? 0.f : clip_f[f] * xs;
+        ((float2*)smem_raw)[f] = make_float2(P, Q);
+      } else {
+        double* tab = (double*)smem_raw;
+        tab[3 * f] = inv_d[f];
+        tab[3 * f + 1] = clip_d[f];
+        tab[3 * f + 2] = xf;
+      }
       mux += mu[f] * xf;
     }
-  } else {
-    double* tab = (double*)smem_raw;
-    for (int64_t f = threadIdx.x; f < nf; f += blockDim.x) {
-      double xf = x[f];
-      tab[3 * f] = std_d[f];
-      tab[3 * f + 1] = clip_d[f];
-      tab[3 * f + 2] = xf;
-      mux += mu[f] * xf;
+    mux = sv_warp_sum(mux);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mux;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+      v = sv_warp_sum(v);
+      if (threadIdx.x == 0) red[0] = v;
     }
+    __syncthreads();
+    mux = red[0];
   }
-  mux = sv_warp_sum(mux);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mux;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-    v = sv_warp_sum(v);
-    if (threadIdx.x == 0) red[0] = v;
-  }
-  __syncthreads();
-  mux = red[0];
   double cs = csub ? *csub : 0.0;
 
   int lane = threadIdx.x & 31;
@@ -257,7 +255,8 @@ __global__ void __launch_bounds__(256) k_spmv_csr(
     int64_t s = rowptr[r], e = rowptr[r + 1];
     int64_t a0 = s & ~3ll;
     AccT acc = 0;
-    // two 4-element groups per lane in flight (memory-level parallelism)
+    // two 4-element groups per lane in flight; the first load pair is
+    // unconditional (a guarded-loop form of the same loads measured 23% slower)
     for (int64_t g = a0 + 4 * lane; g < e; g += 256) {
       int ci[2][4];
       AccT av[2][4];
@@ -410,6 +409,126 @@ __global__ void k_spmv_t_finish(const AccT* __restrict__ partial, int nblocks, i
   }
 }
 
+// ---- X^T u over the row-blocked CSC copy ---------------------------------------
+// The feature subset is stored once more, ordered (row block, feature, row): for
+// every block of RB consecutive cells and every feature, the entries of that
+// feature in those cells, with the row as a 16-bit offset into the block.  A CTA
+// (row block b, feature group g) stages u[b*RB : (b+1)*RB] in shared memory as
+// FP32 and gathers from there, so the product streams 4 B per entry (uint16 row +
+// BF16 value) and no gather reaches L2.
+constexpr int64_t RB_ROWS = 16384;
+constexpr int RB_THREADS = 512;
+
+__device__ __forceinline__ int64_t lower_bound_rows(const int32_t* __restrict__ r, int64_t lo,
+                                                    int64_t hi, int64_t key) {
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if ((int64_t)r[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_rb_count(const int64_t* __restrict__ fstart, const int64_t* __restrict__ fend,
+                           const int32_t* __restrict__ rowidx, int64_t nf, int64_t n_rb,
+                           int64_t* __restrict__ cnt, int64_t* __restrict__ src) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n_rb * nf;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b = p / nf, f = p % nf;
+    int64_t s = fstart[f], e = fend[f];
+    int64_t lo = lower_bound_rows(rowidx, s, e, b * RB_ROWS);
+    int64_t hi = lower_bound_rows(rowidx, lo, e, (b + 1) * RB_ROWS);
+    cnt[p] = hi - lo;
+    src[p] = lo;
+  }
+}
+
+template <typename ValT>
+__global__ void k_rb_copy(const int64_t* __restrict__ src, const int64_t* __restrict__ dst,
+                          const int32_t* __restrict__ rowidx, const ValT* __restrict__ val,
+                          int64_t npairs, int64_t nf, uint16_t* __restrict__ oidx,
+                          ValT* __restrict__ oval) {
+  int lane = threadIdx.x & 31;
+  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t p = warp; p < npairs; p += nwarps) {
+    int64_t b = p / nf;
+    int64_t s = src[p], d = dst[p], n = dst[p + 1] - d;
+    for (int64_t i = lane; i < n; i += 32) {
+      oidx[d + i] = (uint16_t)(rowidx[s + i] - b * RB_ROWS);
+      oval[d + i] = val[s + i];
+    }
+  }
+}
+
+template <typename ValT>
+__global__ void __launch_bounds__(RB_THREADS) k_spmv_rb(
+    const int64_t* __restrict__ rb_ptr, const uint16_t* __restrict__ rb_idx,
+    const ValT* __restrict__ rb_val, int64_t nf, int64_t n_cells, const float* __restrict__ inv_f,
+    const float* __restrict__ clip_f, const float* __restrict__ uf, float* __restrict__ partial) {
+  extern __shared__ __align__(16) float us[];
+  int64_t b = blockIdx.x;
+  int64_t r0 = b * RB_ROWS;
+  int64_t nr = n_cells - r0 < RB_ROWS ? n_cells - r0 : RB_ROWS;
+  for (int64_t i = threadIdx.x; i < RB_ROWS; i += blockDim.x) us[i] = i < nr ? uf[r0 + i] : 0.f;
+  __syncthreads();
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int fg = gridDim.y, g = blockIdx.y;
+  for (int64_t f = g + (int64_t)fg * w; f < nf; f += (int64_t)fg * nw) {
+    int64_t s = rb_ptr[b * nf + f], e = rb_ptr[b * nf + f + 1];
+    float inv = inv_f[f], clip = clip_f[f];
+    float acc = 0.f;
+    int64_t a0 = s & ~3ll;
+    for (int64_t gg = a0 + 4 * lane; gg < e; gg += 256) {
+      int ci[2][4];
+      float av[2][4];
+      bool two = gg + 128 < e;
+      ld4(rb_idx, gg, ci[0]);
+      ld4v(rb_val, gg, av[0]);
+      if (two) {
+        ld4(rb_idx, gg + 128, ci[1]);
+        ld4v(rb_val, gg + 128, av[1]);
+      }
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (h == 1 && !two) break;
+        int64_t gh = gg + 128 * h;
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+          if (gh + t >= s && gh + t < e) acc += fminf(av[h][t] * inv, clip) * us[ci[h][t]];
+      }
+    }
+    acc = sv_warp_sum(acc);
+    if (lane == 0) partial[b * nf + f] = acc;
+  }
+}
+
+// y_f = alpha * (sum_b partial[b][f] - mu_f * sum(u)) + beta*y_f - csub*z_f
+__global__ void k_rb_finish(const float* __restrict__ partial, int64_t n_rb, int64_t nf,
+                            const double* __restrict__ mu, const double* __restrict__ upart,
+                            int nupart, double alpha, double beta, double* __restrict__ y,
+                            const double* __restrict__ csub, const double* __restrict__ z) {
+  __shared__ double su_s;
+  if (threadIdx.x < 32) {
+    double v = 0;
+    for (int i = threadIdx.x; i < nupart; i += 32) v += upart[i];
+    v = sv_warp_sum(v);
+    if (threadIdx.x == 0) su_s = v;
+  }
+  __syncthreads();
+  double su = su_s;
+  double cs = csub ? *csub : 0.0;
+  for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < nf;
+       f += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0;
+    for (int64_t bb = 0; bb < n_rb; ++bb) acc += (double)partial[bb * nf + f];
+    double out = alpha * (acc - mu[f] * su);
+    if (beta != 0.0) out += beta * y[f];
+    if (z) out -= cs * z[f];
+    y[f] = out;
+  }
+}
+
 // ---- X^T u over the CSC feature ranges ---------------------------------------
 // Prologue: u -> FP32 copy and per-block partial sums of u (FP64).
 __global__ void k_u_prep(const double* __restrict__ u, int64_t n, float* __restrict__ uf,
@@ -518,13 +637,14 @@ void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const 
                        double alpha, double beta, const double* csub, const double* z) {
   if (trans == 'N') {
     size_t smem = S->dtype == SV_F64 ? (size_t)S->nf * 24 : (size_t)S->nf * 8;
+    smem = (smem + 15) & ~(size_t)15;
     int grid = sv_grid_for(ctx, S->n_cells * 32, 256, 8);
-    const double* sd = S->inv_std_d.get();
-#define LAUNCH_CSR(VT, IT, COL)                                                                   \
-  sv_launch(ctx, "spmv_csr_h", k_spmv_csr<VT, IT>, dim3(grid), dim3(256), smem,                   \
-            (const int64_t*)S->h_rowptr.get(), (const IT*)COL, (const VT*)S->h_val.get(),          \
+#define LAUNCH_CSR(VT, IT, COL)                                                                  \
+  sv_launch(ctx, "spmv_csr_h", k_spmv_csr<VT, IT>, dim3(grid), dim3(256), smem,                  \
+            (const int64_t*)S->h_rowptr.get(), (const IT*)COL, (const VT*)S->h_val.get(),         \
             S->n_cells, S->nf, x, (const float*)S->inv_std_f.get(), (const float*)S->clip_f.get(), \
-            sd, (const double*)S->clip_d.get(), (const double*)S->mu.get(), alpha, beta, y, csub, z)
+            (const double*)S->inv_std_d.get(), (const double*)S->clip_d.get(),                    \
+            (const double*)S->mu.get(), alpha, beta, y, csub, z)
     bool small = S->nf <= 65536;
     switch (S->dtype) {
       case SV_F64:
@@ -541,6 +661,29 @@ void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const 
         break;
     }
 #undef LAUNCH_CSR
+  } else if (S->n_rb > 0) {
+    // row-blocked CSC: u staged per row block in shared memory
+    sv_centered* Sm = const_cast<sv_centered*>(S);
+    sv_launch(ctx, "spmv_csc_uprep", k_u_prep, dim3(UPREP_BLOCKS), dim3(256), 0, x, S->n_cells,
+              Sm->u_f32.get(), Sm->red_partial.get());
+    int resident = ctx->num_sms * 3;
+    int fg = (int)std::max<int64_t>(1, std::min<int64_t>(S->nf, (3 * resident + S->n_rb - 1) / S->n_rb));
+    dim3 grid((unsigned)S->n_rb, (unsigned)fg);
+    size_t smem = RB_ROWS * sizeof(float);
+    if (S->dtype == SV_F32)
+      sv_launch(ctx, "spmv_rb", k_spmv_rb<float>, grid, dim3(RB_THREADS), smem,
+                (const int64_t*)S->rb_ptr.get(), (const uint16_t*)S->rb_idx.get(),
+                (const float*)S->rb_val.get(), S->nf, S->n_cells, (const float*)S->inv_std_f.get(),
+                (const float*)S->clip_f.get(), (const float*)Sm->u_f32.get(), Sm->rb_partial.get());
+    else
+      sv_launch(ctx, "spmv_rb", k_spmv_rb<__nv_bfloat16>, grid, dim3(RB_THREADS), smem,
+                (const int64_t*)S->rb_ptr.get(), (const uint16_t*)S->rb_idx.get(),
+                (const __nv_bfloat16*)S->rb_val.get(), S->nf, S->n_cells,
+                (const float*)S->inv_std_f.get(), (const float*)S->clip_f.get(),
+                (const float*)Sm->u_f32.get(), Sm->rb_partial.get());
+    sv_launch(ctx, "spmv_rb_finish", k_rb_finish, dim3(sv_grid_for(ctx, S->nf, 256, 4)), dim3(256), 0,
+              (const float*)Sm->rb_partial.get(), S->n_rb, S->nf, (const double*)S->mu.get(),
+              (const double*)Sm->red_partial.get(), UPREP_BLOCKS, alpha, beta, y, csub, z);
   } else if (S->t_blocks > 0) {
     // warp per cell over CSR_h, shared-memory accumulation per block
     sv_centered* Sm = const_cast<sv_centered*>(S);
@@ -741,6 +884,51 @@ static sv_centered* make_centered(sv_context* ctx, const sv_data* data, const st
 #undef LAUNCH_HW
     S->u_f32.alloc(C->n_cells);
     S->scal.alloc(64);
+    // row-blocked CSC copy for X^T u (FP32 / BF16 storage; SV_TPRODUCT=csc or csr
+    // selects the other forms)
+    {
+      const char* mode = getenv("SV_TPRODUCT");
+      bool use_rb = data->dtype != SV_F64 && !(mode && (strcmp(mode, "csc") == 0 || strcmp(mode, "csr") == 0));
+      if (use_rb) {
+        S->rb_rows = RB_ROWS;
+        S->n_rb = (C->n_cells + RB_ROWS - 1) / RB_ROWS;
+        int64_t np = S->n_rb * nf;
+        DevBuf<int64_t> cnt(np + 1), src(np + 1);
+        sv_launch(ctx, "scale_rb_count", k_rb_count, dim3(sv_grid_for(ctx, np, 256, 8)), dim3(256), 0,
+                  (const int64_t*)S->feat_start.get(), (const int64_t*)S->feat_end.get(),
+                  (const int32_t*)C->csc_rowidx.get(), nf, S->n_rb, cnt.get(), src.get());
+        S->rb_ptr.alloc(np + 1);
+        sv_scan_i64(ctx, cnt.get(), S->rb_ptr.get(), np);
+        int64_t tot = sv_read_i64(ctx, S->rb_ptr.get() + np);
+        if (tot != nnz_h)
+          sv_throw(SV_ERR_DEVICE, "row-blocked copy size mismatch (%lld vs %lld)", (long long)tot,
+                   (long long)nnz_h);
+        size_t es2 = sv_elem_size(data->dtype);
+        S->rb_idx.alloc(std::max<int64_t>(1, nnz_h));
+        S->rb_val.alloc(std::max<int64_t>(1, nnz_h) * es2);
+        S->rb_partial.alloc(std::max<int64_t>(1, np));
+        int gridc = sv_grid_for(ctx, np * 32, 256, 8);
+        if (data->dtype == SV_F32)
+          sv_launch(ctx, "scale_rb_copy", k_rb_copy<float>, dim3(gridc), dim3(256), 0,
+                    (const int64_t*)src.get(), (const int64_t*)S->rb_ptr.get(),
+                    (const int32_t*)C->csc_rowidx.get(), (const float*)data->csc_val.get(), np, nf,
+                    S->rb_idx.get(), (float*)S->rb_val.get());
+        else
+          sv_launch(ctx, "scale_rb_copy", k_rb_copy<__nv_bfloat16>, dim3(gridc), dim3(256), 0,
+                    (const int64_t*)src.get(), (const int64_t*)S->rb_ptr.get(),
+                    (const int32_t*)C->csc_rowidx.get(), (const __nv_bfloat16*)data->csc_val.get(), np,
+                    nf, S->rb_idx.get(), (__nv_bfloat16*)S->rb_val.get());
+        SV_CUDA(cudaFuncSetAttribute(k_spmv_rb<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(RB_ROWS * sizeof(float))));
+        SV_CUDA(cudaFuncSetAttribute(k_spmv_rb<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(RB_ROWS * sizeof(float))));
+        // three 64 KB blocks per SM: prefer the largest shared-memory carve-out
+        SV_CUDA(cudaFuncSetAttribute(k_spmv_rb<float>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        SV_CUDA(cudaFuncSetAttribute(k_spmv_rb<__nv_bfloat16>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     100));
+        sv_sync(ctx);
+      }
+    }
     // X^T u: CSC chunks by default (measured faster on GB300: the CSR_h form is
     // bound by shared-memory atomics); SV_TPRODUCT=csr selects the warp-per-cell
     // form over CSR_h when its per-block feature arrays fit in shared memory
@@ -760,12 +948,16 @@ static sv_centered* make_centered(sv_context* ctx, const sv_data* data, const st
       }
       S->red_partial.alloc(std::max<int64_t>(UPREP_BLOCKS, S->t_blocks));
     }
-    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<double, uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<double, int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<float, uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<float, int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<__nv_bfloat16, uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<__nv_bfloat16, int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+#define SET_SMEM(VT, IT)                                                                         \
+  SV_CUDA(cudaFuncSetAttribute(k_spmv_csr<VT, IT>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                               200 * 1024))
+    SET_SMEM(double, uint16_t);
+    SET_SMEM(double, int32_t);
+    SET_SMEM(float, uint16_t);
+    SET_SMEM(float, int32_t);
+    SET_SMEM(__nv_bfloat16, uint16_t);
+    SET_SMEM(__nv_bfloat16, int32_t);
+#undef SET_SMEM
     sv_sync(ctx);
   } catch (...) {
     delete S;

@@ -98,6 +98,28 @@ def test_centered_golden(sv, ctx, variant):
     assert np.allclose(S.rmul(y, 2.0, 1.0, r), e["r1"], rtol=1e-14)
 
 
+@pytest.mark.parametrize("dtype", ["float32", "bfloat16"])
+def test_transpose_product_forms_agree(sv, ctx, O, dtype, monkeypatch):
+    """X^T u over the row-blocked copy (default), the CSC chunks and the CSR_h
+    shared-memory form give the same result (FP32 accumulation order only).
+    40,000 cells span three 16,384-cell row blocks."""
+    X = O.synth_counts(40000, 600, -1.0, 1.5, depth=0.5, seed=23)
+    d = sv.normalize_cells(X, scale_factor=1e4, dtype=dtype, ctx=ctx)
+    hvf = np.arange(1, 601, 2)
+    u = np.random.default_rng(1).standard_normal(40000)
+    out = {}
+    for mode in ("rb", "csc", "csr"):
+        if mode == "rb":
+            monkeypatch.delenv("SV_TPRODUCT", raising=False)
+        else:
+            monkeypatch.setenv("SV_TPRODUCT", mode)
+        S = sv.scale_features(d, scale_max=10.0, features=hvf)
+        out[mode] = S.rmul(u)
+    ref = out["csc"]
+    for mode in ("rb", "csr"):
+        assert np.linalg.norm(out[mode] - ref) <= 1e-5 * np.linalg.norm(ref)
+
+
 def test_scale_rejects_bad_features(sv, ctx, O):
     X = O.synth_counts(50, 40, -1.0, 1.5, depth=0.5, seed=1)
     d = sv.normalize_cells(X, ctx=ctx)
