@@ -408,6 +408,37 @@ def knn_exact(X, k, include_self=True, metric="euclidean", block=2048):
     return idx_out, d_out
 
 
+def knn_exact_queries(X, queries, k, include_self=True, block=262144):
+    """Exact FP64 Euclidean kNN of a sample of query rows against all of X (the
+    ground truth of knn_exact for large n, where the full n x n sweep is too
+    slow).  The database is swept in blocks, keeping each block's k+1 nearest;
+    returns the 0-based (len(queries) x k) index array, ascending distance, ties
+    by index, the query itself first (include_self) or excluded."""
+    X = np.asarray(X, dtype=np.float64)
+    queries = np.asarray(queries)
+    n = X.shape[0]
+    Q = X[queries]
+    sqq = np.einsum("ij,ij->i", Q, Q)
+    kk = k + 1
+    cand_i, cand_d = [], []
+    for s in range(0, n, block):
+        e = min(n, s + block)
+        B = X[s:e]
+        D = sqq[:, None] + np.einsum("ij,ij->i", B, B)[None, :] - 2.0 * (Q @ B.T)
+        np.maximum(D, 0.0, out=D)
+        inb = (queries >= s) & (queries < e)
+        D[np.nonzero(inb)[0], queries[inb] - s] = -1.0      # self sorts first
+        m = min(kk, e - s)
+        part = np.argpartition(D, m - 1, axis=1)[:, :m] if m < e - s else np.tile(np.arange(e - s), (len(Q), 1))
+        cand_d.append(np.take_along_axis(D, part, axis=1))
+        cand_i.append(part + s)
+    ci = np.concatenate(cand_i, axis=1)
+    cd = np.concatenate(cand_d, axis=1)
+    order = np.lexsort((ci, cd), axis=1)
+    ci = np.take_along_axis(ci, order, axis=1)
+    return ci[:, :k] if include_self else ci[:, 1:k + 1]
+
+
 def knn_graph(nn_index_1based, n):
     """src/neighbours.jl:79: sparse(vec(nn_index'), repeat(1:n, inner=k), trues(n*k)).
     Column j holds the neighbour rows of cell j (Bool, duplicates OR-ed)."""

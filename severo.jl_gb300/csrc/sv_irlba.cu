@@ -24,6 +24,7 @@
 // per restart; everything else stays on the device.
 #include "sv_internal.cuh"
 #include <math.h>
+#include <stdlib.h>
 
 void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const double* x, double* y,
                        double alpha, double beta, const double* csub, const double* z);
@@ -239,17 +240,28 @@ __device__ __forceinline__ double normal_at(unsigned long long seed, unsigned lo
   return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);    // Box-Muller
 }
 
+// Control block of a Lanczos run, read by the kernels so that a captured cycle
+// replays without host-side arguments: [0] breakdown threshold, [1] largest
+// Ritz value so far, [2] cycle number (selects the random restart vectors).
+#define CTL_THRESH 0
+#define CTL_SMAX 1
+#define CTL_CYCLE 2
+__device__ __forceinline__ unsigned long long breakdown_tag(const double* ctl, unsigned step) {
+  return (unsigned long long)ctl[CTL_CYCLE] * 1024ull + step;
+}
+
 // Basis column := x / *nrm (double-float) and cur := the same in FP64; the B
-// entry := *nrm.  When *nrm < thresh the Krylov space is (numerically)
+// entry := *nrm.  When *nrm < ctl[CTL_THRESH] the Krylov space is (numerically)
 // invariant: cur := a random vector, B entry := 0, flag set for k_fix_df, which
 // orthonormalises cur against the basis and writes the column.
 __global__ void k_scal_df(const float* __restrict__ xh, const float* __restrict__ xl, int64_t len,
-                          const double* __restrict__ nrm, double thresh, float* __restrict__ colh,
-                          float* __restrict__ coll, double* __restrict__ cur,
+                          const double* __restrict__ nrm, const double* __restrict__ ctl,
+                          float* __restrict__ colh, float* __restrict__ coll, double* __restrict__ cur,
                           double* __restrict__ bentry, int* __restrict__ flag,
-                          unsigned long long seed, unsigned long long tag) {
+                          unsigned long long seed, unsigned step) {
   double s = *nrm;
-  bool brk = !(s >= thresh);
+  bool brk = !(s >= ctl[CTL_THRESH]);
+  unsigned long long tag = breakdown_tag(ctl, step);
   double inv = brk ? 0.0 : 1.0 / s;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -373,10 +385,11 @@ __device__ double vside_norm(const float* __restrict__ xh, const float* __restri
 __global__ void __launch_bounds__(1024) k_vside(const double* __restrict__ F, int64_t len,
                                                 float* __restrict__ Vh, float* __restrict__ Vl,
                                                 int ncols, int write_col, double* __restrict__ nrm,
-                                                double thresh, double* __restrict__ bentry,
+                                                const double* __restrict__ ctl,
+                                                double* __restrict__ bentry,
                                                 double* __restrict__ cur, float* __restrict__ xh,
                                                 float* __restrict__ xl, unsigned long long seed,
-                                                unsigned long long tag) {
+                                                unsigned step) {
   __shared__ double c[MAX_WORK];
   __shared__ float ch[MAX_WORK], cl[MAX_WORK];
   __shared__ double sh[32];
@@ -389,8 +402,9 @@ __global__ void __launch_bounds__(1024) k_vside(const double* __restrict__ F, in
     if (threadIdx.x == 0) *nrm = s;
     return;
   }
-  bool brk = !(s >= thresh);
+  bool brk = !(s >= ctl[CTL_THRESH]);
   if (brk) {
+    unsigned long long tag = breakdown_tag(ctl, step);
     for (int64_t i = threadIdx.x; i < len; i += blockDim.x) df_split(normal_at(seed, tag, i), xh[i], xl[i]);
     __syncthreads();
     vside_cgs2(xh, xl, len, Vh, Vl, ncols, c, ch, cl);
@@ -419,26 +433,70 @@ __global__ void __launch_bounds__(1024) k_vside(const double* __restrict__ F, in
   }
 }
 
-// One-sided (Hestenes) Jacobi SVD of B (m x m, row-major) in FP64, one block.
-// Columns of A = B are orthogonalised by plane rotations J accumulated in Qm;
-// then s_i = |A e_i|, P_i = A e_i / s_i, sorted by descending s.
+// One-sided (Hestenes) Jacobi SVD of B (m x m, row-major), one block, in
+// double-float arithmetic: FP64 runs at 1/57 of the FP32 rate on this part, and
+// one FP64 block spent ~4 ms per 57 x 57 SVD, so the columns of A = B and the
+// accumulated rotations J are held as (hi, lo) FP32 pairs in shared memory and
+// updated on the FP32 pipe; only the rotation parameters are formed in FP64.
+// Columns are paired by the circle method (slot 0 fixed, the others rotating),
+// one warp per pair; a pair is rotated while |a_p . a_q| > 1e-13 |a_p| |a_q|
+// (the double-float dot products carry ~3e-15 relative error, so the FP64
+// threshold of 1e-15 would never be met).  Then s_i = |A e_i|, P_i = A e_i / s_i,
+// Q = J, sorted by descending s.
 // Outputs: P (m x m col-major), s (m), Q (m x m col-major), summary =
-// [s (m), P[m-1, :] (m), rf, sweeps].
-__global__ void k_jacobi_svd(const double* __restrict__ B, int m, double* __restrict__ Pout,
-                             double* __restrict__ sout, double* __restrict__ Qout,
-                             double* __restrict__ summary, const double* __restrict__ rf,
-                             int max_sweeps, int* __restrict__ status) {
-  extern __shared__ double sm[];
-  double* A = sm;              // m*m, column c at A[c*m]
-  double* J = sm + m * m;      // m*m
+// [s (m), P[m-1, :] (m), rf, sweeps].  Closes the cycle in the control block:
+// largest Ritz value so far, the next breakdown threshold eps_b * max(smax, 1)
+// and the cycle number.
+__device__ __forceinline__ void df_warp_sum(float& h, float& l) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    float h2 = __shfl_xor_sync(0xffffffffu, h, o);
+    float l2 = __shfl_xor_sync(0xffffffffu, l, o);
+    float s = h + h2;
+    float v = s - h;
+    float err = (h - (s - v)) + (h2 - v);
+    float lo = err + l + l2;
+    h = s + lo;
+    l = lo - (h - s);
+  }
+}
+
+// (x, y) <- (c x - s y, s x + c y) on double-float entries
+__device__ __forceinline__ void df_rot(float& xh, float& xl, float& yh, float& yl, float ch, float cl,
+                                       float sh, float sl) {
+  float ah = 0.f, al = 0.f, bh = 0.f, bl = 0.f;
+  df_fma(ah, al, ch, cl, xh, xl);
+  df_fma(ah, al, -sh, -sl, yh, yl);
+  df_fma(bh, bl, sh, sl, xh, xl);
+  df_fma(bh, bl, ch, cl, yh, yl);
+  xh = ah + al;
+  xl = al - (xh - ah);
+  yh = bh + bl;
+  yl = bl - (yh - bh);
+}
+
+__global__ void __launch_bounds__(1024) k_jacobi_svd(const double* __restrict__ B, int m,
+                                                     double* __restrict__ Pout,
+                                                     double* __restrict__ sout,
+                                                     double* __restrict__ Qout,
+                                                     double* __restrict__ summary,
+                                                     const double* __restrict__ rf, int max_sweeps,
+                                                     int* __restrict__ status,
+                                                     double* __restrict__ ctl, double eps_b) {
+  extern __shared__ float smf[];
+  float* Ah = smf;              // m*m, column c at [c*m]
+  float* Al = Ah + m * m;
+  float* Jh = Al + m * m;
+  float* Jl = Jh + m * m;
   __shared__ int rotated;
   __shared__ int order[MAX_WORK];
   __shared__ double nrm[MAX_WORK];
   int tid = threadIdx.x;
   for (int idx = tid; idx < m * m; idx += blockDim.x) {
     int r = idx % m, c = idx / m;
-    A[idx] = B[r * m + c];
-    J[idx] = r == c ? 1.0 : 0.0;
+    df_split(B[r * m + c], Ah[idx], Al[idx]);
+    Jh[idx] = r == c ? 1.f : 0.f;
+    Jl[idx] = 0.f;
   }
   __syncthreads();
   int mp = (m + 1) & ~1;   // even number of slots (one dummy when m is odd)
@@ -450,39 +508,36 @@ __global__ void k_jacobi_svd(const double* __restrict__ B, int m, double* __rest
     __syncthreads();
     for (int round = 0; round < mp - 1; ++round) {
       for (int pi = wid; pi < npairs; pi += nw) {
-        // circle method: slot 0 fixed, slots 1..mp-1 rotate by `round`
         int a = pi == 0 ? 0 : 1 + (pi - 1 + round) % (mp - 1);
         int b = 1 + (mp - 2 - pi + round) % (mp - 1);
         if (a >= m || b >= m) continue;
         int p = min(a, b), q = max(a, b);
-        double* ap = A + p * m;
-        double* aq = A + q * m;
-        double al = 0, be = 0, ga = 0;
+        float* aph = Ah + p * m;
+        float* apl = Al + p * m;
+        float* aqh = Ah + q * m;
+        float* aql = Al + q * m;
+        float alh = 0.f, all = 0.f, beh = 0.f, bel = 0.f, gah = 0.f, gal = 0.f;
         for (int r = lane; r < m; r += 32) {
-          double x = ap[r], y = aq[r];
-          al += x * x;
-          be += y * y;
-          ga += x * y;
+          float xh = aph[r], xl = apl[r], yh = aqh[r], yl = aql[r];
+          df_fma(alh, all, xh, xl, xh, xl);
+          df_fma(beh, bel, yh, yl, yh, yl);
+          df_fma(gah, gal, xh, xl, yh, yl);
         }
-        al = sv_warp_sum(al);
-        be = sv_warp_sum(be);
-        ga = sv_warp_sum(ga);
-        if (fabs(ga) > 1e-15 * sqrt(al * be) && ga != 0.0) {
+        df_warp_sum(alh, all);
+        df_warp_sum(beh, bel);
+        df_warp_sum(gah, gal);
+        double al = df_val(alh, all), be = df_val(beh, bel), ga = df_val(gah, gal);
+        if (fabs(ga) > 1e-13 * sqrt(al * be) && ga != 0.0) {
           double zeta = (be - al) / (2.0 * ga);
           double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + hypot(1.0, zeta));
           double cth = 1.0 / sqrt(1.0 + t * t);
           double sth = cth * t;
+          float ch, cl, sh, sl;
+          df_split(cth, ch, cl);
+          df_split(sth, sh, sl);
           for (int r = lane; r < m; r += 32) {
-            double x = ap[r], y = aq[r];
-            ap[r] = cth * x - sth * y;
-            aq[r] = sth * x + cth * y;
-          }
-          double* jp = J + p * m;
-          double* jq = J + q * m;
-          for (int r = lane; r < m; r += 32) {
-            double x = jp[r], y = jq[r];
-            jp[r] = cth * x - sth * y;
-            jq[r] = sth * x + cth * y;
+            df_rot(aph[r], apl[r], aqh[r], aql[r], ch, cl, sh, sl);
+            df_rot(Jh[p * m + r], Jl[p * m + r], Jh[q * m + r], Jl[q * m + r], ch, cl, sh, sl);
           }
           if (lane == 0) rotated = 1;
         }
@@ -495,10 +550,13 @@ __global__ void k_jacobi_svd(const double* __restrict__ B, int m, double* __rest
   if (sweep >= max_sweeps && tid == 0) atomicOr(status, SV_STATUS_LIMIT);
   // singular values and ordering
   for (int c = wid; c < m; c += nw) {
-    double s = 0;
-    for (int r = lane; r < m; r += 32) s += A[c * m + r] * A[c * m + r];
-    s = sv_warp_sum(s);
-    if (lane == 0) nrm[c] = sqrt(s);
+    float sh = 0.f, sl = 0.f;
+    for (int r = lane; r < m; r += 32) {
+      float xh = Ah[c * m + r], xl = Al[c * m + r];
+      df_fma(sh, sl, xh, xl, xh, xl);
+    }
+    df_warp_sum(sh, sl);
+    if (lane == 0) nrm[c] = sqrt(df_val(sh, sl));
   }
   __syncthreads();
   if (tid == 0) {
@@ -519,18 +577,23 @@ __global__ void k_jacobi_svd(const double* __restrict__ B, int m, double* __rest
     int r = idx % m, i = idx / m;
     int c = order[i];
     double s = nrm[c];
-    Pout[i * m + r] = s > 0 ? A[c * m + r] / s : (r == i ? 1.0 : 0.0);
-    Qout[i * m + r] = J[c * m + r];
+    double a = df_val(Ah[c * m + r], Al[c * m + r]);
+    Pout[i * m + r] = s > 0 ? a / s : (r == i ? 1.0 : 0.0);
+    Qout[i * m + r] = df_val(Jh[c * m + r], Jl[c * m + r]);
   }
   for (int i = tid; i < m; i += blockDim.x) {
-    sout[i] = nrm[order[i]];
-    summary[i] = nrm[order[i]];
     double s = nrm[order[i]];
-    summary[m + i] = s > 0 ? A[order[i] * m + (m - 1)] / s : 0.0;
+    sout[i] = s;
+    summary[i] = s;
+    summary[m + i] = s > 0 ? df_val(Ah[order[i] * m + (m - 1)], Al[order[i] * m + (m - 1)]) / s : 0.0;
   }
   if (tid == 0) {
     summary[2 * m] = rf ? *rf : 0.0;
     summary[2 * m + 1] = (double)sweep;
+    double smax = fmax(ctl[CTL_SMAX], nrm[order[0]]);
+    ctl[CTL_SMAX] = smax;
+    ctl[CTL_THRESH] = eps_b * fmax(smax, 1.0);
+    ctl[CTL_CYCLE] += 1.0;
   }
 }
 
@@ -635,6 +698,9 @@ struct Op {
   virtual void N(const double* x, double* y, const double* csub, const double* z) = 0;
   // y = A^T x - (csub ? *csub : 0) * z      (x in R^m, y in R^n)
   virtual void T(const double* x, double* y, const double* csub, const double* z) = 0;
+  // true when N and T only enqueue device work (no host round trip), so that a
+  // Lanczos cycle over them can be captured as a CUDA graph
+  virtual bool device_only() const { return false; }
 };
 
 struct CenteredOp : Op {
@@ -647,6 +713,7 @@ struct CenteredOp : Op {
   void T(const double* x, double* y, const double* csub, const double* z) override {
     sv_centered_apply(ctx, S, 'T', x, y, 1.0, 0.0, csub, z);
   }
+  bool device_only() const override { return true; }
 };
 
 struct CallbackOp : Op {
@@ -680,27 +747,46 @@ struct IrlbaResult {
   int64_t iters = 0, nmatvec = 0;
 };
 
-// One side of the bidiagonalisation: a double-float basis (len x work), its
-// rotation buffer, the double-float working vector and the FP64 copy of the
-// current basis vector (the input of the next product).
+// One side of the bidiagonalisation: two double-float bases (len x work) --
+// the current one and the target of the thick-restart rotation, which swap
+// roles every restart -- the double-float working vector and the FP64 copy of
+// the current basis vector (the input of the next product).
 struct Side {
   int64_t len = 0;
-  DevBuf<float> h, l, th, tl;   // basis and rotation target
+  DevBuf<float> h[2], l[2];     // basis sets
+  int set = 0;                  // the current set
   DevBuf<float> xh, xl;         // working vector
   DevBuf<double> cur;           // current basis vector, FP64
   void alloc(int64_t n, int work) {
     len = n;
-    h.alloc(n * work);
-    l.alloc(n * work);
-    th.alloc(n * work);
-    tl.alloc(n * work);
+    for (int t = 0; t < 2; ++t) {
+      h[t].alloc(n * work);
+      l[t].alloc(n * work);
+    }
     xh.alloc(n);
     xl.alloc(n);
     cur.alloc(n);
   }
-  float* ch(int j) { return h.get() + (int64_t)j * len; }
-  float* cl(int j) { return l.get() + (int64_t)j * len; }
+  float* bh() { return h[set].get(); }
+  float* bl() { return l[set].get(); }
+  float* ch(int j) { return bh() + (int64_t)j * len; }
+  float* cl(int j) { return bl() + (int64_t)j * len; }
+  float* th() { return h[1 - set].get(); }
+  float* tl() { return l[1 - set].get(); }
+  void flip() { set = 1 - set; }
 };
+
+// A captured Lanczos cycle: its executable graph and what one replay does.
+struct CycleGraph {
+  cudaGraphExec_t exec = nullptr;
+  int64_t launches = 0, matvecs = 0;
+};
+
+// Control-block slots in Lanczos::scal (after the two norm slots).
+#define SCAL_S 0        // W-side norm (alpha of the bidiagonal)
+#define SCAL_R 1        // V-side norm (beta)
+#define SCAL_CTL 2      // control block of the cycles (3 slots)
+#define SCAL_CTL0 5     // control block of the start vector: threshold 1e-300
 
 // The Lanczos driver.  m = rows of A (the W side), n = columns (the V side).
 struct Lanczos {
@@ -712,7 +798,10 @@ struct Lanczos {
   DevBuf<double> ytmp, F, B, P, Q, sig, summary, scal, part, cvec, Ufin, Vfin;
   DevBuf<unsigned int> counter;
   DevBuf<int> flag;
-  std::vector<double> hsum;
+  double* hsum = nullptr;       // pinned copy of the cycle summary
+  double eps_b = 0;
+  // graphs of the first cycle and of restart cycles from basis set 0 / set 1
+  CycleGraph graphs[3];
 
   Lanczos(sv_context* c, Op* o, int64_t m_, int64_t n_, int nu_, int work_)
       : ctx(c), op(o), m(m_), n(n_), nu(nu_), work(work_) {
@@ -733,12 +822,21 @@ struct Lanczos {
     sv_memset(ctx, counter.get(), 0, 16);
     sv_memset(ctx, flag.get(), 0, 16);
     sv_memset(ctx, B.get(), 0, work * work * 8);
-    hsum.resize(2 * work + 2);
+    SV_CUDA(cudaMallocHost((void**)&hsum, (2 * work + 2) * 8));
     SV_CUDA(cudaFuncSetAttribute(k_jacobi_svd, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 2 * MAX_WORK * MAX_WORK * 8));
+                                 4 * MAX_WORK * MAX_WORK * 4));
     SV_CUDA(cudaFuncSetAttribute(k_rotate_df<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  MAX_WORK * MAX_WORK * 8));
   }
+  ~Lanczos() {
+    for (auto& g : graphs)
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (hsum) cudaFreeHost(hsum);
+  }
+  Lanczos(const Lanczos&) = delete;
+  Lanczos& operator=(const Lanczos&) = delete;
+
+  double* ctl() { return scal.get() + SCAL_CTL; }
 
   int red_grid(int64_t len) {
     return (int)std::min<int64_t>(RED_BLOCKS, std::max<int64_t>(1, (len + 255) / 256));
@@ -750,45 +848,43 @@ struct Lanczos {
     // the update has no per-block partials besides the norm: more, smaller blocks
     int gu = (int)std::min<int64_t>(2 * RED_BLOCKS, std::max<int64_t>(1, (s.len + 255) / 256));
     for (int pass = 0; pass < 2 && ncols > 0; ++pass) {
-      sv_launch(ctx, "irlba_dots", k_dots_df, dim3(g), dim3(256), 0, (const float*)s.h.get(),
-                (const float*)s.l.get(), s.len, ncols, (const float*)s.xh.get(),
+      sv_launch(ctx, "irlba_dots", k_dots_df, dim3(g), dim3(256), 0, (const float*)s.bh(),
+                (const float*)s.bl(), s.len, ncols, (const float*)s.xh.get(),
                 (const float*)s.xl.get(), s.len, part.get(), cvec.get(), counter.get());
       sv_launch(ctx, "irlba_update", k_update_df, dim3(gu), dim3(256), 0, s.xh.get(), s.xl.get(), s.len,
-                (const float*)s.h.get(), (const float*)s.l.get(), s.len, ncols,
+                (const float*)s.bh(), (const float*)s.bl(), s.len, ncols,
                 (const double*)cvec.get(), part.get(), pass == 1 ? nrm : (double*)nullptr,
                 counter.get());
     }
     if (ncols == 0)
       sv_launch(ctx, "irlba_update", k_update_df, dim3(g), dim3(256), 0, s.xh.get(), s.xl.get(), s.len,
-                (const float*)s.h.get(), (const float*)s.l.get(), s.len, 0,
+                (const float*)s.bh(), (const float*)s.bl(), s.len, 0,
                 (const double*)cvec.get(), part.get(), nrm, counter.get());
   }
 
   // basis column j := working vector / *nrm (FP64 copy in cur), breakdown handling
-  void scal_fix(Side& s, int j, double* nrm, double thresh, double* bentry, uint64_t seed,
-                uint64_t tag) {
+  void scal_fix(Side& s, int j, double* nrm, const double* c, double* bentry, uint64_t seed,
+                unsigned step) {
     sv_launch(ctx, "irlba_scal", k_scal_df, dim3(sv_grid_for(ctx, s.len, 256, 4)), dim3(256), 0,
-              (const float*)s.xh.get(), (const float*)s.xl.get(), s.len, (const double*)nrm, thresh,
-              s.ch(j), s.cl(j), s.cur.get(), bentry, flag.get(), (unsigned long long)seed,
-              (unsigned long long)tag);
+              (const float*)s.xh.get(), (const float*)s.xl.get(), s.len, (const double*)nrm, c,
+              s.ch(j), s.cl(j), s.cur.get(), bentry, flag.get(), (unsigned long long)seed, step);
     sv_launch(ctx, "irlba_scal_post", k_scal_post, dim3(1), dim3(1), 0, nrm, (const int*)flag.get());
     sv_launch(ctx, "irlba_fix", k_fix_df, dim3(1), dim3(1024), 0, s.cur.get(), s.len,
-              (const float*)s.h.get(), (const float*)s.l.get(), s.len, j, s.ch(j), s.cl(j),
-              flag.get());
+              (const float*)s.bh(), (const float*)s.bl(), s.len, j, s.ch(j), s.cl(j), flag.get());
   }
 
   // the feature-side step in one launch (see k_vside)
-  void vside(int ncols, int write_col, double* nrm, double thresh, double* bentry, uint64_t seed,
-             uint64_t tag) {
+  void vside(int ncols, int write_col, double* nrm, const double* c, double* bentry, uint64_t seed,
+             unsigned step) {
     if (n > 32768) {   // long feature side: the multi-block kernels
       to_working(Vs, F.get());
       orth_norm(Vs, ncols, nrm);
-      if (write_col >= 0) scal_fix(Vs, write_col, nrm, thresh, bentry, seed, tag);
+      if (write_col >= 0) scal_fix(Vs, write_col, nrm, c, bentry, seed, step);
       return;
     }
-    sv_launch(ctx, "irlba_vside", k_vside, dim3(1), dim3(1024), 0, (const double*)F.get(), n,
-              Vs.h.get(), Vs.l.get(), ncols, write_col, nrm, thresh, bentry, Vs.cur.get(),
-              Vs.xh.get(), Vs.xl.get(), (unsigned long long)seed, (unsigned long long)tag);
+    sv_launch(ctx, "irlba_vside", k_vside, dim3(1), dim3(1024), 0, (const double*)F.get(), n, Vs.bh(),
+              Vs.bl(), ncols, write_col, nrm, c, bentry, Vs.cur.get(), Vs.xh.get(), Vs.xl.get(),
+              (unsigned long long)seed, step);
   }
 
   void to_working(Side& s, const double* y) {
@@ -796,55 +892,121 @@ struct Lanczos {
               s.len, s.xh.get(), s.xl.get());
   }
 
+  // out = basis * M[:, :nout]: into the other basis set (outd null) or FP64 outd
   void rotate(Side& s, const double* M, int nout, double* outd) {
     sv_launch(ctx, "irlba_rotate", k_rotate_df<16>, dim3(sv_grid_for(ctx, s.len, 256, 8)), dim3(256),
-              (size_t)work * nout * 8, (const float*)s.h.get(), (const float*)s.l.get(), s.len, s.len,
-              work, M, nout, outd ? (float*)nullptr : s.th.get(), outd ? (float*)nullptr : s.tl.get(),
-              outd, s.len);
+              (size_t)work * nout * 8, (const float*)s.bh(), (const float*)s.bl(), s.len, s.len,
+              work, M, nout, outd ? (float*)nullptr : s.th(), outd ? (float*)nullptr : s.tl(), outd,
+              s.len);
+  }
+
+  // One cycle, enqueued on the context stream without any host round trip:
+  // for a restart, V <- V Q_k, W <- W P_k, V[:, k] = f/|f| and B reset; the
+  // Lanczos steps k..work-1; the SVD of B; its summary copied to hsum.
+  // Returns the number of operator products.
+  int64_t cycle(bool restart, int k, uint64_t seed) {
+    double* s0 = scal.get() + SCAL_S;
+    double* s1 = scal.get() + SCAL_R;
+    const double* c = ctl();
+    int64_t nmv = 0;
+    if (restart) {
+      rotate(Vs, Q.get(), k, nullptr);
+      rotate(Ws, P.get(), k, nullptr);
+      Vs.flip();
+      Ws.flip();
+      df_residual_to_fp64();
+      sv_launch(ctx, "irlba_restart", k_restart_tail, dim3(sv_grid_for(ctx, n, 256, 4)), dim3(256), 0,
+                Vs.ch(k), Vs.cl(k), Vs.cur.get(), (const double*)F.get(), n,
+                (const double*)summary.get(), work, k, B.get());
+    }
+    unsigned step = 1;
+    int j = k;
+    // W[:, j] = A V[:, j]; CGS2 against W[:, :j]
+    op->N(Vs.cur.get(), ytmp.get(), nullptr, nullptr);
+    nmv++;
+    to_working(Ws, ytmp.get());
+    orth_norm(Ws, j, s0);
+    scal_fix(Ws, j, s0, c, B.get() + (int64_t)j * work + j, seed, step++);
+    while (true) {
+      // F = A^T W[:, j] - S V[:, j]; CGS2 against V[:, :j+1]
+      op->T(Ws.cur.get(), F.get(), s0, Vs.cur.get());
+      nmv++;
+      if (j + 1 < work) {
+        vside(j + 1, j + 1, s1, c, B.get() + (int64_t)j * work + j + 1, seed, step++);
+        // W[:, j+1] = A V[:, j+1] - R W[:, j]
+        op->N(Vs.cur.get(), ytmp.get(), s1, Ws.cur.get());
+        nmv++;
+        to_working(Ws, ytmp.get());
+        orth_norm(Ws, j + 1, s0);
+        scal_fix(Ws, j + 1, s0, c, B.get() + (int64_t)(j + 1) * work + j + 1, seed, step++);
+        ++j;
+      } else {
+        vside(j + 1, -1, s1, c, nullptr, seed, step++);   // residual f and |f|
+        break;
+      }
+    }
+    sv_launch(ctx, "irlba_svd", k_jacobi_svd, dim3(1), dim3(1024), (size_t)4 * work * work * 4,
+              (const double*)B.get(), work, P.get(), sig.get(), Q.get(), summary.get(),
+              (const double*)s1, 60, ctx->d_status, ctl(), eps_b);
+    SV_CUDA(cudaMemcpyAsync(hsum, summary.get(), (2 * work + 2) * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    return nmv;
+  }
+
+  // Enqueue one cycle: replay its graph (captured on first use), or launch it
+  // directly when the operator calls back to the host or launches are profiled
+  // one by one.
+  int64_t enqueue_cycle(bool restart, int k, uint64_t seed, bool graphs_on) {
+    if (!graphs_on) return cycle(restart, k, seed);
+    CycleGraph& g = graphs[restart ? 1 + Vs.set : 0];
+    if (!g.exec) {
+      // capturing runs the host side of the cycle (basis sets flip) but
+      // launches nothing: the launch count is charged per replay instead
+      int64_t l0 = ctx->launches;
+      cudaGraph_t graph = nullptr;
+      SV_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      try {
+        g.matvecs = cycle(restart, k, seed);
+      } catch (...) {
+        cudaStreamEndCapture(ctx->stream, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        ctx->launches = l0;
+        throw;
+      }
+      SV_CUDA(cudaStreamEndCapture(ctx->stream, &graph));
+      g.launches = ctx->launches - l0;
+      ctx->launches = l0;
+      cudaError_t e = cudaGraphInstantiate(&g.exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) {
+        g.exec = nullptr;
+        SV_CUDA(e);
+      }
+    } else if (restart) {
+      Vs.flip();
+      Ws.flip();
+    }
+    SV_CUDA(cudaGraphLaunch(g.exec, ctx->stream));
+    ctx->launches += g.launches;
+    return g.matvecs;
   }
 
   IrlbaResult run(const double* init_host, int maxit, double tol, uint64_t seed) {
     IrlbaResult res;
-    double* s0 = scal.get();       // S (W-side norm)
-    double* s1 = scal.get() + 1;   // R (V-side norm)
+    eps_b = sqrt(2.220446049250313e-16);
+    // control blocks: cycles start at threshold eps_b (smax = 0), the start
+    // vector is normalised unless it is zero
+    double ctl_init[6] = {eps_b, 0.0, 0.0, 1e-300, 0.0, 0.0};
+    sv_h2d(ctx, scal.get() + SCAL_CTL, ctl_init, sizeof(ctl_init));
     sv_h2d(ctx, F.get(), init_host, n * 8);
-    const double eps_b = sqrt(2.220446049250313e-16);
-    vside(0, 0, s1, 1e-300, nullptr, seed, 0);
-    int k = 0;
+    vside(0, 0, scal.get() + SCAL_R, scal.get() + SCAL_CTL0, nullptr, seed, 0);
+    bool graphs_on = op->device_only() && !ctx->profiling && !getenv("SV_NO_GRAPH");
+    const int kr = std::min(nu, work - 1);
     double smax = 0;
-    uint64_t tag = 1;
     int it = 0;
     for (; it < maxit; ++it) {
-      double thresh = eps_b * std::max(smax, 1.0);
-      int j = k;
-      // W[:, j] = A V[:, j]; CGS2 against W[:, :j]
-      op->N(Vs.cur.get(), ytmp.get(), nullptr, nullptr);
-      res.nmatvec++;
-      to_working(Ws, ytmp.get());
-      orth_norm(Ws, j, s0);
-      scal_fix(Ws, j, s0, thresh, B.get() + (int64_t)j * work + j, seed, tag++);
-      while (true) {
-        // F = A^T W[:, j] - S V[:, j]; CGS2 against V[:, :j+1]
-        op->T(Ws.cur.get(), F.get(), s0, Vs.cur.get());
-        res.nmatvec++;
-        if (j + 1 < work) {
-          vside(j + 1, j + 1, s1, thresh, B.get() + (int64_t)j * work + j + 1, seed, tag++);
-          // W[:, j+1] = A V[:, j+1] - R W[:, j]
-          op->N(Vs.cur.get(), ytmp.get(), s1, Ws.cur.get());
-          res.nmatvec++;
-          to_working(Ws, ytmp.get());
-          orth_norm(Ws, j + 1, s0);
-          scal_fix(Ws, j + 1, s0, thresh, B.get() + (int64_t)(j + 1) * work + j + 1, seed, tag++);
-          ++j;
-        } else {
-          vside(j + 1, -1, s1, thresh, nullptr, seed, tag++);   // residual f and |f|
-          break;
-        }
-      }
-      sv_launch(ctx, "irlba_svd", k_jacobi_svd, dim3(1), dim3(1024), (size_t)2 * work * work * 8,
-                (const double*)B.get(), work, P.get(), sig.get(), Q.get(), summary.get(),
-                (const double*)s1, 60, ctx->d_status);
-      sv_d2h(ctx, hsum.data(), summary.get(), (2 * work + 2) * 8);
+      res.nmatvec += enqueue_cycle(it > 0, it > 0 ? kr : 0, seed, graphs_on);
+      sv_sync(ctx);
       double rf = hsum[2 * work];
       smax = std::max(smax, hsum[0]);
       int nconv = 0;
@@ -855,19 +1017,6 @@ struct Lanczos {
         res.info = 0;
         break;
       }
-      if (it + 1 >= maxit) break;   // keep P, Q consistent with the bases
-      k = std::min(nu, work - 1);
-      // thick restart: V <- V Q_k, W <- W P_k, V[:, k] = F/|F|
-      rotate(Vs, Q.get(), k, nullptr);
-      rotate(Ws, P.get(), k, nullptr);
-      std::swap(Vs.h, Vs.th);
-      std::swap(Vs.l, Vs.tl);
-      std::swap(Ws.h, Ws.th);
-      std::swap(Ws.l, Ws.tl);
-      df_residual_to_fp64();
-      sv_launch(ctx, "irlba_restart", k_restart_tail, dim3(sv_grid_for(ctx, n, 256, 4)), dim3(256), 0,
-                Vs.ch(k), Vs.cl(k), Vs.cur.get(), (const double*)F.get(), n,
-                (const double*)summary.get(), work, k, B.get());
     }
     if (it >= maxit) res.iters = maxit;
     sv_check_device_status(ctx, "irlba");

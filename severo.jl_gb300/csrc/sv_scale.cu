@@ -479,19 +479,21 @@ __global__ void __launch_bounds__(RB_THREADS) k_spmv_rb(
     float inv = inv_f[f], clip = clip_f[f];
     float acc = 0.f;
     int64_t a0 = s & ~3ll;
+    // guarded loads for both groups: measured faster here than the
+    // unconditional-first form (1.37 vs 1.72 ms at 1.3M cells), the opposite of
+    // k_spmv_csr
     for (int64_t gg = a0 + 4 * lane; gg < e; gg += 256) {
       int ci[2][4];
       float av[2][4];
-      bool two = gg + 128 < e;
-      ld4(rb_idx, gg, ci[0]);
-      ld4v(rb_val, gg, av[0]);
-      if (two) {
-        ld4(rb_idx, gg + 128, ci[1]);
-        ld4v(rb_val, gg + 128, av[1]);
-      }
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+        if (gg + 128 * h < e) {
+          ld4(rb_idx, gg + 128 * h, ci[h]);
+          ld4v(rb_val, gg + 128 * h, av[h]);
+        }
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        if (h == 1 && !two) break;
+        if (gg + 128 * h >= e) break;
         int64_t gh = gg + 128 * h;
 #pragma unroll
         for (int t = 0; t < 4; ++t)

@@ -126,3 +126,36 @@ def test_pca_pipeline(sv, ctx, O, dtype, tol_s):
     # coordinates are U diag(s) (embedding.jl:67)
     assert np.allclose(np.abs(em.coordinates.T @ em.coordinates), np.diag(s ** 2), rtol=1e-6,
                        atol=1e-6 * s[0] ** 2)
+
+
+@pytest.mark.parametrize("rank", [None, 4])
+def test_irlba_graph_replay_matches_direct_launches(sv, ctx, monkeypatch, rank):
+    """Each Lanczos cycle over a device matrix is captured once as a CUDA graph
+    and replayed; the replay issues the same kernels in the same order as direct
+    launches, so the results agree bit for bit (rank 4 < work also exercises the
+    breakdown restarts inside the graph)."""
+    rng = np.random.default_rng(18)
+    if rank is None:
+        X = sp.random(5000, 600, density=0.05, random_state=19, format="csc")
+    else:
+        X = sp.csc_matrix(rng.standard_normal((5000, rank)) @ rng.standard_normal((rank, 600)))
+    mu = np.asarray(X.mean(axis=0)).ravel()
+    S = sv.CenteredMatrix.from_sparse(X, mu, dtype="float32", ctx=ctx)
+    nu = 3
+    out = {}
+    for mode in ("graph", "direct"):
+        if mode == "direct":
+            monkeypatch.setenv("SV_NO_GRAPH", "1")
+        else:
+            monkeypatch.delenv("SV_NO_GRAPH", raising=False)
+        l0 = ctx.launches()
+        U, s, V, info = sv.irlba(S, nu, tol=1e-8, seed=6, return_info=True)
+        out[mode] = (U, s, V, info, ctx.launches() - l0)
+    Ug, sg, Vg, ig, lg = out["graph"]
+    Ud, sd, Vd, idd, ld = out["direct"]
+    assert ig == idd and lg == ld
+    assert np.array_equal(sg, sd) and np.array_equal(Ug, Ud) and np.array_equal(Vg, Vd)
+    ss = np.linalg.svd(X.toarray() - mu, compute_uv=False)
+    assert np.max(np.abs(sg - ss[:nu]) / ss[:nu]) < 1e-5
+    if rank is None:
+        assert ig["iters"] > 2   # several replays of the restart graphs

@@ -128,3 +128,29 @@ def test_knn_bf16_exclude_self_and_cosine(sv, ctx, O):
 def test_knn_bad_k(sv, ctx):
     with pytest.raises(sv.SeveroGPUError):
         sv.ann(np.zeros((5, 3)), 6, ctx=ctx)
+
+
+def gmm_points(n, d, ncomp, seed):
+    """n points of a ncomp-component Gaussian mixture in d dimensions: means
+    ~ N(0, 4^2), unit noise, dimension i scaled by 1/sqrt(i)."""
+    rng = np.random.default_rng(seed)
+    means = rng.normal(0, 4, (ncomp, d))
+    X = means[rng.integers(0, ncomp, n)]
+    X += rng.standard_normal((n, d))
+    X *= 1.0 / np.sqrt(np.arange(1, d + 1))
+    return X.astype(np.float32)
+
+
+def test_knn_stress_2m_bf16_recall(sv, ctx, O):
+    """2,000,000 x 50 FP32 points (60-component mixture), k = 30: BF16 tensor-core
+    candidates (64 per point) with the FP32 re-rank against FP64 brute force on
+    500 sampled queries; recall@30 >= 0.999."""
+    n, d, k = 2_000_000, 50, 30
+    X = gmm_points(n, d, 60, 20261205)
+    idx, dist = sv.ann(X, k, precision="bf16", ctx=ctx)
+    q = np.random.default_rng(5).choice(n, 500, replace=False)
+    ref = O.knn_exact_queries(X, q, k)
+    hits = sum(len(set(a - 1) & set(b)) for a, b in zip(idx[q], ref))
+    assert hits / ref.size >= 0.999, hits / ref.size
+    assert np.all(idx[q, 0] == q + 1)
+    assert np.all(np.diff(dist[q], axis=1) >= 0)
