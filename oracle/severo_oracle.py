@@ -25,6 +25,53 @@ import numpy as np
 import scipy.sparse as sp
 
 # ---------------------------------------------------------------------------
+# filtering -- src/filtering.jl
+# ---------------------------------------------------------------------------
+
+
+def filter_cells(A, min_features=0, min_feature_count=0, min_umi=0):
+    """src/filtering.jl:22-35.  A: cells x genes CSC of counts.  A feature is
+    detected in a cell when its count exceeds min_feature_count; every entry,
+    implicit zeros included, is tested (sum(>(t), A, dims=2)).  Keeps cells with
+    at least min_features detected features and, when min_umi > 0, a count
+    total strictly above min_umi.  Returns (A[CI, :], CI)."""
+    A = sp.csc_matrix(A)
+    R = A.tocsr()
+    n_genes = A.shape[1]
+    lens = np.diff(R.indptr)
+    det = np.add.reduceat((R.data > min_feature_count).astype(np.int64), R.indptr[:-1]) if R.nnz else np.zeros(A.shape[0], np.int64)
+    det = np.where(lens > 0, det, 0)
+    if min_feature_count < 0:                  # implicit zeros are detected too
+        det = det + (n_genes - lens)
+    CI = det >= min_features
+    if min_umi > 0:
+        tot = np.asarray(R.sum(axis=1)).ravel()
+        CI &= tot > min_umi
+    if not CI.all():
+        A = sp.csc_matrix(A[CI, :])
+    return A, CI
+
+
+def filter_features(A, min_cells=0):
+    """src/filtering.jl:15-20: keeps genes with at least min_cells entries > 0.
+    Returns (A[:, FI], FI)."""
+    A = sp.csc_matrix(A)
+    pos = (A.data > 0).astype(np.int64)
+    cnt = np.add.reduceat(pos, A.indptr[:-1]) if A.nnz else np.zeros(A.shape[1], np.int64)
+    cnt = np.where(np.diff(A.indptr) > 0, cnt, 0)
+    FI = cnt >= min_cells
+    return sp.csc_matrix(A[:, FI]), FI
+
+
+def filter_counts(A, min_cells=0, min_features=0, min_feature_count=0, min_umi=0):
+    """src/filtering.jl:98-103: filter_cells, then filter_features on the result.
+    Returns (A', CI, FI)."""
+    A, CI = filter_cells(A, min_features, min_feature_count, min_umi)
+    A, FI = filter_features(A, min_cells)
+    return A, CI, FI
+
+
+# ---------------------------------------------------------------------------
 # normalisation -- src/normalize.jl
 # ---------------------------------------------------------------------------
 

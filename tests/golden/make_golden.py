@@ -3,6 +3,9 @@ this path, with the expected values those tests assert, evaluated from the tests
 own right-hand-side expressions (plain dense numpy, independent of the oracle).
 
 Sources (Severo.jl project paths):
+  test/test_input.jl:19-43    filter_counts(min_features=1, min_cells=2, min_umi=2)
+                              on the 10 x 5 count literal keeps cells 1,2,3,4,5,8,9
+                              and genes 1,2,4,5 (:40-42).
   test/test_input.jl:45-101   normalize_cells on the 10 x 5 count literal, after
                               filter_counts(min_features=1, min_cells=2, min_umi=2),
                               whose result the test pins as cells 1,2,3,4,5,8,9 and
@@ -52,6 +55,13 @@ def normalize_fixture():
         "log": np.log1p(rel).tolist(),
     }
     return out
+
+
+def filter_fixture():
+    return {"counts": X10.tolist(), "min_features": 1, "min_cells": 2, "min_umi": 2,
+            "cells": [1, 2, 3, 4, 5, 8, 9], "genes": [1, 2, 4, 5],
+            "filtered": X10[np.ix_(np.array([1, 2, 3, 4, 5, 8, 9]) - 1,
+                                   np.array([1, 2, 4, 5]) - 1)].tolist()}
 
 
 def scaling_fixture():
@@ -133,6 +143,7 @@ def snn_fixture():
 
 def main():
     data = {
+        "filter": filter_fixture(),
         "normalize": normalize_fixture(),
         "scaling": scaling_fixture(),
         "centered": centered_fixture(),
