@@ -125,6 +125,19 @@ int sv_counts_download_csr(sv_context* ctx, const sv_counts* c, int64_t* rowptr,
                            int32_t* colidx, int32_t* counts);
 int sv_counts_free(sv_counts* c);
 
+/* ---- filter_counts (src/filtering.jl:15-35,98-103) --------------------------
+ * Cells first: a cell is kept when at least min_features of its genes have a
+ * count > min_feature_count (implicit zeros included in the test) and, when
+ * min_umi > 0, its count total is > min_umi.  Then genes: kept when at least
+ * min_cells of the kept cells have a count > 0.  *out is a new count matrix
+ * (kept rows and columns, in order, stored entries copied as they are);
+ * cells_kept (n_cells) / genes_kept (n_genes) receive the 0/1 masks the
+ * reference returns as CI / FI (either may be NULL).  filter_cells is
+ * min_cells = 0; filter_features is the cell thresholds at 0. */
+int sv_filter_counts(sv_context* ctx, const sv_counts* counts, int64_t min_cells,
+                     int64_t min_features, int64_t min_feature_count, int64_t min_umi,
+                     uint8_t* cells_kept, uint8_t* genes_kept, sv_counts** out);
+
 /* ---- normalize_cells (src/normalize.jl:17-55,76-79) -------------------------
  * method SV_LOGNORMALIZE or SV_RELATIVECOUNTS; value dtype SV_F64 (the
  * reference default), SV_F32 or SV_BF16 (values computed in FP32 and stored
@@ -292,6 +305,18 @@ int sv_graph_info(const sv_graph* g, int64_t* n, int64_t* nnz);
  * (nnz) as 1-based Int64, nzval (nnz) in the graph's dtype.  Any may be NULL. */
 int sv_graph_download(sv_context* ctx, const sv_graph* g, int64_t* colptr, int64_t* rowval,
                       void* nzval);
+/* Hand-off to Louvain: the arrays of Network(snn) (src/modularity.jl:163-194)
+ * written in Julia's isbits layouts, so that the caller's Vector{Node{T}} and
+ * Vector{Edge{T}} receive them without a host rebuild:
+ *   Edge{T}: { int64 node (1-based); T weight; }                 16 bytes
+ *   Node{T}: { T weight; int64 first; int64 last; }              24 bytes
+ *            (weight = sum of the column's non-self weights, in column order;
+ *             edges first:last, 1-based, empty when first > last)
+ * Self links are excluded; *totw (T) is the sum of all edge weights taken edge
+ * by edge in order, as the reference accumulates it (tot_self is zero).  Call
+ * with nodes = edges = totw = NULL to obtain *nedges first. */
+int sv_graph_network(sv_context* ctx, const sv_graph* g, int64_t* nedges, void* nodes,
+                     void* edges, void* totw);
 int sv_graph_free(sv_graph* g);
 
 #ifdef __cplusplus

@@ -11,7 +11,7 @@ reference file:line it follows (paths relative to the Severo.jl project).
 Parity status: the reference is Julia and cannot be executed on this machine
 (no Julia toolchain; its native ``libcell`` is a binary-only dependency that is
 not available).  The restatement is pinned against every literal fixture the
-reference's own tests hold for this path (test/test_input.jl:45-101,
+reference's own tests hold for this path (test/test_input.jl:19-101,
 test/test_scaling.jl:20-131, test/test_irlba.jl:24-116, test/test_nn.jl:21-96)
 through the committed fixtures in ``tests/golden``; irlba, kNN and SNN have no
 stored expected outputs in the reference, so they are pinned by the reference
@@ -29,6 +29,12 @@ import scipy.sparse as sp
 # ---------------------------------------------------------------------------
 
 
+def _segment_sum(x, ptr):
+    """Sum of x over each segment [ptr[i], ptr[i+1]) (empty segments give 0)."""
+    c = np.concatenate(([0], np.cumsum(x, dtype=np.int64)))
+    return c[ptr[1:]] - c[ptr[:-1]]
+
+
 def filter_cells(A, min_features=0, min_feature_count=0, min_umi=0):
     """src/filtering.jl:22-35.  A: cells x genes CSC of counts.  A feature is
     detected in a cell when its count exceeds min_feature_count; every entry,
@@ -39,8 +45,7 @@ def filter_cells(A, min_features=0, min_feature_count=0, min_umi=0):
     R = A.tocsr()
     n_genes = A.shape[1]
     lens = np.diff(R.indptr)
-    det = np.add.reduceat((R.data > min_feature_count).astype(np.int64), R.indptr[:-1]) if R.nnz else np.zeros(A.shape[0], np.int64)
-    det = np.where(lens > 0, det, 0)
+    det = _segment_sum((R.data > min_feature_count).astype(np.int64), R.indptr)
     if min_feature_count < 0:                  # implicit zeros are detected too
         det = det + (n_genes - lens)
     CI = det >= min_features
@@ -56,9 +61,7 @@ def filter_features(A, min_cells=0):
     """src/filtering.jl:15-20: keeps genes with at least min_cells entries > 0.
     Returns (A[:, FI], FI)."""
     A = sp.csc_matrix(A)
-    pos = (A.data > 0).astype(np.int64)
-    cnt = np.add.reduceat(pos, A.indptr[:-1]) if A.nnz else np.zeros(A.shape[1], np.int64)
-    cnt = np.where(np.diff(A.indptr) > 0, cnt, 0)
+    cnt = _segment_sum((A.data > 0).astype(np.int64), A.indptr)
     FI = cnt >= min_cells
     return sp.csc_matrix(A[:, FI]), FI
 
@@ -165,10 +168,9 @@ def mean_var(A, acc=np.float64):
     T = np.dtype(acc)
     data = A.data.astype(np.float64)
     nnz_col = np.diff(A.indptr)
-    sums = np.add.reduceat(data, A.indptr[:-1]) if data.size else np.zeros(d)
-    sums = np.where(nnz_col > 0, sums, 0.0)
-    mu = sums / n
     col = np.repeat(np.arange(d), nnz_col)
+    sums = np.bincount(col, weights=data, minlength=d)
+    mu = sums / n
     dev = data - mu[col]
     m2 = np.bincount(col, weights=dev * dev, minlength=d) + (n - nnz_col) * mu * mu
     var = m2 / (n - 1)
@@ -539,6 +541,44 @@ def shared_nearest_neighbours(X, k, prune=1.0 / 15.0, include_self=True, dtype=N
     idx, _ = knn_exact(X, k, include_self)
     G = knn_graph(idx + 1, X.shape[0])
     return jaccard_index(G, k, prune, dt)
+
+
+# ---------------------------------------------------------------------------
+# Louvain input -- src/modularity.jl
+# ---------------------------------------------------------------------------
+
+
+def network(snn):
+    """src/modularity.jl:163-194: Network(snn) of a square CSC graph with sorted
+    rows.  Returns (node_weight, first, last, edge_node, edge_weight, totw):
+    self links skipped; node weight = the column's non-self weights summed in
+    order in the graph's dtype; edges first:last (1-based); totw summed edge by
+    edge in order.  Pure-Python loop: small graphs."""
+    A = sp.csc_matrix(snn)
+    n = A.shape[0]
+    T = A.dtype.type
+    node_w = np.zeros(n, A.dtype)
+    first = np.zeros(n, np.int64)
+    last = np.zeros(n, np.int64)
+    e_node, e_w = [], []
+    totw = T(0)
+    so_far = 0
+    for i in range(n):
+        w = T(0)
+        start = so_far + 1
+        for e in range(A.indptr[i], A.indptr[i + 1]):
+            rv, nz = A.indices[e], A.data[e]
+            if rv == i:
+                continue
+            totw = T(totw + nz)
+            w = T(w + nz)
+            so_far += 1
+            e_node.append(rv + 1)
+            e_w.append(nz)
+        node_w[i] = w
+        first[i] = start
+        last[i] = so_far
+    return (node_w, first, last, np.array(e_node, np.int64), np.array(e_w, A.dtype), totw)
 
 
 # ---------------------------------------------------------------------------

@@ -33,7 +33,7 @@ from ._lib import (ConvergenceError, SeveroGPUError, SV_BF16, SV_COSINE, SV_EUCL
 
 __all__ = [
     "Context", "CountMatrix", "DataMatrix", "CenteredMatrix", "LinearEmbedding",
-    "normalize_cells", "scale_features", "irlba", "irlba_callback", "pca", "embedding", "ann",
+    "filter_counts", "filter_cells", "filter_features", "normalize_cells", "scale_features", "irlba", "irlba_callback", "pca", "embedding", "ann",
     "nearest_neighbours", "jaccard_index", "shared_nearest_neighbours", "SeveroGPUError",
     "ConvergenceError", "default_context",
 ]
@@ -272,6 +272,33 @@ class DataMatrix(_Handle):
     def to_csc(self):
         c = self.counts.to_csc()
         return sp.csc_matrix((self.values_csc(), c.indices, c.indptr), shape=c.shape)
+
+
+def filter_counts(X: CountMatrix, min_cells=0, min_features=0, min_feature_count=0, min_umi=0):
+    """src/filtering.jl:98-103 on the device: cells first (filter_cells), then
+    genes (filter_features).  Returns (filtered CountMatrix, CI, FI), CI / FI the
+    boolean masks of the kept cells / genes."""
+    ctx = X.ctx
+    m, n = X.shape
+    ci = np.zeros(m, np.uint8)
+    fi = np.zeros(n, np.uint8)
+    h = C.c_void_p()
+    L.check(ctx.lib.sv_filter_counts(ctx.h, X.h, int(min_cells), int(min_features),
+                                     int(min_feature_count), int(min_umi), _ptr(ci), _ptr(fi),
+                                     C.byref(h)))
+    return CountMatrix(ctx, h), ci.astype(bool), fi.astype(bool)
+
+
+def filter_cells(X: CountMatrix, min_features=0, min_feature_count=0, min_umi=0):
+    """src/filtering.jl:22-35: (filtered CountMatrix, CI)."""
+    A, ci, _ = filter_counts(X, 0, min_features, min_feature_count, min_umi)
+    return A, ci
+
+
+def filter_features(X: CountMatrix, min_cells=0):
+    """src/filtering.jl:15-20: (filtered CountMatrix, FI)."""
+    A, _, fi = filter_counts(X, min_cells, 0, 0, 0)
+    return A, fi
 
 
 def normalize_cells(X, method="lognormalize", scale_factor=1.0, dtype="float64",
@@ -536,10 +563,32 @@ class Graph(_Handle):
         L.check(self.ctx.lib.sv_graph_download(self.ctx.h, self.h, _ptr(cp), _ptr(rv), _ptr(vv)))
         return sp.csc_matrix((vv, rv - 1, cp - 1), shape=(n.value, n.value))
 
+    def network(self, dtype):
+        """Network(snn) of src/modularity.jl:163-194 (the Louvain input), as
+        numpy structured arrays in Julia's Node{T} / Edge{T} layouts:
+        (nodes[weight, first, last], edges[node, weight], totw)."""
+        T = np.dtype(dtype)
+        node_t = np.dtype({"names": ["weight", "first", "last"], "formats": [T, np.int64, np.int64],
+                           "offsets": [0, 8, 16], "itemsize": 24})
+        edge_t = np.dtype({"names": ["node", "weight"], "formats": [np.int64, T],
+                           "offsets": [0, 8], "itemsize": 16})
+        n, nnz = C.c_int64(), C.c_int64()
+        L.check(self.ctx.lib.sv_graph_info(self.h, C.byref(n), C.byref(nnz)))
+        ne = C.c_int64()
+        L.check(self.ctx.lib.sv_graph_network(self.ctx.h, self.h, C.byref(ne), None, None, None))
+        nodes = np.zeros(n.value, node_t)
+        edges = np.zeros(ne.value, edge_t)
+        tot = np.zeros(1, T)
+        L.check(self.ctx.lib.sv_graph_network(self.ctx.h, self.h, C.byref(ne), _ptr(nodes), _ptr(edges),
+                                              _ptr(tot)))
+        return nodes, edges, tot[0]
 
-def jaccard_index(nn_index, k=None, prune=1.0 / 15.0, dtype=np.float64, ctx: Context | None = None):
+
+def jaccard_index(nn_index, k=None, prune=1.0 / 15.0, dtype=np.float64, ctx: Context | None = None,
+                  keep=False):
     """src/neighbours.jl:127-155 from neighbour lists (n x k, 1-based Int32);
-    k=None selects the diag variant (:96-108)."""
+    k=None selects the diag variant (:96-108).  keep=True also returns the
+    device graph (for Graph.network)."""
     ctx = ctx or default_context()
     nn = np.asfortranarray(nn_index, dtype=np.int32)
     n, kk = nn.shape
@@ -547,7 +596,9 @@ def jaccard_index(nn_index, k=None, prune=1.0 / 15.0, dtype=np.float64, ctx: Con
     h = C.c_void_p()
     L.check(ctx.lib.sv_snn_host(ctx.h, _ptr(nn), n, kk, -1 if k is None else int(k), float(prune), dt,
                                  C.byref(h)))
-    return Graph(ctx, h).to_csc(np.float64 if dt == SV_F64 else np.float32)
+    g = Graph(ctx, h)
+    A = g.to_csc(np.float64 if dt == SV_F64 else np.float32)
+    return (A, g) if keep else A
 
 
 def shared_nearest_neighbours(X, k, prune=1.0 / 15.0, metric="euclidean", include_self=True,

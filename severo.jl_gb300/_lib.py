@@ -77,6 +77,7 @@ SIGNATURES = {
     "sv_counts_download_csc": (i32, [vp, vp, vp, vp, vp]),
     "sv_counts_download_csr": (i32, [vp, vp, vp, vp, vp]),
     "sv_counts_free": (i32, [vp]),
+    "sv_filter_counts": (i32, [vp, vp, i64, i64, i64, i64, vp, vp, P(vp)]),
     "sv_normalize_cells": (i32, [vp, vp, i32, dbl, i32, P(vp)]),
     "sv_normalize_csc_noalloc": (i32, [vp, vp, vp, i64, i64, i64, i32, dbl, vp, vp]),
     "sv_data_download_csc": (i32, [vp, vp, vp]),
@@ -107,6 +108,7 @@ SIGNATURES = {
     "sv_snn_knn": (i32, [vp, vp, i64, dbl, i32, P(vp)]),
     "sv_graph_info": (i32, [vp, P(i64), P(i64)]),
     "sv_graph_download": (i32, [vp, vp, vp, vp, vp]),
+    "sv_graph_network": (i32, [vp, vp, P(i64), vp, vp, vp]),
     "sv_graph_free": (i32, [vp]),
 }
 

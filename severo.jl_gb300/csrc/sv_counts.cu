@@ -306,7 +306,7 @@ void upload_idx(sv_context* ctx, const void* host, int64_t n, int64_t base, int6
 }  // namespace
 
 // Builds the CSR copy from the CSC copy already on the device.
-static void build_csr_from_csc(sv_context* ctx, sv_counts* c) {
+void sv_build_csr_from_csc(sv_context* ctx, sv_counts* c) {
   DevBuf<unsigned long long> rcnt(c->n_cells + 1);
   sv_memset(ctx, rcnt.get(), 0, (c->n_cells + 1) * sizeof(unsigned long long));
   sv_launch(ctx, "counts_check_hist", k_csc_check_hist, dim3(sv_grid_for(ctx, c->n_genes * 32, 256)),
@@ -410,7 +410,7 @@ SV_API int sv_counts_upload_csc(sv_context* ctx, int64_t n_cells, int64_t n_gene
       upload_idx<int64_t>(ctx, nzval, nnz, 0, (1ll << 31) - 1, c->csc_count.get());
     }
     sv_check_device_status(ctx, "sv_counts_upload_csc");
-    build_csr_from_csc(ctx, c);
+    sv_build_csr_from_csc(ctx, c);
   } catch (...) {
     delete c;
     throw;

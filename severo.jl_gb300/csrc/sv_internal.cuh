@@ -184,6 +184,8 @@ struct sv_centered {
   DevBuf<int64_t> feat_start;  // nf: CSC range of the feature
   DevBuf<int64_t> feat_end;
   DevBuf<double> mean, std_, mu;      // nf (FP64)
+  DevBuf<float> mu_h, mu_l;           // nf: mu as double-float (the FP64-free products)
+  int grid_csr = 1, grid_csr_df = 1;  // resident blocks of the X v kernels (one wave)
   DevBuf<float> inv_std_f, clip_f;    // nf (FP32 form of the scale / clip)
   DevBuf<double> inv_std_d, clip_d;   // nf (FP64 form, for FP64 data)
   // chunk table of the CSC (X^T u) product
@@ -283,3 +285,6 @@ void sv_h2d(sv_context* ctx, void* dst, const void* src, size_t bytes);
 void sv_d2h(sv_context* ctx, void* dst, const void* src, size_t bytes);
 void sv_sync(sv_context* ctx);
 int sv_grid_for(sv_context* ctx, int64_t work_items, int per_block, int max_per_sm = 8);
+// builds (or rebuilds) the CSR copy of a count matrix from its device CSC copy
+// (sv_counts.cu); checks the CSC invariants on the way
+void sv_build_csr_from_csc(sv_context* ctx, sv_counts* c);

@@ -11,29 +11,32 @@
 // FP32 pipe with exact two-product / two-sum steps: GB300 executes FP64 at
 // 1/57 of its FP32 rate, and the reorthogonalisation and restart rotation are
 // the only O(m * work) arithmetic of the method.  Reductions across blocks,
-// the norms, the small matrix B and its SVD are FP64.
+// the norms and the small matrix B are FP64; the SVD of B is double-float.
 //
 // Every new vector is reorthogonalised against its basis by classical
 // Gram-Schmidt applied twice (CGS2).  After `work` steps B (work x work, upper
-// triangular) is decomposed by a one-block FP64 one-sided Jacobi SVD; the nu
+// triangular) is decomposed by a one-block one-sided Jacobi SVD; the nu
 // leading Ritz vectors are kept (thick restart):
 //   V <- [V Q_k, f/|f|],  W <- W P_k,  B <- [diag(s_k) rho; 0 ...],
 //   rho_i = |f| P[work-1, i]
 // and convergence is declared when every |rho_i| < tol * max singular value
-// (the residual ||A^T u_i - s_i v_i||).  The host reads back 2*work+2 doubles
-// per restart; everything else stays on the device.
+// (the residual ||A^T u_i - s_i v_i||).  A cycle (restart, Lanczos steps, SVD)
+// is enqueued without host round trips and, over a device operator, captured
+// once as a CUDA graph and replayed; the host reads back 2*work+2 doubles per
+// cycle to test convergence.
 #include "sv_internal.cuh"
 #include <math.h>
 #include <stdlib.h>
 
 void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const double* x, double* y,
                        double alpha, double beta, const double* csub, const double* z);
+bool sv_centered_apply_df(sv_context* ctx, const sv_centered* S, const float* xh, const float* xl,
+                          float* yh, float* yl, const double* csub, const float* zh, const float* zl);
 
 namespace {
 
 constexpr int RED_BLOCKS = 608;    // blocks of the tall reductions (4 per SM)
 constexpr int MAX_WORK = 96;       // largest Lanczos basis the Jacobi kernel holds in smem
-constexpr int JB = 8;              // basis columns per pass of the dot-product kernel
 
 // ---- double-float arithmetic --------------------------------------------------
 __device__ __forceinline__ void df_split(double x, float& h, float& l) {
@@ -92,129 +95,190 @@ __device__ __forceinline__ bool last_block(unsigned int* counter, bool* flag_sme
   return *flag_smem;
 }
 
-// c[j] = Q[:, j] . x  (j < ncols): Q and x double-float; per-block FP64 partials.
-// Block of 8 warps over a contiguous row segment; warp w owns the columns
-// j = w, w + 8, ... (at most NJ of them), lanes walk 32 consecutive rows, so every
-// basis element is read once with coalesced loads and each warp reduces its
-// columns across lanes once at the end.
-constexpr int NJ = (MAX_WORK + 7) / 8;
-__global__ void __launch_bounds__(256) k_dots_df(const float* __restrict__ Qh,
-                                                 const float* __restrict__ Ql, int64_t ld,
-                                                 int ncols, const float* __restrict__ xh,
-                                                 const float* __restrict__ xl, int64_t len,
-                                                 double* __restrict__ part, double* __restrict__ c,
-                                                 unsigned int* __restrict__ counter) {
+// One pass of the CGS2 reorthogonalisation of the working vector x against the
+// basis Q[:, :ncols] (both double-float), in three fusable parts:
+//   UPDATE  x -= Q cin (cin from the previous pass), x written back;
+//   DOTS    cout = Q^T x (of the updated x when UPDATE);
+//   NORM    *nrm = ||x|| (after the update).
+// A CGS2 step is then three launches that read the basis three times: DOTS
+// (x taken from the FP64 product y and stored as the working vector), UPDATE +
+// DOTS, UPDATE + NORM.  Block of 8 warps over a contiguous row segment, 64 rows
+// per iteration (two per lane); warp w owns the columns j = w + 8t, so every
+// basis element is loaded once, coalesced, with 4*NJ loads in flight per thread.
+// The update sums each row's 8 per-warp partial products through shared memory;
+// the dot products accumulate per lane and reduce across lanes once at the end.
+// Per-block FP64 partials; the last block reduces them in block order
+// (deterministic).  NJ = columns per warp: 8 for bases of up to 64 columns,
+// 12 up to MAX_WORK (fewer registers, more resident blocks for the usual
+// nu + 7 basis).
+
+// (sh, sl) += (bh, bl), unnormalised
+__device__ __forceinline__ void df_acc(float& sh, float& sl, float bh, float bl) {
+  float t = sh + bh;
+  float v = t - sh;
+  float err = (sh - (t - v)) + (bh - v);
+  sh = t;
+  sl += err + bl;
+}
+
+template <int NJ, bool UPDATE, bool DOTS, bool NORM>
+__global__ void __launch_bounds__(256) k_cgs_df(const float* __restrict__ Qh,
+                                                const float* __restrict__ Ql, int64_t ld, int ncols,
+                                                float* __restrict__ xh, float* __restrict__ xl,
+                                                const double* __restrict__ y, int64_t len,
+                                                const double* __restrict__ cin,
+                                                double* __restrict__ part, double* __restrict__ npart,
+                                                double* __restrict__ cout, double* __restrict__ nrm,
+                                                unsigned int* __restrict__ counter) {
+  __shared__ float csh[MAX_WORK], csl[MAX_WORK];
+  __shared__ float redh[8][64], redl[8][64];
+  __shared__ float xsh[64], xsl[64];
+  __shared__ double nsh[32];
   __shared__ bool last;
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  if (UPDATE)
+    for (int j = tid; j < ncols; j += blockDim.x) df_split(cin[j], csh[j], csl[j]);
+  __syncthreads();
   int64_t seg = (len + gridDim.x - 1) / gridDim.x;
   int64_t r0 = (int64_t)blockIdx.x * seg, r1 = min(len, r0 + seg);
   float ah[NJ], al[NJ];
 #pragma unroll
   for (int t = 0; t < NJ; ++t) ah[t] = al[t] = 0.f;
-  // two 32-row groups per iteration: all loads of both groups are issued before
-  // the arithmetic (memory-level parallelism)
-  for (int64_t i = r0 + lane; i < r1; i += 64) {
-    bool two = i + 32 < r1;
-    float bh0 = xh[i], bl0 = xl[i];
-    float bh1 = two ? xh[i + 32] : 0.f, bl1 = two ? xl[i + 32] : 0.f;
+  double nacc = 0;
+  for (int64_t i0 = r0; i0 < r1; i0 += 64) {
+    int64_t ia = i0 + lane, ib = ia + 32;
+    bool va = ia < r1, vb = ib < r1;
     float q0h[NJ], q0l[NJ], q1h[NJ], q1l[NJ];
 #pragma unroll
     for (int t = 0; t < NJ; ++t) {
       int j = w + 8 * t;
-      int64_t o = (int64_t)j * ld + i;
+      int64_t o = (int64_t)j * ld + ia;
       q0h[t] = q0l[t] = q1h[t] = q1l[t] = 0.f;
       if (j < ncols) {
-        q0h[t] = Qh[o];
-        q0l[t] = Ql[o];
-        if (two) {
+        if (va) {
+          q0h[t] = Qh[o];
+          q0l[t] = Ql[o];
+        }
+        if (vb) {
           q1h[t] = Qh[o + 32];
           q1l[t] = Ql[o + 32];
         }
       }
     }
+    float x0h, x0l, x1h, x1l;
+    if (UPDATE) {
+      float s0h = 0.f, s0l = 0.f, s1h = 0.f, s1l = 0.f;
+#pragma unroll
+      for (int t = 0; t < NJ; ++t) {
+        int j = w + 8 * t;
+        if (j < ncols) {
+          df_fma(s0h, s0l, q0h[t], q0l[t], csh[j], csl[j]);
+          df_fma(s1h, s1l, q1h[t], q1l[t], csh[j], csl[j]);
+        }
+      }
+      redh[w][lane] = s0h;
+      redl[w][lane] = s0l;
+      redh[w][lane + 32] = s1h;
+      redl[w][lane + 32] = s1l;
+      __syncthreads();
+      if (tid < 64) {
+        int64_t i = i0 + tid;
+        float h = 0.f, l = 0.f;
+        if (i < r1) {
+          float sh = 0.f, sl = 0.f;
+#pragma unroll
+          for (int u = 0; u < 8; ++u) df_acc(sh, sl, redh[u][tid], redl[u][tid]);
+          h = xh[i];
+          l = xl[i];
+          df_sub(h, l, sh, sl);
+          xh[i] = h;
+          xl[i] = l;
+          if (NORM) {
+            double v = df_val(h, l);
+            nacc += v * v;
+          }
+        }
+        xsh[tid] = h;
+        xsl[tid] = l;
+      }
+      __syncthreads();
+      x0h = xsh[lane];
+      x0l = xsl[lane];
+      x1h = xsh[lane + 32];
+      x1l = xsl[lane + 32];
+    } else if (y) {
+      // x from the FP64 product; warp 0 stores the working copy
+      double ya = va ? y[ia] : 0.0, yb = vb ? y[ib] : 0.0;
+      df_split(ya, x0h, x0l);
+      df_split(yb, x1h, x1l);
+      if (w == 0) {
+        if (va) {
+          xh[ia] = x0h;
+          xl[ia] = x0l;
+        }
+        if (vb) {
+          xh[ib] = x1h;
+          xl[ib] = x1l;
+        }
+      }
+    } else {
+      x0h = va ? xh[ia] : 0.f;
+      x0l = va ? xl[ia] : 0.f;
+      x1h = vb ? xh[ib] : 0.f;
+      x1l = vb ? xl[ib] : 0.f;
+    }
+    if (DOTS) {
+#pragma unroll
+      for (int t = 0; t < NJ; ++t) {
+        if (w + 8 * t < ncols) {
+          df_fma(ah[t], al[t], q0h[t], q0l[t], x0h, x0l);
+          df_fma(ah[t], al[t], q1h[t], q1l[t], x1h, x1l);
+        }
+      }
+    }
+  }
+  if (DOTS) {
 #pragma unroll
     for (int t = 0; t < NJ; ++t) {
-      if (w + 8 * t < ncols) {
-        df_fma(ah[t], al[t], q0h[t], q0l[t], bh0, bl0);
-        df_fma(ah[t], al[t], q1h[t], q1l[t], bh1, bl1);
+      int j = w + 8 * t;
+      if (j < ncols) {
+        // warp reduction in double-float (FP32 shuffles), one FP64 value per warp
+        float h = ah[t], l = al[t];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          float h2 = __shfl_xor_sync(0xffffffffu, h, o);
+          float l2 = __shfl_xor_sync(0xffffffffu, l, o);
+          float s = h + h2;
+          float v = s - h;
+          float err = (h - (s - v)) + (h2 - v);
+          float lo = err + l + l2;
+          h = s + lo;
+          l = lo - (h - s);
+        }
+        if (lane == 0) part[(int64_t)blockIdx.x * ncols + j] = df_val(h, l);
       }
     }
   }
-#pragma unroll
-  for (int t = 0; t < NJ; ++t) {
-    int j = w + 8 * t;
-    if (j < ncols) {
-      // warp reduction in double-float (FP32 shuffles), one FP64 value per warp
-      float h = ah[t], l = al[t];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        float h2 = __shfl_xor_sync(0xffffffffu, h, o);
-        float l2 = __shfl_xor_sync(0xffffffffu, l, o);
-        float s = h + h2;
-        float v = s - h;
-        float err = (h - (s - v)) + (h2 - v);
-        float lo = err + l + l2;
-        h = s + lo;
-        l = lo - (h - s);
-      }
-      if (lane == 0) part[(int64_t)blockIdx.x * ncols + j] = df_val(h, l);
-    }
+  if (NORM) {
+    nacc = block_sum(nacc, nsh);
+    if (tid == 0) npart[blockIdx.x] = nacc;
   }
   if (last_block(counter, &last)) {
-    // one warp per column, lanes over blocks (block order fixed: deterministic)
-    for (int j = w; j < ncols; j += 8) {
-      double s = 0;
-      for (unsigned b = lane; b < gridDim.x; b += 32) s += part[(int64_t)b * ncols + j];
-      s = sv_warp_sum(s);
-      if (lane == 0) c[j] = s;
-    }
-    if (threadIdx.x == 0) *counter = 0;
-  }
-}
-
-// x -= Q[:, :ncols] c (double-float); optionally *nrm = ||x|| afterwards.
-__global__ void __launch_bounds__(256) k_update_df(float* __restrict__ xh, float* __restrict__ xl,
-                                                   int64_t len, const float* __restrict__ Qh,
-                                                   const float* __restrict__ Ql, int64_t ld,
-                                                   int ncols, const double* __restrict__ c,
-                                                   double* __restrict__ part,
-                                                   double* __restrict__ nrm,
-                                                   unsigned int* __restrict__ counter) {
-  __shared__ double sh[32];
-  __shared__ float chs[MAX_WORK], cls[MAX_WORK];
-  __shared__ bool last;
-  for (int j = threadIdx.x; j < ncols; j += blockDim.x) df_split(c[j], chs[j], cls[j]);
-  __syncthreads();
-  double acc = 0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    float h = xh[i], l = xl[i];
-    if (ncols) {
-      float sh_ = 0.f, sl_ = 0.f;
-#pragma unroll 8
-      for (int j = 0; j < ncols; ++j) {
-        int64_t o = (int64_t)j * ld + i;
-        df_fma(sh_, sl_, Qh[o], Ql[o], chs[j], cls[j]);
+    if (DOTS) {
+      // one warp per column, lanes over blocks (block order fixed: deterministic)
+      for (int j = w; j < ncols; j += 8) {
+        double s = 0;
+        for (unsigned b = lane; b < gridDim.x; b += 32) s += part[(int64_t)b * ncols + j];
+        s = sv_warp_sum(s);
+        if (lane == 0) cout[j] = s;
       }
-      df_sub(h, l, sh_, sl_);
-      xh[i] = h;
-      xl[i] = l;
     }
-    if (nrm) {
-      double v = df_val(h, l);
-      acc += v * v;
-    }
-  }
-  if (!nrm) return;
-  acc = block_sum(acc, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = acc;
-  if (last_block(counter, &last)) {
-    if (threadIdx.x == 0) {
+    if (NORM && tid == 0) {
       double s = 0;
-      for (unsigned b = 0; b < gridDim.x; ++b) s += part[b];
+      for (unsigned b = 0; b < gridDim.x; ++b) s += npart[b];
       *nrm = sqrt(s);
-      *counter = 0;
     }
+    if (tid == 0) *counter = 0;
   }
 }
 
@@ -434,10 +498,12 @@ __global__ void __launch_bounds__(1024) k_vside(const double* __restrict__ F, in
 }
 
 // One-sided (Hestenes) Jacobi SVD of B (m x m, row-major), one block, in
-// double-float arithmetic: FP64 runs at 1/57 of the FP32 rate on this part, and
-// one FP64 block spent ~4 ms per 57 x 57 SVD, so the columns of A = B and the
+// double-float arithmetic: FP64 runs at 1/57 of the FP32 rate on this part (one
+// warp-wide FP64 instruction occupies an SM's FP64 pipe for ~17 cycles), and an
+// FP64 block spent ~4 ms per 57 x 57 SVD, so the columns of A = B and the
 // accumulated rotations J are held as (hi, lo) FP32 pairs in shared memory and
-// updated on the FP32 pipe; only the rotation parameters are formed in FP64.
+// updated on the FP32 pipe, and the rotation parameters are formed in FP32 and
+// normalised in double-float.
 // Columns are paired by the circle method (slot 0 fixed, the others rotating),
 // one warp per pair; a pair is rotated while |a_p . a_q| > 1e-13 |a_p| |a_q|
 // (the double-float dot products carry ~3e-15 relative error, so the FP64
@@ -526,15 +592,29 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(const double* __restrict__ 
         df_warp_sum(alh, all);
         df_warp_sum(beh, bel);
         df_warp_sum(gah, gal);
-        double al = df_val(alh, all), be = df_val(beh, bel), ga = df_val(gah, gal);
-        if (fabs(ga) > 1e-13 * sqrt(al * be) && ga != 0.0) {
-          double zeta = (be - al) / (2.0 * ga);
-          double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + hypot(1.0, zeta));
-          double cth = 1.0 / sqrt(1.0 + t * t);
-          double sth = cth * t;
-          float ch, cl, sh, sl;
-          df_split(cth, ch, cl);
-          df_split(sth, sh, sl);
+        // every lane holds the sums; the test and the angle are FP32 (from
+        // double-float sums): the angle only steers convergence, while the
+        // orthogonality of the applied rotation comes from normalising (c, s)
+        // in double-float
+        if (fabsf(gah) > 1e-13f * sqrtf(alh) * sqrtf(beh) && gah != 0.f) {
+          // be - al in double-float: close singular values still give an
+          // accurate angle
+          float dh = beh, dl = bel;
+          df_sub(dh, dl, alh, all);
+          float zeta = dh / (2.f * gah);
+          float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + hypotf(1.f, zeta));
+          float c0 = rsqrtf(1.f + t * t);
+          float s0 = c0 * t;
+          // q = c0^2 + s0^2 = 1 + d exactly in double-float; (c, s) = (c0, s0) q^(-1/2)
+          // with q^(-1/2) = 1 - d/2 (+ O(d^2), d ~ 1e-7)
+          float qh = 0.f, ql = 0.f;
+          df_fma(qh, ql, c0, 0.f, c0, 0.f);
+          df_fma(qh, ql, s0, 0.f, s0, 0.f);
+          float d = (qh - 1.f) + ql;
+          float fh = 1.f, fl = -0.5f * d;
+          float ch = 0.f, cl = 0.f, sh = 0.f, sl = 0.f;
+          df_fma(ch, cl, c0, 0.f, fh, fl);
+          df_fma(sh, sl, s0, 0.f, fh, fl);
           for (int r = lane; r < m; r += 32) {
             df_rot(aph[r], apl[r], aqh[r], aql[r], ch, cl, sh, sl);
             df_rot(Jh[p * m + r], Jl[p * m + r], Jh[q * m + r], Jl[q * m + r], ch, cl, sh, sl);
@@ -598,16 +678,18 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(const double* __restrict__ 
 }
 
 // Out[:, c] = sum_r In[:, r] * M[r + c*nin] for c < nout (tall x small), In
-// double-float; Out double-float (outh/outl) or FP64 (outd).
-template <int KB>
+// double-float; Out double-float (outh/outl) or FP64 (outd).  KB output columns
+// per pass; EXACT when KB divides nout (no column guards).  M sits in shared
+// memory as (hi, lo) pairs read with one broadcast 8-byte load per term.
+template <int KB, bool EXACT>
 __global__ void __launch_bounds__(256) k_rotate_df(const float* __restrict__ Inh,
                                                    const float* __restrict__ Inl, int64_t ld_in,
                                                    int64_t len, int nin, const double* __restrict__ M,
                                                    int nout, float* __restrict__ outh,
                                                    float* __restrict__ outl, double* __restrict__ outd,
                                                    int64_t ld_out) {
-  extern __shared__ float Ms[];   // nin*nout pairs (hi, lo)
-  for (int i = threadIdx.x; i < nin * nout; i += blockDim.x) df_split(M[i], Ms[2 * i], Ms[2 * i + 1]);
+  extern __shared__ float2 Ms[];   // nin*nout pairs (hi, lo)
+  for (int i = threadIdx.x; i < nin * nout; i += blockDim.x) df_split(M[i], Ms[i].x, Ms[i].y);
   __syncthreads();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -620,14 +702,14 @@ __global__ void __launch_bounds__(256) k_rotate_df(const float* __restrict__ Inh
         float wh = Inh[o], wl = Inl[o];
 #pragma unroll
         for (int t = 0; t < KB; ++t)
-          if (c0 + t < nout) {
-            int mi = 2 * (r + (c0 + t) * nin);
-            df_fma(ah[t], al[t], wh, wl, Ms[mi], Ms[mi + 1]);
+          if (EXACT || c0 + t < nout) {
+            float2 m = Ms[r + (c0 + t) * nin];
+            df_fma(ah[t], al[t], wh, wl, m.x, m.y);
           }
       }
 #pragma unroll
       for (int t = 0; t < KB; ++t)
-        if (c0 + t < nout) {
+        if (EXACT || c0 + t < nout) {
           int64_t o = (int64_t)(c0 + t) * ld_out + i;
           if (outd) {
             outd[o] = df_val(ah[t], al[t]);
@@ -701,6 +783,12 @@ struct Op {
   // true when N and T only enqueue device work (no host round trip), so that a
   // Lanczos cycle over them can be captured as a CUDA graph
   virtual bool device_only() const { return false; }
+  // y = A x - (csub ? *csub : 0) * z with x, z, y double-float vectors (hi, lo);
+  // false when the operator has no such form (the FP64 N is used instead)
+  virtual bool N_df(const float* xh, const float* xl, float* yh, float* yl, const double* csub,
+                    const float* zh, const float* zl) {
+    return false;
+  }
 };
 
 struct CenteredOp : Op {
@@ -714,6 +802,10 @@ struct CenteredOp : Op {
     sv_centered_apply(ctx, S, 'T', x, y, 1.0, 0.0, csub, z);
   }
   bool device_only() const override { return true; }
+  bool N_df(const float* xh, const float* xl, float* yh, float* yl, const double* csub,
+            const float* zh, const float* zl) override {
+    return sv_centered_apply_df(ctx, S, xh, xl, yh, yl, csub, zh, zl);
+  }
 };
 
 struct CallbackOp : Op {
@@ -800,6 +892,7 @@ struct Lanczos {
   DevBuf<int> flag;
   double* hsum = nullptr;       // pinned copy of the cycle summary
   double eps_b = 0;
+  int cgs_blocks = RED_BLOCKS;  // resident blocks of the CGS kernels (one wave)
   // graphs of the first cycle and of restart cycles from basis set 0 / set 1
   CycleGraph graphs[3];
 
@@ -816,16 +909,26 @@ struct Lanczos {
     summary.alloc(2 * work + 2);
     scal.alloc(8);
     part.alloc((size_t)RED_BLOCKS * (work + 1));
-    cvec.alloc(work + 1);
+    cvec.alloc(2 * MAX_WORK);
     counter.alloc(4);
     flag.alloc(4);
     sv_memset(ctx, counter.get(), 0, 16);
     sv_memset(ctx, flag.get(), 0, 16);
     sv_memset(ctx, B.get(), 0, work * work * 8);
     SV_CUDA(cudaMallocHost((void**)&hsum, (2 * work + 2) * 8));
+    int per_sm = 0;
+    if (work <= 64)
+      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_df<8, true, true, false>, 256, 0));
+    else
+      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_df<12, true, true, false>, 256, 0));
+    cgs_blocks = std::max(1, std::min(RED_BLOCKS, per_sm * ctx->num_sms));
     SV_CUDA(cudaFuncSetAttribute(k_jacobi_svd, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  4 * MAX_WORK * MAX_WORK * 4));
-    SV_CUDA(cudaFuncSetAttribute(k_rotate_df<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    SV_CUDA(cudaFuncSetAttribute(k_rotate_df<10, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 MAX_WORK * MAX_WORK * 8));
+    SV_CUDA(cudaFuncSetAttribute(k_rotate_df<8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 MAX_WORK * MAX_WORK * 8));
+    SV_CUDA(cudaFuncSetAttribute(k_rotate_df<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  MAX_WORK * MAX_WORK * 8));
   }
   ~Lanczos() {
@@ -838,28 +941,35 @@ struct Lanczos {
 
   double* ctl() { return scal.get() + SCAL_CTL; }
 
-  int red_grid(int64_t len) {
-    return (int)std::min<int64_t>(RED_BLOCKS, std::max<int64_t>(1, (len + 255) / 256));
-  }
-
-  // working vector <- CGS2(working vector, basis[:, :ncols]); *nrm = its norm
-  void orth_norm(Side& s, int ncols, double* nrm) {
-    int g = red_grid(s.len);
-    // the update has no per-block partials besides the norm: more, smaller blocks
-    int gu = (int)std::min<int64_t>(2 * RED_BLOCKS, std::max<int64_t>(1, (s.len + 255) / 256));
-    for (int pass = 0; pass < 2 && ncols > 0; ++pass) {
-      sv_launch(ctx, "irlba_dots", k_dots_df, dim3(g), dim3(256), 0, (const float*)s.bh(),
-                (const float*)s.bl(), s.len, ncols, (const float*)s.xh.get(),
-                (const float*)s.xl.get(), s.len, part.get(), cvec.get(), counter.get());
-      sv_launch(ctx, "irlba_update", k_update_df, dim3(gu), dim3(256), 0, s.xh.get(), s.xl.get(), s.len,
-                (const float*)s.bh(), (const float*)s.bl(), s.len, ncols,
-                (const double*)cvec.get(), part.get(), pass == 1 ? nrm : (double*)nullptr,
-                counter.get());
+  // working vector <- CGS2(y, basis[:, :ncols]) (y FP64; null: the working
+  // vector already holds it); *nrm = its norm
+  template <int NJ>
+  void orth_norm_nj(Side& s, const double* y, int ncols, double* nrm) {
+    int g = (int)std::max<int64_t>(1, std::min<int64_t>(cgs_blocks, (s.len + 63) / 64));
+    double* c1 = cvec.get();
+    double* c2 = cvec.get() + MAX_WORK;
+    double* np = part.get() + (size_t)RED_BLOCKS * work;
+    if (ncols == 0) {
+      if (y) to_working(s, y);
+      sv_launch(ctx, "irlba_upd_norm", k_cgs_df<NJ, true, false, true>, dim3(g), dim3(256), 0,
+                (const float*)s.bh(), (const float*)s.bl(), s.len, 0, s.xh.get(), s.xl.get(),
+                (const double*)nullptr, s.len, (const double*)c1, part.get(), np, c2, nrm, counter.get());
+      return;
     }
-    if (ncols == 0)
-      sv_launch(ctx, "irlba_update", k_update_df, dim3(g), dim3(256), 0, s.xh.get(), s.xl.get(), s.len,
-                (const float*)s.bh(), (const float*)s.bl(), s.len, 0,
-                (const double*)cvec.get(), part.get(), nrm, counter.get());
+    sv_launch(ctx, "irlba_dots", k_cgs_df<NJ, false, true, false>, dim3(g), dim3(256), 0,
+              (const float*)s.bh(), (const float*)s.bl(), s.len, ncols, s.xh.get(), s.xl.get(), y, s.len,
+              (const double*)nullptr, part.get(), np, c1, (double*)nullptr, counter.get());
+    sv_launch(ctx, "irlba_upd_dots", k_cgs_df<NJ, true, true, false>, dim3(g), dim3(256), 0,
+              (const float*)s.bh(), (const float*)s.bl(), s.len, ncols, s.xh.get(), s.xl.get(),
+              (const double*)nullptr, s.len, (const double*)c1, part.get(), np, c2, (double*)nullptr,
+              counter.get());
+    sv_launch(ctx, "irlba_upd_norm", k_cgs_df<NJ, true, false, true>, dim3(g), dim3(256), 0,
+              (const float*)s.bh(), (const float*)s.bl(), s.len, ncols, s.xh.get(), s.xl.get(),
+              (const double*)nullptr, s.len, (const double*)c2, part.get(), np, c1, nrm, counter.get());
+  }
+  void orth_norm(Side& s, const double* y, int ncols, double* nrm) {
+    if (work <= 64) orth_norm_nj<8>(s, y, ncols, nrm);
+    else orth_norm_nj<12>(s, y, ncols, nrm);
   }
 
   // basis column j := working vector / *nrm (FP64 copy in cur), breakdown handling
@@ -877,8 +987,7 @@ struct Lanczos {
   void vside(int ncols, int write_col, double* nrm, const double* c, double* bentry, uint64_t seed,
              unsigned step) {
     if (n > 32768) {   // long feature side: the multi-block kernels
-      to_working(Vs, F.get());
-      orth_norm(Vs, ncols, nrm);
+      orth_norm(Vs, F.get(), ncols, nrm);
       if (write_col >= 0) scal_fix(Vs, write_col, nrm, c, bentry, seed, step);
       return;
     }
@@ -894,7 +1003,9 @@ struct Lanczos {
 
   // out = basis * M[:, :nout]: into the other basis set (outd null) or FP64 outd
   void rotate(Side& s, const double* M, int nout, double* outd) {
-    sv_launch(ctx, "irlba_rotate", k_rotate_df<16>, dim3(sv_grid_for(ctx, s.len, 256, 8)), dim3(256),
+    auto kern = nout % 10 == 0 ? k_rotate_df<10, true> : nout % 8 == 0 ? k_rotate_df<8, true>
+                                                                       : k_rotate_df<16, false>;
+    sv_launch(ctx, "irlba_rotate", kern, dim3(sv_grid_for(ctx, s.len, 256, 8)), dim3(256),
               (size_t)work * nout * 8, (const float*)s.bh(), (const float*)s.bl(), s.len, s.len,
               work, M, nout, outd ? (float*)nullptr : s.th(), outd ? (float*)nullptr : s.tl(), outd,
               s.len);
@@ -922,10 +1033,13 @@ struct Lanczos {
     unsigned step = 1;
     int j = k;
     // W[:, j] = A V[:, j]; CGS2 against W[:, :j]
-    op->N(Vs.cur.get(), ytmp.get(), nullptr, nullptr);
+    if (op->N_df(Vs.ch(j), Vs.cl(j), Ws.xh.get(), Ws.xl.get(), nullptr, nullptr, nullptr)) {
+      orth_norm(Ws, nullptr, j, s0);
+    } else {
+      op->N(Vs.cur.get(), ytmp.get(), nullptr, nullptr);
+      orth_norm(Ws, ytmp.get(), j, s0);
+    }
     nmv++;
-    to_working(Ws, ytmp.get());
-    orth_norm(Ws, j, s0);
     scal_fix(Ws, j, s0, c, B.get() + (int64_t)j * work + j, seed, step++);
     while (true) {
       // F = A^T W[:, j] - S V[:, j]; CGS2 against V[:, :j+1]
@@ -934,10 +1048,13 @@ struct Lanczos {
       if (j + 1 < work) {
         vside(j + 1, j + 1, s1, c, B.get() + (int64_t)j * work + j + 1, seed, step++);
         // W[:, j+1] = A V[:, j+1] - R W[:, j]
-        op->N(Vs.cur.get(), ytmp.get(), s1, Ws.cur.get());
+        if (op->N_df(Vs.ch(j + 1), Vs.cl(j + 1), Ws.xh.get(), Ws.xl.get(), s1, Ws.ch(j), Ws.cl(j))) {
+          orth_norm(Ws, nullptr, j + 1, s0);
+        } else {
+          op->N(Vs.cur.get(), ytmp.get(), s1, Ws.cur.get());
+          orth_norm(Ws, ytmp.get(), j + 1, s0);
+        }
         nmv++;
-        to_working(Ws, ytmp.get());
-        orth_norm(Ws, j + 1, s0);
         scal_fix(Ws, j + 1, s0, c, B.get() + (int64_t)(j + 1) * work + j + 1, seed, step++);
         ++j;
       } else {
@@ -1023,7 +1140,7 @@ struct Lanczos {
     return res;
   }
 
-  // F holds the residual in FP64 only before to_working; the orthogonalised
+  // F holds the residual in FP64 only before the first CGS pass; the orthogonalised
   // residual lives in the V-side working vector: bring it back to FP64
   void df_residual_to_fp64() {
     sv_launch(ctx, "irlba_f_fp64", k_df_to_fp64, dim3(sv_grid_for(ctx, n, 256, 4)), dim3(256), 0,

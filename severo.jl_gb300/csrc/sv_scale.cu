@@ -298,6 +298,131 @@ __global__ void __launch_bounds__(256) k_spmv_csr(
   }
 }
 
+// ---- X v for the Lanczos W side, double-float in and out (FP32 storage) -------
+// The same row loop as k_spmv_csr with every FP64 operation removed: this part
+// issues one warp-wide FP64 instruction per ~17 cycles per SM, and the FP64
+// prologue and epilogue of k_spmv_csr kept its FP64 pipe 30% busy.  The vector
+// arrives as a double-float basis column (its FP32 high part is the FP32 x of
+// the table), mu.x is accumulated in double-float, and the result
+//   y = (B x - mu.x) - csub * z      (z a double-float basis column)
+// is written as a double-float working vector, ready for reorthogonalisation.
+__device__ __forceinline__ void dfx_fma(float& sh, float& sl, float ah, float al, float bh, float bl) {
+  float p = ah * bh;
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, e);
+  e = fmaf(al, bh, e);
+  float t = sh + p;
+  float v = t - sh;
+  float err = (sh - (t - v)) + (p - v);
+  sh = t;
+  sl += err + e;
+}
+
+template <typename ValT, typename IdxT>
+__global__ void __launch_bounds__(256) k_spmv_csr_df(
+    const int64_t* __restrict__ rowptr, const IdxT* __restrict__ hcol, const ValT* __restrict__ hval,
+    int64_t n_rows, int64_t nf, const float* __restrict__ xh, const float* __restrict__ xl,
+    const float* __restrict__ inv_f, const float* __restrict__ clip_f, const float* __restrict__ mu_h,
+    const float* __restrict__ mu_l, float* __restrict__ yh, float* __restrict__ yl,
+    const double* __restrict__ csub, const float* __restrict__ zh, const float* __restrict__ zl) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ float redh[32], redl[32];
+  __shared__ float sc[4];
+  float mh = 0.f, ml = 0.f;
+  for (int64_t f = threadIdx.x; f < nf; f += blockDim.x) {
+    float xs = xh[f];
+    float P = inv_f[f] * xs;
+    float Q = xs == 0.f ? 0.f : clip_f[f] * xs;
+    ((float2*)smem_raw)[f] = make_float2(P, Q);
+    dfx_fma(mh, ml, mu_h[f], mu_l[f], xs, xl[f]);
+  }
+  // mu.x: warp reduction in double-float, then warp 0 over the warps
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    float h2 = __shfl_xor_sync(0xffffffffu, mh, o);
+    float l2 = __shfl_xor_sync(0xffffffffu, ml, o);
+    float t = mh + h2;
+    float v = t - mh;
+    float err = (mh - (t - v)) + (h2 - v);
+    ml = err + ml + l2;
+    mh = t;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    redh[threadIdx.x >> 5] = mh;
+    redl[threadIdx.x >> 5] = ml;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float h = 0.f, l = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      float t = h + redh[w];
+      float v = t - h;
+      float err = (h - (t - v)) + (redh[w] - v);
+      l += err + redl[w];
+      h = t;
+    }
+    float t = h + l;
+    sc[0] = t;
+    sc[1] = l - (t - h);
+    if (csub) {
+      double c = *csub;
+      sc[2] = (float)c;
+      sc[3] = (float)(c - (double)sc[2]);
+    } else {
+      sc[2] = sc[3] = 0.f;
+    }
+  }
+  __syncthreads();
+  const float muxh = sc[0], muxl = sc[1], csh = -sc[2], csl = -sc[3];
+
+  int lane = threadIdx.x & 31;
+  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n_rows; r += nwarps) {
+    int64_t s = rowptr[r], e = rowptr[r + 1];
+    int64_t a0 = s & ~3ll;
+    float acc = 0.f;
+    for (int64_t g = a0 + 4 * lane; g < e; g += 256) {
+      int ci[2][4];
+      float av[2][4];
+      bool two = g + 128 < e;
+      ld4(hcol, g, ci[0]);
+      ld4v(hval, g, av[0]);
+      if (two) {
+        ld4(hcol, g + 128, ci[1]);
+        ld4v(hval, g + 128, av[1]);
+      }
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (h == 1 && !two) break;
+        int64_t gh = g + 128 * h;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          if (gh + t >= s && gh + t < e) {
+            float2 pq = ((const float2*)smem_raw)[ci[h][t]];
+            float rr = av[h][t] * pq.x;
+            acc += pq.x >= 0.f ? fminf(rr, pq.y) : fmaxf(rr, pq.y);
+          }
+        }
+      }
+    }
+    acc = sv_warp_sum(acc);
+    if (lane == 0) {
+      // (acc - mu.x) - csub * z in double-float
+      float h = acc, l = 0.f;
+      float t = h - muxh;
+      float v = t - h;
+      float err = (h - (t - v)) + (-muxh - v);
+      h = t;
+      l = err - muxl;
+      if (zh) dfx_fma(h, l, csh, csl, zh[r], zl[r]);
+      t = h + l;
+      yl[r] = l - (t - h);
+      yh[r] = t;
+    }
+  }
+}
+
 // ---- X^T u over CSR_h (warp per cell, shared-memory accumulation) -----------
 // Each block accumulates sum_i min(a_if * inv_f, clip_f) * u_i for its cells into
 // a shared array of nf partial sums (shared atomics), then writes the array to
@@ -533,6 +658,16 @@ __global__ void k_rb_finish(const float* __restrict__ partial, int64_t n_rb, int
 
 // ---- X^T u over the CSC feature ranges ---------------------------------------
 // Prologue: u -> FP32 copy and per-block partial sums of u (FP64).
+__global__ void k_split_df(const double* __restrict__ x, int64_t n, float* __restrict__ h,
+                           float* __restrict__ l) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float a = (float)x[i];
+    h[i] = a;
+    l[i] = (float)(x[i] - (double)a);
+  }
+}
+
 __global__ void k_u_prep(const double* __restrict__ u, int64_t n, float* __restrict__ uf,
                          double* __restrict__ part) {
   __shared__ double red[32];
@@ -640,7 +775,7 @@ void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const 
   if (trans == 'N') {
     size_t smem = S->dtype == SV_F64 ? (size_t)S->nf * 24 : (size_t)S->nf * 8;
     smem = (smem + 15) & ~(size_t)15;
-    int grid = sv_grid_for(ctx, S->n_cells * 32, 256, 8);
+    int grid = (int)std::max<int64_t>(1, std::min<int64_t>(S->grid_csr, (S->n_cells + 7) / 8));
 #define LAUNCH_CSR(VT, IT, COL)                                                                  \
   sv_launch(ctx, "spmv_csr_h", k_spmv_csr<VT, IT>, dim3(grid), dim3(256), smem,                  \
             (const int64_t*)S->h_rowptr.get(), (const IT*)COL, (const VT*)S->h_val.get(),         \
@@ -754,6 +889,31 @@ void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const 
 // Builds the implicit matrix over the features `fg` (0-based genes) of `data`.
 // mu_given == nullptr: per-feature moments (scale_features).  Otherwise the
 // CenteredMatrix(A, mu) constructor of src/scaling.jl:224-232: std = 1, no clip.
+// X v with double-float input and output (the Lanczos W step): false when the
+// matrix stores FP64 values (the FP64 product is used then)
+bool sv_centered_apply_df(sv_context* ctx, const sv_centered* S, const float* xh, const float* xl,
+                          float* yh, float* yl, const double* csub, const float* zh, const float* zl) {
+  if (S->dtype == SV_F64) return false;
+  size_t smem = ((size_t)S->nf * 8 + 15) & ~(size_t)15;
+  int grid = (int)std::max<int64_t>(1, std::min<int64_t>(S->grid_csr_df, (S->n_cells + 7) / 8));
+#define LAUNCH_CSRDF(VT, IT, COL)                                                                \
+  sv_launch(ctx, "spmv_csr_h", k_spmv_csr_df<VT, IT>, dim3(grid), dim3(256), smem,               \
+            (const int64_t*)S->h_rowptr.get(), (const IT*)COL, (const VT*)S->h_val.get(),         \
+            S->n_cells, S->nf, xh, xl, (const float*)S->inv_std_f.get(),                          \
+            (const float*)S->clip_f.get(), (const float*)S->mu_h.get(), (const float*)S->mu_l.get(), \
+            yh, yl, csub, zh, zl)
+  bool small = S->nf <= 65536;
+  if (S->dtype == SV_F32) {
+    if (small) LAUNCH_CSRDF(float, uint16_t, S->h_col16.get());
+    else LAUNCH_CSRDF(float, int32_t, S->h_col32.get());
+  } else {
+    if (small) LAUNCH_CSRDF(__nv_bfloat16, uint16_t, S->h_col16.get());
+    else LAUNCH_CSRDF(__nv_bfloat16, int32_t, S->h_col32.get());
+  }
+#undef LAUNCH_CSRDF
+  return true;
+}
+
 static sv_centered* make_centered(sv_context* ctx, const sv_data* data, const std::vector<int32_t>& fg,
                                   double scale_max, const double* mu_given) {
   const sv_counts* C = data->counts;
@@ -812,6 +972,10 @@ static sv_centered* make_centered(sv_context* ctx, const sv_data* data, const st
       sv_sync(ctx);
     }
 #undef LAUNCH_MOM
+    S->mu_h.alloc(nf);
+    S->mu_l.alloc(nf);
+    sv_launch(ctx, "scale_mu_split", k_split_df, dim3(sv_grid_for(ctx, nf, 256)), dim3(256), 0,
+              (const double*)S->mu.get(), nf, S->mu_h.get(), S->mu_l.get());
     // chunk table of the CSC product (built on the host from the nf ranges)
     std::vector<int64_t> hs(nf), he(nf);
     sv_d2h(ctx, hs.data(), S->feat_start.get(), nf * 8);
@@ -960,6 +1124,45 @@ static sv_centered* make_centered(sv_context* ctx, const sv_data* data, const st
     SET_SMEM(__nv_bfloat16, uint16_t);
     SET_SMEM(__nv_bfloat16, int32_t);
 #undef SET_SMEM
+    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr_df<float, uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr_df<float, int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr_df<__nv_bfloat16, uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    SV_CUDA(cudaFuncSetAttribute(k_spmv_csr_df<__nv_bfloat16, int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    // the X v kernels loop over rows: one wave of resident blocks (a second,
+    // partial wave left SMs idle at the tail)
+    {
+      size_t tsm = ((size_t)nf * (data->dtype == SV_F64 ? 24 : 8) + 15) & ~(size_t)15;
+      size_t tsm_df = ((size_t)nf * 8 + 15) & ~(size_t)15;
+      int b1 = 0, b2 = 0;
+      bool small16 = nf <= 65536;
+      switch (data->dtype) {
+        case SV_F64:
+          SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+              &b1, small16 ? (const void*)k_spmv_csr<double, uint16_t> : (const void*)k_spmv_csr<double, int32_t>,
+              256, tsm));
+          break;
+        case SV_F32:
+          SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+              &b1, small16 ? (const void*)k_spmv_csr<float, uint16_t> : (const void*)k_spmv_csr<float, int32_t>,
+              256, tsm));
+          SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+              &b2, small16 ? (const void*)k_spmv_csr_df<float, uint16_t> : (const void*)k_spmv_csr_df<float, int32_t>,
+              256, tsm_df));
+          break;
+        default:
+          SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+              &b1, small16 ? (const void*)k_spmv_csr<__nv_bfloat16, uint16_t>
+                           : (const void*)k_spmv_csr<__nv_bfloat16, int32_t>,
+              256, tsm));
+          SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+              &b2, small16 ? (const void*)k_spmv_csr_df<__nv_bfloat16, uint16_t>
+                           : (const void*)k_spmv_csr_df<__nv_bfloat16, int32_t>,
+              256, tsm_df));
+          break;
+      }
+      S->grid_csr = std::max(1, b1) * ctx->num_sms;
+      S->grid_csr_df = std::max(1, b2) * ctx->num_sms;
+    }
     sv_sync(ctx);
   } catch (...) {
     delete S;

@@ -354,6 +354,78 @@ void snn_dispatch(sv_context* ctx, const int32_t* nn, int64_t n, int k, int64_t 
   else snn_run<float>(ctx, nn, n, k, kparam, prune, g);
 }
 
+
+// ---- hand-off to Louvain: Network(snn) of src/modularity.jl:163-194 ----------
+// Julia's isbits layouts of Edge{T} (node::Int64, weight::T) and Node{T}
+// (weight::T, edges::UnitRange{Int64}), written directly so that the caller's
+// Vector{Edge{T}} / Vector{Node{T}} are filled without a host rebuild.
+template <typename T>
+struct JlEdge {
+  int64_t node;
+  T weight;
+};
+template <typename T>
+struct JlNode {
+  T weight;
+  int64_t first, last;
+};
+static_assert(sizeof(JlEdge<double>) == 16 && sizeof(JlEdge<float>) == 16, "Edge{T} layout");
+static_assert(sizeof(JlNode<double>) == 24 && sizeof(JlNode<float>) == 24, "Node{T} layout");
+
+// non-self entries per column (rows are sorted; at most one self entry)
+__global__ void k_net_count(const int64_t* __restrict__ cp, const int32_t* __restrict__ ri, int64_t n,
+                            int64_t* __restrict__ cnt) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t c = 0;
+    for (int64_t e = cp[i]; e < cp[i + 1]; ++e) c += ri[e] != i;
+    cnt[i] = c;
+  }
+}
+
+// one thread per column, in column order: the node weight is accumulated in T
+// in the same order as the reference's loop (bit-identical)
+template <typename T>
+__global__ void k_net_write(const int64_t* __restrict__ cp, const int32_t* __restrict__ ri,
+                            const T* __restrict__ val, int64_t n, const int64_t* __restrict__ off,
+                            JlNode<T>* __restrict__ nodes, JlEdge<T>* __restrict__ edges) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t o = off[i];
+    T w = T(0);
+    for (int64_t e = cp[i]; e < cp[i + 1]; ++e) {
+      if (ri[e] == i) continue;
+      w += val[e];
+      JlEdge<T> ed;
+      ed.node = (int64_t)ri[e] + 1;
+      ed.weight = val[e];
+      edges[o++] = ed;
+    }
+    JlNode<T> nd;
+    nd.weight = w;
+    nd.first = off[i] + 1;
+    nd.last = o;
+    nodes[i] = nd;
+  }
+}
+
+// totw: the sequential sum over all edges in order (the reference accumulates
+// edge by edge); one warp loads 32 edges at a time, lane 0 adds them in order
+template <typename T>
+__global__ void k_net_total(const JlEdge<T>* __restrict__ edges, int64_t nedges, T* __restrict__ tot) {
+  int lane = threadIdx.x & 31;
+  T s = T(0);
+  for (int64_t b = 0; b < nedges; b += 32) {
+    T v = b + lane < nedges ? edges[b + lane].weight : T(0);
+    int m = nedges - b < 32 ? (int)(nedges - b) : 32;
+    for (int j = 0; j < m; ++j) {
+      T x = __shfl_sync(0xffffffffu, v, j);
+      if (lane == 0) s += x;
+    }
+  }
+  if (lane == 0) *tot = s;
+}
+
 }  // namespace
 
 SV_API int sv_snn_host(sv_context* ctx, const int32_t* nn_index, int64_t n, int64_t k, int64_t k_param,
@@ -417,6 +489,43 @@ SV_API int sv_graph_download(sv_context* ctx, const sv_graph* g, int64_t* colptr
     if (rowval) sv_d2h(ctx, rowval, ori.get(), g->nnz * 8);
   }
   if (nzval) sv_d2h(ctx, nzval, g->val.get(), g->nnz * sv_elem_size(g->dtype));
+  SV_CATCH
+}
+
+SV_API int sv_graph_network(sv_context* ctx, const sv_graph* g, int64_t* nedges, void* nodes,
+                            void* edges, void* totw) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(g && g->ctx == ctx, "bad handle");
+  SV_REQUIRE(nedges, "nedges is required");
+  DevBuf<int64_t> cnt(g->n + 1), off(g->n + 1);
+  sv_launch(ctx, "snn_net_count", k_net_count, dim3(sv_grid_for(ctx, g->n, 256, 8)), dim3(256), 0,
+            (const int64_t*)g->colptr.get(), (const int32_t*)g->rowidx.get(), g->n, cnt.get());
+  sv_scan_i64(ctx, cnt.get(), off.get(), g->n);
+  int64_t ne = sv_read_i64(ctx, off.get() + g->n);
+  *nedges = ne;
+  if (!nodes && !edges && !totw) return SV_OK;
+  bool f64 = g->dtype == SV_F64;
+  DevBuf<unsigned char> dn((size_t)g->n * 24), de((size_t)std::max<int64_t>(1, ne) * 16), dt(8);
+  if (f64) {
+    sv_launch(ctx, "snn_net_write", k_net_write<double>, dim3(sv_grid_for(ctx, g->n, 256, 8)), dim3(256),
+              0, (const int64_t*)g->colptr.get(), (const int32_t*)g->rowidx.get(),
+              (const double*)g->val.get(), g->n, (const int64_t*)off.get(), (JlNode<double>*)dn.get(),
+              (JlEdge<double>*)de.get());
+    sv_launch(ctx, "snn_net_total", k_net_total<double>, dim3(1), dim3(32), 0,
+              (const JlEdge<double>*)de.get(), ne, (double*)dt.get());
+  } else {
+    sv_launch(ctx, "snn_net_write", k_net_write<float>, dim3(sv_grid_for(ctx, g->n, 256, 8)), dim3(256),
+              0, (const int64_t*)g->colptr.get(), (const int32_t*)g->rowidx.get(),
+              (const float*)g->val.get(), g->n, (const int64_t*)off.get(), (JlNode<float>*)dn.get(),
+              (JlEdge<float>*)de.get());
+    sv_launch(ctx, "snn_net_total", k_net_total<float>, dim3(1), dim3(32), 0,
+              (const JlEdge<float>*)de.get(), ne, (float*)dt.get());
+  }
+  if (nodes) sv_d2h(ctx, nodes, dn.get(), (size_t)g->n * 24);
+  if (edges) sv_d2h(ctx, edges, de.get(), (size_t)ne * 16);
+  if (totw) sv_d2h(ctx, totw, dt.get(), f64 ? 8 : 4);
+  sv_sync(ctx);
   SV_CATCH
 }
 

@@ -70,3 +70,24 @@ def test_shared_nearest_neighbours_pipeline(sv, ctx, O):
     idx, _ = sv.ann(X, 15, ctx=ctx)
     R = O.jaccard_index(O.knn_graph(idx, 2000), 15, 1 / 15, np.float32)
     assert W.dtype == np.float32 and _same(W, R)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_network_handoff_matches_oracle(sv, ctx, O, dtype):
+    """Network(snn) (src/modularity.jl:163-194) emitted from the device graph:
+    node weights, edge ranges, edges and totw bit-identical to the reference's
+    sequential construction."""
+    rng = np.random.default_rng(7)
+    n, k = 3000, 20
+    X = rng.standard_normal((n, 8)).astype(np.float32)
+    idx, _ = O.knn_exact(X, k)
+    nn = (idx + 1).astype(np.int32)
+    A, g = sv.jaccard_index(nn, k, dtype=dtype, ctx=ctx, keep=True)
+    nodes, edges, totw = g.network(dtype)
+    nw, first, last, en, ew, rt = O.network(A)
+    assert np.array_equal(nodes["weight"], nw)
+    assert np.array_equal(nodes["first"], first) and np.array_equal(nodes["last"], last)
+    assert np.array_equal(edges["node"], en) and np.array_equal(edges["weight"], ew)
+    assert totw == rt and type(totw) == type(rt)
+    # every self link is dropped: one per node (include_self lists)
+    assert len(edges) == A.nnz - n
