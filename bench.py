@@ -332,7 +332,12 @@ def main():
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-knn-stress", action="store_true")
+    ap.add_argument("--kernel-case", choices=["irlba", "knn"], default=None,
+                    help="run one small case of a kernel family (for profiler captures) and exit")
     args = ap.parse_args()
+    if args.kernel_case:
+        return kernel_case(args)
     w = dict(WORKLOADS[args.workload])
     if args.cells:
         w["n_cells"] = args.cells
@@ -400,6 +405,11 @@ def main():
     if rank == 0 and not args.no_accuracy:
         acc = accuracy(sv, ctx, counts, hvf, w, init, form)
 
+    # ---- kNN stress case (untimed in the step; rank 0) ---------------------------
+    stress = None
+    if rank == 0 and not args.no_knn_stress and form[1] == "bf16":
+        stress = knn_stress(sv, ctx, with_fp32=not args.no_fp32)
+
     # ---- e2e through the C ABI with host buffers ------------------------------
     e2e = None
     if not args.no_e2e:
@@ -465,6 +475,7 @@ def main():
             "mixed_vs_fp32": round(fp32["ms_per_step"] / ms_per_step, 3) if fp32 else None,
             "cpu_baseline": cpu,
             "accuracy": acc,
+            "knn_stress": stress,
             "gpu_launches": res["launches"],
             "clocks": clocks,
             "generate_s": round(gen_s, 2),
@@ -474,12 +485,114 @@ def main():
         td.destroy_process_group()
 
 
+def kernel_case(args):
+    """Small inputs that still exceed L2, for kernel-level profiler captures
+    (a few GB on the device):
+      irlba: a random sparse 600,000 x 3,000 CenteredMatrix (40 non-zeros per
+             cell, FP32) and 3 restart cycles of irlba 50 -- the Lanczos kernels
+             on a 274 MB cell-side basis;
+      knn:   400,000 x 50 mixture points, k = 20, BF16 tensor-core path."""
+    import __graft_entry__ as ge
+    import scipy.sparse as sp
+    ge._build_module().build()
+    sv = ge.load_package()
+    ctx = sv.Context(0)
+    rng = np.random.default_rng(SEED)
+    if args.kernel_case == "irlba":
+        n, nf, per = args.cells or 600_000, 3000, 40
+        cols = rng.integers(0, nf, n * per)
+        rows = np.repeat(np.arange(n), per)
+        X = sp.csc_matrix((rng.random(n * per).astype(np.float32) * 4, (rows, cols)), shape=(n, nf))
+        X.sum_duplicates()
+        mu = np.asarray(X.mean(axis=0)).ravel()
+        S = sv.CenteredMatrix.from_sparse(X, mu, dtype="float32", ctx=ctx)
+        t0 = time.perf_counter()
+        try:
+            sv.irlba(S, 50, tol=1e-5, maxit=3)
+        except sv.ConvergenceError:
+            pass
+        ctx.sync()
+        out = {"kernel_case": "irlba", "n_cells": n, "features": nf, "nnz": int(X.nnz),
+               "cycles": 3, "s": round(time.perf_counter() - t0, 4)}
+    else:
+        n, d = args.cells or 400_000, 50
+        means = rng.normal(0, 4, (60, d))
+        X = means[rng.integers(0, 60, n)] + rng.standard_normal((n, d))
+        X = (X / np.sqrt(np.arange(1, d + 1))).astype(np.float32)
+        t0 = time.perf_counter()
+        sv.ann(X, 20, precision="bf16" if knn_tc_available(sv, ctx) else "fp32", ctx=ctx)
+        out = {"kernel_case": "knn", "n": n, "d": d, "k": 20, "s": round(time.perf_counter() - t0, 4)}
+    print(json.dumps(out))
+
+
+def principal_angles(A, B):
+    """Principal angles (radians) between the column spaces of A and B."""
+    qa, _ = np.linalg.qr(A)
+    qb, _ = np.linalg.qr(B)
+    c = np.clip(np.linalg.svd(qa.T @ qb, compute_uv=False), -1.0, 1.0)
+    return np.arccos(c)
+
+
+def exact_knn_sample(Z, q, k, include_self=True, block=262144):
+    """Exact FP64 Euclidean neighbours of the query rows q against all of Z
+    (0-based, the query itself included): the recall reference."""
+    Z = np.asarray(Z, dtype=np.float64)
+    Q = Z[q]
+    sqq = np.einsum("ij,ij->i", Q, Q)
+    ci, cd = [], []
+    for s0 in range(0, Z.shape[0], block):
+        B = Z[s0:s0 + block]
+        D = sqq[:, None] + np.einsum("ij,ij->i", B, B)[None, :] - 2.0 * (Q @ B.T)
+        inb = (q >= s0) & (q < s0 + len(B))
+        D[np.nonzero(inb)[0], q[inb] - s0] = -1.0
+        m = min(k, len(B))
+        part = np.argpartition(D, m - 1, axis=1)[:, :m]
+        ci.append(part + s0)
+        cd.append(np.take_along_axis(D, part, axis=1))
+    ci = np.concatenate(ci, axis=1)
+    cd = np.concatenate(cd, axis=1)
+    order = np.argsort(cd, axis=1, kind="stable")[:, :k]
+    return np.take_along_axis(ci, order, axis=1)
+
+
+def knn_stress(sv, ctx, with_fp32):
+    """kNN stress case: 2,000,000 x 50 FP32 points of a 60-component Gaussian
+    mixture (means ~ N(0, 4^2), dimension i scaled by 1/sqrt(i)), k = 30: BF16
+    tensor-core candidates (64 per point) + FP32 re-rank through the host API,
+    recall@30 against FP64 brute force on 500 sampled points."""
+    n, d, k = 2_000_000, 50, 30
+    rng = np.random.default_rng(SEED + 5)
+    means = rng.normal(0, 4, (60, d))
+    X = means[rng.integers(0, 60, n)]
+    X += rng.standard_normal((n, d))
+    X *= 1.0 / np.sqrt(np.arange(1, d + 1))
+    X = X.astype(np.float32)
+    sv.ann(X[:4096], k, precision="bf16", ctx=ctx)          # warm-up
+    t0 = time.perf_counter()
+    idx, _ = sv.ann(X, k, precision="bf16", ctx=ctx)
+    t_bf16 = time.perf_counter() - t0
+    q = np.random.default_rng(11).choice(n, 500, replace=False)
+    ref = exact_knn_sample(X, q, k)
+    hits = sum(len(set(a - 1) & set(b)) for a, b in zip(idx[q], ref))
+    flops = 2.0 * n * n * d
+    out = {"n": n, "d": d, "k": k, "bf16_s": round(t_bf16, 4),
+           "bf16_distance_tflops": round(flops / t_bf16 / 1e12, 1),
+           "recall_at_30": hits / ref.size, "recall_queries": 500,
+           "note": "host API: includes the 400 MB upload and the result download"}
+    if with_fp32:
+        t0 = time.perf_counter()
+        sv.ann(X, k, precision="fp32", ctx=ctx)
+        t32 = time.perf_counter() - t0
+        out["fp32_cuda_core_s"] = round(t32, 4)
+        out["bf16_speedup_vs_fp32"] = round(t32 / t_bf16, 2)
+    return out
+
+
 def accuracy(sv, ctx, counts, hvf, w, init, form, n_queries=1000):
     """Errors of the measured form against the same pipeline in FP64: relative
     error of the singular values, largest principal angle of the PC (loading)
     subspace, and kNN recall@k against exact FP64 neighbours (brute force on the
     host, for a sample of query cells, over the measured form's coordinates)."""
-    from oracle import severo_oracle as O
     out = {}
     d = sv.normalize_cells(counts, scale_factor=SCALE_FACTOR, dtype=form[0], ctx=ctx)
     S = sv.scale_features(d, scale_max=SCALE_MAX, features=hvf)
@@ -493,11 +606,11 @@ def accuracy(sv, ctx, counts, hvf, w, init, form, n_queries=1000):
     s = em.stdev
     s64 = em64.stdev
     out["sigma_rel_err_max"] = float(np.max(np.abs(s - s64) / s64))
-    ang = O.principal_angles(em.basis, em64.basis)
+    ang = principal_angles(em.basis, em64.basis)
     out["pc_subspace_angle_max_rad"] = float(ang.max())
     out["sigma_gap_last"] = float(s64[-2] / s64[-1] - 1)
     k10 = min(10, w["npcs"])
-    out["pc1_10_angle_max_rad"] = float(O.principal_angles(em.basis[:, :k10], em64.basis[:, :k10]).max())
+    out["pc1_10_angle_max_rad"] = float(principal_angles(em.basis[:, :k10], em64.basis[:, :k10]).max())
     Z = np.ascontiguousarray(em.coordinates)
     n = Z.shape[0]
     q = np.random.default_rng(7).choice(n, min(n_queries, n), replace=False)

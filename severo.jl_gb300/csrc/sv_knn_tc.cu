@@ -33,7 +33,7 @@ constexpr long long TIMEOUT = 4000000000ll;   // cycles (~2 s) per wait
 struct __align__(1024) Smem {
   __nv_bfloat16 A[BM * BK];              // 16 KB
   __nv_bfloat16 B[STAGES][BN * BK];      // 4 x 32 KB
-  float keys[EPI_WARPS * 32][33];        // per-epilogue-thread key slot (padded: no bank conflicts)
+  float keys[EPI_WARPS * 32][65];        // per-epilogue-thread key slot, two chunks (padded: no bank conflicts)
   unsigned long long full[STAGES];
   unsigned long long empty[STAGES];
   unsigned long long tfull[2];
@@ -125,8 +125,9 @@ __device__ __forceinline__ void fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-  uint32_t r[32];
+// tcgen05.ld of 32 consecutive columns of this warp's lane quarter; the values
+// are valid after tmem_ld_wait()
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
       "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -136,9 +137,56 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
         "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
         "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Keys of one 32-column chunk (in place) and the mask of those below thr.
+// FOLD: acc holds D = q.p - |p|^2/2; the chunk is rejected by one compare of its
+// maximum (key < thr  <=>  D > -thr/2, exact: scaling by powers of two), and
+// only a surviving chunk is converted to keys -2 D.  Otherwise key = |p|^2 - 2 acc.
+template <bool FOLD>
+__device__ __forceinline__ uint32_t chunk_mask(float (&acc)[32], const float* __restrict__ pn, int64_t col0,
+                                               int64_t n, float thr) {
+  uint32_t m = 0;
+  if constexpr (FOLD) {
+    // columns past the last point read zero rows (TMA fill): never candidates
+    if (col0 + 32 > n) {
 #pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+      for (int i = 0; i < 32; ++i)
+        if (col0 + i >= n) acc[i] = -FLT_MAX;
+    }
+    float thrD = -0.5f * thr;
+    float t16[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) t16[i] = fmaxf(acc[2 * i], acc[2 * i + 1]);
+#pragma unroll
+    for (int w2 = 8; w2 >= 1; w2 >>= 1)
+#pragma unroll
+      for (int i = 0; i < w2; ++i) t16[i] = fmaxf(t16[i], t16[i + w2]);
+    if (t16[0] > thrD) {
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        acc[i] = -2.0f * acc[i];
+        m |= (acc[i] < thr ? 1u : 0u) << i;
+      }
+    }
+  } else {
+    const float4* np = (const float4*)pn;   // squared norms of the chunk's points
+#pragma unroll
+    for (int i4 = 0; i4 < 8; ++i4) {
+      float4 v = __ldg(np + i4);
+      float pv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        int i = 4 * i4 + u;
+        acc[i] = fmaf(-2.0f, acc[i], pv[u]);
+        m |= (acc[i] < thr ? 1u : 0u) << i;
+      }
+    }
+  }
+  return m;
 }
 
 // FOLD: |p|^2 is part of the MMA (see k_pack_fold): the accumulator is
@@ -259,75 +307,46 @@ __global__ void __launch_bounds__(THREADS, 1)
       fence_after();
       int j0 = t * BN + half * (BN / 2);
       uint32_t tbase = tmem + lane_off + (uint32_t)(ab * BN + half * (BN / 2));
+      // two chunks per TMEM round trip: both loads are issued before one wait
 #pragma unroll 1
-      for (int c = 0; c < BN / 2 / 32; ++c) {
-        float acc[32];
-        float pn[32];
-        if constexpr (!FOLD) {
-          const float4* np = (const float4*)(sqpad + j0 + c * 32);
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            float4 v = __ldg(np + i);
-            pn[4 * i] = v.x;
-            pn[4 * i + 1] = v.y;
-            pn[4 * i + 2] = v.z;
-            pn[4 * i + 3] = v.w;
-          }
-        }
+      for (int c = 0; c < BN / 2 / 32; c += 2) {
+        uint32_t r0[32], r1[32];
+        float a0[32], a1[32];
         __syncwarp();
-        tmem_ld32(tbase + c * 32, acc);
-        if (c == BN / 2 / 32 - 1) {
+        tmem_ld32(tbase + c * 32, r0);
+        tmem_ld32(tbase + (c + 1) * 32, r1);
+        tmem_ld_wait();
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          a0[i] = __uint_as_float(r0[i]);
+          a1[i] = __uint_as_float(r1[i]);
+        }
+        if (c + 2 == BN / 2 / 32) {
           // accumulator values are in registers: release the buffer to the MMA warp
           fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(&s->tempty[ab]);
         }
         float thr = best[KH - 1];
-        uint32_t m = 0;
-        if constexpr (FOLD) {
-          // columns past the last point read zero rows (TMA fill): never candidates
-          if (j0 + c * 32 + 32 > n) {
-#pragma unroll
-            for (int i = 0; i < 32; ++i)
-              if (j0 + c * 32 + i >= n) acc[i] = -FLT_MAX;
-          }
-          // key < thr  <=>  D > -thr/2 (exact: scaling by powers of two)
-          float thrD = -0.5f * thr;
-          float t16[16];
-#pragma unroll
-          for (int i = 0; i < 16; ++i) t16[i] = fmaxf(acc[2 * i], acc[2 * i + 1]);
-#pragma unroll
-          for (int w2 = 8; w2 >= 1; w2 >>= 1)
-#pragma unroll
-            for (int i = 0; i < w2; ++i) t16[i] = fmaxf(t16[i], t16[i + w2]);
-          if (t16[0] > thrD) {
-#pragma unroll
-            for (int i = 0; i < 32; ++i) {
-              acc[i] = -2.0f * acc[i];
-              m |= (acc[i] < thr ? 1u : 0u) << i;
-            }
-          }
-        } else {
-          // keys and the mask of those below the current threshold
-#pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            acc[i] = fmaf(-2.0f, acc[i], pn[i]);
-            m |= (acc[i] < thr ? 1u : 0u) << i;
-          }
-        }
-        if (m) {
+        int64_t cbase = j0 + c * 32;
+        uint32_t m0 = chunk_mask<FOLD>(a0, sqpad + cbase, cbase, n, thr);
+        uint32_t m1 = chunk_mask<FOLD>(a1, sqpad + cbase + 32, cbase + 32, n, thr);
+        if (m0 | m1) {
           // rare: park the keys in this thread's shared slot and insert one by one
           // (one copy of the insertion code keeps the loop small in the I-cache)
           float* slot = s->keys[threadIdx.x - 64];
 #pragma unroll
-          for (int i = 0; i < 32; ++i) slot[i] = acc[i];
-          int cbase = j0 + c * 32;
+          for (int i = 0; i < 32; ++i) {
+            slot[i] = a0[i];
+            slot[32 + i] = a1[i];
+          }
+          unsigned long long m = (unsigned long long)m0 | ((unsigned long long)m1 << 32);
           while (m) {
-            int i = __ffs(m) - 1;
+            int i = __ffsll((long long)m) - 1;
             m &= m - 1;
             float cd = slot[i];
             if (!(cd < best[KH - 1])) continue;
-            int ci = cbase + i;
+            int ci = (int)(cbase + i);
 #pragma unroll
             for (int u = 0; u < KH; ++u) {
               if (cd < best[u]) {
