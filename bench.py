@@ -45,7 +45,14 @@ WORKLOADS = {
     "small": dict(n_cells=2_000, n_genes=20_000, mu_mean=-1.0, mu_sd=1.5, nnz_per_cell=1000,
                   n_clusters=0, n_hvf=2000, npcs=50, k=20, dtype="float64", knn="fp32"),
 }
+# batched samples: many samples of different sizes through one launch per stage
+BATCHED = dict(n_samples=64, n_genes=20_000, cells_min=500, cells_max=50_000, depth_sd=0.5,
+               mu_mean=-1.2, mu_sd=1.6, nnz_per_cell=1000, n_clusters=10, n_hvf=2000, npcs=30,
+               k=15, dtype="bfloat16", knn="bf16")
 SEED = 20261203
+# DRAM bytes per algorithmic byte of the X v product kernel, from an ncu capture
+# of the 100,000-cell case (429.1 MB read + written for 425.7 MB algorithmic)
+SPMV_TRAFFIC_PER_BYTE = 429.1 / 425.7
 SCALE_FACTOR = 1e4
 SCALE_MAX = 10.0
 DISPERSION = 0.2
@@ -335,9 +342,13 @@ def main():
     ap.add_argument("--no-knn-stress", action="store_true")
     ap.add_argument("--kernel-case", choices=["irlba", "knn"], default=None,
                     help="run one small case of a kernel family (for profiler captures) and exit")
+    ap.add_argument("--batched", action="store_true",
+                    help="the batched-samples workload (64 samples) instead of the atlas")
     args = ap.parse_args()
     if args.kernel_case:
         return kernel_case(args)
+    if args.batched:
+        return batched_bench(args)
     w = dict(WORKLOADS[args.workload])
     if args.cells:
         w["n_cells"] = args.cells
@@ -450,7 +461,11 @@ def main():
             name, r = dom
             roof = {"kernel": name, "bound": "hbm", "achieved": round(r["gbs"], 1),
                     "peak": hbm_peak, "unit": "GB/s", "frac": round(r["gbs"] / hbm_peak, 4),
-                    "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
+                    "traffic": round(r["bytes"] * SPMV_TRAFFIC_PER_BYTE),
+                    "traffic_source": "ncu dram__bytes_read+write of the same kernel on the 100,000-cell "
+                                      "case (profiles/spmv_products_100k.md), per algorithmic byte, "
+                                      "scaled to this launch",
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
                     "bytes_per_launch": r["bytes"], "avg_launch_ms": round(r["avg_ms"], 4)}
         out = {
             "metric": METRIC, "value": round(value, 1), "unit": "cells/s", "n_gpus": world,
@@ -483,6 +498,97 @@ def main():
         print(json.dumps(out), flush=True)
     if td is not None:
         td.destroy_process_group()
+
+
+def batched_bench(args):
+    """64 samples x 20,000 genes, cells per sample log-uniform in [500, 50,000],
+    per-sample depth LogNormal(0, 0.5): normalise -> scale (per sample) -> PCA
+    30 -> kNN 15 for every sample, (a) batched: one launch per stage over all
+    samples (the Lanczos cycles of all samples in the same graph), (b) one
+    sample after another through the single-sample calls.  Aggregate cells/s
+    of both, on the same device-resident counts."""
+    import __graft_entry__ as ge
+    ge._build_module().build()
+    sv = ge.load_package()
+    ctx = sv.Context(0)
+    w = dict(BATCHED)
+    rng = np.random.default_rng(SEED + 4)
+    sizes = np.exp(rng.uniform(np.log(w["cells_min"]), np.log(w["cells_max"]), w["n_samples"])).astype(np.int64)
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    n = int(off[-1])
+    mu_g, s_c, cl, lfc = gen_params(w, n, SEED + 4)
+    depth = rng.lognormal(0.0, w["depth_sd"], w["n_samples"])
+    s_c = s_c * np.repeat(depth, sizes)
+    D = calibrate_depth(mu_g, s_c, cl, lfc, w["nnz_per_cell"])
+    counts = sv.CountMatrix.generate(n, w["n_genes"], mu_g, s_c, cl, lfc, depth=D, dispersion=DISPERSION,
+                                     seed=SEED + 4, ctx=ctx)
+    d0 = sv.normalize_cells(counts, scale_factor=SCALE_FACTOR, dtype=w["dtype"], ctx=ctx)
+    _, var = d0.gene_moments()
+    hvf = np.sort(np.argsort(-var, kind="stable")[: w["n_hvf"]]) + 1
+    del d0
+    per = [counts.select_cells(int(off[i]), int(off[i + 1])) for i in range(w["n_samples"])]
+    init = np.random.default_rng(SEED).standard_normal(w["n_hvf"])
+
+    def batched():
+        d = sv.normalize_cells(counts, scale_factor=SCALE_FACTOR, dtype=w["dtype"], ctx=ctx)
+        B = sv.Batch.create(d, off, features=hvf, scale_max=SCALE_MAX)
+        em = sv.batch_pca(B, w["npcs"], tol=1e-5, init=init, download=False)
+        sv.batch_ann(B, em, w["k"], precision=w["knn"], download=False)
+        ctx.sync()
+        return em
+
+    def loop():
+        out = []
+        for c in per:
+            d = sv.normalize_cells(c, scale_factor=SCALE_FACTOR, dtype=w["dtype"], ctx=ctx)
+            S = sv.scale_features(d, scale_max=SCALE_MAX, features=hvf)
+            em = sv.pca(S, w["npcs"], tol=1e-5, init=init, download=False)
+            sv.ann(em, w["k"], precision=w["knn"], ctx=ctx, keep=True, download=False)
+            out.append(em.stdev)
+        ctx.sync()
+        return out
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        ctx.sync()
+        l0 = ctx.launches()
+        t0 = time.perf_counter()
+        r = None
+        for _ in range(steps):
+            r = fn()
+        ctx.sync()
+        return (time.perf_counter() - t0) / steps, (ctx.launches() - l0) / steps, r
+
+    steps, warmup = max(1, min(args.steps, 3)), max(1, min(args.warmup, 2))
+    clk = ClockSampler(0)
+    clk.start()
+    tb, lb, emb = timed(batched, steps, warmup)
+    clocks = clk.stop()
+    tl, ll, st_loop = timed(loop, 1, 1)
+    sb = emb.stdev
+    err = max(float(np.max(np.abs(sb[i] - st_loop[i]) / st_loop[i])) for i in range(w["n_samples"]))
+    it = emb.info["iters"]
+    out = {
+        "metric": "cells/s, 64 samples (500-50,000 cells each) normalise→PCA30→kNN15: batched vs one sample per launch",
+        "value": round(n / tb, 1), "unit": "cells/s", "n_gpus": 1, "steps": steps, "warmup": warmup,
+        "ms_per_step": round(tb * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16",
+        "data": "synthetic: seeded negative-binomial counts generated on the device (no dataset)",
+        "config": {"workload": f"batched: {w['n_samples']} samples, {n} cells x {w['n_genes']} genes, "
+                               f"{counts.nnz / n:.0f} nnz/cell, {w['n_hvf']} features, PCA {w['npcs']}, "
+                               f"kNN {w['k']}",
+                   "n_cells": n, "sample_cells_min": int(sizes.min()), "sample_cells_max": int(sizes.max()),
+                   "nnz": counts.nnz, "depth_factor": round(D, 5), "value_dtype": w["dtype"],
+                   "knn_kernel": w["knn"], "irlba_cycles_min": int(it.min()), "irlba_cycles_max": int(it.max()),
+                   "timing": "wall clock with the stream synchronised on both sides"},
+        "loop": {"value": round(n / tl, 1), "ms_per_step": round(tl * 1e3, 3), "gpu_launches": int(ll)},
+        "batched_vs_loop": round(tl / tb, 3),
+        "stdev_rel_diff_batched_vs_loop_max": err,
+        "gpu_launches": int(lb),
+        "clocks": clocks,
+    }
+    print(json.dumps(out))
 
 
 def kernel_case(args):

@@ -68,6 +68,7 @@ typedef struct sv_centered sv_centered;  /* implicit CenteredMatrix over a featu
 typedef struct sv_embed    sv_embed;     /* device-resident PCA result                 */
 typedef struct sv_knn      sv_knn;       /* device-resident neighbour lists            */
 typedef struct sv_graph    sv_graph;     /* device-resident SNN graph (CSC)            */
+typedef struct sv_batch    sv_batch;     /* samples stacked by cells, scaled per sample */
 
 /* ---- context, errors, diagnostics ----------------------------------------- */
 int  sv_version(void);                                   /* 100 * major + minor */
@@ -137,6 +138,22 @@ int sv_counts_free(sv_counts* c);
 int sv_filter_counts(sv_context* ctx, const sv_counts* counts, int64_t min_cells,
                      int64_t min_features, int64_t min_feature_count, int64_t min_umi,
                      uint8_t* cells_kept, uint8_t* genes_kept, sv_counts** out);
+/* The cells [r0, r1) (0-based, end exclusive) of a count matrix as a count
+ * matrix of their own, every gene kept (one sample of samples stacked by cells). */
+int sv_counts_select_cells(sv_context* ctx, const sv_counts* counts, int64_t r0, int64_t r1,
+                           sv_counts** out);
+
+/* ---- find_variable_features(:vst) (src/variablefeatures.jl:19-50,128-160) ----
+ * Per-gene mean and std (n - 1) of the counts; over the genes with std > 0 a
+ * local quadratic regression (loess, span loess_span, tricube weights,
+ * evaluated directly at every gene) of log10(std) on log10(mean); expected std
+ * 10^fit (NaN -> 0); metric = variance of min((x - mean)/expected std,
+ * sqrt(n_cells)) over all cells (implicit zeros included).  features receives
+ * the nfeatures genes of largest metric (1-based, largest first, ties by
+ * index); metric (n_genes) may be NULL.  The reference's Loess.jl interpolates
+ * the same fit between kd-tree vertices; that interpolation is not restated. */
+int sv_find_variable_features_vst(sv_context* ctx, const sv_counts* counts, int64_t nfeatures,
+                                  double loess_span, int64_t* features, double* metric);
 
 /* ---- normalize_cells (src/normalize.jl:17-55,76-79) -------------------------
  * method SV_LOGNORMALIZE or SV_RELATIVECOUNTS; value dtype SV_F64 (the
@@ -271,6 +288,34 @@ int sv_knn_embed(sv_context* ctx, const sv_embed* e, int64_t ndims, int64_t k, i
                  sv_knn** out);
 int sv_knn_info(const sv_knn* k, int64_t* n, int64_t* kk);
 int sv_knn_free(sv_knn* k);
+
+/* ---- batched samples ------------------------------------------------------------
+ * No single counterpart in the reference: several samples, stacked by cells in
+ * one count matrix over the same genes (sample s = cells cell_offsets[s] ..
+ * cell_offsets[s+1]-1), each taken through scale_features, pca and ann as the
+ * reference would take it on its own (src/scaling.jl:335-357,
+ * src/embedding.jl:46-76, src/neighbours.jl:19-74), with one launch per stage
+ * covering every sample.  normalize_cells works per cell, so sv_normalize_cells
+ * of the stacked counts is already per sample.  Values FP32 or BF16.
+ * sv_batch_create: per-(sample, feature) moments and the implicit scaled
+ * matrices (features as in sv_scale_features).  sv_batch_stats: sample-major
+ * (nseg x nf) mu, mean, std.  sv_batch_pca: the irlba of every sample in the same
+ * launches (each converges and is finished on its own); Z is n_cells x npcs
+ * column-major (samples' rows stacked), stdev nseg x npcs, iters nseg; init (nf)
+ * is every sample's start vector; SV_ERR_NOCONV when a sample did not converge.
+ * sv_batch_knn: each cell's k neighbours among the cells of its own sample;
+ * indices are 1-based stacked rows. */
+int sv_batch_create(sv_context* ctx, const sv_data* data, const int64_t* cell_offsets, int64_t nseg,
+                    const int64_t* features, int64_t nfeatures, double scale_max, sv_batch** out);
+int sv_batch_info(const sv_batch* b, int64_t* nseg, int64_t* n_cells, int64_t* nf);
+int sv_batch_stats(sv_context* ctx, const sv_batch* b, double* mu, double* mean, double* sd);
+int sv_batch_pca(sv_context* ctx, const sv_batch* b, int64_t npcs, int64_t maxit, double tol,
+                 const double* init, uint64_t seed, sv_embed** out, double* Z, double* stdev,
+                 int64_t* iters, int64_t* nmatvec);
+int sv_batch_knn(sv_context* ctx, const sv_batch* b, const sv_embed* e, int64_t ndims, int64_t k,
+                 int metric, int include_self, int precision, int32_t* nn_index, double* distances,
+                 sv_knn** out);
+int sv_batch_free(sv_batch* b);
 
 /* Drop-ins for the native libcell symbols of src/neighbours.jl:37-72 (the Julia
  * side declares every X / distances pointer as Ptr{Float64}; the element type is

@@ -628,6 +628,82 @@ def synth_counts(n_cells, n_genes, mu_mean=-1.0, mu_sd=1.5, depth=1.0, size_sd=0
     return X
 
 
+def loess_direct(x, y, span=0.5):
+    """Local quadratic regression (Cleveland 1979; Cleveland & Grosse 1991),
+    evaluated directly at every x: the q = floor(n * span) nearest x (a
+    contiguous window of the sorted x; ties in distance resolved toward the
+    lower index), tricube weights (1 - (d / d_q)^3)^3 with d_q the largest
+    distance in the window, weighted least squares in the centred x - x0.
+    Returns the fitted values at x (in the input order).  The reference calls
+    Loess.jl (loess(xs, ys, span), degree 2, src/variablefeatures.jl:41), whose
+    default evaluates this fit at kd-tree vertices and interpolates between
+    them; this direct form is the fit itself, not that interpolation."""
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    n = len(x)
+    q = max(3, min(n, int(np.floor(n * span))))
+    order = np.argsort(x, kind="stable")
+    xs, ys = x[order], y[order]
+    out = np.empty(n)
+    a = 0
+    for i in range(n):
+        x0 = xs[i]
+        # slide the window [a, a + q) while the next point is strictly closer
+        while a + q < n and (x0 - xs[a]) > (xs[a + q] - x0):
+            a += 1
+        win = slice(a, a + q)
+        d = np.abs(xs[win] - x0)
+        dq = d.max()
+        if dq > 0:
+            w = (1.0 - (d / dq) ** 3) ** 3
+        else:
+            w = np.ones(q)
+        t = xs[win] - x0
+        s0, s1, s2, s3, s4 = (np.sum(w * t ** k) for k in range(5))
+        r0, r1, r2 = (np.sum(w * t ** k * ys[win]) for k in range(3))
+        M = np.array([[s0, s1, s2], [s1, s2, s3], [s2, s3, s4]])
+        try:
+            beta = np.linalg.solve(M, [r0, r1, r2])
+        except np.linalg.LinAlgError:
+            beta = np.linalg.lstsq(M, [r0, r1, r2], rcond=None)[0]
+        out[order[i]] = beta[0]
+    return out
+
+
+def vst_metric(A, loess_span=0.5):
+    """src/variablefeatures.jl:19-50: per-gene mean and std of the counts (n - 1),
+    loess of log10(std) on log10(mean) over the non-constant genes, expected
+    std = 10^fit (NaN -> 0), then the variance of the standardised values
+    clipped at sqrt(n_cells) (implicit zeros included).  A: cells x genes CSC."""
+    A = _as_csc(A)
+    n = A.shape[0]
+    mu, var = mean_var(A.astype(np.float64))
+    sd = np.sqrt(var)
+    nc = sd > 0
+    exp_sd = sd.copy()
+    fit = loess_direct(np.log10(mu[nc]), np.log10(sd[nc]), loess_span)
+    exp_sd[nc] = 10.0 ** fit
+    exp_sd[np.isnan(exp_sd)] = 0.0
+    vmax = math.sqrt(n)
+    out = np.zeros(A.shape[1])
+    for g in range(A.shape[1]):
+        if exp_sd[g] == 0.0:
+            continue
+        v = A.data[A.indptr[g]:A.indptr[g + 1]].astype(np.float64)
+        z = np.minimum((v - mu[g]) / exp_sd[g], vmax)
+        z0 = min((0.0 - mu[g]) / exp_sd[g], vmax)
+        out[g] = (np.sum(z * z) + (n - len(v)) * z0 * z0) / (n - 1)
+    return out
+
+
+def find_variable_features_vst(A, nfeatures=2000, loess_span=0.5):
+    """src/variablefeatures.jl:128-160 with method=:vst: the nfeatures genes of
+    largest vst metric, 1-based, in decreasing metric order (ties by index)."""
+    m = vst_metric(A, loess_span)
+    order = np.lexsort((np.arange(len(m)), -m))[:nfeatures]
+    return order + 1, m
+
+
 def top_variable_genes(Xn, nfeat):
     """Stand-in HVF selection: the nfeat genes with the largest variance of the
     normalised data (1-based, ascending).  The reference's vst selection

@@ -33,7 +33,9 @@ from ._lib import (ConvergenceError, SeveroGPUError, SV_BF16, SV_COSINE, SV_EUCL
 
 __all__ = [
     "Context", "CountMatrix", "DataMatrix", "CenteredMatrix", "LinearEmbedding",
-    "filter_counts", "filter_cells", "filter_features", "normalize_cells", "scale_features", "irlba", "irlba_callback", "pca", "embedding", "ann",
+    "filter_counts", "filter_cells", "filter_features", "find_variable_features", "normalize_cells",
+    "Batch", "batch_pca",
+    "batch_ann", "scale_features", "irlba", "irlba_callback", "pca", "embedding", "ann",
     "nearest_neighbours", "jaccard_index", "shared_nearest_neighbours", "SeveroGPUError",
     "ConvergenceError", "default_context",
 ]
@@ -216,6 +218,12 @@ class CountMatrix(_Handle):
         L.check(self.ctx.lib.sv_counts_download_csc(self.ctx.h, self.h, _ptr(cp), _ptr(rv), _ptr(cv)))
         return sp.csc_matrix((cv, rv, cp), shape=(m, n))
 
+    def select_cells(self, r0, r1):
+        """Cells r0 .. r1-1 (0-based) as a count matrix of their own (device copy)."""
+        h = C.c_void_p()
+        L.check(self.ctx.lib.sv_counts_select_cells(self.ctx.h, self.h, int(r0), int(r1), C.byref(h)))
+        return CountMatrix(self.ctx, h)
+
     def to_csr(self):
         m, n = self.shape
         rp = np.empty(m + 1, np.int64)
@@ -299,6 +307,20 @@ def filter_features(X: CountMatrix, min_cells=0):
     """src/filtering.jl:15-20: (filtered CountMatrix, FI)."""
     A, _, fi = filter_counts(X, min_cells, 0, 0, 0)
     return A, fi
+
+
+def find_variable_features(X: CountMatrix, nfeatures=2000, method="vst", loess_span=0.5):
+    """src/variablefeatures.jl:128-160 with method=:vst on the device counts:
+    (features 1-based, largest metric first; metric per gene)."""
+    if str(method).lstrip(":") != "vst":
+        raise ValueError("only method=:vst runs on the device")
+    ctx = X.ctx
+    n_genes = X.shape[1]
+    feats = np.zeros(nfeatures, np.int64)
+    metric = np.zeros(n_genes)
+    L.check(ctx.lib.sv_find_variable_features_vst(ctx.h, X.h, int(nfeatures), float(loess_span),
+                                                  _ptr(feats), _ptr(metric)))
+    return feats, metric
 
 
 def normalize_cells(X, method="lognormalize", scale_factor=1.0, dtype="float64",
@@ -501,6 +523,81 @@ def embedding(S, npcs, method="pca", algorithm="irlba", **kw):
 
 class KNN(_Handle):
     _free = "sv_knn_free"
+
+
+class Batch(_Handle):
+    """Samples stacked by cells in one normalised data matrix (same genes), each
+    scaled with its own moments (scale_features per sample); the batched path
+    runs every sample's PCA and kNN in the same launches."""
+    _free = "sv_batch_free"
+
+    @classmethod
+    def create(cls, data: DataMatrix, cell_offsets, features=None, scale_max=np.inf):
+        ctx = data.ctx
+        off = np.ascontiguousarray(cell_offsets, dtype=np.int64)
+        feats = None if features is None else np.ascontiguousarray(features, dtype=np.int64)
+        h = C.c_void_p()
+        L.check(ctx.lib.sv_batch_create(ctx.h, data.h, _ptr(off), len(off) - 1, _ptr(feats),
+                                         0 if feats is None else len(feats), float(scale_max),
+                                         C.byref(h)))
+        b = cls(ctx, h)
+        b.offsets = off
+        b._data = data
+        return b
+
+    @property
+    def nseg(self):
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        L.check(self.ctx.lib.sv_batch_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value
+
+    @property
+    def nf(self):
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        L.check(self.ctx.lib.sv_batch_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return c.value
+
+    def stats(self):
+        """(mu, mean, std), each nseg x nf."""
+        S, nf = self.nseg, self.nf
+        mu, mean, sd = (np.zeros((S, nf)) for _ in range(3))
+        L.check(self.ctx.lib.sv_batch_stats(self.ctx.h, self.h, _ptr(mu), _ptr(mean), _ptr(sd)))
+        return mu, mean, sd
+
+
+def batch_pca(B: Batch, npcs, tol=1e-5, maxit=1000, init=None, seed=0, download=True):
+    """pca (src/embedding.jl:46-76) of every sample of the batch: coordinates
+    n_cells x npcs (samples' rows stacked), stdev nseg x npcs, info["iters"] per
+    sample."""
+    ctx = B.ctx
+    nf, S = B.nf, B.nseg
+    n = int(B.offsets[-1])
+    k = min(int(np.min(np.diff(B.offsets))), nf, npcs)
+    if init is None:
+        init = np.random.default_rng(seed).standard_normal(nf)
+    init = np.ascontiguousarray(init, dtype=np.float64)
+    Z = np.zeros((n, k), order="F") if download else None
+    stdev = np.zeros((S, k))
+    iters = np.zeros(S, np.int64)
+    nmv = C.c_int64()
+    h = C.c_void_p()
+    L.check(ctx.lib.sv_batch_pca(ctx.h, B.h, npcs, maxit, tol, _ptr(init), seed, C.byref(h), _ptr(Z),
+                                 _ptr(stdev), _ptr(iters), C.byref(nmv)))
+    return LinearEmbedding(Z, stdev, None, _Embed(ctx, h), {"iters": iters, "nmatvec": nmv.value})
+
+
+def batch_ann(B: Batch, em: LinearEmbedding, k, metric="euclidean", include_self=True, precision="bf16",
+              download=True):
+    """ann (src/neighbours.jl:19-30) within each sample of the batch: nn_index
+    n_cells x k (1-based stacked rows), distances."""
+    ctx = B.ctx
+    n = int(B.offsets[-1])
+    idx = np.zeros((n, k), dtype=np.int32, order="F") if download else None
+    dist = np.zeros((n, k), dtype=np.float64, order="F") if download else None
+    h = C.c_void_p()
+    L.check(ctx.lib.sv_batch_knn(ctx.h, B.h, em.handle.h, 0, k, _METRICS[metric], int(include_self),
+                                 _PREC[precision], _ptr(idx), _ptr(dist), C.byref(h)))
+    return idx, dist, KNN(ctx, h)
 
 
 _METRICS = {"euclidean": SV_EUCLIDEAN, "cosine": SV_COSINE}

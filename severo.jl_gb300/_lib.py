@@ -78,6 +78,8 @@ SIGNATURES = {
     "sv_counts_download_csr": (i32, [vp, vp, vp, vp, vp]),
     "sv_counts_free": (i32, [vp]),
     "sv_filter_counts": (i32, [vp, vp, i64, i64, i64, i64, vp, vp, P(vp)]),
+    "sv_counts_select_cells": (i32, [vp, vp, i64, i64, P(vp)]),
+    "sv_find_variable_features_vst": (i32, [vp, vp, i64, C.c_double, vp, vp]),
     "sv_normalize_cells": (i32, [vp, vp, i32, dbl, i32, P(vp)]),
     "sv_normalize_csc_noalloc": (i32, [vp, vp, vp, i64, i64, i64, i32, dbl, vp, vp]),
     "sv_data_download_csc": (i32, [vp, vp, vp]),
@@ -110,6 +112,12 @@ SIGNATURES = {
     "sv_graph_download": (i32, [vp, vp, vp, vp, vp]),
     "sv_graph_network": (i32, [vp, vp, P(i64), vp, vp, vp]),
     "sv_graph_free": (i32, [vp]),
+    "sv_batch_create": (i32, [vp, vp, vp, i64, vp, i64, C.c_double, P(vp)]),
+    "sv_batch_info": (i32, [vp, P(i64), P(i64), P(i64)]),
+    "sv_batch_stats": (i32, [vp, vp, vp, vp, vp]),
+    "sv_batch_pca": (i32, [vp, vp, i64, i64, C.c_double, vp, C.c_uint64, P(vp), vp, vp, vp, P(i64)]),
+    "sv_batch_knn": (i32, [vp, vp, vp, i64, i64, i32, i32, i32, vp, vp, P(vp)]),
+    "sv_batch_free": (i32, [vp]),
 }
 
 _lib = None

@@ -105,19 +105,12 @@ __global__ void k_set_i64(int64_t* p, int64_t v) { *p = v; }
 
 }  // namespace
 
-SV_API int sv_filter_counts(sv_context* ctx, const sv_counts* A, int64_t min_cells,
-                            int64_t min_features, int64_t min_feature_count, int64_t min_umi,
-                            uint8_t* cells_kept, uint8_t* genes_kept, sv_counts** out) {
-  SV_TRY
-  sv_ctx_check(ctx);
-  SV_REQUIRE(A && A->ctx == ctx, "bad count-matrix handle");
-  SV_REQUIRE(out, "out is required");
+// The compaction shared by filter_counts and select_cells: rows with
+// ckeep[c] (device mask, ck64 its 0/1 copy), genes passing min_cells.
+static sv_counts* compact(sv_context* ctx, const sv_counts* A, DevBuf<unsigned char>& ckeep,
+                          DevBuf<int64_t>& ck64, int64_t min_cells, DevBuf<unsigned char>& gkeep) {
   const int64_t nc = A->n_cells, ng = A->n_genes;
-  DevBuf<unsigned char> ckeep(nc), gkeep(ng);
-  DevBuf<int64_t> ck64(nc + 1), cnew(nc + 1), gk64(ng + 1), gnew(ng + 1), glen(ng + 1), gstart(ng + 1);
-  sv_launch(ctx, "filter_cells", k_filter_cells, dim3(sv_grid_for(ctx, nc * 32, 256)), dim3(256), 0,
-            (const int64_t*)A->csr_rowptr.get(), (const int32_t*)A->csr_count.get(), nc, ng,
-            min_feature_count, min_features, min_umi, ckeep.get(), ck64.get());
+  DevBuf<int64_t> cnew(nc + 1), gk64(ng + 1), gnew(ng + 1), glen(ng + 1), gstart(ng + 1);
   sv_scan_i64(ctx, ck64.get(), cnew.get(), nc);
   sv_launch(ctx, "filter_genes", k_filter_genes, dim3(sv_grid_for(ctx, ng * 32, 256)), dim3(256), 0,
             (const int64_t*)A->csc_colptr.get(), (const int32_t*)A->csc_rowidx.get(),
@@ -144,6 +137,55 @@ SV_API int sv_filter_counts(sv_context* ctx, const sv_counts* A, int64_t min_cel
               (const int64_t*)gstart.get(), c->csc_colptr.get(), c->csc_rowidx.get(), c->csc_count.get());
     sv_launch(ctx, "filter_write", k_set_i64, dim3(1), dim3(1), 0, c->csc_colptr.get() + ng2, nnz2);
     sv_build_csr_from_csc(ctx, c);
+  } catch (...) {
+    delete c;
+    throw;
+  }
+  return c;
+}
+
+__global__ void k_range_mask(int64_t n, int64_t r0, int64_t r1, unsigned char* __restrict__ keep,
+                             int64_t* __restrict__ keep64) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    bool k = i >= r0 && i < r1;
+    keep[i] = k;
+    keep64[i] = k;
+  }
+}
+
+// The cells [r0, r1) of a count matrix as a count matrix of their own (all
+// genes kept), e.g. one sample of samples stacked by cells.
+SV_API int sv_counts_select_cells(sv_context* ctx, const sv_counts* A, int64_t r0, int64_t r1,
+                                  sv_counts** out) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(A && A->ctx == ctx && out, "bad argument");
+  SV_REQUIRE(0 <= r0 && r0 < r1 && r1 <= A->n_cells, "cell range out of bounds");
+  DevBuf<unsigned char> ckeep(A->n_cells), gkeep(A->n_genes);
+  DevBuf<int64_t> ck64(A->n_cells + 1);
+  sv_launch(ctx, "filter_cells", k_range_mask, dim3(sv_grid_for(ctx, A->n_cells, 256)), dim3(256), 0,
+            A->n_cells, r0, r1, ckeep.get(), ck64.get());
+  *out = compact(ctx, A, ckeep, ck64, 0, gkeep);
+  sv_sync(ctx);
+  SV_CATCH
+}
+
+SV_API int sv_filter_counts(sv_context* ctx, const sv_counts* A, int64_t min_cells,
+                            int64_t min_features, int64_t min_feature_count, int64_t min_umi,
+                            uint8_t* cells_kept, uint8_t* genes_kept, sv_counts** out) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(A && A->ctx == ctx, "bad count-matrix handle");
+  SV_REQUIRE(out, "out is required");
+  const int64_t nc = A->n_cells, ng = A->n_genes;
+  DevBuf<unsigned char> ckeep(nc), gkeep(ng);
+  DevBuf<int64_t> ck64(nc + 1);
+  sv_launch(ctx, "filter_cells", k_filter_cells, dim3(sv_grid_for(ctx, nc * 32, 256)), dim3(256), 0,
+            (const int64_t*)A->csr_rowptr.get(), (const int32_t*)A->csr_count.get(), nc, ng,
+            min_feature_count, min_features, min_umi, ckeep.get(), ck64.get());
+  sv_counts* c = compact(ctx, A, ckeep, ck64, min_cells, gkeep);
+  try {
     if (cells_kept) sv_d2h(ctx, cells_kept, ckeep.get(), nc);
     if (genes_kept) sv_d2h(ctx, genes_kept, gkeep.get(), ng);
     sv_sync(ctx);

@@ -217,6 +217,43 @@ struct sv_centered {
   sv_data* own_data = nullptr;
 };
 
+// Rows of a stacked matrix that holds several independent samples: a block
+// schedule covers each sample's rows with contiguous ranges (never crossing a
+// sample boundary), the blocks of one sample consecutive.
+struct BlkRange {
+  int64_t r0, r1;
+  int seg, pad;
+};
+
+// Several samples stacked by cells over the same genes (one normalised data
+// matrix), each scaled with its own moments: the batched path.
+struct sv_batch {
+  sv_context* ctx = nullptr;
+  const sv_data* data = nullptr;
+  int64_t nseg = 0, n_cells = 0, nf = 0;
+  double scale_max = 0;
+  std::vector<int64_t> hoff;          // nseg + 1 cell offsets
+  DevBuf<int64_t> off;
+  sv_centered* base = nullptr;        // the feature-subset copies of the stacked data
+  // per (sample, feature), sample-major: index s * nf + f
+  DevBuf<double> mean, std_, mu, inv_d, clip_d;
+  DevBuf<float> inv_f, clip_f, mu_h, mu_l;
+  // X v: blocks of cells within one sample
+  DevBuf<BlkRange> xblk;
+  int nxblk = 0;
+  // X^T u: row blocks aligned to the samples
+  int64_t n_rb = 0;
+  std::vector<int64_t> h_rb_first;    // nseg + 1: first row block of each sample
+  DevBuf<int64_t> rb_row0;            // n_rb + 1 first rows
+  DevBuf<int> rb_seg;                 // n_rb
+  DevBuf<int64_t> rb_first;           // nseg + 1
+  DevBuf<int64_t> rb_ptr;             // n_rb * nf + 1
+  DevBuf<uint16_t> rb_idx;
+  DevBuf<unsigned char> rb_val;
+  DevBuf<float> rb_partial;           // n_rb x nf
+  DevBuf<double> upart;               // n_rb sums of u
+};
+
 struct sv_embed {
   sv_context* ctx = nullptr;
   int64_t n_cells = 0, npcs = 0, nf = 0;
@@ -272,6 +309,7 @@ __device__ __forceinline__ float sv_load_val(const __nv_bfloat16* p, int64_t i) 
   return __bfloat162float(p[i]);
 }
 __device__ __forceinline__ double sv_load_val(const double* p, int64_t i) { return p[i]; }
+__device__ __forceinline__ double sv_load_val(const int32_t* p, int64_t i) { return (double)p[i]; }
 
 // ---------------------------------------------------------------------------
 // host helpers implemented in sv_core.cu

@@ -32,6 +32,11 @@ void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const 
                        double alpha, double beta, const double* csub, const double* z);
 bool sv_centered_apply_df(sv_context* ctx, const sv_centered* S, const float* xh, const float* xl,
                           float* yh, float* yl, const double* csub, const float* zh, const float* zl);
+void sv_batch_apply_N_df(sv_context* ctx, const sv_batch* b, const float* xh, const float* xl,
+                         float* yh, float* yl, const double* csub, const float* zh, const float* zl,
+                         const int* active);
+void sv_batch_apply_T(sv_context* ctx, const sv_batch* b, const double* u, double* y,
+                      const double* csub, const double* z, const int* active);
 
 namespace {
 
@@ -95,6 +100,12 @@ __device__ __forceinline__ bool last_block(unsigned int* counter, bool* flag_sme
   return *flag_smem;
 }
 
+// Rows of a stacked side: the bases of several independent problems (samples)
+// are stacked by rows, sample s owning rows [off[s], off[s+1]); a block schedule
+// (BlkRange) covers them, the blocks of sample s being seg_blk[s] ..
+// seg_blk[s+1]-1.  One sample is the usual case; the kernels below take the
+// schedule in either case.
+
 // One pass of the CGS2 reorthogonalisation of the working vector x against the
 // basis Q[:, :ncols] (both double-float), in three fusable parts:
 //   UPDATE  x -= Q cin (cin from the previous pass), x written back;
@@ -107,8 +118,9 @@ __device__ __forceinline__ bool last_block(unsigned int* counter, bool* flag_sme
 // basis element is loaded once, coalesced, with 4*NJ loads in flight per thread.
 // The update sums each row's 8 per-warp partial products through shared memory;
 // the dot products accumulate per lane and reduce across lanes once at the end.
-// Per-block FP64 partials; the last block reduces them in block order
-// (deterministic).  NJ = columns per warp: 8 for bases of up to 64 columns,
+// Per-block FP64 partials; the last block reduces them per sample in block
+// order (deterministic); cin / cout hold MAX_WORK coefficients per sample, nrm
+// one norm per sample; blocks of inactive samples skip the rows.  NJ = columns per warp: 8 for bases of up to 64 columns,
 // 12 up to MAX_WORK (fewer registers, more resident blocks for the usual
 // nu + 7 basis).
 
@@ -125,7 +137,10 @@ template <int NJ, bool UPDATE, bool DOTS, bool NORM>
 __global__ void __launch_bounds__(256) k_cgs_df(const float* __restrict__ Qh,
                                                 const float* __restrict__ Ql, int64_t ld, int ncols,
                                                 float* __restrict__ xh, float* __restrict__ xl,
-                                                const double* __restrict__ y, int64_t len,
+                                                const double* __restrict__ y,
+                                                const BlkRange* __restrict__ blk,
+                                                const int* __restrict__ seg_blk, int nseg,
+                                                const int* __restrict__ active,
                                                 const double* __restrict__ cin,
                                                 double* __restrict__ part, double* __restrict__ npart,
                                                 double* __restrict__ cout, double* __restrict__ nrm,
@@ -136,11 +151,12 @@ __global__ void __launch_bounds__(256) k_cgs_df(const float* __restrict__ Qh,
   __shared__ double nsh[32];
   __shared__ bool last;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const BlkRange br = blk[blockIdx.x];
+  const int sg = br.seg;
   if (UPDATE)
-    for (int j = tid; j < ncols; j += blockDim.x) df_split(cin[j], csh[j], csl[j]);
+    for (int j = tid; j < ncols; j += blockDim.x) df_split(cin[sg * MAX_WORK + j], csh[j], csl[j]);
   __syncthreads();
-  int64_t seg = (len + gridDim.x - 1) / gridDim.x;
-  int64_t r0 = (int64_t)blockIdx.x * seg, r1 = min(len, r0 + seg);
+  int64_t r0 = br.r0, r1 = (active == nullptr || active[sg]) ? br.r1 : br.r0;
   float ah[NJ], al[NJ];
 #pragma unroll
   for (int t = 0; t < NJ; ++t) ah[t] = al[t] = 0.f;
@@ -265,18 +281,22 @@ __global__ void __launch_bounds__(256) k_cgs_df(const float* __restrict__ Qh,
   }
   if (last_block(counter, &last)) {
     if (DOTS) {
-      // one warp per column, lanes over blocks (block order fixed: deterministic)
-      for (int j = w; j < ncols; j += 8) {
+      // one warp per (sample, column), lanes over the sample's blocks (block
+      // order fixed: deterministic)
+      for (int pq = w; pq < nseg * ncols; pq += 8) {
+        int s2 = pq / ncols, j = pq - s2 * ncols;
         double s = 0;
-        for (unsigned b = lane; b < gridDim.x; b += 32) s += part[(int64_t)b * ncols + j];
+        for (int b = seg_blk[s2] + lane; b < seg_blk[s2 + 1]; b += 32) s += part[(int64_t)b * ncols + j];
         s = sv_warp_sum(s);
-        if (lane == 0) cout[j] = s;
+        if (lane == 0) cout[s2 * MAX_WORK + j] = s;
       }
     }
-    if (NORM && tid == 0) {
-      double s = 0;
-      for (unsigned b = 0; b < gridDim.x; ++b) s += npart[b];
-      *nrm = sqrt(s);
+    if (NORM) {
+      for (int s2 = tid; s2 < nseg; s2 += blockDim.x) {
+        double s = 0;
+        for (int b = seg_blk[s2]; b < seg_blk[s2 + 1]; ++b) s += npart[b];
+        nrm[s2] = sqrt(s);
+      }
     }
     if (tid == 0) *counter = 0;
   }
@@ -310,55 +330,74 @@ __device__ __forceinline__ double normal_at(unsigned long long seed, unsigned lo
 #define CTL_THRESH 0
 #define CTL_SMAX 1
 #define CTL_CYCLE 2
+#define CTL_N 3          // control-block doubles per sample
 __device__ __forceinline__ unsigned long long breakdown_tag(const double* ctl, unsigned step) {
   return (unsigned long long)ctl[CTL_CYCLE] * 1024ull + step;
 }
 
-// Basis column := x / *nrm (double-float) and cur := the same in FP64; the B
-// entry := *nrm.  When *nrm < ctl[CTL_THRESH] the Krylov space is (numerically)
-// invariant: cur := a random vector, B entry := 0, flag set for k_fix_df, which
-// orthonormalises cur against the basis and writes the column.
-__global__ void k_scal_df(const float* __restrict__ xh, const float* __restrict__ xl, int64_t len,
+// Basis column := x / nrm[s] (double-float) and cur := the same in FP64; the B
+// entry of sample s (B + s*bstride + boff, when B is given) := nrm[s].  When
+// nrm[s] < the sample's threshold the Krylov space is (numerically) invariant:
+// cur := a random vector, B entry := 0, flag[s] set for k_fix_df, which
+// orthonormalises cur against the basis and writes the column.  Rows of sample
+// s are indexed from its offset for the random vector (i - off).
+__global__ void k_scal_df(const float* __restrict__ xh, const float* __restrict__ xl,
+                          const BlkRange* __restrict__ blk, const int* __restrict__ seg_blk,
+                          const int64_t* __restrict__ off, const int* __restrict__ active,
                           const double* __restrict__ nrm, const double* __restrict__ ctl,
                           float* __restrict__ colh, float* __restrict__ coll, double* __restrict__ cur,
-                          double* __restrict__ bentry, int* __restrict__ flag,
+                          double* __restrict__ B, int64_t boff, int64_t bstride, int* __restrict__ flag,
                           unsigned long long seed, unsigned step) {
-  double s = *nrm;
-  bool brk = !(s >= ctl[CTL_THRESH]);
-  unsigned long long tag = breakdown_tag(ctl, step);
+  const BlkRange br = blk[blockIdx.x];
+  const int sg = br.seg;
+  if (active && !active[sg]) return;
+  const double* c = ctl + sg * CTL_N;
+  double s = nrm[sg];
+  bool brk = !(s >= c[CTL_THRESH]);
+  unsigned long long tag = breakdown_tag(c, step);
   double inv = brk ? 0.0 : 1.0 / s;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t i = br.r0 + threadIdx.x; i < br.r1; i += blockDim.x) {
     if (brk) {
-      cur[i] = normal_at(seed, tag, i);
+      cur[i] = normal_at(seed, tag, i - off[sg]);
     } else {
       double v = df_val(xh[i], xl[i]) * inv;
       cur[i] = v;
       df_split(v, colh[i], coll[i]);
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    if (bentry) *bentry = brk ? 0.0 : s;
-    if (brk) *flag = 1;
+  if ((int)blockIdx.x == seg_blk[sg] && threadIdx.x == 0) {
+    if (B) B[sg * bstride + boff] = brk ? 0.0 : s;
+    if (brk) flag[sg] = 1;
   }
 }
 
-// zero the norm slot (the sub-diagonal scalar the next product uses) when a
-// breakdown was flagged; separate launch so every k_scal_df block has read it
-__global__ void k_scal_post(double* nrm, const int* flag) {
-  if (*flag) *nrm = 0.0;
+// zero the norm slot (the sub-diagonal scalar the next product uses) of every
+// sample whose breakdown was flagged; separate launch so every k_scal_df block
+// has read it
+__global__ void k_scal_post(double* nrm, const int* flag, int nseg) {
+  for (int s = threadIdx.x; s < nseg; s += blockDim.x)
+    if (flag[s]) nrm[s] = 0.0;
 }
 
-// One block: if *flag, cur <- CGS2(cur, Q[:, :ncols]) normalised (FP64
-// arithmetic on the double-float basis), written to the basis column as well;
-// clears the flag.  Runs only on a breakdown.
-__global__ void k_fix_df(double* __restrict__ cur, int64_t len, const float* __restrict__ Qh,
-                         const float* __restrict__ Ql, int64_t ld, int ncols, float* __restrict__ colh,
-                         float* __restrict__ coll, int* __restrict__ flag) {
+// One block per sample: if flag[s], cur <- CGS2(cur, Q[:, :ncols]) normalised
+// (FP64 arithmetic on the double-float basis) over the sample's rows, written to
+// the basis column as well; clears the flag.  Runs only on a breakdown.
+__global__ void k_fix_df(double* __restrict__ cur0, const int64_t* __restrict__ off,
+                         const float* __restrict__ Qh0, const float* __restrict__ Ql0, int64_t ld,
+                         int ncols, float* __restrict__ colh0, float* __restrict__ coll0,
+                         int* __restrict__ flags) {
   __shared__ double sh[32];
   __shared__ double cs[MAX_WORK];
   __shared__ double tot;
+  const int sg = blockIdx.x;
+  int* flag = flags + sg;
   if (*flag == 0) return;
+  const int64_t o0 = off[sg], len = off[sg + 1] - o0;
+  double* cur = cur0 + o0;
+  const float* Qh = Qh0 + o0;
+  const float* Ql = Ql0 + o0;
+  float* colh = colh0 + o0;
+  float* coll = coll0 + o0;
   for (int pass = 0; pass < 2; ++pass) {
     for (int j = 0; j < ncols; ++j) {
       double acc = 0;
@@ -395,22 +434,22 @@ __global__ void k_fix_df(double* __restrict__ cur, int64_t len, const float* __r
   if (threadIdx.x == 0) *flag = 0;
 }
 
-// The whole feature-side step in one block (the feature side is short: a few
-// thousand entries): x = F (FP64 in, double-float working copy in xh/xl); CGS2
-// against V[:, :ncols]; *nrm = |x|; when write_col >= 0 the column write_col :=
-// x/|x| (double-float, FP64 copy in cur) and *bentry = |x|, or on a breakdown
-// (|x| < thresh) a random vector orthonormalised against V[:, :ncols] with
-// *bentry = *nrm = 0.  write_col < 0 (last step of a cycle) leaves the residual
-// in xh/xl.
+// The whole feature-side step of a sample in one block (the feature side is
+// short: a few thousand entries), one block per sample: x = F (FP64 in,
+// double-float working copy in xh/xl); CGS2 against V[:, :ncols]; nrm[s] = |x|;
+// when write_col >= 0 the column write_col := x/|x| (double-float, FP64 copy in
+// cur) and the B entry = |x|, or on a breakdown (|x| < threshold) a random vector
+// orthonormalised against V[:, :ncols] with B entry = nrm[s] = 0.  write_col < 0
+// (last step of a cycle) leaves the residual in xh/xl.
 __device__ void vside_cgs2(float* __restrict__ xh, float* __restrict__ xl, int64_t len,
-                           const float* __restrict__ Vh, const float* __restrict__ Vl, int ncols,
-                           double* c, float* ch, float* cl) {
+                           const float* __restrict__ Vh, const float* __restrict__ Vl, int64_t ld,
+                           int ncols, double* c, float* ch, float* cl) {
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int pass = 0; pass < 2 && ncols > 0; ++pass) {
     for (int j = w; j < ncols; j += nw) {
       float ah = 0.f, al = 0.f;
-      const float* qh = Vh + (int64_t)j * len;
-      const float* ql = Vl + (int64_t)j * len;
+      const float* qh = Vh + (int64_t)j * ld;
+      const float* ql = Vl + (int64_t)j * ld;
       for (int64_t i = lane; i < len; i += 32) df_fma(ah, al, qh[i], ql[i], xh[i], xl[i]);
       double v = sv_warp_sum(df_val(ah, al));
       if (lane == 0) c[j] = v;
@@ -421,7 +460,7 @@ __device__ void vside_cgs2(float* __restrict__ xh, float* __restrict__ xl, int64
     for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
       float sh_ = 0.f, sl_ = 0.f;
       for (int j = 0; j < ncols; ++j) {
-        int64_t o = (int64_t)j * len + i;
+        int64_t o = (int64_t)j * ld + i;
         df_fma(sh_, sl_, Vh[o], Vl[o], ch[j], cl[j]);
       }
       float h = xh[i], l = xl[i];
@@ -446,41 +485,53 @@ __device__ double vside_norm(const float* __restrict__ xh, const float* __restri
   return *tot;
 }
 
-__global__ void __launch_bounds__(1024) k_vside(const double* __restrict__ F, int64_t len,
-                                                float* __restrict__ Vh, float* __restrict__ Vl,
+__global__ void __launch_bounds__(1024) k_vside(const double* __restrict__ F0,
+                                                const int64_t* __restrict__ off, int64_t ld,
+                                                float* __restrict__ Vh0, float* __restrict__ Vl0,
                                                 int ncols, int write_col, double* __restrict__ nrm,
                                                 const double* __restrict__ ctl,
-                                                double* __restrict__ bentry,
-                                                double* __restrict__ cur, float* __restrict__ xh,
-                                                float* __restrict__ xl, unsigned long long seed,
-                                                unsigned step) {
+                                                double* __restrict__ B, int64_t boff, int64_t bstride,
+                                                double* __restrict__ cur0, float* __restrict__ xh0,
+                                                float* __restrict__ xl0, const int* __restrict__ active,
+                                                unsigned long long seed, unsigned step) {
   __shared__ double c[MAX_WORK];
   __shared__ float ch[MAX_WORK], cl[MAX_WORK];
   __shared__ double sh[32];
   __shared__ double tot;
+  const int sg = blockIdx.x;   // one block per sample
+  if (active && !active[sg]) return;
+  const int64_t o0 = off[sg], len = off[sg + 1] - o0;
+  const double* F = F0 + o0;
+  float* Vh = Vh0 + o0;
+  float* Vl = Vl0 + o0;
+  double* cur = cur0 + o0;
+  float* xh = xh0 + o0;
+  float* xl = xl0 + o0;
+  const double* cb = ctl + sg * CTL_N;
+  double* bentry = B ? B + sg * bstride + boff : nullptr;
   for (int64_t i = threadIdx.x; i < len; i += blockDim.x) df_split(F[i], xh[i], xl[i]);
   __syncthreads();
-  vside_cgs2(xh, xl, len, Vh, Vl, ncols, c, ch, cl);
+  vside_cgs2(xh, xl, len, Vh, Vl, ld, ncols, c, ch, cl);
   double s = vside_norm(xh, xl, len, sh, &tot);
   if (write_col < 0) {
-    if (threadIdx.x == 0) *nrm = s;
+    if (threadIdx.x == 0) nrm[sg] = s;
     return;
   }
-  bool brk = !(s >= ctl[CTL_THRESH]);
+  bool brk = !(s >= cb[CTL_THRESH]);
   if (brk) {
-    unsigned long long tag = breakdown_tag(ctl, step);
+    unsigned long long tag = breakdown_tag(cb, step);
     for (int64_t i = threadIdx.x; i < len; i += blockDim.x) df_split(normal_at(seed, tag, i), xh[i], xl[i]);
     __syncthreads();
-    vside_cgs2(xh, xl, len, Vh, Vl, ncols, c, ch, cl);
+    vside_cgs2(xh, xl, len, Vh, Vl, ld, ncols, c, ch, cl);
     double r = vside_norm(xh, xl, len, sh, &tot);
     double inv = 1.0 / r;
     for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
       double v = df_val(xh[i], xl[i]) * inv;
       cur[i] = v;
-      df_split(v, Vh[(int64_t)write_col * len + i], Vl[(int64_t)write_col * len + i]);
+      df_split(v, Vh[(int64_t)write_col * ld + i], Vl[(int64_t)write_col * ld + i]);
     }
     if (threadIdx.x == 0) {
-      *nrm = 0.0;
+      nrm[sg] = 0.0;
       if (bentry) *bentry = 0.0;
     }
   } else {
@@ -488,16 +539,16 @@ __global__ void __launch_bounds__(1024) k_vside(const double* __restrict__ F, in
     for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
       double v = df_val(xh[i], xl[i]) * inv;
       cur[i] = v;
-      df_split(v, Vh[(int64_t)write_col * len + i], Vl[(int64_t)write_col * len + i]);
+      df_split(v, Vh[(int64_t)write_col * ld + i], Vl[(int64_t)write_col * ld + i]);
     }
     if (threadIdx.x == 0) {
-      *nrm = s;
+      nrm[sg] = s;
       if (bentry) *bentry = s;
     }
   }
 }
 
-// One-sided (Hestenes) Jacobi SVD of B (m x m, row-major), one block, in
+// One-sided (Hestenes) Jacobi SVD of B (m x m, row-major), one block per sample, in
 // double-float arithmetic: FP64 runs at 1/57 of the FP32 rate on this part (one
 // warp-wide FP64 instruction occupies an SM's FP64 pipe for ~17 cycles), and an
 // FP64 block spent ~4 ms per 57 x 57 SVD, so the columns of A = B and the
@@ -505,9 +556,11 @@ __global__ void __launch_bounds__(1024) k_vside(const double* __restrict__ F, in
 // updated on the FP32 pipe, and the rotation parameters are formed in FP32 and
 // normalised in double-float.
 // Columns are paired by the circle method (slot 0 fixed, the others rotating),
-// one warp per pair; a pair is rotated while |a_p . a_q| > 1e-13 |a_p| |a_q|
-// (the double-float dot products carry ~3e-15 relative error, so the FP64
-// threshold of 1e-15 would never be met).  Then s_i = |A e_i|, P_i = A e_i / s_i,
+// one warp per pair; a pair is rotated while |a_p . a_q| > tau |a_p| |a_q| with
+// tau = 1e-12 max(1, m / 16): a double-float dot product of m terms carries an
+// absolute error of about m 2^-48 |a_p| |a_q| (the low parts are summed in FP32),
+// so a threshold below that floor (FP64's 1e-15, or 1e-13 for m ~ 40) can keep
+// a sweep rotating on rounding noise.  Then s_i = |A e_i|, P_i = A e_i / s_i,
 // Q = J, sorted by descending s.
 // Outputs: P (m x m col-major), s (m), Q (m x m col-major), summary =
 // [s (m), P[m-1, :] (m), rf, sweeps].  Closes the cycle in the control block:
@@ -541,15 +594,26 @@ __device__ __forceinline__ void df_rot(float& xh, float& xl, float& yh, float& y
   yl = bl - (yh - bh);
 }
 
-__global__ void __launch_bounds__(1024) k_jacobi_svd(const double* __restrict__ B, int m,
-                                                     double* __restrict__ Pout,
-                                                     double* __restrict__ sout,
-                                                     double* __restrict__ Qout,
-                                                     double* __restrict__ summary,
-                                                     const double* __restrict__ rf, int max_sweeps,
+__global__ void __launch_bounds__(1024) k_jacobi_svd(const double* __restrict__ B0, int m,
+                                                     double* __restrict__ Pout0,
+                                                     double* __restrict__ sout0,
+                                                     double* __restrict__ Qout0,
+                                                     double* __restrict__ summary0,
+                                                     const double* __restrict__ rf0, int max_sweeps,
                                                      int* __restrict__ status,
-                                                     double* __restrict__ ctl, double eps_b) {
+                                                     double* __restrict__ ctl0, double eps_b,
+                                                     const int* __restrict__ active) {
   extern __shared__ float smf[];
+  // one block per sample
+  const int sg = blockIdx.x;
+  if (active && !active[sg]) return;
+  const double* B = B0 + (int64_t)sg * m * m;
+  double* Pout = Pout0 + (int64_t)sg * m * m;
+  double* Qout = Qout0 + (int64_t)sg * m * m;
+  double* sout = sout0 + (int64_t)sg * m;
+  double* summary = summary0 + (int64_t)sg * (2 * m + 2);
+  const double* rf = rf0 ? rf0 + sg : nullptr;
+  double* ctl = ctl0 + sg * CTL_N;
   float* Ah = smf;              // m*m, column c at [c*m]
   float* Al = Ah + m * m;
   float* Jh = Al + m * m;
@@ -568,6 +632,7 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(const double* __restrict__ 
   int mp = (m + 1) & ~1;   // even number of slots (one dummy when m is odd)
   int npairs = mp / 2;
   int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  const float tau = 1e-12f * fmaxf(1.f, (float)m / 16.f);
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     if (tid == 0) rotated = 0;
@@ -596,7 +661,7 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(const double* __restrict__ 
         // double-float sums): the angle only steers convergence, while the
         // orthogonality of the applied rotation comes from normalising (c, s)
         // in double-float
-        if (fabsf(gah) > 1e-13f * sqrtf(alh) * sqrtf(beh) && gah != 0.f) {
+        if (fabsf(gah) > tau * sqrtf(alh) * sqrtf(beh) && gah != 0.f) {
           // be - al in double-float: close singular values still give an
           // accurate angle
           float dh = beh, dl = bel;
@@ -684,15 +749,19 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(const double* __restrict__ 
 template <int KB, bool EXACT>
 __global__ void __launch_bounds__(256) k_rotate_df(const float* __restrict__ Inh,
                                                    const float* __restrict__ Inl, int64_t ld_in,
-                                                   int64_t len, int nin, const double* __restrict__ M,
+                                                   const BlkRange* __restrict__ blk,
+                                                   const int* __restrict__ sel, int nin,
+                                                   const double* __restrict__ M0, int64_t mstride,
                                                    int nout, float* __restrict__ outh,
                                                    float* __restrict__ outl, double* __restrict__ outd,
                                                    int64_t ld_out) {
   extern __shared__ float2 Ms[];   // nin*nout pairs (hi, lo)
+  const BlkRange br = blk[blockIdx.x];
+  if (sel && !sel[br.seg]) return;   // samples not selected keep their rows
+  const double* M = M0 + br.seg * mstride;
   for (int i = threadIdx.x; i < nin * nout; i += blockDim.x) df_split(M[i], Ms[i].x, Ms[i].y);
   __syncthreads();
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t i = br.r0 + threadIdx.x; i < br.r1; i += blockDim.x) {
     for (int c0 = 0; c0 < nout; c0 += KB) {
       float ah[KB], al[KB];
 #pragma unroll
@@ -724,13 +793,18 @@ __global__ void __launch_bounds__(256) k_rotate_df(const float* __restrict__ Inh
   }
 }
 
-// V[:, k] = F / rf (double-float column + FP64 current vector) and B reset.
+// V[:, k] = F / rf (double-float column + FP64 current vector) and B reset, per
+// sample (blockIdx.y; rows off[s] .. off[s+1]).
 __global__ void k_restart_tail(float* __restrict__ vkh, float* __restrict__ vkl,
-                               double* __restrict__ vcur, const double* __restrict__ F, int64_t n,
-                               const double* __restrict__ summary, int m, int k,
-                               double* __restrict__ B) {
+                               double* __restrict__ vcur, const double* __restrict__ F,
+                               const int64_t* __restrict__ off, const double* __restrict__ summary0,
+                               int m, int k, double* __restrict__ B0, const int* __restrict__ active) {
+  const int sg = blockIdx.y;
+  if (active && !active[sg]) return;
+  const double* summary = summary0 + (int64_t)sg * (2 * m + 2);
+  double* B = B0 + (int64_t)sg * m * m;
   double rf = summary[2 * m];
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+  for (int64_t i = off[sg] + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < off[sg + 1];
        i += (int64_t)gridDim.x * blockDim.x) {
     double v = F[i] / rf;
     vcur[i] = v;
@@ -762,12 +836,18 @@ __global__ void k_axpy_sub(double* __restrict__ y, const double* __restrict__ z,
     y[i] -= c * z[i];
 }
 
-__global__ void k_scale_cols(double* __restrict__ X, int64_t len, int ncols,
-                             const double* __restrict__ s) {
+// X[r, c] *= s[seg(r) * sstride + c] for the rows of sample blockIdx.y (X
+// column-major with leading dimension ld)
+__global__ void k_scale_cols(double* __restrict__ X, int64_t ld, const int64_t* __restrict__ off,
+                             int ncols, const double* __restrict__ s, int sstride) {
+  const int sg = blockIdx.y;
+  const int64_t o0 = off[sg], len = off[sg + 1] - o0;
+  const double* sc = s + (int64_t)sg * sstride;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < len * ncols;
        idx += (int64_t)gridDim.x * blockDim.x) {
     int c = (int)(idx / len);
-    X[idx] *= s[c];
+    int64_t r = idx - (int64_t)c * len;
+    X[(int64_t)c * ld + o0 + r] *= sc[c];
   }
 }
 
@@ -789,6 +869,8 @@ struct Op {
                     const float* zh, const float* zl) {
     return false;
   }
+  // the driver's per-sample active mask (device), for operators over stacked samples
+  virtual void bind_active(const int* active) { (void)active; }
 };
 
 struct CenteredOp : Op {
@@ -806,6 +888,28 @@ struct CenteredOp : Op {
             const float* zh, const float* zl) override {
     return sv_centered_apply_df(ctx, S, xh, xl, yh, yl, csub, zh, zl);
   }
+};
+
+// Block-diagonal operator of stacked samples (sv_batch): csub and the vectors
+// are per sample; frozen samples are skipped.
+struct BatchOp : Op {
+  sv_context* ctx;
+  const sv_batch* b;
+  const int* active = nullptr;
+  BatchOp(sv_context* c, const sv_batch* bb) : ctx(c), b(bb) {}
+  void N(const double*, double*, const double*, const double*) override {
+    sv_throw(SV_ERR_UNSUPPORTED, "batched samples use the double-float product");
+  }
+  void T(const double* x, double* y, const double* csub, const double* z) override {
+    sv_batch_apply_T(ctx, b, x, y, csub, z, active);
+  }
+  bool device_only() const override { return true; }
+  bool N_df(const float* xh, const float* xl, float* yh, float* yl, const double* csub,
+            const float* zh, const float* zl) override {
+    sv_batch_apply_N_df(ctx, b, xh, xl, yh, yl, csub, zh, zl, active);
+    return true;
+  }
+  void bind_active(const int* a) override { active = a; }
 };
 
 struct CallbackOp : Op {
@@ -834,30 +938,85 @@ struct CallbackOp : Op {
   }
 };
 
-struct IrlbaResult {
-  int info = 1;
-  int64_t iters = 0, nmatvec = 0;
+
+// Block schedule of a stacked side: each sample's rows split into contiguous
+// ranges, about `target` blocks in total in proportion to the sample sizes (at
+// least one per sample); a single sample gets ceil(len / target) rows per block.
+static void build_schedule(const std::vector<int64_t>& off, int target, std::vector<BlkRange>& blk,
+                           std::vector<int>& seg_blk) {
+  int nseg = (int)off.size() - 1;
+  int64_t total = std::max<int64_t>(1, off[nseg] - off[0]);
+  blk.clear();
+  seg_blk.assign(nseg + 1, 0);
+  for (int s = 0; s < nseg; ++s) {
+    seg_blk[s] = (int)blk.size();
+    int64_t ns = off[s + 1] - off[s];
+    int64_t nb = nseg == 1 ? target : (int64_t)llround((double)target * (double)ns / (double)total);
+    nb = std::max<int64_t>(1, std::min<int64_t>(nb, std::max<int64_t>(1, ns)));
+    int64_t per = std::max<int64_t>(1, (ns + nb - 1) / nb);
+    for (int64_t r = 0; r < std::max<int64_t>(ns, 1); r += per) {
+      BlkRange b;
+      b.r0 = off[s] + r;
+      b.r1 = off[s] + std::min(ns, r + per);
+      b.seg = s;
+      b.pad = 0;
+      blk.push_back(b);
+    }
+  }
+  seg_blk[nseg] = (int)blk.size();
+}
+
+// A device block schedule (see build_schedule).
+struct Sched {
+  DevBuf<BlkRange> blk;
+  DevBuf<int> seg_blk;
+  int nblk = 0;
+  void build(sv_context* ctx, const std::vector<int64_t>& off, int target) {
+    std::vector<BlkRange> hb;
+    std::vector<int> hs;
+    build_schedule(off, target, hb, hs);
+    nblk = (int)hb.size();
+    blk.alloc(nblk);
+    seg_blk.alloc(hs.size());
+    sv_h2d(ctx, blk.get(), hb.data(), nblk * sizeof(BlkRange));
+    sv_h2d(ctx, seg_blk.get(), hs.data(), hs.size() * sizeof(int));
+  }
 };
 
 // One side of the bidiagonalisation: two double-float bases (len x work) --
 // the current one and the target of the thick-restart rotation, which swap
 // roles every restart -- the double-float working vector and the FP64 copy of
-// the current basis vector (the input of the next product).
+// the current basis vector (the input of the next product).  Rows may stack
+// several samples (offsets hoff); `red` schedules the reductions, `rows` the
+// row-parallel kernels.
 struct Side {
   int64_t len = 0;
+  int nseg = 1;
+  int64_t max_seg = 0;           // longest sample
+  std::vector<int64_t> hoff;     // nseg + 1 row offsets
+  DevBuf<int64_t> off;
+  Sched red, rows;
   DevBuf<float> h[2], l[2];     // basis sets
   int set = 0;                  // the current set
   DevBuf<float> xh, xl;         // working vector
   DevBuf<double> cur;           // current basis vector, FP64
-  void alloc(int64_t n, int work) {
-    len = n;
+  void alloc(sv_context* ctx, const std::vector<int64_t>& offsets, int work, int red_target,
+             int rows_target) {
+    hoff = offsets;
+    nseg = (int)hoff.size() - 1;
+    len = hoff[nseg];
+    for (int s = 0; s < nseg; ++s) max_seg = std::max(max_seg, hoff[s + 1] - hoff[s]);
+    off.alloc(nseg + 1);
+    sv_h2d(ctx, off.get(), hoff.data(), (nseg + 1) * 8);
+    red.build(ctx, hoff, red_target);
+    rows.build(ctx, hoff, rows_target);
     for (int t = 0; t < 2; ++t) {
-      h[t].alloc(n * work);
-      l[t].alloc(n * work);
+      h[t].alloc(len * work);
+      l[t].alloc(len * work);
     }
-    xh.alloc(n);
-    xl.alloc(n);
-    cur.alloc(n);
+    xh.alloc(len);
+    xl.alloc(len);
+    cur.alloc(len);
   }
   float* bh() { return h[set].get(); }
   float* bl() { return l[set].get(); }
@@ -874,54 +1033,77 @@ struct CycleGraph {
   int64_t launches = 0, matvecs = 0;
 };
 
-// Control-block slots in Lanczos::scal (after the two norm slots).
-#define SCAL_S 0        // W-side norm (alpha of the bidiagonal)
-#define SCAL_R 1        // V-side norm (beta)
-#define SCAL_CTL 2      // control block of the cycles (3 slots)
-#define SCAL_CTL0 5     // control block of the start vector: threshold 1e-300
+// Per-sample outcome of a run.
+struct IrlbaResult {
+  std::vector<int> info;        // 0 converged, 1 not
+  std::vector<int64_t> iters;   // cycles until convergence (or maxit)
+  int64_t nmatvec = 0;          // operator products (each covers every active sample)
+};
 
-// The Lanczos driver.  m = rows of A (the W side), n = columns (the V side).
+// The Lanczos driver.  m = rows of A (the W side), n = columns (the V side);
+// with several samples A is block diagonal (sample s: W rows woff[s]..,
+// V rows voff[s]..) and every sample runs its own bidiagonalisation in the
+// same launches; a sample that converges is finished (U, V written) and
+// frozen while the others continue.
 struct Lanczos {
   sv_context* ctx;
   Op* op;
   int64_t m, n;
-  int nu, work;
+  int nu, work, nseg;
   Side Ws, Vs;
   DevBuf<double> ytmp, F, B, P, Q, sig, summary, scal, part, cvec, Ufin, Vfin;
   DevBuf<unsigned int> counter;
-  DevBuf<int> flag;
-  double* hsum = nullptr;       // pinned copy of the cycle summary
+  DevBuf<int> flag, active, finsel;
+  double* hsum = nullptr;       // pinned copy of the cycle summaries
+  int* hflags = nullptr;        // pinned staging of the active / finish masks
   double eps_b = 0;
   int cgs_blocks = RED_BLOCKS;  // resident blocks of the CGS kernels (one wave)
   // graphs of the first cycle and of restart cycles from basis set 0 / set 1
   CycleGraph graphs[3];
 
-  Lanczos(sv_context* c, Op* o, int64_t m_, int64_t n_, int nu_, int work_)
-      : ctx(c), op(o), m(m_), n(n_), nu(nu_), work(work_) {
-    Ws.alloc(m, work);
-    Vs.alloc(n, work);
-    ytmp.alloc(std::max(m, n));
-    F.alloc(n);
-    B.alloc(work * work);
-    P.alloc(work * work);
-    Q.alloc(work * work);
-    sig.alloc(work);
-    summary.alloc(2 * work + 2);
-    scal.alloc(8);
-    part.alloc((size_t)RED_BLOCKS * (work + 1));
-    cvec.alloc(2 * MAX_WORK);
-    counter.alloc(4);
-    flag.alloc(4);
-    sv_memset(ctx, counter.get(), 0, 16);
-    sv_memset(ctx, flag.get(), 0, 16);
-    sv_memset(ctx, B.get(), 0, work * work * 8);
-    SV_CUDA(cudaMallocHost((void**)&hsum, (2 * work + 2) * 8));
+  Lanczos(sv_context* c, Op* o, const std::vector<int64_t>& woff, const std::vector<int64_t>& voff,
+          int nu_, int work_)
+      : ctx(c), op(o), nu(nu_), work(work_) {
+    nseg = (int)woff.size() - 1;
+    m = woff[nseg];
+    n = voff[nseg];
     int per_sm = 0;
     if (work <= 64)
       SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_df<8, true, true, false>, 256, 0));
     else
       SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_df<12, true, true, false>, 256, 0));
     cgs_blocks = std::max(1, std::min(RED_BLOCKS, per_sm * ctx->num_sms));
+    auto red_target = [&](int64_t len) {
+      return (int)std::max<int64_t>(1, std::min<int64_t>(cgs_blocks, (len + 63) / 64));
+    };
+    auto rows_target = [&](int64_t len) {
+      return (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->num_sms * 8, (len + 255) / 256));
+    };
+    Ws.alloc(ctx, woff, work, red_target(m), rows_target(m));
+    Vs.alloc(ctx, voff, work, red_target(n), rows_target(n));
+    ytmp.alloc(std::max(m, n));
+    F.alloc(n);
+    B.alloc((size_t)nseg * work * work);
+    P.alloc((size_t)nseg * work * work);
+    Q.alloc((size_t)nseg * work * work);
+    sig.alloc((size_t)nseg * work);
+    summary.alloc((size_t)nseg * (2 * work + 2));
+    scal.alloc((size_t)nseg * (2 + 2 * CTL_N));
+    int maxblk = std::max(Ws.red.nblk, Vs.red.nblk);
+    part.alloc((size_t)maxblk * (work + 1));
+    cvec.alloc((size_t)2 * nseg * MAX_WORK);
+    counter.alloc(4);
+    flag.alloc(nseg);
+    active.alloc(nseg);
+    finsel.alloc(nseg);
+    Ufin.alloc(m * nu);
+    Vfin.alloc(n * nu);
+    sv_memset(ctx, counter.get(), 0, 16);
+    sv_memset(ctx, flag.get(), 0, nseg * 4);
+    sv_memset(ctx, B.get(), 0, (size_t)nseg * work * work * 8);
+    SV_CUDA(cudaMallocHost((void**)&hsum, (size_t)nseg * (2 * work + 2) * 8));
+    SV_CUDA(cudaMallocHost((void**)&hflags, (size_t)nseg * 4));
+    op->bind_active(active.get());
     SV_CUDA(cudaFuncSetAttribute(k_jacobi_svd, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  4 * MAX_WORK * MAX_WORK * 4));
     SV_CUDA(cudaFuncSetAttribute(k_rotate_df<10, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -935,65 +1117,80 @@ struct Lanczos {
     for (auto& g : graphs)
       if (g.exec) cudaGraphExecDestroy(g.exec);
     if (hsum) cudaFreeHost(hsum);
+    if (hflags) cudaFreeHost(hflags);
   }
   Lanczos(const Lanczos&) = delete;
   Lanczos& operator=(const Lanczos&) = delete;
 
-  double* ctl() { return scal.get() + SCAL_CTL; }
+  double* sS() { return scal.get(); }                      // W-side norms (alpha), per sample
+  double* sR() { return scal.get() + nseg; }               // V-side norms (beta), per sample
+  double* ctl() { return scal.get() + 2 * nseg; }          // cycle control blocks
+  double* ctl0() { return scal.get() + 2 * nseg + CTL_N * nseg; }   // start-vector control blocks
 
   // working vector <- CGS2(y, basis[:, :ncols]) (y FP64; null: the working
-  // vector already holds it); *nrm = its norm
+  // vector already holds it); nrm[s] = its norm per sample
   template <int NJ>
   void orth_norm_nj(Side& s, const double* y, int ncols, double* nrm) {
-    int g = (int)std::max<int64_t>(1, std::min<int64_t>(cgs_blocks, (s.len + 63) / 64));
+    int g = s.red.nblk;
+    const BlkRange* bk = s.red.blk.get();
+    const int* sb = s.red.seg_blk.get();
+    const int* act = active.get();
     double* c1 = cvec.get();
-    double* c2 = cvec.get() + MAX_WORK;
-    double* np = part.get() + (size_t)RED_BLOCKS * work;
+    double* c2 = cvec.get() + (size_t)nseg * MAX_WORK;
+    double* np = part.get() + (size_t)g * work;
     if (ncols == 0) {
       if (y) to_working(s, y);
       sv_launch(ctx, "irlba_upd_norm", k_cgs_df<NJ, true, false, true>, dim3(g), dim3(256), 0,
                 (const float*)s.bh(), (const float*)s.bl(), s.len, 0, s.xh.get(), s.xl.get(),
-                (const double*)nullptr, s.len, (const double*)c1, part.get(), np, c2, nrm, counter.get());
+                (const double*)nullptr, bk, sb, nseg, act, (const double*)c1, part.get(), np, c2, nrm,
+                counter.get());
       return;
     }
     sv_launch(ctx, "irlba_dots", k_cgs_df<NJ, false, true, false>, dim3(g), dim3(256), 0,
-              (const float*)s.bh(), (const float*)s.bl(), s.len, ncols, s.xh.get(), s.xl.get(), y, s.len,
-              (const double*)nullptr, part.get(), np, c1, (double*)nullptr, counter.get());
+              (const float*)s.bh(), (const float*)s.bl(), s.len, ncols, s.xh.get(), s.xl.get(), y, bk, sb,
+              nseg, act, (const double*)nullptr, part.get(), np, c1, (double*)nullptr, counter.get());
     sv_launch(ctx, "irlba_upd_dots", k_cgs_df<NJ, true, true, false>, dim3(g), dim3(256), 0,
               (const float*)s.bh(), (const float*)s.bl(), s.len, ncols, s.xh.get(), s.xl.get(),
-              (const double*)nullptr, s.len, (const double*)c1, part.get(), np, c2, (double*)nullptr,
-              counter.get());
+              (const double*)nullptr, bk, sb, nseg, act, (const double*)c1, part.get(), np, c2,
+              (double*)nullptr, counter.get());
     sv_launch(ctx, "irlba_upd_norm", k_cgs_df<NJ, true, false, true>, dim3(g), dim3(256), 0,
               (const float*)s.bh(), (const float*)s.bl(), s.len, ncols, s.xh.get(), s.xl.get(),
-              (const double*)nullptr, s.len, (const double*)c2, part.get(), np, c1, nrm, counter.get());
+              (const double*)nullptr, bk, sb, nseg, act, (const double*)c2, part.get(), np, c1, nrm,
+              counter.get());
   }
   void orth_norm(Side& s, const double* y, int ncols, double* nrm) {
     if (work <= 64) orth_norm_nj<8>(s, y, ncols, nrm);
     else orth_norm_nj<12>(s, y, ncols, nrm);
   }
 
-  // basis column j := working vector / *nrm (FP64 copy in cur), breakdown handling
-  void scal_fix(Side& s, int j, double* nrm, const double* c, double* bentry, uint64_t seed,
+  // basis column j := working vector / nrm[s] (FP64 copy in cur), breakdown
+  // handling; the B entry at offset boff of each sample's B (boff < 0: none)
+  void scal_fix(Side& s, int j, double* nrm, const double* c, int64_t boff, uint64_t seed,
                 unsigned step) {
-    sv_launch(ctx, "irlba_scal", k_scal_df, dim3(sv_grid_for(ctx, s.len, 256, 4)), dim3(256), 0,
-              (const float*)s.xh.get(), (const float*)s.xl.get(), s.len, (const double*)nrm, c,
-              s.ch(j), s.cl(j), s.cur.get(), bentry, flag.get(), (unsigned long long)seed, step);
-    sv_launch(ctx, "irlba_scal_post", k_scal_post, dim3(1), dim3(1), 0, nrm, (const int*)flag.get());
-    sv_launch(ctx, "irlba_fix", k_fix_df, dim3(1), dim3(1024), 0, s.cur.get(), s.len,
-              (const float*)s.bh(), (const float*)s.bl(), s.len, j, s.ch(j), s.cl(j), flag.get());
+    sv_launch(ctx, "irlba_scal", k_scal_df, dim3(s.red.nblk), dim3(256), 0, (const float*)s.xh.get(),
+              (const float*)s.xl.get(), (const BlkRange*)s.red.blk.get(), (const int*)s.red.seg_blk.get(),
+              (const int64_t*)s.off.get(), (const int*)active.get(), (const double*)nrm, c, s.ch(j),
+              s.cl(j), s.cur.get(), boff >= 0 ? B.get() : (double*)nullptr, boff,
+              (int64_t)work * work, flag.get(), (unsigned long long)seed, step);
+    sv_launch(ctx, "irlba_scal_post", k_scal_post, dim3(1), dim3(64), 0, nrm, (const int*)flag.get(),
+              nseg);
+    sv_launch(ctx, "irlba_fix", k_fix_df, dim3(nseg), dim3(1024), 0, s.cur.get(),
+              (const int64_t*)s.off.get(), (const float*)s.bh(), (const float*)s.bl(), s.len, j, s.bh() + (int64_t)j * s.len,
+              s.bl() + (int64_t)j * s.len, flag.get());
   }
 
-  // the feature-side step in one launch (see k_vside)
-  void vside(int ncols, int write_col, double* nrm, const double* c, double* bentry, uint64_t seed,
+  // the feature-side step, one block per sample (see k_vside)
+  void vside(int ncols, int write_col, double* nrm, const double* c, int64_t boff, uint64_t seed,
              unsigned step) {
-    if (n > 32768) {   // long feature side: the multi-block kernels
+    if (Vs.max_seg > 32768) {   // long feature side: the multi-block kernels
       orth_norm(Vs, F.get(), ncols, nrm);
-      if (write_col >= 0) scal_fix(Vs, write_col, nrm, c, bentry, seed, step);
+      if (write_col >= 0) scal_fix(Vs, write_col, nrm, c, boff, seed, step);
       return;
     }
-    sv_launch(ctx, "irlba_vside", k_vside, dim3(1), dim3(1024), 0, (const double*)F.get(), n, Vs.bh(),
-              Vs.bl(), ncols, write_col, nrm, c, bentry, Vs.cur.get(), Vs.xh.get(), Vs.xl.get(),
-              (unsigned long long)seed, step);
+    sv_launch(ctx, "irlba_vside", k_vside, dim3(nseg), dim3(1024), 0, (const double*)F.get(),
+              (const int64_t*)Vs.off.get(), Vs.len, Vs.bh(), Vs.bl(), ncols, write_col, nrm, c,
+              boff >= 0 ? B.get() : (double*)nullptr, boff, (int64_t)work * work, Vs.cur.get(),
+              Vs.xh.get(), Vs.xl.get(), (const int*)active.get(), (unsigned long long)seed, step);
   }
 
   void to_working(Side& s, const double* y) {
@@ -1001,34 +1198,38 @@ struct Lanczos {
               s.len, s.xh.get(), s.xl.get());
   }
 
-  // out = basis * M[:, :nout]: into the other basis set (outd null) or FP64 outd
-  void rotate(Side& s, const double* M, int nout, double* outd) {
+  // out = basis * M_s[:, :nout] per sample: into the other basis set (outd null)
+  // or FP64 outd (ld = the side's length); only the samples with sel[s] != 0
+  void rotate(Side& s, const double* M, int nout, double* outd, const int* sel) {
     auto kern = nout % 10 == 0 ? k_rotate_df<10, true> : nout % 8 == 0 ? k_rotate_df<8, true>
                                                                        : k_rotate_df<16, false>;
-    sv_launch(ctx, "irlba_rotate", kern, dim3(sv_grid_for(ctx, s.len, 256, 8)), dim3(256),
-              (size_t)work * nout * 8, (const float*)s.bh(), (const float*)s.bl(), s.len, s.len,
-              work, M, nout, outd ? (float*)nullptr : s.th(), outd ? (float*)nullptr : s.tl(), outd,
-              s.len);
+    sv_launch(ctx, "irlba_rotate", kern, dim3(s.rows.nblk), dim3(256), (size_t)work * nout * 8,
+              (const float*)s.bh(), (const float*)s.bl(), s.len, (const BlkRange*)s.rows.blk.get(), sel,
+              work, M, (int64_t)work * work, nout, outd ? (float*)nullptr : s.th(),
+              outd ? (float*)nullptr : s.tl(), outd, s.len);
   }
 
   // One cycle, enqueued on the context stream without any host round trip:
   // for a restart, V <- V Q_k, W <- W P_k, V[:, k] = f/|f| and B reset; the
-  // Lanczos steps k..work-1; the SVD of B; its summary copied to hsum.
+  // Lanczos steps k..work-1; the SVD of B; the summaries copied to hsum.
+  // Samples that are no longer active are skipped by every kernel.
   // Returns the number of operator products.
   int64_t cycle(bool restart, int k, uint64_t seed) {
-    double* s0 = scal.get() + SCAL_S;
-    double* s1 = scal.get() + SCAL_R;
+    double* s0 = sS();
+    double* s1 = sR();
     const double* c = ctl();
+    const int* act = active.get();
     int64_t nmv = 0;
     if (restart) {
-      rotate(Vs, Q.get(), k, nullptr);
-      rotate(Ws, P.get(), k, nullptr);
+      rotate(Vs, Q.get(), k, nullptr, act);
+      rotate(Ws, P.get(), k, nullptr, act);
       Vs.flip();
       Ws.flip();
       df_residual_to_fp64();
-      sv_launch(ctx, "irlba_restart", k_restart_tail, dim3(sv_grid_for(ctx, n, 256, 4)), dim3(256), 0,
-                Vs.ch(k), Vs.cl(k), Vs.cur.get(), (const double*)F.get(), n,
-                (const double*)summary.get(), work, k, B.get());
+      dim3 grid((unsigned)std::max(1, std::min(sv_grid_for(ctx, Vs.max_seg, 256, 4), 64)), (unsigned)nseg);
+      sv_launch(ctx, "irlba_restart", k_restart_tail, grid, dim3(256), 0, Vs.ch(k), Vs.cl(k),
+                Vs.cur.get(), (const double*)F.get(), (const int64_t*)Vs.off.get(),
+                (const double*)summary.get(), work, k, B.get(), act);
     }
     unsigned step = 1;
     int j = k;
@@ -1040,13 +1241,13 @@ struct Lanczos {
       orth_norm(Ws, ytmp.get(), j, s0);
     }
     nmv++;
-    scal_fix(Ws, j, s0, c, B.get() + (int64_t)j * work + j, seed, step++);
+    scal_fix(Ws, j, s0, c, (int64_t)j * work + j, seed, step++);
     while (true) {
       // F = A^T W[:, j] - S V[:, j]; CGS2 against V[:, :j+1]
       op->T(Ws.cur.get(), F.get(), s0, Vs.cur.get());
       nmv++;
       if (j + 1 < work) {
-        vside(j + 1, j + 1, s1, c, B.get() + (int64_t)j * work + j + 1, seed, step++);
+        vside(j + 1, j + 1, s1, c, (int64_t)j * work + j + 1, seed, step++);
         // W[:, j+1] = A V[:, j+1] - R W[:, j]
         if (op->N_df(Vs.ch(j + 1), Vs.cl(j + 1), Ws.xh.get(), Ws.xl.get(), s1, Ws.ch(j), Ws.cl(j))) {
           orth_norm(Ws, nullptr, j + 1, s0);
@@ -1055,17 +1256,18 @@ struct Lanczos {
           orth_norm(Ws, ytmp.get(), j + 1, s0);
         }
         nmv++;
-        scal_fix(Ws, j + 1, s0, c, B.get() + (int64_t)(j + 1) * work + j + 1, seed, step++);
+        scal_fix(Ws, j + 1, s0, c, (int64_t)(j + 1) * work + j + 1, seed, step++);
         ++j;
       } else {
-        vside(j + 1, -1, s1, c, nullptr, seed, step++);   // residual f and |f|
+        vside(j + 1, -1, s1, c, -1, seed, step++);   // residual f and |f|
         break;
       }
     }
-    sv_launch(ctx, "irlba_svd", k_jacobi_svd, dim3(1), dim3(1024), (size_t)4 * work * work * 4,
+    sv_launch(ctx, "irlba_svd", k_jacobi_svd, dim3(nseg), dim3(1024), (size_t)4 * work * work * 4,
               (const double*)B.get(), work, P.get(), sig.get(), Q.get(), summary.get(),
-              (const double*)s1, 60, ctx->d_status, ctl(), eps_b);
-    SV_CUDA(cudaMemcpyAsync(hsum, summary.get(), (2 * work + 2) * 8, cudaMemcpyDeviceToHost, ctx->stream));
+              (const double*)s1, 60, ctx->d_status, ctl(), eps_b, act);
+    SV_CUDA(cudaMemcpyAsync(hsum, summary.get(), (size_t)nseg * (2 * work + 2) * 8,
+                            cudaMemcpyDeviceToHost, ctx->stream));
     return nmv;
   }
 
@@ -1108,34 +1310,76 @@ struct Lanczos {
     return g.matvecs;
   }
 
+  // U_s = W_s P_s[:, :nu], V_s = V_s Q_s[:, :nu] (FP64) for the samples in hflags
+  void finish_selected() {
+    sv_h2d(ctx, finsel.get(), hflags, (size_t)nseg * 4);
+    rotate(Ws, P.get(), nu, Ufin.get(), finsel.get());
+    rotate(Vs, Q.get(), nu, Vfin.get(), finsel.get());
+  }
+
   IrlbaResult run(const double* init_host, int maxit, double tol, uint64_t seed) {
     IrlbaResult res;
+    res.info.assign(nseg, 1);
+    res.iters.assign(nseg, maxit);
     eps_b = sqrt(2.220446049250313e-16);
     // control blocks: cycles start at threshold eps_b (smax = 0), the start
-    // vector is normalised unless it is zero
-    double ctl_init[6] = {eps_b, 0.0, 0.0, 1e-300, 0.0, 0.0};
-    sv_h2d(ctx, scal.get() + SCAL_CTL, ctl_init, sizeof(ctl_init));
+    // vector is normalised unless it is zero; every sample active
+    {
+      std::vector<double> ci((size_t)2 * CTL_N * nseg);
+      for (int s = 0; s < nseg; ++s) {
+        ci[s * CTL_N + CTL_THRESH] = eps_b;
+        ci[s * CTL_N + CTL_SMAX] = 0.0;
+        ci[s * CTL_N + CTL_CYCLE] = 0.0;
+        ci[CTL_N * nseg + s * CTL_N + CTL_THRESH] = 1e-300;
+        ci[CTL_N * nseg + s * CTL_N + CTL_SMAX] = 0.0;
+        ci[CTL_N * nseg + s * CTL_N + CTL_CYCLE] = 0.0;
+      }
+      sv_h2d(ctx, ctl(), ci.data(), ci.size() * 8);
+      for (int s = 0; s < nseg; ++s) hflags[s] = 1;
+      sv_h2d(ctx, active.get(), hflags, (size_t)nseg * 4);
+    }
     sv_h2d(ctx, F.get(), init_host, n * 8);
-    vside(0, 0, scal.get() + SCAL_R, scal.get() + SCAL_CTL0, nullptr, seed, 0);
+    vside(0, 0, sR(), ctl0(), -1, seed, 0);
     bool graphs_on = op->device_only() && !ctx->profiling && !getenv("SV_NO_GRAPH");
     const int kr = std::min(nu, work - 1);
-    double smax = 0;
-    int it = 0;
-    for (; it < maxit; ++it) {
+    std::vector<double> smax(nseg, 0.0);
+    std::vector<int> act(nseg, 1);
+    int nact = nseg;
+    for (int it = 0; it < maxit && nact > 0; ++it) {
       res.nmatvec += enqueue_cycle(it > 0, it > 0 ? kr : 0, seed, graphs_on);
       sv_sync(ctx);
-      double rf = hsum[2 * work];
-      smax = std::max(smax, hsum[0]);
-      int nconv = 0;
-      for (int i = 0; i < nu; ++i)
-        if (fabs(rf * hsum[work + i]) < tol * smax) ++nconv;
-      res.iters = it + 1;
-      if (nconv >= nu || rf < eps_b * smax) {
-        res.info = 0;
-        break;
+      bool any = false;
+      for (int s = 0; s < nseg; ++s) {
+        hflags[s] = 0;
+        if (!act[s]) continue;
+        const double* hs = hsum + (size_t)s * (2 * work + 2);
+        double rf = hs[2 * work];
+        smax[s] = std::max(smax[s], hs[0]);
+        int nconv = 0;
+        for (int i = 0; i < nu; ++i)
+          if (fabs(rf * hs[work + i]) < tol * smax[s]) ++nconv;
+        if (nconv >= nu || rf < eps_b * smax[s]) {
+          res.info[s] = 0;
+          res.iters[s] = it + 1;
+          act[s] = 0;
+          hflags[s] = 1;
+          --nact;
+          any = true;
+        }
+      }
+      if (any) {
+        // finish the converged samples now: the next restart skips them
+        finish_selected();
+        for (int s = 0; s < nseg; ++s) hflags[s] = act[s];
+        sv_h2d(ctx, active.get(), hflags, (size_t)nseg * 4);
+        sv_sync(ctx);
       }
     }
-    if (it >= maxit) res.iters = maxit;
+    if (nact > 0) {
+      for (int s = 0; s < nseg; ++s) hflags[s] = act[s];
+      finish_selected();
+      sv_sync(ctx);
+    }
     sv_check_device_status(ctx, "irlba");
     return res;
   }
@@ -1145,14 +1389,6 @@ struct Lanczos {
   void df_residual_to_fp64() {
     sv_launch(ctx, "irlba_f_fp64", k_df_to_fp64, dim3(sv_grid_for(ctx, n, 256, 4)), dim3(256), 0,
               (const float*)Vs.xh.get(), (const float*)Vs.xl.get(), n, F.get());
-  }
-
-  // U = W P[:, :nu], V = V Q[:, :nu] (FP64)
-  void finish() {
-    Ufin.alloc(m * nu);
-    Vfin.alloc(n * nu);
-    rotate(Ws, P.get(), nu, Ufin.get());
-    rotate(Vs, Q.get(), nu, Vfin.get());
   }
 };
 
@@ -1166,33 +1402,51 @@ int default_work(int64_t m, int64_t n, int64_t nu) {
 
 }  // namespace
 
-static int irlba_core(sv_context* ctx, Op* op, int64_t m, int64_t n, int64_t nu, int64_t work,
-                      int64_t maxit, double tol, const double* init, uint64_t seed, double* s_out,
-                      double* U, double* V, int64_t* iters, int64_t* nmatvec, sv_embed* emb) {
-  SV_REQUIRE(nu >= 1 && nu <= std::min(m, n), "nu must be in 1..min(m, n)");
-  if (work <= 0) work = default_work(m, n, nu);
-  SV_REQUIRE(work > nu || work == std::min(m, n), "work must exceed nu (or equal min(m, n))");
-  SV_REQUIRE(work <= std::min(m, n), "work exceeds min(m, n)");
+// irlba over nseg stacked samples (one sample: woff = {0, m}, voff = {0, n}).
+// s_out: nseg x nu, U: m x nu, V: n x nu (column-major, stacked rows); emb
+// (optional) receives Z = U diag(s) and s.  Returns the number of samples that
+// did not converge; iters (nseg) and nmatvec as in the reference.
+static int irlba_core(sv_context* ctx, Op* op, const std::vector<int64_t>& woff,
+                      const std::vector<int64_t>& voff, int64_t nu, int64_t work, int64_t maxit,
+                      double tol, const double* init, uint64_t seed, double* s_out, double* U,
+                      double* V, int64_t* iters, int64_t* nmatvec, sv_embed* emb) {
+  int nseg = (int)woff.size() - 1;
+  int64_t m = woff[nseg], n = voff[nseg];
+  int64_t mmin = m, nmin = n;
+  for (int s = 0; s < nseg; ++s) {
+    mmin = std::min(mmin, woff[s + 1] - woff[s]);
+    nmin = std::min(nmin, voff[s + 1] - voff[s]);
+  }
+  SV_REQUIRE(nu >= 1 && nu <= std::min(mmin, nmin), "nu must be in 1..min(m, n)");
+  if (work <= 0) work = default_work(mmin, nmin, nu);
+  SV_REQUIRE(work > nu || work == std::min(mmin, nmin), "work must exceed nu (or equal min(m, n))");
+  SV_REQUIRE(work <= std::min(mmin, nmin), "work exceeds min(m, n)");
   if (work > MAX_WORK) sv_throw(SV_ERR_UNSUPPORTED, "work %lld exceeds %d", (long long)work, MAX_WORK);
   SV_REQUIRE(maxit >= 1, "maxit must be >= 1");
   SV_REQUIRE(init != nullptr, "init (length n) is required");
-  Lanczos L(ctx, op, m, n, (int)nu, (int)work);
+  Lanczos L(ctx, op, woff, voff, (int)nu, (int)work);
   IrlbaResult r = L.run(init, (int)maxit, tol, seed);
-  L.finish();
-  if (s_out) sv_d2h(ctx, s_out, L.sig.get(), nu * 8);
+  if (s_out)
+    SV_CUDA(cudaMemcpy2DAsync(s_out, nu * 8, L.sig.get(), work * 8, nu * 8, nseg, cudaMemcpyDeviceToHost,
+                              ctx->stream));
   if (U) sv_d2h(ctx, U, L.Ufin.get(), m * nu * 8);
   if (V) sv_d2h(ctx, V, L.Vfin.get(), n * nu * 8);
   if (emb) {
-    emb->s.alloc(nu);
-    SV_CUDA(cudaMemcpyAsync(emb->s.get(), L.sig.get(), nu * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    emb->s.alloc((size_t)nseg * nu);
+    SV_CUDA(cudaMemcpy2DAsync(emb->s.get(), nu * 8, L.sig.get(), work * 8, nu * 8, nseg,
+                              cudaMemcpyDeviceToDevice, ctx->stream));
     emb->Z = std::move(L.Ufin);
-    sv_launch(ctx, "pca_scale", k_scale_cols, dim3(sv_grid_for(ctx, m * nu, 256, 8)), dim3(256), 0,
-              emb->Z.get(), m, (int)nu, (const double*)emb->s.get());
-    sv_sync(ctx);
+    dim3 grid((unsigned)sv_grid_for(ctx, (m / nseg + 1) * nu, 256, 8), (unsigned)nseg);
+    sv_launch(ctx, "pca_scale", k_scale_cols, grid, dim3(256), 0, emb->Z.get(), m,
+              (const int64_t*)L.Ws.off.get(), (int)nu, (const double*)emb->s.get(), (int)nu);
   }
-  if (iters) *iters = r.iters;
+  sv_sync(ctx);
+  if (iters)
+    for (int s = 0; s < nseg; ++s) iters[s] = r.iters[s];
   if (nmatvec) *nmatvec = r.nmatvec;
-  return r.info;
+  int bad = 0;
+  for (int s = 0; s < nseg; ++s) bad += r.info[s] != 0;
+  return bad;
 }
 
 SV_API int sv_irlba(sv_context* ctx, const sv_centered* s, int64_t nu, int64_t work, int64_t maxit,
@@ -1202,8 +1456,8 @@ SV_API int sv_irlba(sv_context* ctx, const sv_centered* s, int64_t nu, int64_t w
   sv_ctx_check(ctx);
   SV_REQUIRE(s && s->ctx == ctx, "bad centered handle");
   CenteredOp op(ctx, s);
-  int info = irlba_core(ctx, &op, s->n_cells, s->nf, nu, work, maxit, tol, init, seed, s_out, U, V,
-                        iters, nmatvec, nullptr);
+  int info = irlba_core(ctx, &op, {0, s->n_cells}, {0, s->nf}, nu, work, maxit, tol, init, seed, s_out,
+                        U, V, iters, nmatvec, nullptr);
   if (info != 0) {
     sv_set_error("convergence failed");   // src/irlba.jl:73
     return SV_ERR_NOCONV;
@@ -1230,8 +1484,8 @@ SV_API int sv_pca(sv_context* ctx, const sv_centered* s, int64_t npcs, int64_t m
     e->npcs = k;
     e->nf = s->nf;
     std::vector<double> sv(k);
-    int info = irlba_core(ctx, &op, s->n_cells, s->nf, k, 0, maxit, tol, init, seed, sv.data(),
-                          nullptr, loadings, iters, nmatvec, e);
+    int info = irlba_core(ctx, &op, {0, s->n_cells}, {0, s->nf}, k, 0, maxit, tol, init, seed,
+                          sv.data(), nullptr, loadings, iters, nmatvec, e);
     if (info != 0) {
       delete e;
       sv_set_error("convergence failed");
@@ -1241,6 +1495,59 @@ SV_API int sv_pca(sv_context* ctx, const sv_centered* s, int64_t npcs, int64_t m
     if (stdev)
       for (int64_t i = 0; i < k; ++i)
         stdev[i] = sv[i] / sqrt((double)std::max<int64_t>(1, s->n_cells - 1));   // embedding.jl:68
+  } catch (...) {
+    delete e;
+    throw;
+  }
+  if (out) *out = e;
+  else delete e;
+  SV_CATCH
+}
+
+// embedding(X, npcs; method=:pca, algorithm=:irlba) for every sample of a batch
+// (src/embedding.jl:46-76 per sample), all samples in the same launches.
+// Z: n_cells x npcs column-major (the samples' rows stacked), stdev: nseg x
+// npcs (sample-major), iters: nseg cycles until convergence.  init is the start
+// vector (nf) used for every sample.
+SV_API int sv_batch_pca(sv_context* ctx, const sv_batch* b, int64_t npcs, int64_t maxit, double tol,
+                        const double* init, uint64_t seed, sv_embed** out, double* Z, double* stdev,
+                        int64_t* iters, int64_t* nmatvec) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(b && b->ctx == ctx, "bad batch handle");
+  SV_REQUIRE(npcs >= 1, "npcs must be >= 1");
+  SV_REQUIRE(init != nullptr, "init (length nf) is required");
+  int64_t minc = b->n_cells;
+  for (int64_t s = 0; s < b->nseg; ++s) minc = std::min(minc, b->hoff[s + 1] - b->hoff[s]);
+  int64_t k = std::min(std::min(minc, b->nf), npcs);
+  if (k > 0.5 * std::min(minc, b->nf))
+    sv_throw(SV_ERR_UNSUPPORTED,
+             "npcs > 0.5 min(m, n) for a sample: the reference switches to a dense svd (embedding.jl:50-53)");
+  std::vector<int64_t> voff(b->nseg + 1);
+  for (int64_t s = 0; s <= b->nseg; ++s) voff[s] = s * b->nf;
+  std::vector<double> init_all((size_t)b->nseg * b->nf);
+  for (int64_t s = 0; s < b->nseg; ++s) std::copy(init, init + b->nf, init_all.begin() + s * b->nf);
+  BatchOp op(ctx, b);
+  auto* e = new sv_embed();
+  try {
+    e->ctx = ctx;
+    e->n_cells = b->n_cells;
+    e->npcs = k;
+    e->nf = b->nf;
+    std::vector<double> sv((size_t)b->nseg * k);
+    int bad = irlba_core(ctx, &op, b->hoff, voff, k, 0, maxit, tol, init_all.data(), seed, sv.data(),
+                         nullptr, nullptr, iters, nmatvec, e);
+    if (Z) sv_d2h(ctx, Z, e->Z.get(), b->n_cells * k * 8);
+    if (stdev)
+      for (int64_t s = 0; s < b->nseg; ++s) {
+        double m1 = (double)std::max<int64_t>(1, b->hoff[s + 1] - b->hoff[s] - 1);
+        for (int64_t i = 0; i < k; ++i) stdev[s * k + i] = sv[s * k + i] / sqrt(m1);   // embedding.jl:68
+      }
+    if (bad) {
+      delete e;
+      sv_set_error("convergence failed for %d of %lld samples", bad, (long long)b->nseg);
+      return SV_ERR_NOCONV;
+    }
   } catch (...) {
     delete e;
     throw;
@@ -1292,7 +1599,7 @@ SV_API int irlba(int64_t m, int64_t n, int64_t nu, int64_t work, int64_t maxit, 
   sv_context* ctx = sv_default_context();
   sv_ctx_check(ctx);
   CallbackOp op(ctx, m, n, matmul, data);
-  int info = irlba_core(ctx, &op, m, n, nu, work, maxit, tol, init, 0x5EEDull, s, U, V, nullptr,
+  int info = irlba_core(ctx, &op, {0, m}, {0, n}, nu, work, maxit, tol, init, 0x5EEDull, s, U, V, nullptr,
                         nullptr, nullptr);
   return info == 0 ? 0 : 1;
   SV_CATCH

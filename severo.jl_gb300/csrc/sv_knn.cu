@@ -17,7 +17,8 @@
 #include <float.h>
 
 int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq, int64_t n, int dp, int d,
-                         int K2, int include_self, int32_t* cand);
+                         int K2, int include_self, int32_t* cand,
+                         const std::vector<int64_t>* segs);
 sv_context* sv_default_context();
 
 namespace {
@@ -229,6 +230,13 @@ void launch_rerank(sv_context* ctx, const float* X, int64_t n, const int32_t* ca
             (size_t)8 * K2 * 8, X, n, cand, K2, k, inc, cosine, idx, dist);
 }
 
+// candidate indices of one sample (local, >= 0) -> stacked rows
+__global__ void k_add_offset(int32_t* __restrict__ c, int64_t count, int32_t off) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x)
+    if (c[e] >= 0) c[e] += off;
+}
+
 __global__ void k_to_host_layout(const int32_t* __restrict__ idx, const float* __restrict__ dist,
                                  int64_t n, int k, int32_t* __restrict__ oidx, float* __restrict__ of,
                                  double* __restrict__ od) {
@@ -245,29 +253,45 @@ __global__ void k_to_host_layout(const int32_t* __restrict__ idx, const float* _
 }  // namespace
 
 // Core: X32 row-major [n][dp] FP32 with norms -> knn handle (row-major, 0-based).
+// segs (optional, nseg + 1 row offsets): stacked samples, each point's
+// neighbours searched among the points of its own sample only.
 static void knn_core(sv_context* ctx, const float* X32, const float* sq, int64_t n, int dp, int d, int k,
-                     int include_self, int cosine, int precision, sv_knn* out) {
+                     int include_self, int cosine, int precision, sv_knn* out,
+                     const std::vector<int64_t>* segs = nullptr) {
   // candidates per query: at least 2k; the tensor-core stage always keeps 64
   int K2 = (2 * k <= 32 && precision != SV_KNN_BF16) ? 32 : 64;
   if (2 * k > 64) sv_throw(SV_ERR_UNSUPPORTED, "k = %d exceeds the supported maximum of 32", k);
   DevBuf<int32_t> cand((size_t)n * K2);
   bool done = false;
   if (precision == SV_KNN_BF16) {
-    int st = sv_knn_tc_candidates(ctx, X32, sq, n, dp, d, K2, include_self, cand.get());
+    int st = sv_knn_tc_candidates(ctx, X32, sq, n, dp, d, K2, include_self, cand.get(), segs);
     if (st != SV_OK) sv_throw(st, "tensor-core kNN failed");
     done = true;
   }
   if (!done) {
-    switch (dp) {
-      case 8: launch_fp32<8>(ctx, X32, sq, n, K2, include_self, cand.get()); break;
-      case 16: launch_fp32<16>(ctx, X32, sq, n, K2, include_self, cand.get()); break;
-      case 24: launch_fp32<24>(ctx, X32, sq, n, K2, include_self, cand.get()); break;
-      case 32: launch_fp32<32>(ctx, X32, sq, n, K2, include_self, cand.get()); break;
-      case 40: launch_fp32<40>(ctx, X32, sq, n, K2, include_self, cand.get()); break;
-      case 48: launch_fp32<48>(ctx, X32, sq, n, K2, include_self, cand.get()); break;
-      case 56: launch_fp32<56>(ctx, X32, sq, n, K2, include_self, cand.get()); break;
-      case 64: launch_fp32<64>(ctx, X32, sq, n, K2, include_self, cand.get()); break;
-      default: sv_throw(SV_ERR_UNSUPPORTED, "padded dimension %d", dp);
+    // FP32 tiles: one launch per sample (each on its own rows)
+    std::vector<int64_t> one = {0, n};
+    const std::vector<int64_t>& sg = segs ? *segs : one;
+    for (size_t g = 0; g + 1 < sg.size(); ++g) {
+      int64_t o = sg[g], ns = sg[g + 1] - sg[g];
+      if (ns <= 0) continue;
+      const float* Xs = X32 + o * dp;
+      const float* qs = sq + o;
+      int32_t* cs = cand.get() + o * K2;
+      switch (dp) {
+        case 8: launch_fp32<8>(ctx, Xs, qs, ns, K2, include_self, cs); break;
+        case 16: launch_fp32<16>(ctx, Xs, qs, ns, K2, include_self, cs); break;
+        case 24: launch_fp32<24>(ctx, Xs, qs, ns, K2, include_self, cs); break;
+        case 32: launch_fp32<32>(ctx, Xs, qs, ns, K2, include_self, cs); break;
+        case 40: launch_fp32<40>(ctx, Xs, qs, ns, K2, include_self, cs); break;
+        case 48: launch_fp32<48>(ctx, Xs, qs, ns, K2, include_self, cs); break;
+        case 56: launch_fp32<56>(ctx, Xs, qs, ns, K2, include_self, cs); break;
+        case 64: launch_fp32<64>(ctx, Xs, qs, ns, K2, include_self, cs); break;
+        default: sv_throw(SV_ERR_UNSUPPORTED, "padded dimension %d", dp);
+      }
+      if (o > 0)
+        sv_launch(ctx, "knn_offset", k_add_offset, dim3(sv_grid_for(ctx, ns * K2, 256, 4)), dim3(256), 0,
+                  cs, ns * K2, (int32_t)o);
     }
   }
   out->n = n;
@@ -358,6 +382,42 @@ SV_API int sv_knn_embed(sv_context* ctx, const sv_embed* e, int64_t ndims, int64
   try {
     h->ctx = ctx;
     knn_core(ctx, X32.get(), sq.get(), n, dp, (int)ndims, (int)k, include_self, metric == SV_COSINE, precision, h);
+    knn_outputs(ctx, h, SV_F64, nn_index, distances);
+  } catch (...) {
+    delete h;
+    throw;
+  }
+  if (out) *out = h;
+  else delete h;
+  SV_CATCH
+}
+
+// ann over the PCA coordinates of a batch: every cell's neighbours among the
+// cells of its own sample, all samples in the same launches (the tensor-core
+// candidate kernel takes one sample per CTA).  Indices are stacked rows
+// (1-based), as sv_knn_embed returns them.
+SV_API int sv_batch_knn(sv_context* ctx, const sv_batch* b, const sv_embed* e, int64_t ndims, int64_t k,
+                        int metric, int include_self, int precision, int32_t* nn_index, double* distances,
+                        sv_knn** out) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(b && b->ctx == ctx, "bad batch handle");
+  SV_REQUIRE(e && e->ctx == ctx && e->n_cells == b->n_cells, "bad embedding handle");
+  if (ndims <= 0) ndims = e->npcs;
+  SV_REQUIRE(ndims <= e->npcs, "ndims exceeds the embedding's components");
+  int64_t n = e->n_cells;
+  int64_t minc = n;
+  for (int64_t s = 0; s < b->nseg; ++s) minc = std::min(minc, b->hoff[s + 1] - b->hoff[s]);
+  knn_validate(minc, ndims, k, metric, include_self, precision);
+  int dp = (int)((ndims + 7) / 8 * 8);
+  DevBuf<float> X32((size_t)n * dp), sq(n);
+  sv_launch(ctx, "knn_pack", k_pack_rows<double>, dim3(sv_grid_for(ctx, n, 256, 8)), dim3(256), 0,
+            (const double*)e->Z.get(), n, n, (int)ndims, dp, metric == SV_COSINE, X32.get(), sq.get());
+  auto* h = new sv_knn();
+  try {
+    h->ctx = ctx;
+    knn_core(ctx, X32.get(), sq.get(), n, dp, (int)ndims, (int)k, include_self, metric == SV_COSINE, precision, h,
+             &b->hoff);
     knn_outputs(ctx, h, SV_F64, nn_index, distances);
   } catch (...) {
     delete h;

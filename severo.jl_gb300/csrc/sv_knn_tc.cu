@@ -33,7 +33,9 @@ constexpr long long TIMEOUT = 4000000000ll;   // cycles (~2 s) per wait
 struct __align__(1024) Smem {
   __nv_bfloat16 A[BM * BK];              // 16 KB
   __nv_bfloat16 B[STAGES][BN * BK];      // 4 x 32 KB
-  float keys[EPI_WARPS * 32][65];        // per-epilogue-thread key slot, two chunks (padded: no bank conflicts)
+  // per-epilogue-thread key slot for two chunks, written with 16-byte stores
+  // (row stride 68 words: eight threads per wavefront on distinct banks)
+  float keys[EPI_WARPS * 32][68];
   unsigned long long full[STAGES];
   unsigned long long empty[STAGES];
   unsigned long long tfull[2];
@@ -43,6 +45,8 @@ struct __align__(1024) Smem {
   uint32_t tmem_base;
   int err;
 };
+
+static_assert(sizeof(Smem) + 1024 <= 232448, "the CTA's shared memory (with the alignment slack) fits");
 
 __device__ __forceinline__ uint32_t su32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -173,7 +177,7 @@ __device__ __forceinline__ uint32_t chunk_mask(float (&acc)[32], const float* __
       }
     }
   } else {
-    const float4* np = (const float4*)pn;   // squared norms of the chunk's points
+    const float4* np = (const float4*)pn;   // squared norms of the chunk's points (padded)
 #pragma unroll
     for (int i4 = 0; i4 < 8; ++i4) {
       float4 v = __ldg(np + i4);
@@ -185,6 +189,8 @@ __device__ __forceinline__ uint32_t chunk_mask(float (&acc)[32], const float* __
         m |= (acc[i] < thr ? 1u : 0u) << i;
       }
     }
+    // columns past the point range (another sample's points) are no candidates
+    if (col0 + 32 > n) m &= col0 >= n ? 0u : (0xffffffffu >> (32 - (int)(n - col0)));
   }
   return m;
 }
@@ -196,11 +202,20 @@ template <bool FOLD>
 __global__ void __launch_bounds__(THREADS, 1)
     k_knn_tc(const __grid_constant__ CUtensorMap tmapA, const __grid_constant__ CUtensorMap tmapB,
              const float* __restrict__ sqpad, int64_t n, int ntiles, int32_t* __restrict__ cand,
-             int* __restrict__ status) {
+             int* __restrict__ status, const int64_t* __restrict__ sched) {
   extern __shared__ unsigned char smem_raw[];
   Smem* s = (Smem*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int64_t q0 = (int64_t)blockIdx.x * BM;
+  // queries q0 .. min(q0 + BM, qend) against the points [p0, pend): the whole
+  // set, or one sample of stacked samples (sched: 4 values per CTA)
+  int64_t q0 = (int64_t)blockIdx.x * BM, qend = n, p0 = 0, pend = n;
+  if (sched) {
+    q0 = sched[4 * blockIdx.x];
+    qend = sched[4 * blockIdx.x + 1];
+    p0 = sched[4 * blockIdx.x + 2];
+    pend = sched[4 * blockIdx.x + 3];
+    ntiles = (int)((pend - p0 + BN - 1) / BN);
+  }
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < STAGES; ++i) {
@@ -239,7 +254,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         uint32_t ph = (t / STAGES) & 1;
         if (!mbar_wait(&s->empty[st], ph ^ 1, &s->err)) break;
         mbar_expect_tx(&s->full[st], BN * BK * 2);
-        tma_load_2d(s->B[st], &tmapB, 0, t * BN, &s->full[st]);
+        tma_load_2d(s->B[st], &tmapB, 0, (int)(p0 + (int64_t)t * BN), &s->full[st]);
         issued = t + 1;
       }
       // drain: every issued copy has landed before the CTA may exit
@@ -305,7 +320,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       bool ok = mbar_wait(&s->tfull[ab], aph, &s->err);
       if (!__all_sync(0xffffffffu, ok)) break;   // warp-uniform: the TMEM loads are .aligned
       fence_after();
-      int j0 = t * BN + half * (BN / 2);
+      int64_t j0 = p0 + (int64_t)t * BN + half * (BN / 2);
       uint32_t tbase = tmem + lane_off + (uint32_t)(ab * BN + half * (BN / 2));
       // two chunks per TMEM round trip: both loads are issued before one wait
 #pragma unroll 1
@@ -329,16 +344,23 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         float thr = best[KH - 1];
         int64_t cbase = j0 + c * 32;
-        uint32_t m0 = chunk_mask<FOLD>(a0, sqpad + cbase, cbase, n, thr);
-        uint32_t m1 = chunk_mask<FOLD>(a1, sqpad + cbase + 32, cbase + 32, n, thr);
+        uint32_t m0 = chunk_mask<FOLD>(a0, sqpad + cbase, cbase, pend, thr);
+        uint32_t m1 = chunk_mask<FOLD>(a1, sqpad + cbase + 32, cbase + 32, pend, thr);
         if (m0 | m1) {
           // rare: park the keys in this thread's shared slot and insert one by one
           // (one copy of the insertion code keeps the loop small in the I-cache)
           float* slot = s->keys[threadIdx.x - 64];
+          // (parking is not rare per warp: with 32 queries a warp, about half of
+          // the chunk pairs have a candidate for some query)
+          if (m0) {
 #pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            slot[i] = a0[i];
-            slot[32 + i] = a1[i];
+            for (int i = 0; i < 32; i += 4)
+              *(float4*)(slot + i) = make_float4(a0[i], a0[i + 1], a0[i + 2], a0[i + 3]);
+          }
+          if (m1) {
+#pragma unroll
+            for (int i = 0; i < 32; i += 4)
+              *(float4*)(slot + 32 + i) = make_float4(a1[i], a1[i + 1], a1[i + 2], a1[i + 3]);
           }
           unsigned long long m = (unsigned long long)m0 | ((unsigned long long)m1 << 32);
           while (m) {
@@ -362,10 +384,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
       }
     }
-    if (q < n) {
+    if (q < qend) {
       int32_t* o = cand + q * (2 * KH) + half * KH;
 #pragma unroll
-      for (int i = 0; i < KH; ++i) o[i] = (bidx[i] >= 0 && bidx[i] < n) ? bidx[i] : -1;
+      for (int i = 0; i < KH; ++i) o[i] = (bidx[i] >= p0 && bidx[i] < pend) ? bidx[i] : -1;
     }
   }
   fence_before();
@@ -452,7 +474,7 @@ EncodeTiledFn encode_fn() {
 }  // namespace
 
 int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unused, int64_t n, int dp,
-                         int d, int K2, int include_self, int32_t* cand) {
+                         int d, int K2, int include_self, int32_t* cand, const std::vector<int64_t>* segs) {
   (void)sq_unused;
   (void)include_self;   // the re-rank places or removes the point itself
   try {
@@ -460,7 +482,8 @@ int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unus
     if (K2 != 2 * KH) sv_throw(SV_ERR_UNSUPPORTED, "tensor-core kNN keeps %d candidates", 2 * KH);
     if (n >= (1ll << 31) - BN) sv_throw(SV_ERR_UNSUPPORTED, "too many points");
     int ntiles = (int)((n + BN - 1) / BN);
-    int64_t npad = (int64_t)ntiles * BN;
+    // one spare tile of padding: a sample's last tile may start anywhere
+    int64_t npad = (int64_t)(ntiles + 1) * BN;
     bool fold = d + 3 <= BK && !getenv("SV_KNN_NOFOLD");
     DevBuf<__nv_bfloat16> Xq((size_t)n * BK), Xp;
     DevBuf<float> sq(npad);
@@ -490,14 +513,30 @@ int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unus
     if (r != CUDA_SUCCESS) sv_throw(SV_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     size_t smem = sizeof(Smem) + 1024;
     int nblocks = (int)((n + BM - 1) / BM);
+    // stacked samples: every CTA takes 128 queries of one sample against that
+    // sample's points
+    DevBuf<int64_t> sched;
+    if (segs) {
+      std::vector<int64_t> hs;
+      for (size_t g = 0; g + 1 < segs->size(); ++g)
+        for (int64_t q = (*segs)[g]; q < (*segs)[g + 1]; q += BM) {
+          hs.push_back(q);
+          hs.push_back((*segs)[g + 1]);
+          hs.push_back((*segs)[g]);
+          hs.push_back((*segs)[g + 1]);
+        }
+      nblocks = (int)(hs.size() / 4);
+      sched.alloc(hs.size());
+      sv_h2d(ctx, sched.get(), hs.data(), hs.size() * 8);
+    }
     if (fold) {
       SV_CUDA(cudaFuncSetAttribute(k_knn_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       sv_launch(ctx, "knn_tc_tiles", k_knn_tc<true>, dim3(nblocks), dim3(THREADS), smem, tmapA, tmapB,
-                (const float*)sq.get(), n, ntiles, cand, ctx->d_status);
+                (const float*)sq.get(), n, ntiles, cand, ctx->d_status, (const int64_t*)sched.get());
     } else {
       SV_CUDA(cudaFuncSetAttribute(k_knn_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       sv_launch(ctx, "knn_tc_tiles", k_knn_tc<false>, dim3(nblocks), dim3(THREADS), smem, tmapA, tmapB,
-                (const float*)sq.get(), n, ntiles, cand, ctx->d_status);
+                (const float*)sq.get(), n, ntiles, cand, ctx->d_status, (const int64_t*)sched.get());
     }
     sv_check_device_status(ctx, "tensor-core kNN");
   } catch (const SvError& e) {

@@ -28,16 +28,40 @@ constexpr int64_t CHUNK = 4096;   // non-zeros per warp task in the X^T u produc
 // zeros (scaling.jl:18-34): per-thread Welford over the stored values, merged
 // across the block with the pairwise (Chan) update, then merged with the group
 // of n - nnz zeros, which is the state Welford starts from in the reference.
+// With stacked samples (soff: nseg + 1 cell offsets) every (sample, feature)
+// pair is a column of its own (the sample's rows of the feature, found by
+// binary search in the sorted CSC rows); outputs at index s * nf + f.
+__device__ __forceinline__ int64_t lower_bound_rows(const int32_t* __restrict__ r, int64_t lo,
+                                                    int64_t hi, int64_t key) {
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if ((int64_t)r[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
 template <typename ValT>
 __global__ void k_moments(const ValT* __restrict__ val, const int64_t* __restrict__ fstart,
                           const int64_t* __restrict__ fend, int64_t nf, int64_t n_cells,
                           double scale_max, double* __restrict__ mean_o, double* __restrict__ std_o,
                           double* __restrict__ mu_o, float* __restrict__ inv_f,
                           float* __restrict__ clip_f, double* __restrict__ inv_d,
-                          double* __restrict__ clip_d) {
+                          double* __restrict__ clip_d, const int32_t* __restrict__ rowidx,
+                          const int64_t* __restrict__ soff, int nseg) {
   __shared__ double sh_n[32], sh_m[32], sh_s[32];
-  for (int64_t f = blockIdx.x; f < nf; f += gridDim.x) {
+  for (int64_t task = blockIdx.x; task < nf * nseg; task += gridDim.x) {
+    int64_t f = task % nf;
+    int sg = (int)(task / nf);
     int64_t s = fstart[f], e = fend[f];
+    int64_t ncell = n_cells;
+    if (soff) {
+      int64_t lo = lower_bound_rows(rowidx, s, e, soff[sg]);
+      e = lower_bound_rows(rowidx, lo, e, soff[sg + 1]);
+      s = lo;
+      ncell = soff[sg + 1] - soff[sg];
+    }
+    const int64_t o = (int64_t)sg * nf + f;
     double n = 0, m = 0, M2 = 0;
     for (int64_t i = s + threadIdx.x; i < e; i += blockDim.x) {
       double v = (double)sv_load_val(val, i);
@@ -80,21 +104,21 @@ __global__ void k_moments(const ValT* __restrict__ val, const int64_t* __restric
         N = nt;
       }
       // merge the implicit zeros (count n_cells - nnz, mean 0, M2 0)
-      double nz = (double)(n_cells - (e - s));
+      double nz = (double)(ncell - (e - s));
       double nt = N + nz;
       double d = -Mn;
       double meanv = Mn + d * (nz / nt);
       double M2t = S + d * d * (N * nz / nt);
-      double var = M2t / (double)(n_cells - 1);
+      double var = M2t / (double)(ncell - 1);
       double sd = sqrt(var);
       double mu = meanv / sd;                       // scaling.jl:207
-      mean_o[f] = meanv;
-      std_o[f] = sd;
-      mu_o[f] = mu;
-      inv_d[f] = 1.0 / sd;                          // a * (1/std): within 1 ulp of a/std
-      clip_d[f] = scale_max + mu;                   // scaling.jl:209
-      inv_f[f] = (float)(1.0 / sd);
-      clip_f[f] = (float)(scale_max + mu);
+      mean_o[o] = meanv;
+      std_o[o] = sd;
+      mu_o[o] = mu;
+      inv_d[o] = 1.0 / sd;                          // a * (1/std): within 1 ulp of a/std
+      clip_d[o] = scale_max + mu;                   // scaling.jl:209
+      inv_f[o] = (float)(1.0 / sd);
+      clip_f[o] = (float)(scale_max + mu);
     }
     __syncthreads();
   }
@@ -150,6 +174,138 @@ __global__ void k_hsub_write(const int64_t* __restrict__ rowptr, const int32_t* 
       }
       pos += __popc(m);
     }
+  }
+}
+
+// ---- bank-aware order of each CSR_h row -----------------------------------------
+// The X v kernel reads a row in groups of 128 entries, lane l taking entries
+// 4l .. 4l+3 of the group (from the row start rounded down to 4); for each t
+// the 32 lanes then gather the 8-byte table entries of 32 features from shared
+// memory, which serialise on bank conflicts (about six wavefronts per gather
+// with sorted features).  An 8-byte entry of feature f sits in bank pair
+// f mod 16, so the row is permuted such that slot p (relative to the rounded
+// start) holds a feature of class c(p) = ((p >> 2) + 4 (p & 3)) mod 16 where
+// possible: the 32 slots a gather reads then hold each class twice (two
+// wavefronts).  Entries of class c fill the c-slots in order of appearance; the
+// surplus of over-full classes fills the slots left empty, in slot order.  The
+// row's sum is then taken in another order (a different, equally valid
+// rounding).  Rows longer than BO_MAX keep their order.
+constexpr int BO_MAX = 3072;
+constexpr int BO_WARPS = 4;
+
+__device__ __forceinline__ int bo_class(int64_t p) { return (int)(((p >> 2) + 4 * (p & 3)) & 15); }
+// slots p < X whose class is c: 4 per 64 slots, at offsets 4((c - 4t) & 15) + t
+__device__ __forceinline__ int64_t bo_count(int c, int64_t X) {
+  int64_t n = 4 * (X >> 6);
+  int r = (int)(X & 63);
+#pragma unroll
+  for (int t = 0; t < 4; ++t) n += (4 * ((c - 4 * t) & 15) + t) < r;
+  return n;
+}
+// the idx-th slot (from 0) of class c
+__device__ __forceinline__ int64_t bo_slot(int c, int64_t idx) {
+  int o[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) o[t] = 4 * ((c - 4 * t) & 15) + t;
+  // sort the four offsets
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 3 - i; ++j)
+      if (o[j] > o[j + 1]) {
+        int tmp = o[j];
+        o[j] = o[j + 1];
+        o[j + 1] = tmp;
+      }
+  int k = (int)(idx & 3);
+  int ok = k == 0 ? o[0] : k == 1 ? o[1] : k == 2 ? o[2] : o[3];
+  return 64 * (idx >> 2) + ok;
+}
+
+template <typename VT>
+__global__ void __launch_bounds__(BO_WARPS * 32) k_hsub_bankorder(const int64_t* __restrict__ rowptr,
+                                                                  int64_t n_rows, uint16_t* __restrict__ hcol,
+                                                                  VT* __restrict__ hval) {
+  extern __shared__ __align__(16) unsigned char bo_raw[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t per = (size_t)BO_MAX * (2 + 2 + 2 + sizeof(VT));
+  unsigned char* base = bo_raw + w * per;
+  uint16_t* scol = (uint16_t*)base;
+  uint16_t* srank = scol + BO_MAX;
+  uint16_t* sempty = srank + BO_MAX;
+  VT* sval = (VT*)(sempty + BO_MAX);
+  __shared__ int cnt[BO_WARPS][16];
+  const unsigned lt = (1u << lane) - 1u;
+  for (int64_t r = (int64_t)blockIdx.x * BO_WARPS + w; r < n_rows; r += (int64_t)gridDim.x * BO_WARPS) {
+    const int64_t s = rowptr[r], e = rowptr[r + 1];
+    const int L = (int)(e - s);
+    if (L < 2 || L > BO_MAX) continue;
+    const int64_t P0 = s & 3, P1 = P0 + L;
+    if (lane < 16) cnt[w][lane] = 0;
+    __syncwarp();
+    // stage the row; rank of each entry within its class (order of appearance)
+    for (int i0 = 0; i0 < L; i0 += 32) {
+      int i = i0 + lane;
+      bool v = i < L;
+      int c = 16 + lane;   // distinct dummy class for idle lanes
+      if (v) {
+        uint16_t f = hcol[s + i];
+        scol[i] = f;
+        sval[i] = hval[s + i];
+        c = f & 15;
+      }
+      unsigned same = __match_any_sync(0xffffffffu, c);
+      int base_c = v ? cnt[w][c] : 0;
+      __syncwarp();
+      if (v) {
+        srank[i] = (uint16_t)(base_c + __popc(same & lt));
+        if ((same & lt) == 0) cnt[w][c] = base_c + __popc(same);   // lowest lane of the class
+      }
+      __syncwarp();
+    }
+    // empty slots (classes with fewer entries than slots), in slot order
+    int nempty = 0;
+    for (int64_t p0 = P0; p0 < P1; p0 += 32) {
+      int64_t p = p0 + lane;
+      bool emp = false;
+      if (p < P1) {
+        int c = bo_class(p);
+        emp = bo_count(c, p) - bo_count(c, P0) >= cnt[w][c];
+      }
+      unsigned m = __ballot_sync(0xffffffffu, emp);
+      if (emp) sempty[nempty + __popc(m & lt)] = (uint16_t)(p - P0);
+      nempty += __popc(m);
+    }
+    __syncwarp();
+    // surplus entries before class c (prefix over the 16 classes)
+    int sur = 0;
+    if (lane < 16) {
+      int64_t slots = bo_count(lane, P1) - bo_count(lane, P0);
+      sur = (int)max((int64_t)0, (int64_t)cnt[w][lane] - slots);
+    }
+    int incl = sur;
+#pragma unroll
+    for (int o = 1; o < 16; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    int excl = incl - sur;   // lanes 0..15: surplus entries of classes < lane
+    // place every entry
+    for (int i0 = 0; i0 < L; i0 += 32) {
+      int i = i0 + lane;
+      int c = i < L ? (scol[i] & 15) : 0;
+      int64_t pre = __shfl_sync(0xffffffffu, excl, c);
+      if (i < L) {
+        int rk = srank[i];
+        int64_t slots = bo_count(c, P1) - bo_count(c, P0);
+        int64_t q;
+        if (rk < slots) q = bo_slot(c, bo_count(c, P0) + rk) - P0;
+        else q = sempty[pre + (rk - slots)];
+        hcol[s + q] = scol[i];
+        hval[s + q] = sval[i];
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -306,6 +462,9 @@ __global__ void __launch_bounds__(256) k_spmv_csr(
 // the table), mu.x is accumulated in double-float, and the result
 //   y = (B x - mu.x) - csub * z      (z a double-float basis column)
 // is written as a double-float working vector, ready for reorthogonalisation.
+// With stacked samples (blk non-null) block b handles the cells of blk[b] of
+// sample s = blk[b].seg with that sample's feature parameters (x, 1/std, clip,
+// mu at offset s * nf) and csub[s].
 __device__ __forceinline__ void dfx_fma(float& sh, float& sl, float ah, float al, float bh, float bl) {
   float p = ah * bh;
   float e = fmaf(ah, bh, -p);
@@ -324,10 +483,27 @@ __global__ void __launch_bounds__(256) k_spmv_csr_df(
     int64_t n_rows, int64_t nf, const float* __restrict__ xh, const float* __restrict__ xl,
     const float* __restrict__ inv_f, const float* __restrict__ clip_f, const float* __restrict__ mu_h,
     const float* __restrict__ mu_l, float* __restrict__ yh, float* __restrict__ yl,
-    const double* __restrict__ csub, const float* __restrict__ zh, const float* __restrict__ zl) {
+    const double* __restrict__ csub, const float* __restrict__ zh, const float* __restrict__ zl,
+    const BlkRange* __restrict__ blk, const int* __restrict__ active) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ float redh[32], redl[32];
   __shared__ float sc[4];
+  int sg = 0;
+  int64_t rb0 = 0, rb1 = n_rows;
+  if (blk) {
+    const BlkRange br = blk[blockIdx.x];
+    sg = br.seg;
+    rb0 = br.r0;
+    rb1 = br.r1;
+    if (active && !active[sg]) return;
+    const int64_t po = (int64_t)sg * nf;
+    xh += po;
+    xl += po;
+    inv_f += po;
+    clip_f += po;
+    mu_h += po;
+    mu_l += po;
+  }
   float mh = 0.f, ml = 0.f;
   for (int64_t f = threadIdx.x; f < nf; f += blockDim.x) {
     float xs = xh[f];
@@ -365,7 +541,7 @@ __global__ void __launch_bounds__(256) k_spmv_csr_df(
     sc[0] = t;
     sc[1] = l - (t - h);
     if (csub) {
-      double c = *csub;
+      double c = csub[sg];
       sc[2] = (float)c;
       sc[3] = (float)(c - (double)sc[2]);
     } else {
@@ -376,9 +552,15 @@ __global__ void __launch_bounds__(256) k_spmv_csr_df(
   const float muxh = sc[0], muxl = sc[1], csh = -sc[2], csl = -sc[3];
 
   int lane = threadIdx.x & 31;
-  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t r = warp; r < n_rows; r += nwarps) {
+  int64_t warp, nwarps;
+  if (blk) {
+    warp = rb0 + (threadIdx.x >> 5);
+    nwarps = blockDim.x >> 5;
+  } else {
+    warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  }
+  for (int64_t r = warp; r < rb1; r += nwarps) {
     int64_t s = rowptr[r], e = rowptr[r + 1];
     int64_t a0 = s & ~3ll;
     float acc = 0.f;
@@ -544,25 +726,22 @@ __global__ void k_spmv_t_finish(const AccT* __restrict__ partial, int nblocks, i
 constexpr int64_t RB_ROWS = 16384;
 constexpr int RB_THREADS = 512;
 
-__device__ __forceinline__ int64_t lower_bound_rows(const int32_t* __restrict__ r, int64_t lo,
-                                                    int64_t hi, int64_t key) {
-  while (lo < hi) {
-    int64_t mid = (lo + hi) >> 1;
-    if ((int64_t)r[mid] < key) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
+// first row of row block b: b * RB_ROWS, or row0[b] for blocks aligned to
+// sample boundaries
+__device__ __forceinline__ int64_t rb_first_row(const int64_t* row0, int64_t b) {
+  return row0 ? row0[b] : b * RB_ROWS;
 }
 
 __global__ void k_rb_count(const int64_t* __restrict__ fstart, const int64_t* __restrict__ fend,
                            const int32_t* __restrict__ rowidx, int64_t nf, int64_t n_rb,
-                           int64_t* __restrict__ cnt, int64_t* __restrict__ src) {
+                           int64_t* __restrict__ cnt, int64_t* __restrict__ src,
+                           const int64_t* __restrict__ row0) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n_rb * nf;
        p += (int64_t)gridDim.x * blockDim.x) {
     int64_t b = p / nf, f = p % nf;
     int64_t s = fstart[f], e = fend[f];
-    int64_t lo = lower_bound_rows(rowidx, s, e, b * RB_ROWS);
-    int64_t hi = lower_bound_rows(rowidx, lo, e, (b + 1) * RB_ROWS);
+    int64_t lo = lower_bound_rows(rowidx, s, e, rb_first_row(row0, b));
+    int64_t hi = lower_bound_rows(rowidx, lo, e, rb_first_row(row0, b + 1));
     cnt[p] = hi - lo;
     src[p] = lo;
   }
@@ -572,7 +751,7 @@ template <typename ValT>
 __global__ void k_rb_copy(const int64_t* __restrict__ src, const int64_t* __restrict__ dst,
                           const int32_t* __restrict__ rowidx, const ValT* __restrict__ val,
                           int64_t npairs, int64_t nf, uint16_t* __restrict__ oidx,
-                          ValT* __restrict__ oval) {
+                          ValT* __restrict__ oval, const int64_t* __restrict__ row0) {
   int lane = threadIdx.x & 31;
   int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -580,7 +759,7 @@ __global__ void k_rb_copy(const int64_t* __restrict__ src, const int64_t* __rest
     int64_t b = p / nf;
     int64_t s = src[p], d = dst[p], n = dst[p + 1] - d;
     for (int64_t i = lane; i < n; i += 32) {
-      oidx[d + i] = (uint16_t)(rowidx[s + i] - b * RB_ROWS);
+      oidx[d + i] = (uint16_t)(rowidx[s + i] - rb_first_row(row0, b));
       oval[d + i] = val[s + i];
     }
   }
@@ -590,11 +769,24 @@ template <typename ValT>
 __global__ void __launch_bounds__(RB_THREADS) k_spmv_rb(
     const int64_t* __restrict__ rb_ptr, const uint16_t* __restrict__ rb_idx,
     const ValT* __restrict__ rb_val, int64_t nf, int64_t n_cells, const float* __restrict__ inv_f,
-    const float* __restrict__ clip_f, const float* __restrict__ uf, float* __restrict__ partial) {
+    const float* __restrict__ clip_f, const float* __restrict__ uf, float* __restrict__ partial,
+    const int64_t* __restrict__ row0, const int* __restrict__ rb_seg,
+    const int* __restrict__ active) {
   extern __shared__ __align__(16) float us[];
   int64_t b = blockIdx.x;
-  int64_t r0 = b * RB_ROWS;
-  int64_t nr = n_cells - r0 < RB_ROWS ? n_cells - r0 : RB_ROWS;
+  int64_t r0, nr;
+  if (row0) {
+    // blocks aligned to samples: that sample's feature parameters
+    int sg = rb_seg[b];
+    if (active && !active[sg]) return;
+    r0 = row0[b];
+    nr = row0[b + 1] - r0;
+    inv_f += (int64_t)sg * nf;
+    clip_f += (int64_t)sg * nf;
+  } else {
+    r0 = b * RB_ROWS;
+    nr = n_cells - r0 < RB_ROWS ? n_cells - r0 : RB_ROWS;
+  }
   for (int64_t i = threadIdx.x; i < RB_ROWS; i += blockDim.x) us[i] = i < nr ? uf[r0 + i] : 0.f;
   __syncthreads();
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -653,6 +845,52 @@ __global__ void k_rb_finish(const float* __restrict__ partial, int64_t n_rb, int
     if (beta != 0.0) out += beta * y[f];
     if (z) out -= cs * z[f];
     y[f] = out;
+  }
+}
+
+// Stacked samples: y[s*nf + f] = sum over the sample's row blocks of
+// partial[b][f] - mu[s*nf + f] * (sum of u over the sample) - csub[s] * z[s*nf + f]
+// (blockIdx.y = sample).
+__global__ void k_rb_finish_seg(const float* __restrict__ partial, const int64_t* __restrict__ rb_first,
+                                int64_t nf, const double* __restrict__ mu,
+                                const double* __restrict__ upart, double* __restrict__ y,
+                                const double* __restrict__ csub, const double* __restrict__ z,
+                                const int* __restrict__ active) {
+  const int sg = blockIdx.y;
+  if (active && !active[sg]) return;
+  const int64_t b0 = rb_first[sg], b1 = rb_first[sg + 1];
+  double su = 0;
+  for (int64_t b = b0; b < b1; ++b) su += upart[b];
+  double cs = csub ? csub[sg] : 0.0;
+  for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < nf;
+       f += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0;
+    for (int64_t b = b0; b < b1; ++b) acc += (double)partial[b * nf + f];
+    int64_t o = (int64_t)sg * nf + f;
+    double out = acc - mu[o] * su;
+    if (z) out -= cs * z[o];
+    y[o] = out;
+  }
+}
+
+// u -> FP32 copy and the FP64 sum of u over each sample-aligned row block
+__global__ void k_bu_prep(const double* __restrict__ u, const int64_t* __restrict__ row0,
+                          float* __restrict__ uf, double* __restrict__ upart) {
+  __shared__ double red[32];
+  const int64_t b = blockIdx.x;
+  double s = 0;
+  for (int64_t i = row0[b] + threadIdx.x; i < row0[b + 1]; i += blockDim.x) {
+    double v = u[i];
+    uf[i] = (float)v;
+    s += v;
+  }
+  s = sv_warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    v = sv_warp_sum(v);
+    if (threadIdx.x == 0) upart[b] = v;
   }
 }
 
@@ -811,13 +1049,15 @@ void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const 
       sv_launch(ctx, "spmv_rb", k_spmv_rb<float>, grid, dim3(RB_THREADS), smem,
                 (const int64_t*)S->rb_ptr.get(), (const uint16_t*)S->rb_idx.get(),
                 (const float*)S->rb_val.get(), S->nf, S->n_cells, (const float*)S->inv_std_f.get(),
-                (const float*)S->clip_f.get(), (const float*)Sm->u_f32.get(), Sm->rb_partial.get());
+                (const float*)S->clip_f.get(), (const float*)Sm->u_f32.get(), Sm->rb_partial.get(),
+                (const int64_t*)nullptr, (const int*)nullptr, (const int*)nullptr);
     else
       sv_launch(ctx, "spmv_rb", k_spmv_rb<__nv_bfloat16>, grid, dim3(RB_THREADS), smem,
                 (const int64_t*)S->rb_ptr.get(), (const uint16_t*)S->rb_idx.get(),
                 (const __nv_bfloat16*)S->rb_val.get(), S->nf, S->n_cells,
                 (const float*)S->inv_std_f.get(), (const float*)S->clip_f.get(),
-                (const float*)Sm->u_f32.get(), Sm->rb_partial.get());
+                (const float*)Sm->u_f32.get(), Sm->rb_partial.get(), (const int64_t*)nullptr,
+                (const int*)nullptr, (const int*)nullptr);
     sv_launch(ctx, "spmv_rb_finish", k_rb_finish, dim3(sv_grid_for(ctx, S->nf, 256, 4)), dim3(256), 0,
               (const float*)Sm->rb_partial.get(), S->n_rb, S->nf, (const double*)S->mu.get(),
               (const double*)Sm->red_partial.get(), UPREP_BLOCKS, alpha, beta, y, csub, z);
@@ -901,7 +1141,7 @@ bool sv_centered_apply_df(sv_context* ctx, const sv_centered* S, const float* xh
             (const int64_t*)S->h_rowptr.get(), (const IT*)COL, (const VT*)S->h_val.get(),         \
             S->n_cells, S->nf, xh, xl, (const float*)S->inv_std_f.get(),                          \
             (const float*)S->clip_f.get(), (const float*)S->mu_h.get(), (const float*)S->mu_l.get(), \
-            yh, yl, csub, zh, zl)
+            yh, yl, csub, zh, zl, (const BlkRange*)nullptr, (const int*)nullptr)
   bool small = S->nf <= 65536;
   if (S->dtype == SV_F32) {
     if (small) LAUNCH_CSRDF(float, uint16_t, S->h_col16.get());
@@ -914,8 +1154,61 @@ bool sv_centered_apply_df(sv_context* ctx, const sv_centered* S, const float* xh
   return true;
 }
 
+// 1-based feature indices (null: every gene) -> 0-based genes, checked
+static std::vector<int32_t> feature_genes(const sv_counts* C, const int64_t* features, int64_t nfeatures) {
+  SV_REQUIRE(C->n_cells >= 2, "need at least two cells for a variance");
+  int64_t nf = features ? nfeatures : C->n_genes;
+  SV_REQUIRE(nf >= 1, "no features");
+  std::vector<int32_t> fg(nf);
+  std::vector<char> seen(C->n_genes, 0);
+  for (int64_t f = 0; f < nf; ++f) {
+    int64_t g = features ? features[f] - 1 : f;
+    SV_REQUIRE(g >= 0 && g < C->n_genes, "feature %lld out of range 1..%lld", (long long)(g + 1),
+               (long long)C->n_genes);
+    SV_REQUIRE(!seen[g], "duplicate feature %lld", (long long)(g + 1));
+    seen[g] = 1;
+    fg[f] = (int32_t)g;
+  }
+  return fg;
+}
+
+// Row-blocked CSC copy of the feature subset (the X^T u layout): for every
+// (row block, feature) the block's entries of the feature, each as its row
+// within the block (uint16) and its value.  Row blocks of RB_ROWS rows, or with
+// first rows row0 (n_rb + 1 entries, device) when aligned to samples.
+static void rb_build(sv_context* ctx, const sv_counts* C, const sv_data* data, const int64_t* fstart,
+                     const int64_t* fend, int64_t nf, int64_t nnz_h, int64_t n_rb, const int64_t* row0,
+                     DevBuf<int64_t>& rb_ptr, DevBuf<uint16_t>& rb_idx, DevBuf<unsigned char>& rb_val,
+                     DevBuf<float>& rb_partial) {
+  int64_t np = n_rb * nf;
+  DevBuf<int64_t> cnt(np + 1), src(np + 1);
+  sv_launch(ctx, "scale_rb_count", k_rb_count, dim3(sv_grid_for(ctx, np, 256, 8)), dim3(256), 0, fstart,
+            fend, (const int32_t*)C->csc_rowidx.get(), nf, n_rb, cnt.get(), src.get(), row0);
+  rb_ptr.alloc(np + 1);
+  sv_scan_i64(ctx, cnt.get(), rb_ptr.get(), np);
+  int64_t tot = sv_read_i64(ctx, rb_ptr.get() + np);
+  if (tot != nnz_h)
+    sv_throw(SV_ERR_DEVICE, "row-blocked copy size mismatch (%lld vs %lld)", (long long)tot,
+             (long long)nnz_h);
+  size_t es2 = sv_elem_size(data->dtype);
+  rb_idx.alloc(std::max<int64_t>(1, nnz_h));
+  rb_val.alloc(std::max<int64_t>(1, nnz_h) * es2);
+  rb_partial.alloc(std::max<int64_t>(1, np));
+  int gridc = sv_grid_for(ctx, np * 32, 256, 8);
+  if (data->dtype == SV_F32)
+    sv_launch(ctx, "scale_rb_copy", k_rb_copy<float>, dim3(gridc), dim3(256), 0, (const int64_t*)src.get(),
+              (const int64_t*)rb_ptr.get(), (const int32_t*)C->csc_rowidx.get(),
+              (const float*)data->csc_val.get(), np, nf, rb_idx.get(), (float*)rb_val.get(), row0);
+  else
+    sv_launch(ctx, "scale_rb_copy", k_rb_copy<__nv_bfloat16>, dim3(gridc), dim3(256), 0,
+              (const int64_t*)src.get(), (const int64_t*)rb_ptr.get(), (const int32_t*)C->csc_rowidx.get(),
+              (const __nv_bfloat16*)data->csc_val.get(), np, nf, rb_idx.get(),
+              (__nv_bfloat16*)rb_val.get(), row0);
+  sv_sync(ctx);
+}
+
 static sv_centered* make_centered(sv_context* ctx, const sv_data* data, const std::vector<int32_t>& fg,
-                                  double scale_max, const double* mu_given) {
+                                  double scale_max, const double* mu_given, bool want_rb = true) {
   const sv_counts* C = data->counts;
   int64_t nf = (int64_t)fg.size();
   size_t smem_need = data->dtype == SV_F64 ? (size_t)nf * 24 : (size_t)nf * 8;
@@ -952,7 +1245,7 @@ static sv_centered* make_centered(sv_context* ctx, const sv_data* data, const st
             (const VT*)data->csc_val.get(), (const int64_t*)S->feat_start.get(),                 \
             (const int64_t*)S->feat_end.get(), nf, C->n_cells, scale_max, S->mean.get(),         \
             S->std_.get(), S->mu.get(), S->inv_std_f.get(), S->clip_f.get(), S->inv_std_d.get(), \
-            S->clip_d.get())
+            S->clip_d.get(), (const int32_t*)nullptr, (const int64_t*)nullptr, 1)
     if (!mu_given) {
       switch (data->dtype) {
         case SV_F64: LAUNCH_MOM(double); break;
@@ -1048,42 +1341,35 @@ static sv_centered* make_centered(sv_context* ctx, const sv_data* data, const st
         break;
     }
 #undef LAUNCH_HW
+    if (small && data->dtype != SV_F64 && !getenv("SV_NO_BANKORDER")) {
+      size_t bsm = (size_t)BO_WARPS * BO_MAX * (6 + sv_elem_size(data->dtype));
+      int bgrid = ctx->num_sms * 2;
+      if (data->dtype == SV_F32) {
+        SV_CUDA(cudaFuncSetAttribute(k_hsub_bankorder<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)bsm));
+        sv_launch(ctx, "scale_hsub_order", k_hsub_bankorder<float>, dim3(bgrid), dim3(BO_WARPS * 32), bsm,
+                  (const int64_t*)S->h_rowptr.get(), C->n_cells, S->h_col16.get(), (float*)S->h_val.get());
+      } else {
+        SV_CUDA(cudaFuncSetAttribute(k_hsub_bankorder<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)bsm));
+        sv_launch(ctx, "scale_hsub_order", k_hsub_bankorder<uint16_t>, dim3(bgrid), dim3(BO_WARPS * 32), bsm,
+                  (const int64_t*)S->h_rowptr.get(), C->n_cells, S->h_col16.get(),
+                  (uint16_t*)S->h_val.get());
+      }
+    }
     S->u_f32.alloc(C->n_cells);
     S->scal.alloc(64);
     // row-blocked CSC copy for X^T u (FP32 / BF16 storage; SV_TPRODUCT=csc or csr
     // selects the other forms)
     {
       const char* mode = getenv("SV_TPRODUCT");
-      bool use_rb = data->dtype != SV_F64 && !(mode && (strcmp(mode, "csc") == 0 || strcmp(mode, "csr") == 0));
+      bool use_rb = want_rb && data->dtype != SV_F64 &&
+                    !(mode && (strcmp(mode, "csc") == 0 || strcmp(mode, "csr") == 0));
       if (use_rb) {
         S->rb_rows = RB_ROWS;
         S->n_rb = (C->n_cells + RB_ROWS - 1) / RB_ROWS;
-        int64_t np = S->n_rb * nf;
-        DevBuf<int64_t> cnt(np + 1), src(np + 1);
-        sv_launch(ctx, "scale_rb_count", k_rb_count, dim3(sv_grid_for(ctx, np, 256, 8)), dim3(256), 0,
-                  (const int64_t*)S->feat_start.get(), (const int64_t*)S->feat_end.get(),
-                  (const int32_t*)C->csc_rowidx.get(), nf, S->n_rb, cnt.get(), src.get());
-        S->rb_ptr.alloc(np + 1);
-        sv_scan_i64(ctx, cnt.get(), S->rb_ptr.get(), np);
-        int64_t tot = sv_read_i64(ctx, S->rb_ptr.get() + np);
-        if (tot != nnz_h)
-          sv_throw(SV_ERR_DEVICE, "row-blocked copy size mismatch (%lld vs %lld)", (long long)tot,
-                   (long long)nnz_h);
-        size_t es2 = sv_elem_size(data->dtype);
-        S->rb_idx.alloc(std::max<int64_t>(1, nnz_h));
-        S->rb_val.alloc(std::max<int64_t>(1, nnz_h) * es2);
-        S->rb_partial.alloc(std::max<int64_t>(1, np));
-        int gridc = sv_grid_for(ctx, np * 32, 256, 8);
-        if (data->dtype == SV_F32)
-          sv_launch(ctx, "scale_rb_copy", k_rb_copy<float>, dim3(gridc), dim3(256), 0,
-                    (const int64_t*)src.get(), (const int64_t*)S->rb_ptr.get(),
-                    (const int32_t*)C->csc_rowidx.get(), (const float*)data->csc_val.get(), np, nf,
-                    S->rb_idx.get(), (float*)S->rb_val.get());
-        else
-          sv_launch(ctx, "scale_rb_copy", k_rb_copy<__nv_bfloat16>, dim3(gridc), dim3(256), 0,
-                    (const int64_t*)src.get(), (const int64_t*)S->rb_ptr.get(),
-                    (const int32_t*)C->csc_rowidx.get(), (const __nv_bfloat16*)data->csc_val.get(), np,
-                    nf, S->rb_idx.get(), (__nv_bfloat16*)S->rb_val.get());
+        rb_build(ctx, C, data, S->feat_start.get(), S->feat_end.get(), nf, nnz_h, S->n_rb, nullptr,
+                 S->rb_ptr, S->rb_idx, S->rb_val, S->rb_partial);
         SV_CUDA(cudaFuncSetAttribute(k_spmv_rb<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)(RB_ROWS * sizeof(float))));
         SV_CUDA(cudaFuncSetAttribute(k_spmv_rb<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1179,22 +1465,211 @@ SV_API int sv_scale_features(sv_context* ctx, const sv_data* data, const int64_t
   SV_REQUIRE(data->ctx == ctx, "data handle belongs to another context");
   const sv_counts* C = data->counts;
   SV_REQUIRE(C->n_cells >= 2, "need at least two cells for a variance");
-  int64_t nf = features ? nfeatures : C->n_genes;
-  SV_REQUIRE(nf >= 1, "no features");
-  std::vector<int32_t> fg(nf);
-  {
-    std::vector<char> seen(C->n_genes, 0);
-    for (int64_t f = 0; f < nf; ++f) {
-      int64_t g = features ? features[f] - 1 : f;
-      SV_REQUIRE(g >= 0 && g < C->n_genes, "feature %lld out of range 1..%lld",
-                 (long long)(g + 1), (long long)C->n_genes);
-      SV_REQUIRE(!seen[g], "duplicate feature %lld", (long long)(g + 1));
-      seen[g] = 1;
-      fg[f] = (int32_t)g;
-    }
-  }
+  std::vector<int32_t> fg = feature_genes(C, features, nfeatures);
   *out = make_centered(ctx, data, fg, scale_max, nullptr);
   SV_CATCH
+}
+
+// ---- batched samples ----------------------------------------------------------
+// Samples stacked by cells in one data matrix, each scaled with its own
+// moments (scale_features per sample, src/scaling.jl:335-357): the feature
+// subset copies are those of the stacked matrix; the per-(sample, feature)
+// moments, the X v block schedule and the sample-aligned row blocks of X^T u
+// are the batch's own.  FP32 / BF16 storage.
+constexpr int BATCH_XCELLS = 256;   // cells per X v block (32 per warp)
+
+SV_API int sv_batch_create(sv_context* ctx, const sv_data* data, const int64_t* cell_offsets,
+                           int64_t nseg, const int64_t* features, int64_t nfeatures, double scale_max,
+                           sv_batch** out) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(out && data && cell_offsets, "null argument");
+  SV_REQUIRE(data->ctx == ctx, "data handle belongs to another context");
+  SV_REQUIRE(data->dtype != SV_F64, "batched samples take FP32 or BF16 values");
+  const sv_counts* C = data->counts;
+  SV_REQUIRE(nseg >= 1, "no samples");
+  SV_REQUIRE(cell_offsets[0] == 0 && cell_offsets[nseg] == C->n_cells,
+             "cell offsets must run from 0 to the number of cells");
+  for (int64_t s = 0; s < nseg; ++s)
+    SV_REQUIRE(cell_offsets[s + 1] - cell_offsets[s] >= 2, "sample %lld has fewer than two cells",
+               (long long)(s + 1));
+  std::vector<int32_t> fg = feature_genes(C, features, nfeatures);
+  const int64_t nf = (int64_t)fg.size();
+  auto* B = new sv_batch();
+  try {
+    B->ctx = ctx;
+    B->data = data;
+    B->nseg = nseg;
+    B->n_cells = C->n_cells;
+    B->nf = nf;
+    B->scale_max = scale_max;
+    B->hoff.assign(cell_offsets, cell_offsets + nseg + 1);
+    B->off.alloc(nseg + 1);
+    sv_h2d(ctx, B->off.get(), cell_offsets, (nseg + 1) * 8);
+    B->base = make_centered(ctx, data, fg, scale_max, nullptr, false);
+    sv_centered* S = B->base;
+    // per-(sample, feature) moments
+    size_t sf = (size_t)nseg * nf;
+    B->mean.alloc(sf);
+    B->std_.alloc(sf);
+    B->mu.alloc(sf);
+    B->inv_d.alloc(sf);
+    B->clip_d.alloc(sf);
+    B->inv_f.alloc(sf);
+    B->clip_f.alloc(sf);
+    B->mu_h.alloc(sf);
+    B->mu_l.alloc(sf);
+    int mgrid = sv_grid_for(ctx, (int64_t)sf, 1, 16);
+#define LAUNCH_BMOM(VT)                                                                           \
+  sv_launch(ctx, "scale_moments", k_moments<VT>, dim3(mgrid), dim3(256), 0,                       \
+            (const VT*)data->csc_val.get(), (const int64_t*)S->feat_start.get(),                   \
+            (const int64_t*)S->feat_end.get(), nf, C->n_cells, scale_max, B->mean.get(),           \
+            B->std_.get(), B->mu.get(), B->inv_f.get(), B->clip_f.get(), B->inv_d.get(),            \
+            B->clip_d.get(), (const int32_t*)C->csc_rowidx.get(), (const int64_t*)B->off.get(),    \
+            (int)nseg)
+    if (data->dtype == SV_F32) LAUNCH_BMOM(float);
+    else LAUNCH_BMOM(__nv_bfloat16);
+#undef LAUNCH_BMOM
+    sv_launch(ctx, "scale_mu_split", k_split_df, dim3(sv_grid_for(ctx, (int64_t)sf, 256)), dim3(256), 0,
+              (const double*)B->mu.get(), (int64_t)sf, B->mu_h.get(), B->mu_l.get());
+    // X v schedule: BATCH_XCELLS cells of one sample per block
+    {
+      std::vector<BlkRange> hb;
+      for (int64_t s2 = 0; s2 < nseg; ++s2)
+        for (int64_t r = B->hoff[s2]; r < B->hoff[s2 + 1]; r += BATCH_XCELLS) {
+          BlkRange b;
+          b.r0 = r;
+          b.r1 = std::min(B->hoff[s2 + 1], r + BATCH_XCELLS);
+          b.seg = (int)s2;
+          b.pad = 0;
+          hb.push_back(b);
+        }
+      B->nxblk = (int)hb.size();
+      B->xblk.alloc(hb.size());
+      sv_h2d(ctx, B->xblk.get(), hb.data(), hb.size() * sizeof(BlkRange));
+    }
+    // X^T u: row blocks of at most RB_ROWS cells, aligned to the samples
+    {
+      std::vector<int64_t> row0;
+      std::vector<int> seg;
+      B->h_rb_first.assign(nseg + 1, 0);
+      for (int64_t s2 = 0; s2 < nseg; ++s2) {
+        B->h_rb_first[s2] = (int64_t)row0.size();
+        for (int64_t r = B->hoff[s2]; r < B->hoff[s2 + 1]; r += RB_ROWS) {
+          row0.push_back(r);
+          seg.push_back((int)s2);
+        }
+      }
+      B->h_rb_first[nseg] = (int64_t)row0.size();
+      B->n_rb = (int64_t)row0.size();
+      row0.push_back(C->n_cells);
+      B->rb_row0.alloc(row0.size());
+      B->rb_seg.alloc(seg.size());
+      B->rb_first.alloc(nseg + 1);
+      sv_h2d(ctx, B->rb_row0.get(), row0.data(), row0.size() * 8);
+      sv_h2d(ctx, B->rb_seg.get(), seg.data(), seg.size() * 4);
+      sv_h2d(ctx, B->rb_first.get(), B->h_rb_first.data(), (nseg + 1) * 8);
+      rb_build(ctx, C, data, S->feat_start.get(), S->feat_end.get(), nf, S->nnz_h, B->n_rb,
+               B->rb_row0.get(), B->rb_ptr, B->rb_idx, B->rb_val, B->rb_partial);
+      B->upart.alloc(B->n_rb);
+      SV_CUDA(cudaFuncSetAttribute(k_spmv_rb<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(RB_ROWS * sizeof(float))));
+      SV_CUDA(cudaFuncSetAttribute(k_spmv_rb<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(RB_ROWS * sizeof(float))));
+    }
+    sv_sync(ctx);
+  } catch (...) {
+    if (B->base) sv_centered_free(B->base);
+    delete B;
+    throw;
+  }
+  *out = B;
+  SV_CATCH
+}
+
+SV_API int sv_batch_info(const sv_batch* b, int64_t* nseg, int64_t* n_cells, int64_t* nf) {
+  SV_TRY
+  SV_REQUIRE(b, "null handle");
+  if (nseg) *nseg = b->nseg;
+  if (n_cells) *n_cells = b->n_cells;
+  if (nf) *nf = b->nf;
+  SV_CATCH
+}
+
+// per-(sample, feature) statistics, sample-major (nseg x nf): mu = mean/std,
+// mean, std
+SV_API int sv_batch_stats(sv_context* ctx, const sv_batch* b, double* mu, double* mean, double* sd) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(b && b->ctx == ctx, "bad batch handle");
+  size_t bytes = (size_t)b->nseg * b->nf * 8;
+  if (mu) sv_d2h(ctx, mu, b->mu.get(), bytes);
+  if (mean) sv_d2h(ctx, mean, b->mean.get(), bytes);
+  if (sd) sv_d2h(ctx, sd, b->std_.get(), bytes);
+  SV_CATCH
+}
+
+SV_API int sv_batch_free(sv_batch* b) {
+  if (b) {
+    if (b->ctx) cudaSetDevice(b->ctx->device);
+    sv_centered_free(b->base);
+    delete b;
+  }
+  return SV_OK;
+}
+
+// W step of the batched Lanczos: for every active sample, y = X_s v_s - csub[s] z
+// (double-float in and out, stacked)
+void sv_batch_apply_N_df(sv_context* ctx, const sv_batch* b, const float* xh, const float* xl,
+                         float* yh, float* yl, const double* csub, const float* zh, const float* zl,
+                         const int* active) {
+  const sv_centered* S = b->base;
+  size_t smem = ((size_t)b->nf * 8 + 15) & ~(size_t)15;
+#define LAUNCH_BCSR(VT, IT, COL)                                                                  \
+  sv_launch(ctx, "spmv_csr_h", k_spmv_csr_df<VT, IT>, dim3(b->nxblk), dim3(256), smem,            \
+            (const int64_t*)S->h_rowptr.get(), (const IT*)COL, (const VT*)S->h_val.get(),          \
+            b->n_cells, b->nf, xh, xl, (const float*)b->inv_f.get(), (const float*)b->clip_f.get(), \
+            (const float*)b->mu_h.get(), (const float*)b->mu_l.get(), yh, yl, csub, zh, zl,         \
+            (const BlkRange*)b->xblk.get(), active)
+  bool small = b->nf <= 65536;
+  if (b->data->dtype == SV_F32) {
+    if (small) LAUNCH_BCSR(float, uint16_t, S->h_col16.get());
+    else LAUNCH_BCSR(float, int32_t, S->h_col32.get());
+  } else {
+    if (small) LAUNCH_BCSR(__nv_bfloat16, uint16_t, S->h_col16.get());
+    else LAUNCH_BCSR(__nv_bfloat16, int32_t, S->h_col32.get());
+  }
+#undef LAUNCH_BCSR
+}
+
+// V step of the batched Lanczos: for every active sample, y_s = X_s^T u_s -
+// csub[s] z_s (FP64, stacked by sample: index s * nf + f)
+void sv_batch_apply_T(sv_context* ctx, const sv_batch* b, const double* u, double* y,
+                      const double* csub, const double* z, const int* active) {
+  sv_batch* bm = const_cast<sv_batch*>(b);
+  sv_centered* S = b->base;
+  sv_launch(ctx, "spmv_csc_uprep", k_bu_prep, dim3((unsigned)b->n_rb), dim3(256), 0, u,
+            (const int64_t*)b->rb_row0.get(), S->u_f32.get(), bm->upart.get());
+  int resident = ctx->num_sms * 3;
+  int fg = (int)std::max<int64_t>(1, std::min<int64_t>(b->nf, (3 * resident + b->n_rb - 1) / b->n_rb));
+  dim3 grid((unsigned)b->n_rb, (unsigned)fg);
+  size_t smem = RB_ROWS * sizeof(float);
+  if (b->data->dtype == SV_F32)
+    sv_launch(ctx, "spmv_rb", k_spmv_rb<float>, grid, dim3(RB_THREADS), smem,
+              (const int64_t*)b->rb_ptr.get(), (const uint16_t*)b->rb_idx.get(), (const float*)b->rb_val.get(),
+              b->nf, b->n_cells, (const float*)b->inv_f.get(), (const float*)b->clip_f.get(),
+              (const float*)S->u_f32.get(), bm->rb_partial.get(), (const int64_t*)b->rb_row0.get(),
+              (const int*)b->rb_seg.get(), active);
+  else
+    sv_launch(ctx, "spmv_rb", k_spmv_rb<__nv_bfloat16>, grid, dim3(RB_THREADS), smem,
+              (const int64_t*)b->rb_ptr.get(), (const uint16_t*)b->rb_idx.get(),
+              (const __nv_bfloat16*)b->rb_val.get(), b->nf, b->n_cells, (const float*)b->inv_f.get(),
+              (const float*)b->clip_f.get(), (const float*)S->u_f32.get(), bm->rb_partial.get(),
+              (const int64_t*)b->rb_row0.get(), (const int*)b->rb_seg.get(), active);
+  dim3 fgrid((unsigned)sv_grid_for(ctx, b->nf, 256, 1), (unsigned)b->nseg);
+  sv_launch(ctx, "spmv_rb_finish", k_rb_finish_seg, fgrid, dim3(256), 0, (const float*)bm->rb_partial.get(),
+            (const int64_t*)b->rb_first.get(), b->nf, (const double*)b->mu.get(),
+            (const double*)bm->upart.get(), y, csub, z, active);
 }
 
 sv_counts* sv_counts_upload_positions(sv_context* ctx, int64_t n_rows, int64_t n_cols, int64_t nnz,
@@ -1254,6 +1729,21 @@ SV_API int sv_centered_create(sv_context* ctx, int64_t n_rows, int64_t n_cols, i
   SV_CATCH
 }
 
+// Per-gene mean and standard deviation (n - 1) of the raw counts, implicit
+// zeros included (mean_std on the count matrix, src/scaling.jl:18-44): device
+// arrays of n_genes.
+void sv_count_moments(sv_context* ctx, const sv_counts* C, double* mean, double* sd) {
+  int64_t ng = C->n_genes;
+  DevBuf<double> mu(ng), invd(ng), clipd(ng);
+  DevBuf<float> invf(ng), clipf(ng);
+  sv_launch(ctx, "gene_moments", k_moments<int32_t>, dim3(sv_grid_for(ctx, ng, 1, 16)), dim3(256), 0,
+            (const int32_t*)C->csc_count.get(), (const int64_t*)C->csc_colptr.get(),
+            (const int64_t*)C->csc_colptr.get() + 1, ng, C->n_cells, (double)INFINITY, mean, sd, mu.get(),
+            invf.get(), clipf.get(), invd.get(), clipd.get(), (const int32_t*)nullptr,
+            (const int64_t*)nullptr, 1);
+  sv_sync(ctx);
+}
+
 SV_API int sv_gene_moments(sv_context* ctx, const sv_data* data, double* mean, double* var) {
   SV_TRY
   sv_ctx_check(ctx);
@@ -1271,7 +1761,7 @@ SV_API int sv_gene_moments(sv_context* ctx, const sv_data* data, double* mean, d
   sv_launch(ctx, "gene_moments", k_moments<VT>, dim3(sv_grid_for(ctx, ng, 1, 16)), dim3(256), 0, \
             (const VT*)data->csc_val.get(), (const int64_t*)fs.get(), (const int64_t*)fe.get(), ng, \
             C->n_cells, (double)INFINITY, m.get(), sd.get(), mu.get(), invf.get(), clipf.get(),   \
-            invd.get(), clipd.get())
+            invd.get(), clipd.get(), (const int32_t*)nullptr, (const int64_t*)nullptr, 1)
   switch (data->dtype) {
     case SV_F64: LAUNCH_MOM(double); break;
     case SV_F32: LAUNCH_MOM(float); break;

@@ -80,3 +80,12 @@ def test_filter_cells_and_features_wrappers(sv, ctx, O):
     R, rfi = O.filter_features(X, min_cells=40)
     assert np.array_equal(fi, rfi)
     _same(D.to_csc(), R)
+
+
+def test_select_cells_is_a_row_slice(sv, ctx, O):
+    X = O.synth_counts(700, 300, -1.0, 1.5, depth=0.5, seed=43)
+    C = sv.CountMatrix.from_csc(X, ctx=ctx)
+    D = C.select_cells(120, 455)
+    R = sp.csc_matrix(sp.csr_matrix(X)[120:455])
+    _same(D.to_csc(), R)
+    _same(D.to_csr().tocsc(), R)
