@@ -535,6 +535,7 @@ def batched_bench(args):
         em = sv.batch_pca(B, w["npcs"], tol=1e-5, init=init, download=False)
         sv.batch_ann(B, em, w["k"], precision=w["knn"], download=False)
         ctx.sync()
+        em.info["cells_per_block"] = B.cells_per_block
         return em
 
     def loop():
@@ -581,6 +582,7 @@ def batched_bench(args):
                    "n_cells": n, "sample_cells_min": int(sizes.min()), "sample_cells_max": int(sizes.max()),
                    "nnz": counts.nnz, "depth_factor": round(D, 5), "value_dtype": w["dtype"],
                    "knn_kernel": w["knn"], "irlba_cycles_min": int(it.min()), "irlba_cycles_max": int(it.max()),
+                   "xv_cells_per_block_autotuned": int(emb.info["cells_per_block"]),
                    "timing": "wall clock with the stream synchronised on both sides"},
         "loop": {"value": round(n / tl, 1), "ms_per_step": round(tl * 1e3, 3), "gpu_launches": int(ll)},
         "batched_vs_loop": round(tl / tb, 3),

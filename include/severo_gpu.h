@@ -315,6 +315,9 @@ int sv_batch_pca(sv_context* ctx, const sv_batch* b, int64_t npcs, int64_t maxit
 int sv_batch_knn(sv_context* ctx, const sv_batch* b, const sv_embed* e, int64_t ndims, int64_t k,
                  int metric, int include_self, int precision, int32_t* nn_index, double* distances,
                  sv_knn** out);
+/* The cells per block of the batched X v product, chosen on the first batch of
+ * each shape by timing the candidates 128, 256, 512, 1024. */
+int sv_batch_tuning(const sv_batch* b, int64_t* cells_per_block);
 int sv_batch_free(sv_batch* b);
 
 /* Drop-ins for the native libcell symbols of src/neighbours.jl:37-72 (the Julia

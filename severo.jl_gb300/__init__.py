@@ -557,6 +557,13 @@ class Batch(_Handle):
         L.check(self.ctx.lib.sv_batch_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
         return c.value
 
+    @property
+    def cells_per_block(self):
+        """X v block size chosen by the autotuner for this batch's shape."""
+        v = C.c_int64()
+        L.check(self.ctx.lib.sv_batch_tuning(self.h, C.byref(v)))
+        return v.value
+
     def stats(self):
         """(mu, mean, std), each nseg x nf."""
         S, nf = self.nseg, self.nf

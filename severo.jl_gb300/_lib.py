@@ -117,6 +117,7 @@ SIGNATURES = {
     "sv_batch_stats": (i32, [vp, vp, vp, vp, vp]),
     "sv_batch_pca": (i32, [vp, vp, i64, i64, C.c_double, vp, C.c_uint64, P(vp), vp, vp, vp, P(i64)]),
     "sv_batch_knn": (i32, [vp, vp, vp, i64, i64, i32, i32, i32, vp, vp, P(vp)]),
+    "sv_batch_tuning": (i32, [vp, P(i64)]),
     "sv_batch_free": (i32, [vp]),
 }
 

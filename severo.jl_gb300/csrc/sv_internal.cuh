@@ -10,6 +10,7 @@
 #include <vector>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <algorithm>
 
 #include "../../include/severo_gpu.h"
@@ -241,6 +242,7 @@ struct sv_batch {
   // X v: blocks of cells within one sample
   DevBuf<BlkRange> xblk;
   int nxblk = 0;
+  int xcells = 0;                     // cells per X v block (autotuned)
   // X^T u: row blocks aligned to the samples
   int64_t n_rb = 0;
   std::vector<int64_t> h_rb_first;    // nseg + 1: first row block of each sample

@@ -177,37 +177,43 @@ __global__ void k_hsub_write(const int64_t* __restrict__ rowptr, const int32_t* 
   }
 }
 
-// ---- bank-aware order of each CSR_h row -----------------------------------------
-// The X v kernel reads a row in groups of 128 entries, lane l taking entries
-// 4l .. 4l+3 of the group (from the row start rounded down to 4); for each t
-// the 32 lanes then gather the 8-byte table entries of 32 features from shared
-// memory, which serialise on bank conflicts (about six wavefronts per gather
-// with sorted features).  An 8-byte entry of feature f sits in bank pair
-// f mod 16, so the row is permuted such that slot p (relative to the rounded
-// start) holds a feature of class c(p) = ((p >> 2) + 4 (p & 3)) mod 16 where
-// possible: the 32 slots a gather reads then hold each class twice (two
-// wavefronts).  Entries of class c fill the c-slots in order of appearance; the
-// surplus of over-full classes fills the slots left empty, in slot order.  The
-// row's sum is then taken in another order (a different, equally valid
-// rounding).  Rows longer than BO_MAX keep their order.
-constexpr int BO_MAX = 3072;
-constexpr int BO_WARPS = 4;
+// ---- bank-aware order of the product copies --------------------------------------
+// The product kernels read a segment (a CSR_h row, or a (row block, feature)
+// run of the row-blocked copy) in groups of 128 entries, lane l taking entries
+// 4l .. 4l+3 of the group (from the segment start rounded down to 4); for each
+// t the 32 lanes then gather from a shared-memory table: 8-byte entries per
+// feature for X v (bank pair f mod 16), 4-byte entries per row for X^T u (bank
+// row mod 32).  With sorted indices the gathers serialise on bank conflicts
+// (ncu: ~4 extra wavefronts per gather).  So each segment is permuted such that
+// slot p (relative to the rounded start) holds an index of class
+// c(p) = ((p >> 2) + (NC/4) (p & 3)) mod NC where possible (NC = 16 or 32
+// classes): the 32 slots of a gather then hold each class 32/NC times.
+// Entries of class c fill the c-slots in order of appearance; the surplus of
+// over-full classes fills the slots left empty, in slot order.  The segment's
+// sum is then taken in another order (a different, equally valid rounding).
+constexpr int BO_EMPTY = 1024;   // most empty slots a segment may have to be reordered
+constexpr int BO_WARPS = 8;
 
-__device__ __forceinline__ int bo_class(int64_t p) { return (int)(((p >> 2) + 4 * (p & 3)) & 15); }
-// slots p < X whose class is c: 4 per 64 slots, at offsets 4((c - 4t) & 15) + t
+template <int NC>
+__device__ __forceinline__ int bo_class(int64_t p) {
+  return (int)(((p >> 2) + (NC / 4) * (p & 3)) & (NC - 1));
+}
+// slots p < X of class c: 4 per period of 4 NC slots, at offsets
+// 4 ((c - (NC/4) t) mod NC) + t
+template <int NC>
 __device__ __forceinline__ int64_t bo_count(int c, int64_t X) {
-  int64_t n = 4 * (X >> 6);
-  int r = (int)(X & 63);
+  int64_t n = 4 * (X / (4 * NC));
+  int r = (int)(X % (4 * NC));
 #pragma unroll
-  for (int t = 0; t < 4; ++t) n += (4 * ((c - 4 * t) & 15) + t) < r;
+  for (int t = 0; t < 4; ++t) n += (4 * ((c - (NC / 4) * t) & (NC - 1)) + t) < r;
   return n;
 }
 // the idx-th slot (from 0) of class c
+template <int NC>
 __device__ __forceinline__ int64_t bo_slot(int c, int64_t idx) {
   int o[4];
 #pragma unroll
-  for (int t = 0; t < 4; ++t) o[t] = 4 * ((c - 4 * t) & 15) + t;
-  // sort the four offsets
+  for (int t = 0; t < 4; ++t) o[t] = 4 * ((c - (NC / 4) * t) & (NC - 1)) + t;
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -219,93 +225,97 @@ __device__ __forceinline__ int64_t bo_slot(int c, int64_t idx) {
       }
   int k = (int)(idx & 3);
   int ok = k == 0 ? o[0] : k == 1 ? o[1] : k == 2 ? o[2] : o[3];
-  return 64 * (idx >> 2) + ok;
+  return (int64_t)(4 * NC) * (idx >> 2) + ok;
 }
 
-template <typename VT>
-__global__ void __launch_bounds__(BO_WARPS * 32) k_hsub_bankorder(const int64_t* __restrict__ rowptr,
-                                                                  int64_t n_rows, uint16_t* __restrict__ hcol,
-                                                                  VT* __restrict__ hval) {
-  extern __shared__ __align__(16) unsigned char bo_raw[];
+// One warp per segment, three passes (class counts; the empty slots; ranks and
+// placement), the result written to a second copy (segments with more than
+// BO_EMPTY empty slots are copied unchanged).
+template <int NC, typename VT>
+__global__ void __launch_bounds__(BO_WARPS * 32) k_bankorder(const int64_t* __restrict__ ptr,
+                                                             int64_t nseg,
+                                                             const uint16_t* __restrict__ icol,
+                                                             const VT* __restrict__ ival,
+                                                             uint16_t* __restrict__ ocol,
+                                                             VT* __restrict__ oval) {
+  __shared__ uint16_t sempty[BO_WARPS][BO_EMPTY];
+  __shared__ int cnt[BO_WARPS][NC], run[BO_WARPS][NC];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const size_t per = (size_t)BO_MAX * (2 + 2 + 2 + sizeof(VT));
-  unsigned char* base = bo_raw + w * per;
-  uint16_t* scol = (uint16_t*)base;
-  uint16_t* srank = scol + BO_MAX;
-  uint16_t* sempty = srank + BO_MAX;
-  VT* sval = (VT*)(sempty + BO_MAX);
-  __shared__ int cnt[BO_WARPS][16];
   const unsigned lt = (1u << lane) - 1u;
-  for (int64_t r = (int64_t)blockIdx.x * BO_WARPS + w; r < n_rows; r += (int64_t)gridDim.x * BO_WARPS) {
-    const int64_t s = rowptr[r], e = rowptr[r + 1];
-    const int L = (int)(e - s);
-    if (L < 2 || L > BO_MAX) continue;
+  for (int64_t r = (int64_t)blockIdx.x * BO_WARPS + w; r < nseg; r += (int64_t)gridDim.x * BO_WARPS) {
+    const int64_t s = ptr[r], e = ptr[r + 1];
+    const int64_t L = e - s;
+    if (L <= 0) continue;
     const int64_t P0 = s & 3, P1 = P0 + L;
-    if (lane < 16) cnt[w][lane] = 0;
+    if (lane < NC) {
+      cnt[w][lane] = 0;
+      run[w][lane] = 0;
+    }
     __syncwarp();
-    // stage the row; rank of each entry within its class (order of appearance)
-    for (int i0 = 0; i0 < L; i0 += 32) {
-      int i = i0 + lane;
-      bool v = i < L;
-      int c = 16 + lane;   // distinct dummy class for idle lanes
-      if (v) {
-        uint16_t f = hcol[s + i];
-        scol[i] = f;
-        sval[i] = hval[s + i];
-        c = f & 15;
-      }
+    // pass 1: entries per class
+    for (int64_t i0 = 0; i0 < L; i0 += 32) {
+      int64_t i = i0 + lane;
+      int c = i < L ? (icol[s + i] & (NC - 1)) : NC + lane;
       unsigned same = __match_any_sync(0xffffffffu, c);
-      int base_c = v ? cnt[w][c] : 0;
-      __syncwarp();
-      if (v) {
-        srank[i] = (uint16_t)(base_c + __popc(same & lt));
-        if ((same & lt) == 0) cnt[w][c] = base_c + __popc(same);   // lowest lane of the class
-      }
+      if (i < L && (same & lt) == 0) cnt[w][c] += __popc(same);
       __syncwarp();
     }
-    // empty slots (classes with fewer entries than slots), in slot order
-    int nempty = 0;
+    // pass 2: empty slots (classes with fewer entries than slots), in slot order
+    int64_t nempty = 0;
     for (int64_t p0 = P0; p0 < P1; p0 += 32) {
       int64_t p = p0 + lane;
       bool emp = false;
       if (p < P1) {
-        int c = bo_class(p);
-        emp = bo_count(c, p) - bo_count(c, P0) >= cnt[w][c];
+        int c = bo_class<NC>(p);
+        emp = bo_count<NC>(c, p) - bo_count<NC>(c, P0) >= cnt[w][c];
       }
       unsigned m = __ballot_sync(0xffffffffu, emp);
-      if (emp) sempty[nempty + __popc(m & lt)] = (uint16_t)(p - P0);
+      int64_t at = nempty + __popc(m & lt);
+      if (emp && at < BO_EMPTY) sempty[w][at] = (uint16_t)(p - P0);
       nempty += __popc(m);
     }
     __syncwarp();
-    // surplus entries before class c (prefix over the 16 classes)
+    if (nempty > BO_EMPTY || L > 65535) {
+      for (int64_t i = lane; i < L; i += 32) {
+        ocol[s + i] = icol[s + i];
+        oval[s + i] = ival[s + i];
+      }
+      continue;
+    }
+    // surplus entries of the classes before c (prefix over the classes)
     int sur = 0;
-    if (lane < 16) {
-      int64_t slots = bo_count(lane, P1) - bo_count(lane, P0);
+    if (lane < NC) {
+      int64_t slots = bo_count<NC>(lane, P1) - bo_count<NC>(lane, P0);
       sur = (int)max((int64_t)0, (int64_t)cnt[w][lane] - slots);
     }
     int incl = sur;
 #pragma unroll
-    for (int o = 1; o < 16; o <<= 1) {
+    for (int o = 1; o < 32; o <<= 1) {
       int y = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += y;
     }
-    int excl = incl - sur;   // lanes 0..15: surplus entries of classes < lane
-    // place every entry
-    for (int i0 = 0; i0 < L; i0 += 32) {
-      int i = i0 + lane;
-      int c = i < L ? (scol[i] & 15) : 0;
-      int64_t pre = __shfl_sync(0xffffffffu, excl, c);
-      if (i < L) {
-        int rk = srank[i];
-        int64_t slots = bo_count(c, P1) - bo_count(c, P0);
-        int64_t q;
-        if (rk < slots) q = bo_slot(c, bo_count(c, P0) + rk) - P0;
-        else q = sempty[pre + (rk - slots)];
-        hcol[s + q] = scol[i];
-        hval[s + q] = sval[i];
+    const int excl = incl - sur;
+    // pass 3: rank within the class (order of appearance) and placement
+    for (int64_t i0 = 0; i0 < L; i0 += 32) {
+      int64_t i = i0 + lane;
+      bool v = i < L;
+      uint16_t f = v ? icol[s + i] : 0;
+      int c = v ? (f & (NC - 1)) : NC + lane;
+      unsigned same = __match_any_sync(0xffffffffu, c);
+      int base_c = v ? run[w][c] : 0;
+      int pre = __shfl_sync(0xffffffffu, excl, c & (NC - 1));
+      __syncwarp();
+      if (v) {
+        int rk = base_c + __popc(same & lt);
+        if ((same & lt) == 0) run[w][c] = base_c + __popc(same);
+        int64_t slots = bo_count<NC>(c, P1) - bo_count<NC>(c, P0);
+        int64_t q = rk < slots ? bo_slot<NC>(c, bo_count<NC>(c, P0) + rk) - P0
+                               : (int64_t)sempty[w][pre + (rk - slots)];
+        ocol[s + q] = f;
+        oval[s + q] = ival[s + i];
       }
+      __syncwarp();
     }
-    __syncwarp();
   }
 }
 
@@ -1204,6 +1214,22 @@ static void rb_build(sv_context* ctx, const sv_counts* C, const sv_data* data, c
               (const int64_t*)src.get(), (const int64_t*)rb_ptr.get(), (const int32_t*)C->csc_rowidx.get(),
               (const __nv_bfloat16*)data->csc_val.get(), np, nf, rb_idx.get(),
               (__nv_bfloat16*)rb_val.get(), row0);
+  if (!getenv("SV_NO_BANKORDER")) {
+    // bank-aware order of every (row block, feature) run (X^T u gathers u by row)
+    DevBuf<uint16_t> idx2(std::max<int64_t>(1, nnz_h));
+    DevBuf<unsigned char> val2(std::max<int64_t>(1, nnz_h) * es2);
+    int bgrid = ctx->num_sms * 8;
+    if (data->dtype == SV_F32)
+      sv_launch(ctx, "scale_rb_order", k_bankorder<32, float>, dim3(bgrid), dim3(BO_WARPS * 32), 0,
+                (const int64_t*)rb_ptr.get(), np, (const uint16_t*)rb_idx.get(), (const float*)rb_val.get(),
+                idx2.get(), (float*)val2.get());
+    else
+      sv_launch(ctx, "scale_rb_order", k_bankorder<32, uint16_t>, dim3(bgrid), dim3(BO_WARPS * 32), 0,
+                (const int64_t*)rb_ptr.get(), np, (const uint16_t*)rb_idx.get(), (const uint16_t*)rb_val.get(),
+                idx2.get(), (uint16_t*)val2.get());
+    rb_idx = std::move(idx2);
+    rb_val = std::move(val2);
+  }
   sv_sync(ctx);
 }
 
@@ -1342,20 +1368,20 @@ static sv_centered* make_centered(sv_context* ctx, const sv_data* data, const st
     }
 #undef LAUNCH_HW
     if (small && data->dtype != SV_F64 && !getenv("SV_NO_BANKORDER")) {
-      size_t bsm = (size_t)BO_WARPS * BO_MAX * (6 + sv_elem_size(data->dtype));
-      int bgrid = ctx->num_sms * 2;
-      if (data->dtype == SV_F32) {
-        SV_CUDA(cudaFuncSetAttribute(k_hsub_bankorder<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)bsm));
-        sv_launch(ctx, "scale_hsub_order", k_hsub_bankorder<float>, dim3(bgrid), dim3(BO_WARPS * 32), bsm,
-                  (const int64_t*)S->h_rowptr.get(), C->n_cells, S->h_col16.get(), (float*)S->h_val.get());
-      } else {
-        SV_CUDA(cudaFuncSetAttribute(k_hsub_bankorder<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)bsm));
-        sv_launch(ctx, "scale_hsub_order", k_hsub_bankorder<uint16_t>, dim3(bgrid), dim3(BO_WARPS * 32), bsm,
-                  (const int64_t*)S->h_rowptr.get(), C->n_cells, S->h_col16.get(),
-                  (uint16_t*)S->h_val.get());
-      }
+      // bank-aware order of the rows (into a second copy, then swapped in)
+      DevBuf<uint16_t> col2(std::max<int64_t>(1, nnz_h));
+      DevBuf<unsigned char> val2(std::max<int64_t>(1, nnz_h) * es);
+      int bgrid = ctx->num_sms * 8;
+      if (data->dtype == SV_F32)
+        sv_launch(ctx, "scale_hsub_order", k_bankorder<16, float>, dim3(bgrid), dim3(BO_WARPS * 32), 0,
+                  (const int64_t*)S->h_rowptr.get(), C->n_cells, (const uint16_t*)S->h_col16.get(),
+                  (const float*)S->h_val.get(), col2.get(), (float*)val2.get());
+      else
+        sv_launch(ctx, "scale_hsub_order", k_bankorder<16, uint16_t>, dim3(bgrid), dim3(BO_WARPS * 32), 0,
+                  (const int64_t*)S->h_rowptr.get(), C->n_cells, (const uint16_t*)S->h_col16.get(),
+                  (const uint16_t*)S->h_val.get(), col2.get(), (uint16_t*)val2.get());
+      S->h_col16 = std::move(col2);
+      S->h_val = std::move(val2);
     }
     S->u_f32.alloc(C->n_cells);
     S->scal.alloc(64);
@@ -1476,7 +1502,69 @@ SV_API int sv_scale_features(sv_context* ctx, const sv_data* data, const int64_t
 // subset copies are those of the stacked matrix; the per-(sample, feature)
 // moments, the X v block schedule and the sample-aligned row blocks of X^T u
 // are the batch's own.  FP32 / BF16 storage.
-constexpr int BATCH_XCELLS = 256;   // cells per X v block (32 per warp)
+// cells per X v block: chosen by timing the candidates on the first batch of a
+// given shape (device, cells, features, samples), then reused
+static const int BATCH_XCELLS_CAND[] = {128, 256, 512, 1024};
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int64_t, int64_t, int64_t>, int> g_tune;
+
+static void batch_xschedule(sv_context* ctx, sv_batch* B, int cells) {
+  std::vector<BlkRange> hb;
+  for (int64_t s2 = 0; s2 < B->nseg; ++s2)
+    for (int64_t r = B->hoff[s2]; r < B->hoff[s2 + 1]; r += cells) {
+      BlkRange b;
+      b.r0 = r;
+      b.r1 = std::min(B->hoff[s2 + 1], r + cells);
+      b.seg = (int)s2;
+      b.pad = 0;
+      hb.push_back(b);
+    }
+  B->nxblk = (int)hb.size();
+  B->xblk.alloc(hb.size());
+  sv_h2d(ctx, B->xblk.get(), hb.data(), hb.size() * sizeof(BlkRange));
+  B->xcells = cells;
+}
+
+void sv_batch_apply_N_df(sv_context* ctx, const sv_batch* b, const float* xh, const float* xl,
+                         float* yh, float* yl, const double* csub, const float* zh, const float* zl,
+                         const int* active);
+
+// the autotuner: time every candidate block size on this batch (zero vectors)
+static int batch_tune_xcells(sv_context* ctx, sv_batch* B) {
+  auto key = std::make_tuple(ctx->device, B->n_cells, B->nf, B->nseg);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) return it->second;
+  }
+  DevBuf<float> xh((size_t)B->nseg * B->nf), yh(B->n_cells), yl(B->n_cells);
+  sv_memset(ctx, xh.get(), 0, (size_t)B->nseg * B->nf * 4);
+  cudaEvent_t e0, e1;
+  SV_CUDA(cudaEventCreate(&e0));
+  SV_CUDA(cudaEventCreate(&e1));
+  int best = BATCH_XCELLS_CAND[1];
+  float best_ms = 1e30f;
+  for (int cand : BATCH_XCELLS_CAND) {
+    batch_xschedule(ctx, B, cand);
+    sv_batch_apply_N_df(ctx, B, xh.get(), xh.get(), yh.get(), yl.get(), nullptr, nullptr, nullptr, nullptr);
+    SV_CUDA(cudaEventRecord(e0, ctx->stream));
+    for (int r = 0; r < 3; ++r)
+      sv_batch_apply_N_df(ctx, B, xh.get(), xh.get(), yh.get(), yl.get(), nullptr, nullptr, nullptr, nullptr);
+    SV_CUDA(cudaEventRecord(e1, ctx->stream));
+    SV_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    SV_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = cand;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = best;
+  return best;
+}
 
 SV_API int sv_batch_create(sv_context* ctx, const sv_data* data, const int64_t* cell_offsets,
                            int64_t nseg, const int64_t* features, int64_t nfeatures, double scale_max,
@@ -1532,22 +1620,6 @@ SV_API int sv_batch_create(sv_context* ctx, const sv_data* data, const int64_t* 
 #undef LAUNCH_BMOM
     sv_launch(ctx, "scale_mu_split", k_split_df, dim3(sv_grid_for(ctx, (int64_t)sf, 256)), dim3(256), 0,
               (const double*)B->mu.get(), (int64_t)sf, B->mu_h.get(), B->mu_l.get());
-    // X v schedule: BATCH_XCELLS cells of one sample per block
-    {
-      std::vector<BlkRange> hb;
-      for (int64_t s2 = 0; s2 < nseg; ++s2)
-        for (int64_t r = B->hoff[s2]; r < B->hoff[s2 + 1]; r += BATCH_XCELLS) {
-          BlkRange b;
-          b.r0 = r;
-          b.r1 = std::min(B->hoff[s2 + 1], r + BATCH_XCELLS);
-          b.seg = (int)s2;
-          b.pad = 0;
-          hb.push_back(b);
-        }
-      B->nxblk = (int)hb.size();
-      B->xblk.alloc(hb.size());
-      sv_h2d(ctx, B->xblk.get(), hb.data(), hb.size() * sizeof(BlkRange));
-    }
     // X^T u: row blocks of at most RB_ROWS cells, aligned to the samples
     {
       std::vector<int64_t> row0;
@@ -1577,6 +1649,8 @@ SV_API int sv_batch_create(sv_context* ctx, const sv_data* data, const int64_t* 
       SV_CUDA(cudaFuncSetAttribute(k_spmv_rb<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)(RB_ROWS * sizeof(float))));
     }
+    // X v schedule: cells of one sample per block, the block size tuned once per shape
+    batch_xschedule(ctx, B, batch_tune_xcells(ctx, B));
     sv_sync(ctx);
   } catch (...) {
     if (B->base) sv_centered_free(B->base);
@@ -1593,6 +1667,14 @@ SV_API int sv_batch_info(const sv_batch* b, int64_t* nseg, int64_t* n_cells, int
   if (nseg) *nseg = b->nseg;
   if (n_cells) *n_cells = b->n_cells;
   if (nf) *nf = b->nf;
+  SV_CATCH
+}
+
+// the X v block size (cells per block) the autotuner chose for this batch's shape
+SV_API int sv_batch_tuning(const sv_batch* b, int64_t* cells_per_block) {
+  SV_TRY
+  SV_REQUIRE(b, "null handle");
+  if (cells_per_block) *cells_per_block = b->xcells;
   SV_CATCH
 }
 
