@@ -389,3 +389,97 @@ void sv_scan_i64(sv_context* ctx, const int64_t* in, int64_t* out, int64_t n) {
   // the temporaries are released on return: finish their last use first
   sv_sync(ctx);
 }
+
+// ---- bitonic sort of (key, value) pairs ------------------------------------------
+// Sorts n pairs by key (ascending; equal keys in no particular order) in place,
+// padding to a power of two with the largest key.  Strides below 1024 run in
+// shared memory (2048 pairs per block), larger strides one launch each.
+namespace {
+
+__global__ void k_bitonic_pad(unsigned long long* __restrict__ key, int* __restrict__ val, int64_t n,
+                              int64_t n2) {
+  for (int64_t i = n + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    key[i] = ~0ull;
+    val[i] = -1;
+  }
+}
+
+__device__ __forceinline__ void bitonic_cas(unsigned long long& ka, int& va, unsigned long long& kb, int& vb,
+                                            bool up) {
+  if ((ka > kb) == up) {
+    unsigned long long tk = ka;
+    ka = kb;
+    kb = tk;
+    int tv = va;
+    va = vb;
+    vb = tv;
+  }
+}
+
+// one global step: stride j of the merge of size k
+__global__ void k_bitonic_global(unsigned long long* __restrict__ key, int* __restrict__ val, int64_t n2,
+                                 int64_t k, int64_t j) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n2 / 2;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = (t / j) * 2 * j + (t % j);
+    int64_t l = i + j;
+    bool up = (i & k) == 0;
+    unsigned long long ka = key[i], kb = key[l];
+    int va = val[i], vb = val[l];
+    bitonic_cas(ka, va, kb, vb, up);
+    key[i] = ka;
+    key[l] = kb;
+    val[i] = va;
+    val[l] = vb;
+  }
+}
+
+// every stride j <= 1024 of the merges of size k (kfrom .. kto) in shared memory,
+// 2048 pairs per block
+__global__ void __launch_bounds__(1024) k_bitonic_smem(unsigned long long* __restrict__ key,
+                                                       int* __restrict__ val, int64_t kfrom, int64_t kto,
+                                                       int64_t jfrom) {
+  __shared__ unsigned long long sk[2048];
+  __shared__ int sv[2048];
+  int64_t base = (int64_t)blockIdx.x * 2048;
+  for (int i = threadIdx.x; i < 2048; i += blockDim.x) {
+    sk[i] = key[base + i];
+    sv[i] = val[base + i];
+  }
+  __syncthreads();
+  for (int64_t k = kfrom; k <= kto; k <<= 1) {
+    for (int64_t j = (k == kfrom ? jfrom : k >> 1); j > 0; j >>= 1) {
+      int t = threadIdx.x;
+      int i = (int)((t / j) * 2 * j + (t % j));
+      int l = i + (int)j;
+      bool up = ((base + i) & k) == 0;
+      bitonic_cas(sk[i], sv[i], sk[l], sv[l], up);
+      __syncthreads();
+    }
+  }
+  for (int i = threadIdx.x; i < 2048; i += blockDim.x) {
+    key[base + i] = sk[i];
+    val[base + i] = sv[i];
+  }
+}
+
+}  // namespace
+
+// key / val hold n2 >= n entries (n2 = next power of two, at least 2048)
+void sv_sort_pairs(sv_context* ctx, unsigned long long* key, int* val, int64_t n, int64_t n2) {
+  if (n2 > n)
+    sv_launch(ctx, "sort_pad", k_bitonic_pad, dim3(sv_grid_for(ctx, n2 - n, 256)), dim3(256), 0, key, val, n,
+              n2);
+  int64_t blocks = n2 / 2048;
+  // merges of size up to 2048 entirely in shared memory
+  sv_launch(ctx, "sort_smem", k_bitonic_smem, dim3((unsigned)blocks), dim3(1024), 0, key, val, (int64_t)2,
+            (int64_t)2048, (int64_t)1);
+  for (int64_t k = 4096; k <= n2; k <<= 1) {
+    for (int64_t j = k >> 1; j >= 2048; j >>= 1)
+      sv_launch(ctx, "sort_global", k_bitonic_global, dim3(sv_grid_for(ctx, n2 / 2, 256)), dim3(256), 0, key,
+                val, n2, k, j);
+    sv_launch(ctx, "sort_smem", k_bitonic_smem, dim3((unsigned)blocks), dim3(1024), 0, key, val, k, k,
+              (int64_t)1024);
+  }
+}

@@ -328,3 +328,6 @@ int sv_grid_for(sv_context* ctx, int64_t work_items, int per_block, int max_per_
 // builds (or rebuilds) the CSR copy of a count matrix from its device CSC copy
 // (sv_counts.cu); checks the CSC invariants on the way
 void sv_build_csr_from_csc(sv_context* ctx, sv_counts* c);
+// sorts (key, value) pairs by key on the device; the arrays hold n2 entries, n2
+// a power of two >= max(n, 2048) (sv_core.cu)
+void sv_sort_pairs(sv_context* ctx, unsigned long long* key, int* val, int64_t n, int64_t n2);

@@ -27,6 +27,7 @@
 #include "sv_internal.cuh"
 #include <math.h>
 #include <stdlib.h>
+#include <string.h>
 
 void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const double* x, double* y,
                        double alpha, double beta, const double* csub, const double* z);
@@ -1058,6 +1059,7 @@ struct Lanczos {
   int* hflags = nullptr;        // pinned staging of the active / finish masks
   double eps_b = 0;
   int cgs_blocks = RED_BLOCKS;  // resident blocks of the CGS kernels (one wave)
+  bool vside_multi = false;     // feature side through the multi-block kernels
   // graphs of the first cycle and of restart cycles from basis set 0 / set 1
   CycleGraph graphs[3];
 
@@ -1081,6 +1083,15 @@ struct Lanczos {
     };
     Ws.alloc(ctx, woff, work, red_target(m), rows_target(m));
     Vs.alloc(ctx, voff, work, red_target(n), rows_target(n));
+    {
+      const char* mode = getenv("SV_VSIDE");
+      // one sample: the multi-block kernels (one 1024-thread block per step
+      // measured 0.17 ms against ~0.05 ms for the five multi-block launches at
+      // 3,000 features); several samples: one block per sample in one launch
+      vside_multi = Vs.max_seg > 32768 || (nseg == 1 && Vs.len >= 1024);
+      if (mode && strcmp(mode, "multi") == 0) vside_multi = true;
+      if (mode && strcmp(mode, "block") == 0 && Vs.max_seg <= 32768) vside_multi = false;
+    }
     ytmp.alloc(std::max(m, n));
     F.alloc(n);
     B.alloc((size_t)nseg * work * work);
@@ -1179,10 +1190,11 @@ struct Lanczos {
               s.bl() + (int64_t)j * s.len, flag.get());
   }
 
-  // the feature-side step, one block per sample (see k_vside)
+  // the feature-side step: one block per sample (k_vside), or the multi-block
+  // CGS kernels over the feature side (SV_VSIDE=multi|block forces either)
   void vside(int ncols, int write_col, double* nrm, const double* c, int64_t boff, uint64_t seed,
              unsigned step) {
-    if (Vs.max_seg > 32768) {   // long feature side: the multi-block kernels
+    if (vside_multi) {
       orth_norm(Vs, F.get(), ncols, nrm);
       if (write_col >= 0) scal_fix(Vs, write_col, nrm, c, boff, seed, step);
       return;

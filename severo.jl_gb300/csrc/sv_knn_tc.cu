@@ -195,6 +195,21 @@ __device__ __forceinline__ uint32_t chunk_mask(float (&acc)[32], const float* __
   return m;
 }
 
+// The j-th point tile a CTA visits: with the points in locality order, the
+// tiles nearest to the CTA's own queries first (alternately above and below),
+// so that the top-k thresholds fall early and later tiles rarely hold a
+// candidate; otherwise in order.
+__device__ __forceinline__ int tile_at(int j, int t0, int ntiles, bool around) {
+  if (!around) return j;
+  int L = t0, R = ntiles - 1 - t0, k = min(L, R);
+  if (j == 0) return t0;
+  if (j <= 2 * k) {
+    int m = (j + 1) >> 1;
+    return (j & 1) ? t0 + m : t0 - m;
+  }
+  return R > L ? t0 + (j - k) : t0 - (j - k);
+}
+
 // FOLD: |p|^2 is part of the MMA (see k_pack_fold): the accumulator is
 // D = q.p - |p|^2 / 2 and key = -2 D, so no norm is loaded in the epilogue and a
 // 32-candidate chunk is rejected by one compare of its maximum D.
@@ -202,7 +217,7 @@ template <bool FOLD>
 __global__ void __launch_bounds__(THREADS, 1)
     k_knn_tc(const __grid_constant__ CUtensorMap tmapA, const __grid_constant__ CUtensorMap tmapB,
              const float* __restrict__ sqpad, int64_t n, int ntiles, int32_t* __restrict__ cand,
-             int* __restrict__ status, const int64_t* __restrict__ sched) {
+             int* __restrict__ status, const int64_t* __restrict__ sched, int around) {
   extern __shared__ unsigned char smem_raw[];
   Smem* s = (Smem*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -216,6 +231,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     pend = sched[4 * blockIdx.x + 3];
     ntiles = (int)((pend - p0 + BN - 1) / BN);
   }
+  // the point tile that holds this CTA's first query
+  int64_t tq = (q0 - p0) / BN;
+  const int t0 = tq < 0 ? 0 : (tq > ntiles - 1 ? ntiles - 1 : (int)tq);
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < STAGES; ++i) {
@@ -254,7 +272,8 @@ __global__ void __launch_bounds__(THREADS, 1)
         uint32_t ph = (t / STAGES) & 1;
         if (!mbar_wait(&s->empty[st], ph ^ 1, &s->err)) break;
         mbar_expect_tx(&s->full[st], BN * BK * 2);
-        tma_load_2d(s->B[st], &tmapB, 0, (int)(p0 + (int64_t)t * BN), &s->full[st]);
+        tma_load_2d(s->B[st], &tmapB, 0, (int)(p0 + (int64_t)tile_at(t, t0, ntiles, around) * BN),
+                    &s->full[st]);
         issued = t + 1;
       }
       // drain: every issued copy has landed before the CTA may exit
@@ -320,7 +339,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       bool ok = mbar_wait(&s->tfull[ab], aph, &s->err);
       if (!__all_sync(0xffffffffu, ok)) break;   // warp-uniform: the TMEM loads are .aligned
       fence_after();
-      int64_t j0 = p0 + (int64_t)t * BN + half * (BN / 2);
+      int64_t j0 = p0 + (int64_t)tile_at(t, t0, ntiles, around) * BN + half * (BN / 2);
       uint32_t tbase = tmem + lane_off + (uint32_t)(ab * BN + half * (BN / 2));
       // two chunks per TMEM round trip: both loads are issued before one wait
 #pragma unroll 1
@@ -403,7 +422,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 // FP32 row-major [n][dp] -> BF16 row-major [n][64] (zero padded) and the FP32 squared
 // norms of the rounded rows, padded with FLT_MAX up to npad.
 __global__ void k_pack_bf16(const float* __restrict__ X, int64_t n, int dp, int64_t npad,
-                            __nv_bfloat16* __restrict__ Xb, float* __restrict__ sq) {
+                            __nv_bfloat16* __restrict__ Xb, float* __restrict__ sq,
+                            const int* __restrict__ perm) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npad;
        i += (int64_t)gridDim.x * blockDim.x) {
     if (i >= n) {
@@ -411,8 +431,9 @@ __global__ void k_pack_bf16(const float* __restrict__ X, int64_t n, int dp, int6
       continue;
     }
     float s = 0.f;
+    const int64_t src = perm ? perm[i] : i;
     for (int c = 0; c < BK; ++c) {
-      float v = c < dp ? X[i * dp + c] : 0.f;
+      float v = c < dp ? X[src * dp + c] : 0.f;
       __nv_bfloat16 b = __float2bfloat16_rn(v);
       Xb[i * BK + c] = b;
       float r = __bfloat162float(b);
@@ -427,12 +448,14 @@ __global__ void k_pack_bf16(const float* __restrict__ X, int64_t n, int dp, int6
 // summing to the FP32 norm of the rounded row to ~2^-24), so that the MMA yields
 // D = q.p - |p|^2/2 and the key |p|^2 - 2 q.p is -2 D.
 __global__ void k_pack_fold(const float* __restrict__ X, int64_t n, int dp, int d,
-                            __nv_bfloat16* __restrict__ Xq, __nv_bfloat16* __restrict__ Xp) {
+                            __nv_bfloat16* __restrict__ Xq, __nv_bfloat16* __restrict__ Xp,
+                            const int* __restrict__ perm) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     float s = 0.f;
+    const int64_t src = perm ? perm[i] : i;
     for (int c = 0; c < BK; ++c) {
-      float v = c < d ? X[i * dp + c] : 0.f;
+      float v = c < d ? X[src * dp + c] : 0.f;
       __nv_bfloat16 b = __float2bfloat16_rn(v);
       Xq[i * BK + c] = b;
       Xp[i * BK + c] = b;
@@ -450,6 +473,59 @@ __global__ void k_pack_fold(const float* __restrict__ X, int64_t n, int dp, int 
     Xp[i * BK + d] = p1;
     Xp[i * BK + d + 1] = p2;
     Xp[i * BK + d + 2] = p3;
+  }
+}
+
+// ---- locality order of the points ----------------------------------------------
+// Per-dimension sums and sums of squares (FP64, atomics: only the choice of the
+// widest dimension depends on them).
+__global__ void k_dim_moments(const float* __restrict__ X, int64_t n, int dp, double* __restrict__ acc) {
+  __shared__ double s1[256], s2[256];
+  const int c = threadIdx.x % dp, r0 = threadIdx.x / dp, rstep = blockDim.x / dp;
+  double a = 0, b = 0;
+  if (r0 < rstep)
+    for (int64_t i = blockIdx.x * (int64_t)rstep + r0; i < n; i += (int64_t)gridDim.x * rstep) {
+      double v = X[i * dp + c];
+      a += v;
+      b += v * v;
+    }
+  s1[threadIdx.x] = a;
+  s2[threadIdx.x] = b;
+  __syncthreads();
+  if (threadIdx.x < dp) {
+    double ta = 0, tb = 0;
+    for (int r = 0; r < rstep; ++r) {
+      ta += s1[r * dp + threadIdx.x];
+      tb += s2[r * dp + threadIdx.x];
+    }
+    atomicAdd(acc + threadIdx.x, ta);
+    atomicAdd(acc + dp + threadIdx.x, tb);
+  }
+}
+
+// sort key: sample in the high word, the coordinate (order-preserving bits) low
+__global__ void k_locality_keys(const float* __restrict__ X, int dp, int dim, const int64_t* __restrict__ off,
+                                int nseg, int64_t n, unsigned long long* __restrict__ key, int* __restrict__ val) {
+  const int sg = blockIdx.y;
+  const int64_t a = off ? off[sg] : 0, b = off ? off[sg + 1] : n;
+  for (int64_t i = a + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < b;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    unsigned u = __float_as_uint(X[i * dp + dim]);
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    key[i] = ((unsigned long long)sg << 32) | u;
+    val[i] = (int)i;
+  }
+}
+
+// candidates found in locality order -> original point and query indices
+__global__ void k_cand_unperm(const int32_t* __restrict__ cs, const int* __restrict__ perm, int64_t n, int K2,
+                              int32_t* __restrict__ co) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n * K2;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t q = e / K2;
+    int t = (int)(e - q * K2);
+    int32_t c = cs[e];
+    co[(int64_t)perm[q] * K2 + t] = c >= 0 ? perm[c] : -1;
   }
 }
 
@@ -485,16 +561,54 @@ int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unus
     // one spare tile of padding: a sample's last tile may start anywhere
     int64_t npad = (int64_t)(ntiles + 1) * BN;
     bool fold = d + 3 <= BK && !getenv("SV_KNN_NOFOLD");
+    // locality order: the points sorted (within each sample) along their widest
+    // dimension, and every CTA visiting the tiles around its own queries first
+    bool around = !getenv("SV_KNN_NOSORT") && n >= 4 * BN;
+    DevBuf<int> perm;
+    if (around) {
+      int nseg = segs ? (int)segs->size() - 1 : 1;
+      DevBuf<double> mom(2 * dp);
+      sv_memset(ctx, mom.get(), 0, 2 * dp * 8);
+      sv_launch(ctx, "knn_order", k_dim_moments, dim3(sv_grid_for(ctx, n, 256, 2)), dim3(256 / dp * dp), 0,
+                X32, n, dp, mom.get());
+      std::vector<double> hm(2 * dp);
+      sv_d2h(ctx, hm.data(), mom.get(), 2 * dp * 8);
+      int dim = 0;
+      double best = -1;
+      for (int c = 0; c < d; ++c) {
+        double mean = hm[c] / (double)n, var = hm[dp + c] / (double)n - mean * mean;
+        if (var > best) {
+          best = var;
+          dim = c;
+        }
+      }
+      int64_t n2 = 2048;
+      while (n2 < n) n2 <<= 1;
+      DevBuf<unsigned long long> key(n2);
+      perm.alloc(n2);
+      DevBuf<int64_t> doff;
+      if (segs) {
+        doff.alloc(segs->size());
+        sv_h2d(ctx, doff.get(), segs->data(), segs->size() * 8);
+      }
+      dim3 kg((unsigned)sv_grid_for(ctx, segs ? n / nseg + 1 : n, 256, 4), (unsigned)nseg);
+      sv_launch(ctx, "knn_order", k_locality_keys, kg, dim3(256), 0, X32, dp, dim,
+                segs ? (const int64_t*)doff.get() : (const int64_t*)nullptr, nseg, n, key.get(), perm.get());
+      sv_sort_pairs(ctx, key.get(), perm.get(), n, n2);
+    }
+    const int* pm = around ? (const int*)perm.get() : (const int*)nullptr;
     DevBuf<__nv_bfloat16> Xq((size_t)n * BK), Xp;
     DevBuf<float> sq(npad);
     if (fold) {
       Xp.alloc((size_t)n * BK);
       sv_launch(ctx, "knn_pack_fold", k_pack_fold, dim3(sv_grid_for(ctx, n, 256, 8)), dim3(256), 0, X32,
-                n, dp, d, Xq.get(), Xp.get());
+                n, dp, d, Xq.get(), Xp.get(), pm);
     } else {
       sv_launch(ctx, "knn_pack_bf16", k_pack_bf16, dim3(sv_grid_for(ctx, npad, 256, 8)), dim3(256), 0,
-                X32, n, dp, npad, Xq.get(), sq.get());
+                X32, n, dp, npad, Xq.get(), sq.get(), pm);
     }
+    DevBuf<int32_t> cand_sorted(around ? (size_t)n * K2 : 1);
+    int32_t* cout = around ? cand_sorted.get() : cand;
     // row-major BF16 operands, 64 elements (128 bytes, one swizzle row) wide: the
     // query box is 128 rows, the point box 256 rows
     CUtensorMap tmapA, tmapB;
@@ -532,12 +646,17 @@ int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unus
     if (fold) {
       SV_CUDA(cudaFuncSetAttribute(k_knn_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       sv_launch(ctx, "knn_tc_tiles", k_knn_tc<true>, dim3(nblocks), dim3(THREADS), smem, tmapA, tmapB,
-                (const float*)sq.get(), n, ntiles, cand, ctx->d_status, (const int64_t*)sched.get());
+                (const float*)sq.get(), n, ntiles, cout, ctx->d_status, (const int64_t*)sched.get(),
+                (int)around);
     } else {
       SV_CUDA(cudaFuncSetAttribute(k_knn_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       sv_launch(ctx, "knn_tc_tiles", k_knn_tc<false>, dim3(nblocks), dim3(THREADS), smem, tmapA, tmapB,
-                (const float*)sq.get(), n, ntiles, cand, ctx->d_status, (const int64_t*)sched.get());
+                (const float*)sq.get(), n, ntiles, cout, ctx->d_status, (const int64_t*)sched.get(),
+                (int)around);
     }
+    if (around)
+      sv_launch(ctx, "knn_unperm", k_cand_unperm, dim3(sv_grid_for(ctx, n * K2, 256, 8)), dim3(256), 0,
+                (const int32_t*)cand_sorted.get(), pm, n, K2, cand);
     sv_check_device_status(ctx, "tensor-core kNN");
   } catch (const SvError& e) {
     return e.code;

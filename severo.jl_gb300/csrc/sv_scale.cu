@@ -191,6 +191,9 @@ __global__ void k_hsub_write(const int64_t* __restrict__ rowptr, const int32_t* 
 // Entries of class c fill the c-slots in order of appearance; the surplus of
 // over-full classes fills the slots left empty, in slot order.  The segment's
 // sum is then taken in another order (a different, equally valid rounding).
+// Applied to the CSR_h rows (X v: 1.61 -> 1.52 ms per product at the atlas
+// size, for ~16 ms once per scale_features); for the row-blocked runs (NC = 32)
+// the product gained 1% and the reordering cost more than it saved.
 constexpr int BO_EMPTY = 1024;   // most empty slots a segment may have to be reordered
 constexpr int BO_WARPS = 8;
 
@@ -574,6 +577,9 @@ __global__ void __launch_bounds__(256) k_spmv_csr_df(
     int64_t s = rowptr[r], e = rowptr[r + 1];
     int64_t a0 = s & ~3ll;
     float acc = 0.f;
+    // two 4-element groups per lane in flight, the first load pair
+    // unconditional (a loop over guarded groups -- 2 or 4 of them -- measured
+    // 20-30% slower at the atlas size)
     for (int64_t g = a0 + 4 * lane; g < e; g += 256) {
       int ci[2][4];
       float av[2][4];
@@ -1214,22 +1220,6 @@ static void rb_build(sv_context* ctx, const sv_counts* C, const sv_data* data, c
               (const int64_t*)src.get(), (const int64_t*)rb_ptr.get(), (const int32_t*)C->csc_rowidx.get(),
               (const __nv_bfloat16*)data->csc_val.get(), np, nf, rb_idx.get(),
               (__nv_bfloat16*)rb_val.get(), row0);
-  if (!getenv("SV_NO_BANKORDER")) {
-    // bank-aware order of every (row block, feature) run (X^T u gathers u by row)
-    DevBuf<uint16_t> idx2(std::max<int64_t>(1, nnz_h));
-    DevBuf<unsigned char> val2(std::max<int64_t>(1, nnz_h) * es2);
-    int bgrid = ctx->num_sms * 8;
-    if (data->dtype == SV_F32)
-      sv_launch(ctx, "scale_rb_order", k_bankorder<32, float>, dim3(bgrid), dim3(BO_WARPS * 32), 0,
-                (const int64_t*)rb_ptr.get(), np, (const uint16_t*)rb_idx.get(), (const float*)rb_val.get(),
-                idx2.get(), (float*)val2.get());
-    else
-      sv_launch(ctx, "scale_rb_order", k_bankorder<32, uint16_t>, dim3(bgrid), dim3(BO_WARPS * 32), 0,
-                (const int64_t*)rb_ptr.get(), np, (const uint16_t*)rb_idx.get(), (const uint16_t*)rb_val.get(),
-                idx2.get(), (uint16_t*)val2.get());
-    rb_idx = std::move(idx2);
-    rb_val = std::move(val2);
-  }
   sv_sync(ctx);
 }
 

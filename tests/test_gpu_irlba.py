@@ -159,3 +159,19 @@ def test_irlba_graph_replay_matches_direct_launches(sv, ctx, monkeypatch, rank):
     assert np.max(np.abs(sg - ss[:nu]) / ss[:nu]) < 1e-5
     if rank is None:
         assert ig["iters"] > 2   # several replays of the restart graphs
+
+
+def test_feature_side_paths_agree(sv, ctx, O, monkeypatch):
+    """The feature-side step in one block per sample (k_vside) and through the
+    multi-block CGS kernels give the same embedding (reduction order only)."""
+    X = O.synth_counts(3000, 1500, -1.2, 1.6, depth=0.3, seed=33, n_clusters=5)
+    d = sv.normalize_cells(X, scale_factor=1e4, dtype="float32", ctx=ctx)
+    ref = O.normalize_cells(X, scale_factor=1e4, dtype=np.float32).astype(np.float64)
+    hvf = O.top_variable_genes(ref, 400)
+    S = sv.scale_features(d, scale_max=10.0, features=hvf)
+    init = np.random.default_rng(5).standard_normal(400)
+    out = {}
+    for mode in ("block", "multi"):
+        monkeypatch.setenv("SV_VSIDE", mode)
+        out[mode] = sv.pca(S, 10, tol=1e-8, init=init).stdev
+    assert np.max(np.abs(out["block"] - out["multi"]) / out["block"]) < 1e-7
