@@ -4,7 +4,9 @@ scale_features (3,000 features, implicit centre/scale/clip) -> irlba PCA (50)
 -> kNN (20), on one GB300, with counts already resident in HBM.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload atlas|plain|small] [--cells N]
+                    [--workload atlas|plain|small] [--cells N] [--batched] [--reader]
+                    [--kernel-case irlba|knn] [--no-e2e] [--no-fp32] [--no-cpu]
+                    [--no-accuracy] [--no-knn-stress]
 
 Prints one JSON line (rank 0).  Workload "atlas": 1,300,000 cells x 27,998
 genes, ~2,000 non-zeros per cell, 40 latent clusters, values stored in BF16
@@ -12,7 +14,11 @@ with FP32 product accumulation and FP64 Lanczos reorthogonalisation/restart.
 The plain-FP32 form of the same pipeline is timed on the same data for the
 mixed-vs-FP32 ratio.  Data: seeded synthetic negative-binomial counts (no
 public dataset is read).  --impl reference times the CPU oracle (the
-restatement of the reference's CPU path) on a bounded sample.
+restatement of the reference's CPU path) on a bounded sample.  --batched runs
+the batched-samples workload (64 samples of 500-50,000 cells: one launch per
+stage for all samples against one sample after another); --reader times the
+MatrixMarket reader (text in host memory to the device count matrix);
+--kernel-case runs one small case of a kernel family for profiler captures.
 """
 from __future__ import annotations
 
@@ -281,7 +287,8 @@ def roofline(rep, S_nnz, n_cells, n_hvf, dtype, peaks):
     """Roofline of the dominant HBM-bound kernel pair (the implicit SpMV)."""
     v = {"bfloat16": 2, "float32": 4, "float64": 8}[dtype]
     idx = 2 if n_hvf <= 65536 else 4
-    # bytes per launch (the algorithmic traffic, see DESIGN.md)
+    # algorithmic bytes per launch: every stored entry (index + value) once, the
+    # row pointers, and the input / output vectors
     csr = S_nnz * (idx + v) + 8 * (n_cells + 1) + 8 * n_cells
     csc = S_nnz * (4 + v) + 4 * n_cells
     out = {}
@@ -342,11 +349,15 @@ def main():
     ap.add_argument("--no-knn-stress", action="store_true")
     ap.add_argument("--kernel-case", choices=["irlba", "knn"], default=None,
                     help="run one small case of a kernel family (for profiler captures) and exit")
+    ap.add_argument("--reader", action="store_true",
+                    help="MatrixMarket reader: 10X-layout text in host memory to the device count matrix")
     ap.add_argument("--batched", action="store_true",
                     help="the batched-samples workload (64 samples) instead of the atlas")
     args = ap.parse_args()
     if args.kernel_case:
         return kernel_case(args)
+    if args.reader:
+        return reader_bench(args)
     if args.batched:
         return batched_bench(args)
     w = dict(WORKLOADS[args.workload])
@@ -589,6 +600,150 @@ def batched_bench(args):
         "stdev_rel_diff_batched_vs_loop_max": err,
         "gpu_launches": int(lb),
         "clocks": clocks,
+    }
+    print(json.dumps(out))
+
+
+def _digit_table(vals, width):
+    """Fixed-width digit rows of vals (ASCII) and the mask of their significant digits."""
+    d = (vals[:, None] // (10 ** np.arange(width - 1, -1, -1, dtype=np.int64))[None, :]) % 10
+    nz = np.logical_or.accumulate(d != 0, axis=1)
+    nz[:, -1] = True
+    return (d + 48).astype(np.uint8), nz
+
+
+def mm_format(gene, cell, cnt, header, chunk=1 << 22):
+    """MatrixMarket text of 1-based (gene, cell, count) triplets, built in host
+    memory for the reader bench: digit rows are gathered from per-value tables
+    (counts beyond the table are formatted directly), then the leading zeros
+    are squeezed out chunk by chunk."""
+    widths = (5, 7, 10)
+    cols = [np.asarray(gene, np.int64), np.asarray(cell, np.int64), np.asarray(cnt, np.int64)]
+    tabs = []
+    for f, wd in zip(cols, widths):
+        if len(f) and (f.min() < 0 or f.max() >= 10 ** wd):
+            raise ValueError("field out of the formatter's range")
+        top = int(min(f.max(initial=0), 1 << 20)) + 1
+        tabs.append(_digit_table(np.arange(top, dtype=np.int64), wd))
+    parts = [header.encode()]
+    for a in range(0, len(cols[0]), chunk):
+        m = min(chunk, len(cols[0]) - a)
+        rows, keep = [], []
+        for j, (f, wd) in enumerate(zip(cols, widths)):
+            x = f[a:a + m]
+            T, K = tabs[j]
+            big = x >= len(T)
+            xi = np.where(big, 0, x)
+            r, k = T[xi], K[xi]
+            if big.any():
+                r[big], k[big] = _digit_table(x[big], wd)
+            rows += [r, np.full((m, 1), ord("\n") if j == 2 else ord(" "), np.uint8)]
+            keep += [k, np.ones((m, 1), bool)]
+        parts.append(np.concatenate(rows, axis=1)[np.concatenate(keep, axis=1)].tobytes())
+    return b"".join(parts)
+
+
+def reader_bench(args):
+    """MatrixMarket reader (readMM as read_10X uses it): a 10X-layout text file
+    (features x barcodes, entries ordered by cell) of seeded synthetic counts
+    held in host memory, parsed into the device count matrix (both copies).
+    Metric: text bytes per second, end to end through sv_counts_parse_mtx
+    (the host-to-device copy of the text inside the timed region).  CPU
+    baseline: the single-threaded C restatement of readMM + sparse + copy(X')
+    on a bounded sample."""
+    import __graft_entry__ as ge
+    ge._build_module().build()
+    sv = ge.load_package()
+    ctx = sv.Context(0)
+    w = dict(WORKLOADS["atlas"])
+    n = args.cells or 50_000
+    mu_g, s_c, cl, lfc = gen_params(w, n, SEED + 7)
+    D = calibrate_depth(mu_g, s_c, cl, lfc, w["nnz_per_cell"])
+    counts = sv.CountMatrix.generate(n, w["n_genes"], mu_g, s_c, cl, lfc, depth=D, dispersion=DISPERSION,
+                                     seed=SEED + 7, ctx=ctx)
+    R = counts.to_csr()
+    del counts
+    cell = np.repeat(np.arange(1, n + 1, dtype=np.int64), np.diff(R.indptr))
+    t0 = time.perf_counter()
+    text = mm_format(R.indices.astype(np.int64) + 1, cell, R.data,
+                     f"%%MatrixMarket matrix coordinate integer general\n%\n{w['n_genes']} {n} {R.nnz}\n")
+    gen_s = time.perf_counter() - t0
+    steps, warmup = max(1, args.steps), max(3, args.warmup)
+    for _ in range(warmup):
+        X = sv.CountMatrix.parse_mtx(text, True, ctx=ctx)
+        del X
+    ctx.sync()
+    clk = ClockSampler(0)
+    clk.start()
+    l0 = ctx.launches()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        X = sv.CountMatrix.parse_mtx(text, True, ctx=ctx)
+        del X
+    ctx.sync()
+    dt = (time.perf_counter() - t0) / steps
+    clocks = clk.stop()
+    launches = (ctx.launches() - l0) / steps
+    ctx.profile_reset()
+    ctx.profile(True)
+    X = sv.CountMatrix.parse_mtx(text, True, ctx=ctx)
+    ctx.sync()
+    rep = ctx.profile_report()
+    ctx.profile(False)
+    ok = X.nnz == R.nnz and np.array_equal(X.to_csr().indptr, R.indptr)
+    del X
+    kern = {k: {"launches": c, "ms": round(ms, 3)} for k, (c, ms) in
+            sorted(rep.items(), key=lambda kv: -kv[1][1])}
+    parse_ms = rep.get("mtx_parse", (1, float("nan")))[1]
+    nbytes = len(text)
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    # mtx_parse reads every text byte and 8 bytes of line end per entry, and
+    # writes 12 bytes per entry (cell, gene, count)
+    parse_bytes = nbytes + 20 * R.nnz
+    cpu = None
+    if not args.no_cpu:
+        from oracle import mtx as mo
+        ns = min(n, 4000)
+        hdr = f"%%MatrixMarket matrix coordinate integer general\n{w['n_genes']} {ns} {int(R.indptr[ns])}\n"
+        k = int(R.indptr[ns])
+        sample = mm_format(R.indices[:k].astype(np.int64) + 1, cell[:k], R.data[:k], hdr)
+        t0 = time.perf_counter()
+        reps = 0
+        while time.perf_counter() - t0 < 10.0 or reps == 0:
+            mo.parse(sample, True)
+            reps += 1
+        cs = (time.perf_counter() - t0) / reps
+        cpu = {"value": round(len(sample) / cs / 1e6, 2), "unit": "MB/s", "cores": 1, "kind": "port",
+               "sample": f"{ns} cells ({len(sample) / 1e6:.1f} MB) of the same file, C restatement of "
+                         f"readMM + sparse + copy(X'), single thread"}
+    out = {
+        "metric": "MatrixMarket text → device count matrix (CSC + CSR), bytes/s",
+        "value": round(nbytes / dt / 1e6, 1), "unit": "MB/s", "n_gpus": 1, "steps": steps,
+        "warmup": warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic: seeded negative-binomial counts written as 10X-layout MatrixMarket text",
+        "config": {"workload": f"reader: {n} cells x {w['n_genes']} genes, {R.nnz} entries, "
+                               f"{nbytes / 1e9:.2f} GB of text in host memory",
+                   "entries": int(R.nnz), "text_bytes": nbytes,
+                   "l2": "text larger than L2 (129 MB)",
+                   "timing": "wall clock with the stream synchronised on both sides"},
+        "e2e": {"value": round(nbytes / dt / 1e6, 1), "unit": "MB/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": 0},
+        "entries_per_s": round(R.nnz / dt, 1),
+        "parse_kernel": {"bytes": parse_bytes, "ms": round(parse_ms, 3),
+                         "gbs": round(parse_bytes / (parse_ms / 1e3) / 1e9, 1),
+                         "frac_of_hbm": round(parse_bytes / (parse_ms / 1e3) / 1e9 / hbm, 3)},
+        "kernels_ms": kern,
+        "device_matches_source": bool(ok),
+        "cpu_baseline": cpu,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "generate_s": round(gen_s, 2),
     }
     print(json.dumps(out))
 

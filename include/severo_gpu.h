@@ -99,14 +99,44 @@ int  sv_device_memory(sv_context* ctx, size_t* free_bytes, size_t* total_bytes);
 /* ---- count matrix ------------------------------------------------------------
  * sv_counts_upload_csc replaces holding the CountMatrix of src/Severo.jl:26-27
  * in host memory: it copies a cells x genes SparseMatrixCSC (colptr, rowval,
- * nzval, each SV_I32 or SV_I64 as declared by its *_type; index_base 0 or 1, 1
- * for Julia's arrays) to the device and builds the cell-major (CSR) copy there.
+ * nzval, each SV_I32 or SV_I64 as declared by its *_type, nzval also SV_F32 or
+ * SV_F64; index_base 0 or 1, 1 for Julia's arrays) to the device and builds
+ * the cell-major (CSR) copy there.
  * Row indices must be strictly increasing within each column (Julia's
  * invariant); this is checked on the device and reported as SV_ERR_ARG. */
 int sv_counts_upload_csc(sv_context* ctx, int64_t n_cells, int64_t n_genes, int64_t nnz,
                          const void* colptr, int colptr_type, const void* rowval,
                          int rowval_type, const void* nzval, int val_type, int index_base,
                          sv_counts** out);
+/* sv_counts_upload_csr takes the cell-major arrays as the file formats store
+ * them: the features x barcodes CSC of a 10X CellRanger HDF5 file
+ * (src/input.jl:158-187) and of the "/counts" HDF5 layout (:210-225), or the
+ * cells x genes CSR of an AnnData X (:250-287), which the reference turns into
+ * a cells x genes SparseMatrixCSC on the host with copy(X').  Here the arrays
+ * go to the device as they are and the gene-major (CSC) copy is built there.
+ * Features may be unsorted within a cell (they are sorted on the device);
+ * duplicate features within a cell are SV_ERR_ARG.  For both uploads the counts
+ * may be SV_I32, SV_I64, SV_F32 or SV_F64; wider and floating types must hold
+ * whole numbers in [0, 2^31) (convert_counts, src/input.jl:776-780, converts
+ * real-valued files to Int32), else SV_ERR_ARG. */
+int sv_counts_upload_csr(sv_context* ctx, int64_t n_cells, int64_t n_genes, int64_t nnz,
+                         const void* rowptr, int rowptr_type, const void* colidx,
+                         int colidx_type, const void* nzval, int val_type, int index_base,
+                         sv_counts** out);
+/* MatrixMarket coordinate files (readMM, src/input.jl:27-115, as _read_10X
+ * reads matrix.mtx[.gz], :199-208), parsed on the device: the entry section is
+ * streamed to HBM as it lies in the file and parsed there, one line per thread.
+ * rows_are_features = 1 for the 10X layout (features x barcodes; the reference
+ * transposes it with copy(X')), 0 when the file's rows are the cells.  Entries
+ * naming the same position are summed and explicit zeros kept, as
+ * sparse(I, J, V) does.  Header errors carry the reference's messages; a
+ * malformed entry line, an index outside the declared size or a count that is
+ * not a whole number in [0, 2^31) is SV_ERR_ARG.  Paths ending in ".gz" are
+ * read through libz.so.1 (SV_ERR_UNSUPPORTED when it cannot be loaded).
+ * sv_counts_parse_mtx reads the same format from len bytes of host memory. */
+int sv_counts_read_mtx(sv_context* ctx, const char* path, int rows_are_features, sv_counts** out);
+int sv_counts_parse_mtx(sv_context* ctx, const char* text, int64_t len, int rows_are_features,
+                        sv_counts** out);
 /* Synthetic negative-binomial counts generated on the device (benchmarks).
  * Cells x genes; mean depth * s_c * mu_g * exp(lfc[cluster(c), g]); variance
  * mean + dispersion * mean^2.  mu_g (n_genes), s_c (n_cells), cluster ids

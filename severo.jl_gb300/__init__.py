@@ -37,7 +37,8 @@ __all__ = [
     "Batch", "batch_pca",
     "batch_ann", "scale_features", "irlba", "irlba_callback", "pca", "embedding", "ann",
     "nearest_neighbours", "jaccard_index", "shared_nearest_neighbours", "SeveroGPUError",
-    "ConvergenceError", "default_context",
+    "ConvergenceError", "default_context", "NamedCounts", "make_unique", "convert_counts",
+    "readMM", "read_10X", "read_geo", "read_dge", "read_10X_h5", "read_h5", "read_h5ad", "read_data",
 ]
 
 _DTYPES = {"float64": SV_F64, "float32": SV_F32, "bfloat16": SV_BF16,
@@ -165,20 +166,59 @@ class CountMatrix(_Handle):
     @classmethod
     def upload(cls, colptr, rowval, nzval, shape, index_base=0, ctx: Context | None = None):
         """Upload raw CSC arrays (Julia SparseMatrixCSC layout; 1-based when index_base=1).
-        Each array may be Int32 or Int64; they are read from host memory (pinned
+        colptr and rowval may be Int32 or Int64, the counts also Float32 or
+        Float64 holding whole numbers; they are read from host memory (pinned
         memory gives full link speed)."""
+        return cls._upload("sv_counts_upload_csc", colptr, rowval, nzval, shape, index_base, ctx)
+
+    @classmethod
+    def upload_csr(cls, rowptr, colidx, nzval, shape, index_base=0, ctx: Context | None = None):
+        """Upload cell-major arrays (cells x genes CSR; equivalently the features
+        x barcodes CSC that 10X HDF5 files store); the CSC copy is built on the
+        device.  Features may be unsorted within a cell."""
+        return cls._upload("sv_counts_upload_csr", rowptr, colidx, nzval, shape, index_base, ctx)
+
+    @classmethod
+    def _upload(cls, fn, ptr, idx, nzval, shape, index_base, ctx):
         ctx = ctx or default_context()
-        colptr = np.ascontiguousarray(colptr)
-        rowval = np.ascontiguousarray(rowval)
+        ptr = np.ascontiguousarray(ptr)
+        idx = np.ascontiguousarray(idx)
         nzval = np.ascontiguousarray(nzval)
-        code = lambda a: SV_I64 if a.dtype.itemsize == 8 else SV_I32
-        for a in (colptr, rowval, nzval):
+        for a in (ptr, idx):
             if not np.issubdtype(a.dtype, np.integer) or a.dtype.itemsize not in (4, 8):
-                raise TypeError("colptr, rowval and counts must be Int32 or Int64")
+                raise TypeError("pointers and indices must be Int32 or Int64")
+        if nzval.dtype == np.float64:
+            vcode = SV_F64
+        elif nzval.dtype == np.float32:
+            vcode = SV_F32
+        elif np.issubdtype(nzval.dtype, np.integer) and nzval.dtype.itemsize in (4, 8):
+            vcode = SV_I64 if nzval.dtype.itemsize == 8 else SV_I32
+        else:
+            raise TypeError("counts must be Int32, Int64, Float32 or Float64")
+        code = lambda a: SV_I64 if a.dtype.itemsize == 8 else SV_I32
         h = C.c_void_p()
-        L.check(ctx.lib.sv_counts_upload_csc(ctx.h, shape[0], shape[1], len(rowval), _ptr(colptr),
-                                              code(colptr), _ptr(rowval), code(rowval), _ptr(nzval),
-                                              code(nzval), index_base, C.byref(h)))
+        L.check(getattr(ctx.lib, fn)(ctx.h, int(shape[0]), int(shape[1]), len(idx), _ptr(ptr),
+                                     code(ptr), _ptr(idx), code(idx), _ptr(nzval), vcode,
+                                     index_base, C.byref(h)))
+        return cls(ctx, h)
+
+    @classmethod
+    def read_mtx(cls, path, rows_are_features=True, ctx: Context | None = None):
+        """A MatrixMarket coordinate file (".gz" read through zlib) parsed on the
+        device.  rows_are_features=True for the 10X layout (features x barcodes)."""
+        ctx = ctx or default_context()
+        h = C.c_void_p()
+        L.check(ctx.lib.sv_counts_read_mtx(ctx.h, str(path).encode(), int(rows_are_features),
+                                            C.byref(h)))
+        return cls(ctx, h)
+
+    @classmethod
+    def parse_mtx(cls, text: bytes, rows_are_features=True, ctx: Context | None = None):
+        """The same format from bytes already in host memory."""
+        ctx = ctx or default_context()
+        h = C.c_void_p()
+        L.check(ctx.lib.sv_counts_parse_mtx(ctx.h, text, len(text), int(rows_are_features),
+                                             C.byref(h)))
         return cls(ctx, h)
 
     @classmethod
@@ -717,3 +757,7 @@ def shared_nearest_neighbours(X, k, prune=1.0 / 15.0, metric="euclidean", includ
     h = C.c_void_p()
     L.check(ctx.lib.sv_snn_knn(ctx.h, knn.h, int(k), float(prune), _dtype_code(dt), C.byref(h)))
     return Graph(ctx, h).to_csc(dt)
+
+
+from .readers import (NamedCounts, convert_counts, make_unique, readMM, read_10X, read_geo,  # noqa: E402
+                      read_dge, read_10X_h5, read_h5, read_h5ad, read_data)

@@ -72,6 +72,9 @@ SIGNATURES = {
     "sv_profile_report": (i32, [vp, C.c_char_p, C.c_size_t]),
     "sv_device_memory": (i32, [vp, P(C.c_size_t), P(C.c_size_t)]),
     "sv_counts_upload_csc": (i32, [vp, i64, i64, i64, vp, i32, vp, i32, vp, i32, i32, P(vp)]),
+    "sv_counts_upload_csr": (i32, [vp, i64, i64, i64, vp, i32, vp, i32, vp, i32, i32, P(vp)]),
+    "sv_counts_read_mtx": (i32, [vp, C.c_char_p, i32, P(vp)]),
+    "sv_counts_parse_mtx": (i32, [vp, C.c_char_p, i64, i32, P(vp)]),
     "sv_counts_generate": (i32, [vp, i64, i64, vp, vp, vp, vp, C.c_int32, dbl, dbl, C.c_uint64, P(vp)]),
     "sv_counts_info": (i32, [vp, P(i64), P(i64), P(i64)]),
     "sv_counts_download_csc": (i32, [vp, vp, vp, vp, vp]),

@@ -55,7 +55,7 @@ def build(verbose: bool = False, extra=()) -> Path:
     if out.exists() and all(out.stat().st_mtime >= o.stat().st_mtime for o in objs):
         return out
     tmp = LIBDIR / (LIBNAME + ".tmp")
-    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -108,9 +108,15 @@ void sv_check_device_status(sv_context* ctx, const char* where) {
   int st = *h;
   if (st) {
     SV_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+    if (st & SV_STATUS_PARSE)
+      sv_throw(SV_ERR_ARG, "%s: could not read a matrix entry (three fields per line expected)", where);
     if (st & SV_STATUS_UNSORTED)
-      sv_throw(SV_ERR_ARG, "%s: row indices are not strictly increasing within a column", where);
+      sv_throw(SV_ERR_ARG,
+               "%s: indices are not strictly increasing within a column (unsorted or duplicate entries)",
+               where);
     if (st & SV_STATUS_OOB) sv_throw(SV_ERR_ARG, "%s: an index is out of range", where);
+    if (st & SV_STATUS_VALUE)
+      sv_throw(SV_ERR_ARG, "%s: a count is not an integer in [0, 2^31)", where);
     sv_throw(SV_ERR_DEVICE, "%s: a device-side iteration limit was reached (status %d)", where, st);
   }
 }
@@ -164,6 +170,8 @@ SV_API int sv_context_destroy(sv_context* ctx) {
     if (ctx->marks[i]) cudaEventDestroy(ctx->marks[i]);
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  for (void* p : ctx->h_io)
+    if (p) cudaFreeHost(p);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return SV_OK;

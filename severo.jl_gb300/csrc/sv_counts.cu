@@ -33,6 +33,20 @@ __global__ void k_idx_to_i32(const T* __restrict__ in, int32_t* __restrict__ out
   }
 }
 
+// Counts of a wider or floating type to Int32: whole numbers in [0, 2^31) pass,
+// anything else (fractions, NaN, out of range) flags SV_STATUS_VALUE.
+template <typename T>
+__global__ void k_count_to_i32(const T* __restrict__ in, int32_t* __restrict__ out, int64_t n,
+                               int* status) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    T v = in[i];
+    bool ok = v >= (T)0 && v < (T)2147483648.0 && (T)(int64_t)v == v;
+    if (!ok) sv_flag(status, SV_STATUS_VALUE);
+    out[i] = ok ? (int32_t)v : 0;
+  }
+}
+
 // Checks the CSC invariants (rows in range, strictly increasing per column) and
 // counts entries per row for the transpose.  One warp per column.
 __global__ void k_csc_check_hist(const int64_t* __restrict__ colptr,
@@ -57,6 +71,25 @@ __global__ void k_csc_check_hist(const int64_t* __restrict__ colptr,
       if (i + 1 < e && rowidx[i + 1] <= r) sv_flag(status, SV_STATUS_UNSORTED);
       atomicAdd(&row_cnt[r], 1ull);
     }
+  }
+}
+
+// Sets bit 1 of *flag when an index is not above its predecessor in the same
+// segment, bit 2 when a segment's pointers are out of order or out of range.
+__global__ void k_seg_unsorted(const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                               int64_t n, int64_t nnz, int* flag) {
+  int lane = threadIdx.x & 31;
+  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n; r += nwarps) {
+    int64_t s = ptr[r], e = ptr[r + 1];
+    if (s < 0 || e < s || e > nnz) {
+      if (lane == 0) atomicOr(flag, 2);
+      continue;
+    }
+    bool bad = false;
+    for (int64_t i = s + 1 + lane; i < e; i += 32) bad |= idx[i] <= idx[i - 1];
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flag, 1);
   }
 }
 
@@ -305,56 +338,143 @@ void upload_idx(sv_context* ctx, const void* host, int64_t n, int64_t base, int6
 
 }  // namespace
 
-// Builds the CSR copy from the CSC copy already on the device.
-void sv_build_csr_from_csc(sv_context* ctx, sv_counts* c) {
-  DevBuf<unsigned long long> rcnt(c->n_cells + 1);
-  sv_memset(ctx, rcnt.get(), 0, (c->n_cells + 1) * sizeof(unsigned long long));
-  sv_launch(ctx, "counts_check_hist", k_csc_check_hist, dim3(sv_grid_for(ctx, c->n_genes * 32, 256)),
-            dim3(256), 0, (const int64_t*)c->csc_colptr.get(), (const int32_t*)c->csc_rowidx.get(),
-            c->n_genes, c->n_cells, c->nnz, rcnt.get(), ctx->d_status);
-  sv_check_device_status(ctx, "sv_counts_upload_csc");
-  c->csr_rowptr.alloc(c->n_cells + 1);
-  DevBuf<int64_t> rc64(c->n_cells + 1);
-  sv_launch(ctx, "counts_u64_to_i64", k_u64_to_i64, dim3(sv_grid_for(ctx, c->n_cells, 256)), dim3(256),
-            0, (const unsigned long long*)rcnt.get(), rc64.get(), c->n_cells);
-  sv_scan_i64(ctx, rc64.get(), c->csr_rowptr.get(), c->n_cells);
-  // cursors start at the row offsets
-  sv_launch(ctx, "counts_u64_to_i64", k_colptr_to_i64<int64_t>, dim3(sv_grid_for(ctx, c->n_cells, 256)),
-            dim3(256), 0, (const int64_t*)c->csr_rowptr.get(), (int64_t*)rcnt.get(), c->n_cells,
-            (int64_t)0);
-  c->csr_colidx.alloc(c->nnz);
-  c->csr_count.alloc(c->nnz);
-  sv_launch(ctx, "counts_scatter", k_csc_scatter, dim3(sv_grid_for(ctx, c->n_genes * 32, 256)),
-            dim3(256), 0, (const int64_t*)c->csc_colptr.get(), (const int32_t*)c->csc_rowidx.get(),
-            (const int32_t*)c->csc_count.get(), c->n_genes, rcnt.get(), c->csr_colidx.get(),
-            c->csr_count.get());
-  // per-row sort
+void sv_upload_counts(sv_context* ctx, const void* host, int val_type, int64_t n, int32_t* dst) {
+  if (n == 0) return;
+  if (val_type == SV_I32) {
+    sv_h2d(ctx, dst, host, n * 4);
+    return;
+  }
+  size_t es = sv_elem_size(val_type);
+  DevBuf<unsigned char> tmp(n * es);
+  sv_h2d(ctx, tmp.get(), host, n * es);
+  dim3 g(sv_grid_for(ctx, n, 256)), b(256);
+  if (val_type == SV_I64)
+    sv_launch(ctx, "counts_convert_val", k_count_to_i32<int64_t>, g, b, 0, (const int64_t*)tmp.get(),
+              dst, n, ctx->d_status);
+  else if (val_type == SV_F32)
+    sv_launch(ctx, "counts_convert_val", k_count_to_i32<float>, g, b, 0, (const float*)tmp.get(), dst,
+              n, ctx->d_status);
+  else
+    sv_launch(ctx, "counts_convert_val", k_count_to_i32<double>, g, b, 0, (const double*)tmp.get(),
+              dst, n, ctx->d_status);
+  sv_sync(ctx);
+}
+
+// Sorts the indices of each segment of a compressed pattern (ptr over n
+// segments) in place, counts moving with their indices.  Segments that fit
+// 8192 keys are sorted in shared memory, longer ones in a global pass.
+void sv_sort_segments(sv_context* ctx, const int64_t* ptr, int64_t n, int32_t* idx, int32_t* cnt) {
   const int cap = 8192;
-  DevBuf<int64_t> long_rows(c->n_cells + 1);
+  DevBuf<int64_t> long_rows(n + 1);
   DevBuf<unsigned long long> n_long(1);
   sv_memset(ctx, n_long.get(), 0, sizeof(unsigned long long));
   SV_CUDA(cudaFuncSetAttribute(k_sort_rows_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                cap * 8));
-  sv_launch(ctx, "counts_sort_rows", k_sort_rows_smem, dim3(sv_grid_for(ctx, c->n_cells, 1, 16)),
-            dim3(256), (size_t)cap * 8, (const int64_t*)c->csr_rowptr.get(), c->n_cells,
-            c->csr_colidx.get(), c->csr_count.get(), cap, long_rows.get(), n_long.get());
+  sv_launch(ctx, "counts_sort_rows", k_sort_rows_smem, dim3(sv_grid_for(ctx, n, 1, 16)),
+            dim3(256), (size_t)cap * 8, ptr, n, idx, cnt, cap, long_rows.get(), n_long.get());
   int64_t nl = sv_read_i64(ctx, (const int64_t*)n_long.get());
   if (nl > 0) {
-    // longest row bounds the scratch per block
-    std::vector<int64_t> rp(c->n_cells + 1);
-    sv_d2h(ctx, rp.data(), c->csr_rowptr.get(), (c->n_cells + 1) * sizeof(int64_t));
+    // longest segment bounds the scratch per block
+    std::vector<int64_t> rp(n + 1);
+    sv_d2h(ctx, rp.data(), ptr, (n + 1) * sizeof(int64_t));
     int64_t maxlen = 0;
-    for (int64_t r = 0; r < c->n_cells; ++r) maxlen = std::max(maxlen, rp[r + 1] - rp[r]);
+    for (int64_t r = 0; r < n; ++r) maxlen = std::max(maxlen, rp[r + 1] - rp[r]);
     int64_t n2 = 1;
     while (n2 < maxlen) n2 <<= 1;
     int blocks = (int)std::min<int64_t>(nl, (int64_t)ctx->num_sms * 2);
     DevBuf<unsigned long long> scratch((size_t)blocks * n2);
-    sv_launch(ctx, "counts_sort_rows_long", k_sort_rows_global, dim3(blocks), dim3(1024), 0,
-              (const int64_t*)c->csr_rowptr.get(), (const int64_t*)long_rows.get(), nl,
-              c->csr_colidx.get(), c->csr_count.get(), scratch.get(), n2);
+    sv_launch(ctx, "counts_sort_rows_long", k_sort_rows_global, dim3(blocks), dim3(1024), 0, ptr,
+              (const int64_t*)long_rows.get(), nl, idx, cnt, scratch.get(), n2);
     sv_sync(ctx);
   }
   sv_sync(ctx);
+}
+
+// Transpose of a compressed pattern with its counts: the n_major segments of
+// (ptr, idx, cnt) become n_minor segments (optr, oidx, ocnt) whose indices are
+// the former segment numbers, sorted within each segment.  The source
+// invariants (indices in range, strictly increasing within a segment) are
+// checked on the way and reported as SV_ERR_ARG naming `where`.
+void sv_transpose_counts(sv_context* ctx, int64_t n_major, int64_t n_minor, int64_t nnz,
+                         const int64_t* ptr, const int32_t* idx, const int32_t* cnt,
+                         DevBuf<int64_t>& optr, DevBuf<int32_t>& oidx, DevBuf<int32_t>& ocnt,
+                         const char* where) {
+  DevBuf<unsigned long long> rcnt(n_minor + 1);
+  sv_memset(ctx, rcnt.get(), 0, (n_minor + 1) * sizeof(unsigned long long));
+  sv_launch(ctx, "counts_check_hist", k_csc_check_hist, dim3(sv_grid_for(ctx, n_major * 32, 256)),
+            dim3(256), 0, ptr, idx, n_major, n_minor, nnz, rcnt.get(), ctx->d_status);
+  sv_check_device_status(ctx, where);
+  optr.alloc(n_minor + 1);
+  DevBuf<int64_t> rc64(n_minor + 1);
+  sv_launch(ctx, "counts_u64_to_i64", k_u64_to_i64, dim3(sv_grid_for(ctx, n_minor, 256)), dim3(256),
+            0, (const unsigned long long*)rcnt.get(), rc64.get(), n_minor);
+  sv_scan_i64(ctx, rc64.get(), optr.get(), n_minor);
+  // cursors start at the segment offsets
+  sv_launch(ctx, "counts_u64_to_i64", k_colptr_to_i64<int64_t>, dim3(sv_grid_for(ctx, n_minor, 256)),
+            dim3(256), 0, (const int64_t*)optr.get(), (int64_t*)rcnt.get(), n_minor, (int64_t)0);
+  oidx.alloc(nnz);
+  ocnt.alloc(nnz);
+  sv_launch(ctx, "counts_scatter", k_csc_scatter, dim3(sv_grid_for(ctx, n_major * 32, 256)),
+            dim3(256), 0, ptr, idx, cnt, n_major, rcnt.get(), oidx.get(), ocnt.get());
+  sv_sort_segments(ctx, optr.get(), n_minor, oidx.get(), ocnt.get());
+}
+
+// Builds the CSR copy from the CSC copy already on the device.
+void sv_build_csr_from_csc(sv_context* ctx, sv_counts* c) {
+  sv_transpose_counts(ctx, c->n_genes, c->n_cells, c->nnz, c->csc_colptr.get(), c->csc_rowidx.get(),
+                      c->csc_count.get(), c->csr_rowptr, c->csr_colidx, c->csr_count,
+                      "sv_counts_upload_csc");
+}
+
+// Uploads one compressed copy (n_major segments over n_minor indices) from host
+// arrays of the declared types, converting to the device layout (0-based int64
+// pointers, int32 indices and counts) and checking ranges and values.
+static void upload_compressed(sv_context* ctx, int64_t n_major, int64_t n_minor, int64_t nnz,
+                              const void* ptr, int ptr_type, const void* idx, int idx_type,
+                              const void* val, int val_type, int index_base, DevBuf<int64_t>& optr,
+                              DevBuf<int32_t>& oidx, DevBuf<int32_t>& ocnt, const char* where) {
+  optr.alloc(n_major + 1);
+  {
+    size_t es = ptr_type == SV_I32 ? 4 : 8;
+    DevBuf<unsigned char> tmp((n_major + 1) * es);
+    sv_h2d(ctx, tmp.get(), ptr, (n_major + 1) * es);
+    dim3 g(sv_grid_for(ctx, n_major + 1, 256)), b(256);
+    if (ptr_type == SV_I32)
+      sv_launch(ctx, "counts_colptr", k_colptr_to_i64<int32_t>, g, b, 0, (const int32_t*)tmp.get(),
+                optr.get(), n_major + 1, (int64_t)index_base);
+    else
+      sv_launch(ctx, "counts_colptr", k_colptr_to_i64<int64_t>, g, b, 0, (const int64_t*)tmp.get(),
+                optr.get(), n_major + 1, (int64_t)index_base);
+    int64_t first = sv_read_i64(ctx, optr.get());
+    int64_t last = sv_read_i64(ctx, optr.get() + n_major);
+    SV_REQUIRE(first == 0 && last == nnz, "%s: pointer[0] must equal index_base and pointer[end] nnz+base",
+               where);
+  }
+  oidx.alloc(nnz);
+  ocnt.alloc(nnz);
+  if (idx_type == SV_I32 && index_base == 0) {
+    sv_h2d(ctx, oidx.get(), idx, nnz * 4);
+  } else if (idx_type == SV_I32) {
+    upload_idx<int32_t>(ctx, idx, nnz, index_base, n_minor, oidx.get());
+  } else {
+    upload_idx<int64_t>(ctx, idx, nnz, index_base, n_minor, oidx.get());
+  }
+  sv_upload_counts(ctx, val, val_type, nnz, ocnt.get());
+  sv_check_device_status(ctx, where);
+}
+
+static void check_upload_args(int64_t n_cells, int64_t n_genes, int64_t nnz, const void* ptr,
+                              int ptr_type, const void* idx, int idx_type, const void* val,
+                              int val_type, int index_base) {
+  SV_REQUIRE(n_cells >= 1 && n_genes >= 1 && nnz >= 0, "bad sizes");
+  SV_REQUIRE(n_cells < (1ll << 31) && n_genes < (1ll << 31), "dimension exceeds Int32 indices");
+  SV_REQUIRE(ptr_type == SV_I32 || ptr_type == SV_I64, "pointer type must be SV_I32 or SV_I64");
+  SV_REQUIRE(ptr_type == SV_I64 || nnz < (1ll << 31), "nnz >= 2^31 needs Int64 pointers");
+  SV_REQUIRE(idx_type == SV_I32 || idx_type == SV_I64, "index type must be SV_I32 or SV_I64");
+  SV_REQUIRE(val_type == SV_I32 || val_type == SV_I64 || val_type == SV_F32 || val_type == SV_F64,
+             "val_type must be SV_I32, SV_I64, SV_F32 or SV_F64");
+  SV_REQUIRE(index_base == 0 || index_base == 1, "index_base must be 0 or 1");
+  SV_REQUIRE(ptr && (nnz == 0 || (idx && val)), "null array");
 }
 
 SV_API int sv_counts_upload_csc(sv_context* ctx, int64_t n_cells, int64_t n_genes, int64_t nnz,
@@ -364,53 +484,58 @@ SV_API int sv_counts_upload_csc(sv_context* ctx, int64_t n_cells, int64_t n_gene
   SV_TRY
   sv_ctx_check(ctx);
   SV_REQUIRE(out, "out is null");
-  SV_REQUIRE(n_cells >= 1 && n_genes >= 1 && nnz >= 0, "bad sizes");
-  SV_REQUIRE(n_cells < (1ll << 31) && n_genes < (1ll << 31), "dimension exceeds Int32 indices");
-  SV_REQUIRE(colptr_type == SV_I32 || colptr_type == SV_I64, "colptr_type must be SV_I32 or SV_I64");
-  SV_REQUIRE(colptr_type == SV_I64 || nnz < (1ll << 31), "nnz >= 2^31 needs Int64 colptr");
-  SV_REQUIRE(idx_type == SV_I32 || idx_type == SV_I64, "rowval_type must be SV_I32 or SV_I64");
-  SV_REQUIRE(val_type == SV_I32 || val_type == SV_I64, "val_type must be SV_I32 or SV_I64");
-  SV_REQUIRE(index_base == 0 || index_base == 1, "index_base must be 0 or 1");
-  SV_REQUIRE(colptr && (nnz == 0 || (rowval && nzval)), "null array");
+  check_upload_args(n_cells, n_genes, nnz, colptr, colptr_type, rowval, idx_type, nzval, val_type,
+                    index_base);
   auto* c = new sv_counts();
   try {
     c->ctx = ctx;
     c->n_cells = n_cells;
     c->n_genes = n_genes;
     c->nnz = nnz;
-    c->csc_colptr.alloc(n_genes + 1);
-    {
-      size_t es = colptr_type == SV_I32 ? 4 : 8;
-      DevBuf<unsigned char> tmp((n_genes + 1) * es);
-      sv_h2d(ctx, tmp.get(), colptr, (n_genes + 1) * es);
-      if (colptr_type == SV_I32)
-        sv_launch(ctx, "counts_colptr", k_colptr_to_i64<int32_t>, dim3(sv_grid_for(ctx, n_genes + 1, 256)),
-                  dim3(256), 0, (const int32_t*)tmp.get(), c->csc_colptr.get(), n_genes + 1,
-                  (int64_t)index_base);
-      else
-        sv_launch(ctx, "counts_colptr", k_colptr_to_i64<int64_t>, dim3(sv_grid_for(ctx, n_genes + 1, 256)),
-                  dim3(256), 0, (const int64_t*)tmp.get(), c->csc_colptr.get(), n_genes + 1,
-                  (int64_t)index_base);
-      int64_t first = sv_read_i64(ctx, c->csc_colptr.get());
-      int64_t last = sv_read_i64(ctx, c->csc_colptr.get() + n_genes);
-      SV_REQUIRE(first == 0 && last == nnz, "colptr[0] must equal index_base and colptr[end] nnz+base");
-    }
-    c->csc_rowidx.alloc(nnz);
-    c->csc_count.alloc(nnz);
-    if (idx_type == SV_I32 && index_base == 0) {
-      sv_h2d(ctx, c->csc_rowidx.get(), rowval, nnz * 4);
-    } else if (idx_type == SV_I32) {
-      upload_idx<int32_t>(ctx, rowval, nnz, index_base, n_cells, c->csc_rowidx.get());
-    } else {
-      upload_idx<int64_t>(ctx, rowval, nnz, index_base, n_cells, c->csc_rowidx.get());
-    }
-    if (val_type == SV_I32) {
-      sv_h2d(ctx, c->csc_count.get(), nzval, nnz * 4);
-    } else {
-      upload_idx<int64_t>(ctx, nzval, nnz, 0, (1ll << 31) - 1, c->csc_count.get());
-    }
-    sv_check_device_status(ctx, "sv_counts_upload_csc");
+    upload_compressed(ctx, n_genes, n_cells, nnz, colptr, colptr_type, rowval, idx_type, nzval,
+                      val_type, index_base, c->csc_colptr, c->csc_rowidx, c->csc_count,
+                      "sv_counts_upload_csc");
     sv_build_csr_from_csc(ctx, c);
+  } catch (...) {
+    delete c;
+    throw;
+  }
+  *out = c;
+  SV_CATCH
+}
+
+SV_API int sv_counts_upload_csr(sv_context* ctx, int64_t n_cells, int64_t n_genes, int64_t nnz,
+                                const void* rowptr, int rowptr_type, const void* colidx,
+                                int idx_type, const void* nzval, int val_type, int index_base,
+                                sv_counts** out) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(out, "out is null");
+  check_upload_args(n_cells, n_genes, nnz, rowptr, rowptr_type, colidx, idx_type, nzval, val_type,
+                    index_base);
+  auto* c = new sv_counts();
+  try {
+    c->ctx = ctx;
+    c->n_cells = n_cells;
+    c->n_genes = n_genes;
+    c->nnz = nnz;
+    upload_compressed(ctx, n_cells, n_genes, nnz, rowptr, rowptr_type, colidx, idx_type, nzval,
+                      val_type, index_base, c->csr_rowptr, c->csr_colidx, c->csr_count,
+                      "sv_counts_upload_csr");
+    // Files store each cell's features in the order they were written; the
+    // transpose below requires them increasing, so unsorted cells are sorted.
+    DevBuf<int> unsorted(1);
+    sv_memset(ctx, unsorted.get(), 0, sizeof(int));
+    sv_launch(ctx, "counts_check_sorted", k_seg_unsorted, dim3(sv_grid_for(ctx, n_cells * 32, 256)),
+              dim3(256), 0, (const int64_t*)c->csr_rowptr.get(), (const int32_t*)c->csr_colidx.get(),
+              n_cells, nnz, unsorted.get());
+    int flag = 0;
+    sv_d2h(ctx, &flag, unsorted.get(), sizeof(int));
+    SV_REQUIRE(!(flag & 2), "sv_counts_upload_csr: row pointers are not increasing");
+    if (flag) sv_sort_segments(ctx, c->csr_rowptr.get(), n_cells, c->csr_colidx.get(), c->csr_count.get());
+    sv_transpose_counts(ctx, n_cells, n_genes, nnz, c->csr_rowptr.get(), c->csr_colidx.get(),
+                        c->csr_count.get(), c->csc_colptr, c->csc_rowidx, c->csc_count,
+                        "sv_counts_upload_csr");
   } catch (...) {
     delete c;
     throw;

@@ -82,6 +82,10 @@ struct sv_context {
   // small pinned staging buffer for scalar read-backs
   void* h_stage = nullptr;
   size_t h_stage_bytes = 0;
+  // two pinned staging buffers for streamed uploads (file readers), kept
+  // between calls
+  void* h_io[2] = {nullptr, nullptr};
+  size_t h_io_bytes = 0;
 };
 
 void sv_ctx_check(sv_context* ctx);
@@ -296,6 +300,8 @@ inline size_t sv_elem_size(int dtype) {
 #define SV_STATUS_OOB 1
 #define SV_STATUS_UNSORTED 2
 #define SV_STATUS_LIMIT 4
+#define SV_STATUS_VALUE 8    // a count that is not an integer in [0, 2^31)
+#define SV_STATUS_PARSE 16   // a malformed entry line of a MatrixMarket file
 
 __device__ __forceinline__ void sv_flag(int* status, int bit) { atomicOr(status, bit); }
 
@@ -328,6 +334,18 @@ int sv_grid_for(sv_context* ctx, int64_t work_items, int per_block, int max_per_
 // builds (or rebuilds) the CSR copy of a count matrix from its device CSC copy
 // (sv_counts.cu); checks the CSC invariants on the way
 void sv_build_csr_from_csc(sv_context* ctx, sv_counts* c);
+// transpose of a compressed pattern with its counts, sorted within the output
+// segments; checks the source invariants (sv_counts.cu)
+void sv_transpose_counts(sv_context* ctx, int64_t n_major, int64_t n_minor, int64_t nnz,
+                         const int64_t* ptr, const int32_t* idx, const int32_t* cnt,
+                         DevBuf<int64_t>& optr, DevBuf<int32_t>& oidx, DevBuf<int32_t>& ocnt,
+                         const char* where);
+// sorts the indices within each of the n segments of ptr, counts moving along
+void sv_sort_segments(sv_context* ctx, const int64_t* ptr, int64_t n, int32_t* idx, int32_t* cnt);
+// converts n host counts of type val_type (SV_I32, SV_I64, SV_F32, SV_F64) into
+// device Int32 counts; the wider and floating types must hold integers in
+// [0, 2^31) (checked on the device, reported through the context status)
+void sv_upload_counts(sv_context* ctx, const void* host, int val_type, int64_t n, int32_t* dst);
 // sorts (key, value) pairs by key on the device; the arrays hold n2 entries, n2
 // a power of two >= max(n, 2048) (sv_core.cu)
 void sv_sort_pairs(sv_context* ctx, unsigned long long* key, int* val, int64_t n, int64_t n2);
