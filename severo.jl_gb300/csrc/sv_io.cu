@@ -15,9 +15,14 @@
 #include "sv_internal.cuh"
 
 #include <dlfcn.h>
+#include <fcntl.h>
 #include <sys/stat.h>
+#include <unistd.h>
 
+#include <atomic>
+#include <cerrno>
 #include <memory>
+#include <thread>
 
 namespace {
 
@@ -293,6 +298,20 @@ __global__ void k_coo_scatter(const int32_t* __restrict__ cell, const int32_t* _
   }
 }
 
+// Sets *flag unless the entries are in cell order with strictly increasing
+// features within each cell (the order 10X writes): then they already are the
+// cell-major copy.
+__global__ void k_coo_unsorted(const int32_t* __restrict__ cell, const int32_t* __restrict__ gene,
+                               int64_t n, int* flag) {
+  bool bad = false;
+  for (int64_t e = 1 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int32_t c0 = cell[e - 1], c1 = cell[e];
+    bad |= c1 < c0 || (c1 == c0 && gene[e] <= gene[e - 1]);
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) *flag = 1;
+}
+
 // distinct columns per (sorted) row
 __global__ void k_dup_len(const int64_t* __restrict__ ptr, const int32_t* __restrict__ col, int64_t n,
                           int64_t* __restrict__ len) {
@@ -347,13 +366,35 @@ struct Source {
   virtual int64_t remaining() const { return -1; }
 };
 
+// Runs part(i, a, b) over [0, n) split into up to 8 host threads (large staging
+// copies: one core moves ~10 GB/s, the link several times that).
+template <typename F>
+void split_copy(size_t n, F part) {
+  const size_t PART = (size_t)8 << 20;
+  int t = (int)std::min<size_t>(std::min<size_t>(8, std::max(1u, std::thread::hardware_concurrency())),
+                                (n + PART - 1) / PART);
+  if (t <= 1) {
+    part(0, 0, n);
+    return;
+  }
+  size_t per = (n + t - 1) / t;
+  std::vector<std::thread> th;
+  for (int i = 0; i < t; ++i) {
+    size_t a = (size_t)i * per, b = std::min(n, a + per);
+    if (a >= b) break;
+    th.emplace_back([=] { part(i, a, b); });
+  }
+  for (auto& x : th) x.join();
+}
+
 struct MemSource : Source {
   const char* p;
   size_t n, pos = 0;
   MemSource(const char* p_, size_t n_) : p(p_), n(n_) {}
   size_t read(void* dst, size_t k) override {
     k = std::min(k, n - pos);
-    memcpy(dst, p + pos, k);
+    const char* src = p + pos;
+    split_copy(k, [=](int, size_t a, size_t b) { memcpy((char*)dst + a, src + a, b - a); });
     pos += k;
     return k;
   }
@@ -361,24 +402,48 @@ struct MemSource : Source {
 };
 
 struct FileSource : Source {
-  FILE* f = nullptr;
-  int64_t size = -1, done = 0;
+  int fd = -1;
+  bool regular = false;
+  int64_t size = -1, pos = 0;
   explicit FileSource(const char* path) {
-    f = fopen(path, "rb");
-    if (!f) sv_throw(SV_ERR_ARG, "cannot open %s", path);
+    fd = ::open(path, O_RDONLY);
+    if (fd < 0) sv_throw(SV_ERR_ARG, "cannot open %s", path);
     struct stat st;
-    if (fstat(fileno(f), &st) == 0 && S_ISREG(st.st_mode)) size = st.st_size;
+    if (fstat(fd, &st) == 0 && S_ISREG(st.st_mode)) {
+      regular = true;
+      size = st.st_size;
+    }
   }
   ~FileSource() override {
-    if (f) fclose(f);
+    if (fd >= 0) ::close(fd);
   }
   size_t read(void* dst, size_t k) override {
-    size_t r = fread(dst, 1, k, f);
-    if (r < k && ferror(f)) sv_throw(SV_ERR_ARG, "read error");
-    done += r;
-    return r;
+    if (!regular) {  // pipes and devices: one sequential read
+      ssize_t r;
+      do r = ::read(fd, dst, k); while (r < 0 && errno == EINTR);
+      if (r < 0) sv_throw(SV_ERR_ARG, "read error");
+      pos += r;
+      return (size_t)r;
+    }
+    k = (size_t)std::min<int64_t>((int64_t)k, std::max<int64_t>(0, size - pos));
+    std::atomic<int> bad{0};
+    const int64_t base = pos;
+    split_copy(k, [&, base](int, size_t a, size_t b) {
+      while (a < b) {
+        ssize_t r = ::pread(fd, (char*)dst + a, b - a, (off_t)(base + (int64_t)a));
+        if (r < 0 && errno == EINTR) continue;
+        if (r <= 0) {
+          bad = 1;
+          return;
+        }
+        a += (size_t)r;
+      }
+    });
+    if (bad) sv_throw(SV_ERR_ARG, "read error (the file changed or could not be read)");
+    pos += (int64_t)k;
+    return k;
   }
-  int64_t remaining() const override { return size < 0 ? -1 : size - done; }
+  int64_t remaining() const override { return regular ? size - pos : -1; }
 };
 
 // gzip through the system zlib, loaded when a gzip file is first read
@@ -661,11 +726,30 @@ sv_counts* read_mm(sv_context* ctx, Source& src, int rows_are_features, const ch
     // cell-major order with the features of each cell sorted
     DevBuf<unsigned long long> hist(n_cells + 1);
     DevBuf<int64_t> p0(n_cells + 1), h64(n_cells + 1);
-    DevBuf<int32_t> col(entries), cnt(entries);
     sv_memset(ctx, hist.get(), 0, (n_cells + 1) * sizeof(unsigned long long));
     dim3 ge(sv_grid_for(ctx, entries, 256)), gc(sv_grid_for(ctx, n_cells, 256)), b(256);
     sv_launch(ctx, "mtx_hist", k_coo_hist, ge, b, 0, (const int32_t*)cell.get(), entries, hist.get());
     sv_launch(ctx, "mtx_hist", k_u64_i64, gc, b, 0, (const unsigned long long*)hist.get(), h64.get(), n_cells);
+    DevBuf<int> unsorted(1);
+    sv_memset(ctx, unsorted.get(), 0, sizeof(int));
+    sv_launch(ctx, "mtx_order", k_coo_unsorted, ge, b, 0, (const int32_t*)cell.get(),
+              (const int32_t*)gene.get(), entries, unsorted.get());
+    int flag = 0;
+    sv_d2h(ctx, &flag, unsorted.get(), sizeof(int));
+    if (!flag) {
+      // already the cell-major copy: no scatter, sort or merge
+      c->csr_rowptr.alloc(n_cells + 1);
+      sv_scan_i64(ctx, h64.get(), c->csr_rowptr.get(), n_cells);
+      c->nnz = entries;
+      c->csr_colidx = std::move(gene);
+      c->csr_count = std::move(val);
+      cell.release();
+      sv_transpose_counts(ctx, n_cells, n_genes, c->nnz, c->csr_rowptr.get(), c->csr_colidx.get(),
+                          c->csr_count.get(), c->csc_colptr, c->csc_rowidx, c->csc_count, where);
+      sv_sync(ctx);
+      return c;
+    }
+    DevBuf<int32_t> col(entries), cnt(entries);
     sv_scan_i64(ctx, h64.get(), p0.get(), n_cells);
     sv_launch(ctx, "mtx_hist", k_i64_u64, gc, b, 0, (const int64_t*)p0.get(), hist.get(), n_cells);
     sv_launch(ctx, "mtx_scatter", k_coo_scatter, ge, b, 0, (const int32_t*)cell.get(),

@@ -45,6 +45,28 @@ def test_parse_matches_oracle(sv, ctx, seed, rows_are_features, field, crlf):
     check_both_copies(sv, X, ref)
 
 
+@pytest.mark.parametrize("field", ["integer", "real"])
+def test_parse_cell_ordered(sv, ctx, field):
+    """Entries in cell order with features increasing (the order 10X writes) are
+    taken as the cell-major copy directly; one swapped pair or one repeated
+    entry sends the file down the general path; both agree with the oracle."""
+    A = rand_counts(1500, 700, 0.03, 17).tocsr()
+    A.sort_indices()
+    fmt = "{}.0" if field == "real" else "{}"
+    text = mm_text(A, field=field, fmt=fmt)
+    ref = mtx.parse(text, True)
+    check_both_copies(sv, sv.CountMatrix.parse_mtx(text, True, ctx=ctx), ref)
+    lines = text.split(b"\n")
+    k = 3 + len(lines) // 2
+    for variant in (lines[:k] + [lines[k + 1], lines[k]] + lines[k + 2:],
+                    lines[:k + 1] + [lines[k]] + lines[k + 1:]):
+        v = b"\n".join(variant)
+        if len(variant) != len(lines):  # a repeated entry: one more entry in the size line
+            hdr = lines[2].split()
+            v = v.replace(lines[2], b" ".join(hdr[:2] + [str(int(hdr[2]) + 1).encode()]), 1)
+        check_both_copies(sv, sv.CountMatrix.parse_mtx(v, True, ctx=ctx), mtx.parse(v, True))
+
+
 def test_parse_large_with_long_header(sv, ctx):
     """Two million entries over many 4 KB tiles, after a 3 MB comment line (the
     header reader's buffer grows past its first 1 MB)."""
