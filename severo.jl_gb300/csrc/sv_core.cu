@@ -1,6 +1,8 @@
 // Context, error reporting, profiling, pinned-memory helpers and the device-wide
 // scan used by the other translation units.
 #include "sv_internal.cuh"
+
+#include <thread>
 #include <stdarg.h>
 
 static thread_local std::string g_last_error;
@@ -85,12 +87,102 @@ void sv_memset(sv_context* ctx, void* p, int v, size_t bytes) {
   if (bytes) SV_CUDA(cudaMemsetAsync(p, v, bytes, ctx->stream));
 }
 
+void sv_parallel_memcpy(void* dst, const void* src, size_t n) {
+  const size_t PART = (size_t)4 << 20;
+  int t = (int)std::min<size_t>(std::min<size_t>(8, std::max(1u, std::thread::hardware_concurrency())),
+                                (n + PART - 1) / PART);
+  if (t <= 1) {
+    memcpy(dst, src, n);
+    return;
+  }
+  size_t per = (n + t - 1) / t;
+  std::vector<std::thread> th;
+  for (int i = 0; i < t; ++i) {
+    size_t a = (size_t)i * per, b = std::min(n, a + per);
+    if (a >= b) break;
+    th.emplace_back([=] { memcpy((char*)dst + a, (const char*)src + a, b - a); });
+  }
+  for (auto& x : th) x.join();
+}
+
+void sv_ctx_io(sv_context* ctx, void* buf[2], cudaEvent_t ev[2]) {
+  const size_t CH = SV_IO_CHUNK;
+  if (ctx->h_io_bytes < CH) {
+    for (void*& p : ctx->h_io) {
+      if (p) cudaFreeHost(p);
+      p = nullptr;
+    }
+    ctx->h_io_bytes = 0;
+    for (void*& p : ctx->h_io) SV_CUDA(cudaMallocHost(&p, CH));
+    ctx->h_io_bytes = CH;
+  }
+  for (int b = 0; b < 2; ++b) {
+    if (!ctx->h_io_ev[b]) SV_CUDA(cudaEventCreateWithFlags(&ctx->h_io_ev[b], cudaEventDisableTiming));
+    buf[b] = ctx->h_io[b];
+    ev[b] = ctx->h_io_ev[b];
+  }
+}
+
+// Large copies to or from pageable host memory go through the context's two
+// pinned buffers, the host side copied by several threads: a single-threaded
+// staging copy (what the driver does for pageable memory) runs at a few GB/s
+// when the destination pages are touched for the first time.
+static bool pageable(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return true;
+  }
+  return a.type == cudaMemoryTypeUnregistered;
+}
+
+static const size_t SV_STAGE_MIN = (size_t)32 << 20;
+
 void sv_h2d(sv_context* ctx, void* dst, const void* src, size_t bytes) {
-  if (bytes) SV_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  if (!bytes) return;
+  if (bytes < SV_STAGE_MIN || !pageable(src)) {
+    SV_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return;
+  }
+  void* pin[2];
+  cudaEvent_t ev[2];
+  sv_ctx_io(ctx, pin, ev);
+  int b = 0;
+  for (size_t off = 0; off < bytes; off += SV_IO_CHUNK, b ^= 1) {
+    size_t n = std::min(SV_IO_CHUNK, bytes - off);
+    SV_CUDA(cudaEventSynchronize(ev[b]));
+    sv_parallel_memcpy(pin[b], (const char*)src + off, n);
+    SV_CUDA(cudaMemcpyAsync((char*)dst + off, pin[b], n, cudaMemcpyHostToDevice, ctx->stream));
+    SV_CUDA(cudaEventRecord(ev[b], ctx->stream));
+  }
 }
 
 void sv_d2h(sv_context* ctx, void* dst, const void* src, size_t bytes) {
-  if (bytes) SV_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  if (!bytes) return;
+  if (bytes < SV_STAGE_MIN || !pageable(dst)) {
+    SV_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    sv_sync(ctx);
+    return;
+  }
+  void* pin[2];
+  cudaEvent_t ev[2];
+  sv_ctx_io(ctx, pin, ev);
+  // chunk i lands in pin[i & 1]; its host copy overlaps the transfer of chunk i + 1
+  const size_t nch = (bytes + SV_IO_CHUNK - 1) / SV_IO_CHUNK;
+  auto issue = [&](size_t i) {
+    size_t off = i * SV_IO_CHUNK, n = std::min(SV_IO_CHUNK, bytes - off);
+    SV_CUDA(cudaMemcpyAsync(pin[i & 1], (const char*)src + off, n, cudaMemcpyDeviceToHost, ctx->stream));
+    SV_CUDA(cudaEventRecord(ev[i & 1], ctx->stream));
+  };
+  SV_CUDA(cudaEventSynchronize(ev[0]));
+  SV_CUDA(cudaEventSynchronize(ev[1]));
+  issue(0);
+  for (size_t i = 0; i < nch; ++i) {
+    if (i + 1 < nch) issue(i + 1);
+    SV_CUDA(cudaEventSynchronize(ev[i & 1]));
+    size_t off = i * SV_IO_CHUNK, n = std::min(SV_IO_CHUNK, bytes - off);
+    sv_parallel_memcpy((char*)dst + off, pin[i & 1], n);
+  }
   sv_sync(ctx);
 }
 
@@ -172,6 +264,8 @@ SV_API int sv_context_destroy(sv_context* ctx) {
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   for (void* p : ctx->h_io)
     if (p) cudaFreeHost(p);
+  for (cudaEvent_t e : ctx->h_io_ev)
+    if (e) cudaEventDestroy(e);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return SV_OK;

@@ -47,33 +47,6 @@ __global__ void k_count_to_i32(const T* __restrict__ in, int32_t* __restrict__ o
   }
 }
 
-// Checks the CSC invariants (rows in range, strictly increasing per column) and
-// counts entries per row for the transpose.  One warp per column.
-__global__ void k_csc_check_hist(const int64_t* __restrict__ colptr,
-                                 const int32_t* __restrict__ rowidx, int64_t n_genes,
-                                 int64_t n_cells, int64_t nnz, unsigned long long* __restrict__ row_cnt,
-                                 int* status) {
-  int lane = threadIdx.x & 31;
-  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t c = warp; c < n_genes; c += nwarps) {
-    int64_t s = colptr[c], e = colptr[c + 1];
-    if (s < 0 || e < s || e > nnz) {
-      if (lane == 0) sv_flag(status, SV_STATUS_OOB);
-      continue;
-    }
-    for (int64_t i = s + lane; i < e; i += 32) {
-      int32_t r = rowidx[i];
-      if (r < 0 || r >= n_cells) {
-        sv_flag(status, SV_STATUS_OOB);
-        continue;
-      }
-      if (i + 1 < e && rowidx[i + 1] <= r) sv_flag(status, SV_STATUS_UNSORTED);
-      atomicAdd(&row_cnt[r], 1ull);
-    }
-  }
-}
-
 // Sets bit 1 of *flag when an index is not above its predecessor in the same
 // segment, bit 2 when a segment's pointers are out of order or out of range.
 __global__ void k_seg_unsorted(const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
@@ -93,29 +66,178 @@ __global__ void k_seg_unsorted(const int64_t* __restrict__ ptr, const int32_t* _
   }
 }
 
-__global__ void k_u64_to_i64(const unsigned long long* in, int64_t* out, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = (int64_t)in[i];
-}
+// ---- order-preserving transpose ------------------------------------------------
+// The output segments (e.g. cells, for the CSR copy of a CSC) are cut into tiles
+// of 2^tshift consecutive segments, one warp per tile.  A warp walks the source
+// segments (genes) in order, 32 at a time, one per lane; within such a batch a
+// per-output-segment lane mask in shared memory orders the entries that land in
+// the same output segment by source segment, so every output segment comes out
+// sorted without a sort and without global atomics.  tile_off[t * n_major + m] is
+// where source segment m's entries for tile t begin, relative to its start.
 
-// Scatter of CSC entries into their CSR rows (slot order within a row is
-// arbitrary here and fixed by the per-row sort below).
-__global__ void k_csc_scatter(const int64_t* __restrict__ colptr, const int32_t* __restrict__ rowidx,
-                              const int32_t* __restrict__ cnt, int64_t n_genes,
-                              unsigned long long* __restrict__ cursor, int32_t* __restrict__ out_col,
-                              int32_t* __restrict__ out_cnt) {
+constexpr int TR_WARPS = 8;     // tiles (warps) per block
+constexpr int TR_MAXT = 256;    // largest tile
+
+// Checks the source invariants (indices in range, strictly increasing within a
+// segment) and writes every source segment's tile offsets.  Warp per segment.
+__global__ void k_tr_bounds(const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                            int64_t n_major, int64_t n_minor, int64_t nnz, int tshift, int64_t n_tiles,
+                            int32_t* __restrict__ toff, int* status) {
   int lane = threadIdx.x & 31;
   int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t c = warp; c < n_genes; c += nwarps) {
-    int64_t s = colptr[c], e = colptr[c + 1];
-    for (int64_t i = s + lane; i < e; i += 32) {
-      int32_t r = rowidx[i];
-      unsigned long long pos = atomicAdd(&cursor[r], 1ull);
-      out_col[pos] = (int32_t)c;
-      out_cnt[pos] = cnt[i];
+  for (int64_t m = warp; m < n_major; m += nwarps) {
+    int64_t s = ptr[m], e = ptr[m + 1];
+    if (s < 0 || e < s || e > nnz || e - s > n_minor) {
+      if (lane == 0) sv_flag(status, SV_STATUS_OOB);
+      continue;
     }
+    bool bad = false;
+    for (int64_t i = s + lane; i < e; i += 32) {
+      int32_t c = idx[i];
+      int32_t p = i > s ? idx[i - 1] : -1;
+      if (c < 0 || c >= n_minor) {
+        sv_flag(status, SV_STATUS_OOB);
+        bad = true;
+        continue;
+      }
+      if (i > s && c <= p) {
+        sv_flag(status, SV_STATUS_UNSORTED);
+        bad = true;
+        continue;
+      }
+      int64_t tc = c >> tshift;
+      int64_t tp = (p < 0 || p >= n_minor) ? -1 : (int64_t)(p >> tshift);
+      for (int64_t t = tp + 1; t <= tc; ++t) toff[t * n_major + m] = (int32_t)(i - s);
+    }
+    if (__any_sync(0xffffffffu, bad)) continue;
+    int64_t last = e > s ? (int64_t)(idx[e - 1] >> tshift) : -1;
+    for (int64_t t = last + 1 + lane; t <= n_tiles; t += 32) toff[t * n_major + m] = (int32_t)(e - s);
+  }
+}
+
+// One batch of 32 source segments of a tile: lane l holds its segment's entry
+// range [a, a + n) and the inclusive prefix `incl` of n over the lanes.  The
+// batch's entries are spread evenly over the lanes (a segment present in every
+// cell of the tile would otherwise keep the whole warp waiting on one lane):
+// entry e belongs to lane gl, at position j.  Called by all lanes.
+__device__ __forceinline__ void tr_entry(int e, int incl, int n, int64_t a, int& gl, int64_t& j) {
+  int p = 0;
+#pragma unroll
+  for (int step = 16; step > 0; step >>= 1)
+    if (__shfl_sync(0xffffffffu, incl, p + step - 1) <= e) p += step;
+  // p is the first lane whose inclusive prefix exceeds e
+  int excl = __shfl_sync(0xffffffffu, incl - n, p);
+  int64_t ap = __shfl_sync(0xffffffffu, a, p);
+  gl = p;
+  j = ap + (e - excl);
+}
+
+__device__ __forceinline__ int warp_incl_scan(int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int u = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += u;
+  }
+  return v;
+}
+
+// Entries per output segment.  Warp per tile, shared-memory counters.
+__global__ void __launch_bounds__(TR_WARPS * 32) k_tr_count(
+    const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx, int64_t n_major, int64_t n_minor,
+    int tshift, int64_t n_tiles, const int32_t* __restrict__ toff, int64_t* __restrict__ seg_cnt) {
+  __shared__ int cnt[TR_WARPS][TR_MAXT];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, T = 1 << tshift;
+  const int64_t t = (int64_t)blockIdx.x * TR_WARPS + w;
+  if (t >= n_tiles) return;
+  for (int k = lane; k < T; k += 32) cnt[w][k] = 0;
+  __syncwarp();
+  const int64_t c0 = t << tshift;
+  const int32_t* lo = toff + t * n_major;
+  const int32_t* hi = lo + n_major;
+  for (int64_t g0 = 0; g0 < n_major; g0 += 32) {
+    int64_t g = g0 + lane;
+    int64_t a = 0;
+    int n = 0;
+    if (g < n_major) {
+      a = ptr[g] + lo[g];
+      n = hi[g] - lo[g];
+    }
+    const int incl = warp_incl_scan(n);
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    for (int base = 0; base < total; base += 32) {
+      const int e = base + lane;
+      int gl;
+      int64_t j;
+      tr_entry(e < total ? e : total - 1, incl, n, a, gl, j);
+      if (e < total) atomicAdd(&cnt[w][idx[j] - c0], 1);
+    }
+  }
+  __syncwarp();
+  for (int k = lane; k < T && c0 + k < n_minor; k += 32) seg_cnt[c0 + k] = cnt[w][k];
+}
+
+// Places every entry.  Warp per tile; per batch of 32 source segments a lane
+// mask per output segment gives each entry its rank among the batch's entries
+// of the same output segment.
+__global__ void __launch_bounds__(TR_WARPS * 32) k_tr_write(
+    const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx, const int32_t* __restrict__ val,
+    int64_t n_major, int64_t n_minor, int tshift, int64_t n_tiles, const int32_t* __restrict__ toff,
+    const int64_t* __restrict__ optr, int32_t* __restrict__ oidx, int32_t* __restrict__ oval) {
+  __shared__ unsigned mask[TR_WARPS][TR_MAXT];
+  __shared__ int64_t pos[TR_WARPS][TR_MAXT];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, T = 1 << tshift;
+  const int64_t t = (int64_t)blockIdx.x * TR_WARPS + w;
+  if (t >= n_tiles) return;
+  const int64_t c0 = t << tshift;
+  for (int k = lane; k < T; k += 32) {
+    mask[w][k] = 0u;
+    pos[w][k] = c0 + k < n_minor ? optr[c0 + k] : 0;
+  }
+  __syncwarp();
+  const int32_t* lo = toff + t * n_major;
+  const int32_t* hi = lo + n_major;
+  for (int64_t g0 = 0; g0 < n_major; g0 += 32) {
+    int64_t g = g0 + lane;
+    int64_t a = 0;
+    int n = 0;
+    if (g < n_major) {
+      a = ptr[g] + lo[g];
+      n = hi[g] - lo[g];
+    }
+    const int incl = warp_incl_scan(n);
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) continue;
+    for (int base = 0; base < total; base += 32) {
+      const int e = base + lane;
+      int gl;
+      int64_t j;
+      tr_entry(e < total ? e : total - 1, incl, n, a, gl, j);
+      if (e < total) atomicOr(&mask[w][idx[j] - c0], 1u << gl);
+    }
+    __syncwarp();
+    for (int base = 0; base < total; base += 32) {
+      const int e = base + lane;
+      int gl;
+      int64_t j;
+      tr_entry(e < total ? e : total - 1, incl, n, a, gl, j);
+      if (e < total) {
+        int k = idx[j] - (int32_t)c0;
+        int64_t o = pos[w][k] + __popc(mask[w][k] & ((1u << gl) - 1u));
+        oidx[o] = (int32_t)(g0 + gl);
+        oval[o] = val[j];
+      }
+    }
+    __syncwarp();
+    for (int k = lane; k < T; k += 32) {
+      unsigned mk = mask[w][k];
+      if (mk) {
+        pos[w][k] += __popc(mk);
+        mask[w][k] = 0u;
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -399,24 +521,28 @@ void sv_transpose_counts(sv_context* ctx, int64_t n_major, int64_t n_minor, int6
                          const int64_t* ptr, const int32_t* idx, const int32_t* cnt,
                          DevBuf<int64_t>& optr, DevBuf<int32_t>& oidx, DevBuf<int32_t>& ocnt,
                          const char* where) {
-  DevBuf<unsigned long long> rcnt(n_minor + 1);
-  sv_memset(ctx, rcnt.get(), 0, (n_minor + 1) * sizeof(unsigned long long));
-  sv_launch(ctx, "counts_check_hist", k_csc_check_hist, dim3(sv_grid_for(ctx, n_major * 32, 256)),
-            dim3(256), 0, ptr, idx, n_major, n_minor, nnz, rcnt.get(), ctx->d_status);
+  // tile size: enough warps to fill the device (~8 tiles per SM slot), tile
+  // offsets bounded to ~2 GB
+  int tshift = 8;
+  while (tshift > 5 && ((n_minor + (1ll << tshift) - 1) >> tshift) < (int64_t)ctx->num_sms * 48) --tshift;
+  while (tshift < 8 && (((n_minor + (1ll << tshift) - 1) >> tshift) + 1) * n_major * 4 > (2ll << 30)) ++tshift;
+  const int64_t n_tiles = (n_minor + (1ll << tshift) - 1) >> tshift;
+  DevBuf<int32_t> toff((size_t)(n_tiles + 1) * (size_t)n_major);
+  sv_launch(ctx, "counts_transpose_bounds", k_tr_bounds, dim3(sv_grid_for(ctx, n_major * 32, 256)),
+            dim3(256), 0, ptr, idx, n_major, n_minor, nnz, tshift, n_tiles, toff.get(), ctx->d_status);
   sv_check_device_status(ctx, where);
+  const dim3 gt((unsigned)((n_tiles + TR_WARPS - 1) / TR_WARPS)), bt(TR_WARPS * 32);
+  DevBuf<int64_t> seg(n_minor + 1);
+  sv_launch(ctx, "counts_transpose_count", k_tr_count, gt, bt, 0, ptr, idx, n_major, n_minor, tshift,
+            n_tiles, (const int32_t*)toff.get(), seg.get());
   optr.alloc(n_minor + 1);
-  DevBuf<int64_t> rc64(n_minor + 1);
-  sv_launch(ctx, "counts_u64_to_i64", k_u64_to_i64, dim3(sv_grid_for(ctx, n_minor, 256)), dim3(256),
-            0, (const unsigned long long*)rcnt.get(), rc64.get(), n_minor);
-  sv_scan_i64(ctx, rc64.get(), optr.get(), n_minor);
-  // cursors start at the segment offsets
-  sv_launch(ctx, "counts_u64_to_i64", k_colptr_to_i64<int64_t>, dim3(sv_grid_for(ctx, n_minor, 256)),
-            dim3(256), 0, (const int64_t*)optr.get(), (int64_t*)rcnt.get(), n_minor, (int64_t)0);
+  sv_scan_i64(ctx, seg.get(), optr.get(), n_minor);
   oidx.alloc(nnz);
   ocnt.alloc(nnz);
-  sv_launch(ctx, "counts_scatter", k_csc_scatter, dim3(sv_grid_for(ctx, n_major * 32, 256)),
-            dim3(256), 0, ptr, idx, cnt, n_major, rcnt.get(), oidx.get(), ocnt.get());
-  sv_sort_segments(ctx, optr.get(), n_minor, oidx.get(), ocnt.get());
+  sv_launch(ctx, "counts_transpose_write", k_tr_write, gt, bt, 0, ptr, idx, cnt, n_major, n_minor,
+            tshift, n_tiles, (const int32_t*)toff.get(), (const int64_t*)optr.get(), oidx.get(),
+            ocnt.get());
+  sv_sync(ctx);
 }
 
 // Builds the CSR copy from the CSC copy already on the device.

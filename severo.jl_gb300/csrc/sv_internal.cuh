@@ -86,6 +86,7 @@ struct sv_context {
   // between calls
   void* h_io[2] = {nullptr, nullptr};
   size_t h_io_bytes = 0;
+  cudaEvent_t h_io_ev[2] = {nullptr, nullptr};   // last transfer from / into each buffer
 };
 
 void sv_ctx_check(sv_context* ctx);
@@ -327,8 +328,17 @@ __device__ __forceinline__ double sv_load_val(const int32_t* p, int64_t i) { ret
 void sv_scan_i64(sv_context* ctx, const int64_t* in, int64_t* out, int64_t n);
 int64_t sv_read_i64(sv_context* ctx, const int64_t* dptr);
 void sv_memset(sv_context* ctx, void* p, int v, size_t bytes);
+// host <-> device copies on the context stream; sv_d2h returns when the data
+// are on the host.  Copies of 32 MB or more to or from pageable memory are
+// staged through the context's pinned buffers with several host threads.
 void sv_h2d(sv_context* ctx, void* dst, const void* src, size_t bytes);
 void sv_d2h(sv_context* ctx, void* dst, const void* src, size_t bytes);
+// the context's two pinned staging buffers (SV_IO_CHUNK bytes each) and the
+// events of their last transfers (wait on them before refilling)
+constexpr size_t SV_IO_CHUNK = (size_t)64 << 20;
+void sv_ctx_io(sv_context* ctx, void* buf[2], cudaEvent_t ev[2]);
+// memcpy split over up to 8 host threads
+void sv_parallel_memcpy(void* dst, const void* src, size_t n);
 void sv_sync(sv_context* ctx);
 int sv_grid_for(sv_context* ctx, int64_t work_items, int per_block, int max_per_sm = 8);
 // builds (or rebuilds) the CSR copy of a count matrix from its device CSC copy

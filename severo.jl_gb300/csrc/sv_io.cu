@@ -619,32 +619,18 @@ MMHeader read_header(Head& h) {
 // buffers (the copy of one overlaps the read into the other).  The buffer is
 // zero-padded to whole tiles.
 DevBuf<unsigned char> upload_text(sv_context* ctx, Head& h, int64_t& len_out) {
-  const size_t CH = (size_t)64 << 20;
+  const size_t CH = SV_IO_CHUNK;
   int64_t known = h.src.remaining();
   int64_t cap = known >= 0 ? (int64_t)(h.len - h.pos) + known : std::max<int64_t>(CH, 4 * (int64_t)(h.len - h.pos));
   cap = (cap + TILE - 1) / TILE * TILE + TILE;
   DevBuf<unsigned char> d(cap);
-  if (ctx->h_io_bytes < CH) {
-    for (void*& p : ctx->h_io) {
-      if (p) cudaFreeHost(p);
-      p = nullptr;
-    }
-    ctx->h_io_bytes = 0;
-    for (void*& p : ctx->h_io) SV_CUDA(cudaMallocHost(&p, CH));
-    ctx->h_io_bytes = CH;
-  }
-  void* pin[2] = {ctx->h_io[0], ctx->h_io[1]};
-  cudaEvent_t ev[2] = {nullptr, nullptr};
+  void* pin[2];
+  cudaEvent_t ev[2];
+  sv_ctx_io(ctx, pin, ev);
   int64_t len = 0;
-  auto cleanup = [&] {
-    for (int b = 0; b < 2; ++b)
-      if (ev[b]) cudaEventDestroy(ev[b]);
-  };
   try {
-    for (int b = 0; b < 2; ++b) SV_CUDA(cudaEventCreateWithFlags(&ev[b], cudaEventDisableTiming));
-    bool used[2] = {false, false};
     for (int b = 0;; b ^= 1) {
-      if (used[b]) SV_CUDA(cudaEventSynchronize(ev[b]));
+      SV_CUDA(cudaEventSynchronize(ev[b]));
       size_t n = 0;
       if (h.pos < h.len) {
         n = std::min(CH, h.len - h.pos);
@@ -669,15 +655,13 @@ DevBuf<unsigned char> upload_text(sv_context* ctx, Head& h, int64_t& len_out) {
       }
       SV_CUDA(cudaMemcpyAsync(d.get() + len, pin[b], n, cudaMemcpyHostToDevice, ctx->stream));
       SV_CUDA(cudaEventRecord(ev[b], ctx->stream));
-      used[b] = true;
       len += (int64_t)n;
     }
     sv_sync(ctx);
   } catch (...) {
-    cleanup();
+    cudaStreamSynchronize(ctx->stream);  // no transfer from the staging buffers left in flight
     throw;
   }
-  cleanup();
   // zero the rest of the last tile (at least one tile is scanned)
   int64_t padded = std::max<int64_t>(1, (len + TILE - 1) / TILE) * TILE;
   sv_memset(ctx, d.get() + len, 0, (size_t)(padded - len));

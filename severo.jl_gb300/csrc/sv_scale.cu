@@ -853,16 +853,16 @@ __global__ void __launch_bounds__(RB_THREADS) k_spmv_rb(
       const uint16_t* pi = rb_idx + a0;
       const uint16_t* pv = (const uint16_t*)rb_val + a0;
       const int ls = (int)(s - a0), le = (int)(e - a0);
-      for (int q = 4 * lane; q < le; q += 256) {
-        uint2 ri[2], rv[2];
+      for (int q = 4 * lane; q < le; q += 512) {
+        uint2 ri[4], rv[4];
 #pragma unroll
-        for (int h = 0; h < 2; ++h)
+        for (int h = 0; h < 4; ++h)
           if (q + 128 * h < le) {
             ri[h] = __ldg((const uint2*)(pi + q + 128 * h));
             rv[h] = __ldg((const uint2*)(pv + q + 128 * h));
           }
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < 4; ++h) {
           int qh = q + 128 * h;
           if (qh >= le) break;
 #pragma unroll
