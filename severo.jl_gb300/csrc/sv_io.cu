@@ -366,8 +366,8 @@ struct Source {
   virtual int64_t remaining() const { return -1; }
 };
 
-// Runs part(i, a, b) over [0, n) split into up to 8 host threads (large staging
-// copies: one core moves ~10 GB/s, the link several times that).
+// Runs part(i, a, b) over [0, n) split into up to 8 host threads (parallel
+// reads of a file into the staging buffers).
 template <typename F>
 void split_copy(size_t n, F part) {
   const size_t PART = (size_t)8 << 20;
@@ -393,8 +393,7 @@ struct MemSource : Source {
   MemSource(const char* p_, size_t n_) : p(p_), n(n_) {}
   size_t read(void* dst, size_t k) override {
     k = std::min(k, n - pos);
-    const char* src = p + pos;
-    split_copy(k, [=](int, size_t a, size_t b) { memcpy((char*)dst + a, src + a, b - a); });
+    sv_parallel_memcpy(dst, p + pos, k);
     pos += k;
     return k;
   }

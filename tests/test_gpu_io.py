@@ -205,6 +205,23 @@ def test_upload_csr_equals_csc(sv, ctx):
     check_both_copies(sv, Xc, ref)
 
 
+@pytest.mark.parametrize("n_cells", [1_000_000, 2_000_000])
+def test_upload_large_tiles(sv, ctx, n_cells):
+    """The transpose's largest tiles (128 and 256 cells per warp) on a tall
+    matrix: both device copies equal scipy's."""
+    rng = np.random.default_rng(n_cells)
+    n_genes = 70
+    rows = rng.integers(0, n_cells, n_genes * n_cells // 10)
+    cols = rng.integers(0, n_genes, rows.size)
+    A = sp.csc_matrix((rng.integers(1, 9, rows.size).astype(np.int32), (rows, cols)),
+                      shape=(n_cells, n_genes))
+    A.sum_duplicates()
+    A.sort_indices()
+    X = sv.CountMatrix.upload(A.indptr.astype(np.int64), A.indices.astype(np.int32),
+                              A.data.astype(np.int32), A.shape, ctx=ctx)
+    check_both_copies(sv, X, A)
+
+
 def test_upload_rejects_bad_counts(sv, ctx):
     ptr = np.array([0, 2, 3], np.int64)
     idx = np.array([0, 2, 1], np.int32)
