@@ -116,34 +116,9 @@ __global__ void k_tr_bounds(const int64_t* __restrict__ ptr, const int32_t* __re
   }
 }
 
-// One batch of 32 source segments of a tile: lane l holds its segment's entry
-// range [a, a + n) and the inclusive prefix `incl` of n over the lanes.  The
-// batch's entries are spread evenly over the lanes (a segment present in every
-// cell of the tile would otherwise keep the whole warp waiting on one lane):
-// entry e belongs to lane gl, at position j.  Called by all lanes.
-__device__ __forceinline__ void tr_entry(int e, int incl, int n, int64_t a, int& gl, int64_t& j) {
-  int p = 0;
-#pragma unroll
-  for (int step = 16; step > 0; step >>= 1)
-    if (__shfl_sync(0xffffffffu, incl, p + step - 1) <= e) p += step;
-  // p is the first lane whose inclusive prefix exceeds e
-  int excl = __shfl_sync(0xffffffffu, incl - n, p);
-  int64_t ap = __shfl_sync(0xffffffffu, a, p);
-  gl = p;
-  j = ap + (e - excl);
-}
-
-__device__ __forceinline__ int warp_incl_scan(int v) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    int u = __shfl_up_sync(0xffffffffu, v, o);
-    if (lane >= o) v += u;
-  }
-  return v;
-}
-
-// Entries per output segment.  Warp per tile, shared-memory counters.
+// Entries per output segment.  Warp per tile, shared-memory counters; lane l
+// walks source segment g0 + l of each batch of 32 (spreading a batch's entries
+// evenly over the lanes measured slower: the walk waits on loads, not lanes).
 __global__ void __launch_bounds__(TR_WARPS * 32) k_tr_count(
     const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx, int64_t n_major, int64_t n_minor,
     int tshift, int64_t n_tiles, const int32_t* __restrict__ toff, int64_t* __restrict__ seg_cnt) {
@@ -158,20 +133,10 @@ __global__ void __launch_bounds__(TR_WARPS * 32) k_tr_count(
   const int32_t* hi = lo + n_major;
   for (int64_t g0 = 0; g0 < n_major; g0 += 32) {
     int64_t g = g0 + lane;
-    int64_t a = 0;
-    int n = 0;
     if (g < n_major) {
-      a = ptr[g] + lo[g];
-      n = hi[g] - lo[g];
-    }
-    const int incl = warp_incl_scan(n);
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    for (int base = 0; base < total; base += 32) {
-      const int e = base + lane;
-      int gl;
-      int64_t j;
-      tr_entry(e < total ? e : total - 1, incl, n, a, gl, j);
-      if (e < total) atomicAdd(&cnt[w][idx[j] - c0], 1);
+      const int64_t base = ptr[g], a = base + lo[g], b = base + hi[g];
+#pragma unroll 4
+      for (int64_t j = a; j < b; ++j) atomicAdd(&cnt[w][idx[j] - c0], 1);
     }
   }
   __syncwarp();
@@ -198,36 +163,24 @@ __global__ void __launch_bounds__(TR_WARPS * 32) k_tr_write(
   __syncwarp();
   const int32_t* lo = toff + t * n_major;
   const int32_t* hi = lo + n_major;
+  const unsigned below = (1u << lane) - 1u;
   for (int64_t g0 = 0; g0 < n_major; g0 += 32) {
     int64_t g = g0 + lane;
-    int64_t a = 0;
-    int n = 0;
+    int64_t a = 0, b = 0;
     if (g < n_major) {
-      a = ptr[g] + lo[g];
-      n = hi[g] - lo[g];
+      int64_t base = ptr[g];
+      a = base + lo[g];
+      b = base + hi[g];
     }
-    const int incl = warp_incl_scan(n);
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    if (total == 0) continue;
-    for (int base = 0; base < total; base += 32) {
-      const int e = base + lane;
-      int gl;
-      int64_t j;
-      tr_entry(e < total ? e : total - 1, incl, n, a, gl, j);
-      if (e < total) atomicOr(&mask[w][idx[j] - c0], 1u << gl);
-    }
+#pragma unroll 4
+    for (int64_t j = a; j < b; ++j) atomicOr(&mask[w][idx[j] - c0], 1u << lane);
     __syncwarp();
-    for (int base = 0; base < total; base += 32) {
-      const int e = base + lane;
-      int gl;
-      int64_t j;
-      tr_entry(e < total ? e : total - 1, incl, n, a, gl, j);
-      if (e < total) {
-        int k = idx[j] - (int32_t)c0;
-        int64_t o = pos[w][k] + __popc(mask[w][k] & ((1u << gl) - 1u));
-        oidx[o] = (int32_t)(g0 + gl);
-        oval[o] = val[j];
-      }
+#pragma unroll 4
+    for (int64_t j = a; j < b; ++j) {
+      int k = idx[j] - (int32_t)c0;
+      int64_t o = pos[w][k] + __popc(mask[w][k] & below);
+      oidx[o] = (int32_t)g;
+      oval[o] = val[j];
     }
     __syncwarp();
     for (int k = lane; k < T; k += 32) {

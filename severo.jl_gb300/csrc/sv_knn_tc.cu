@@ -29,6 +29,8 @@ constexpr int EPI_WARPS = 8;
 constexpr int THREADS = (2 + EPI_WARPS) * 32;
 constexpr int KH = 32;             // candidates kept per (query, column half)
 constexpr long long TIMEOUT = 4000000000ll;   // cycles (~2 s) per wait
+constexpr int RING = 16;           // tile-sequence slots (> STAGES + 2 tiles in flight)
+constexpr uint32_t END = 0xffffffffu;   // tile id of the end-of-sequence slot
 
 struct __align__(1024) Smem {
   __nv_bfloat16 A[BM * BK];              // 16 KB
@@ -42,6 +44,10 @@ struct __align__(1024) Smem {
   unsigned long long tempty[2];
   unsigned long long abar;
   unsigned long long drain;
+  // the tile sequence chosen by the producer: slot t % RING holds (t << 32 | tile)
+  unsigned long long seq[RING];
+  // per epilogue warp, the largest (threshold + |q|^2 + margin) of its queries
+  float wmax[EPI_WARPS];
   uint32_t tmem_base;
   int err;
 };
@@ -72,6 +78,22 @@ __device__ __forceinline__ bool mbar_try(unsigned long long* b, uint32_t parity)
       : "memory");
   return ok != 0;
 }
+// The tile of sequence position t (its slot carries the tag t).  Bounded: on a
+// timeout the CTA aborts and the end of the sequence is returned.
+__device__ __forceinline__ uint32_t seq_tile(unsigned long long* seq, int t, int* err) {
+  volatile unsigned long long* p = seq + (t & (RING - 1));
+  unsigned long long v = *p;
+  if ((uint32_t)(v >> 32) == (uint32_t)t) return (uint32_t)v;
+  long long t0 = clock64();
+  while ((uint32_t)((v = *p) >> 32) != (uint32_t)t) {
+    if (*(volatile int*)err || clock64() - t0 > TIMEOUT) {
+      atomicOr(err, 1);
+      return END;
+    }
+  }
+  return (uint32_t)v;
+}
+
 // Bounded wait.  Returns false when the CTA is aborting (timeout here or elsewhere).
 __device__ __forceinline__ bool mbar_wait(unsigned long long* b, uint32_t parity, int* err) {
   if (mbar_try(b, parity)) return true;
@@ -217,7 +239,9 @@ template <bool FOLD>
 __global__ void __launch_bounds__(THREADS, 1)
     k_knn_tc(const __grid_constant__ CUtensorMap tmapA, const __grid_constant__ CUtensorMap tmapB,
              const float* __restrict__ sqpad, int64_t n, int ntiles, int32_t* __restrict__ cand,
-             int* __restrict__ status, const int64_t* __restrict__ sched, int around) {
+             int* __restrict__ status, const int64_t* __restrict__ sched, int around,
+             const float* __restrict__ coord, const float* __restrict__ nrm,
+             const unsigned* __restrict__ pmax) {
   extern __shared__ unsigned char smem_raw[];
   Smem* s = (Smem*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -246,6 +270,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     mbar_init(&s->abar, 1);
     mbar_init(&s->drain, 1);
+    for (int i = 0; i < RING; ++i) s->seq[i] = ~0ull;
+    for (int i = 0; i < EPI_WARPS; ++i) s->wmax[i] = __int_as_float(0x7f800000);
     s->err = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -263,30 +289,104 @@ __global__ void __launch_bounds__(THREADS, 1)
 
   if (warp == 0) {
     // ---------------- TMA producer ----------------
+    // Chooses the tile sequence.  With the points in locality order (coord: the
+    // sort coordinate of every point, as the BF16 operand holds it) a tile whose
+    // coordinate gap to this CTA's queries already exceeds every query's
+    // current threshold is skipped, and so is every tile beyond it: the squared
+    // gap bounds the squared distance of the operands from below.
     if (lane == 0) {
       int issued = 0;
+      bool ok = true;
       mbar_expect_tx(&s->abar, BM * BK * 2);
       tma_load_2d(s->A, &tmapA, 0, (int)q0, &s->abar);
-      for (int t = 0; t < ntiles; ++t) {
+      const bool prune = coord != nullptr;
+      float qlo = 0.f, qhi = 0.f;
+      if (prune) {
+        int64_t ql = q0 + BM < qend ? q0 + BM : qend;
+        qlo = coord[q0];
+        qhi = coord[ql - 1];
+      }
+      int up = t0 + 1, dn = t0 - 1;
+      // first coordinate of the next tile above, last of the next tile below
+      // (loaded one step ahead of their use)
+      auto lo_of = [&](int u) { return u < ntiles ? coord[p0 + (int64_t)u * BN] : 0.f; };
+      auto hi_of = [&](int v) {
+        int64_t hi = p0 + (int64_t)(v + 1) * BN;
+        return v >= 0 ? coord[(hi < pend ? hi : pend) - 1] : 0.f;
+      };
+      float lo_up = prune ? lo_of(up) : 0.f, hi_dn = prune ? hi_of(dn) : 0.f;
+      bool turn_up = true;
+      int t = 0;
+      for (;; ++t) {
+        int tile;
+        if (!prune) {
+          if (t >= ntiles) break;
+          tile = tile_at(t, t0, ntiles, around);
+        } else if (t == 0) {
+          tile = t0;
+        } else {
+          volatile float* wm = s->wmax;
+          float T = wm[0];
+#pragma unroll
+          for (int e = 1; e < EPI_WARPS; ++e) T = fmaxf(T, wm[e]);
+          bool uo = up < ntiles, dok = dn >= 0;
+          if (uo) {
+            float g = lo_up - qhi;
+            if (g > 0.f && g * g > T) uo = false;
+          }
+          if (dok) {
+            float g = qlo - hi_dn;
+            if (g > 0.f && g * g > T) dok = false;
+          }
+          if (!uo) up = ntiles;   // the gap only grows further out
+          if (!dok) dn = -1;
+          if (!uo && !dok) break;
+          bool go_up = uo && (!dok || turn_up);
+          if (uo && dok) turn_up = !turn_up;
+          if (go_up) {
+            tile = up++;
+            lo_up = lo_of(up);
+          } else {
+            tile = dn--;
+            hi_dn = hi_of(dn);
+          }
+        }
         int st = t % STAGES;
         uint32_t ph = (t / STAGES) & 1;
-        if (!mbar_wait(&s->empty[st], ph ^ 1, &s->err)) break;
+        if (!mbar_wait(&s->empty[st], ph ^ 1, &s->err)) {
+          ok = false;
+          break;
+        }
+        ((volatile unsigned long long*)s->seq)[t & (RING - 1)] = ((unsigned long long)t << 32) | (uint32_t)tile;
         mbar_expect_tx(&s->full[st], BN * BK * 2);
-        tma_load_2d(s->B[st], &tmapB, 0, (int)(p0 + (int64_t)tile_at(t, t0, ntiles, around) * BN),
-                    &s->full[st]);
+        tma_load_2d(s->B[st], &tmapB, 0, (int)(p0 + (int64_t)tile * BN), &s->full[st]);
         issued = t + 1;
       }
-      // drain: every issued copy has landed before the CTA may exit
-      {
-        long long t0 = clock64();
-        while (!mbar_try(&s->abar, 0) && clock64() - t0 < TIMEOUT) {
+      // end of the sequence: a stage that completes without a copy
+      bool sent = false;
+      if (ok) {
+        int st = issued % STAGES;
+        uint32_t ph = (issued / STAGES) & 1;
+        if (mbar_wait(&s->empty[st], ph ^ 1, &s->err)) {
+          ((volatile unsigned long long*)s->seq)[issued & (RING - 1)] =
+              ((unsigned long long)issued << 32) | END;
+          mbar_arrive(&s->full[st]);
+          sent = true;
         }
       }
-      for (int t = issued - STAGES < 0 ? 0 : issued - STAGES; t < issued; ++t) {
-        int st = t % STAGES;
-        uint32_t ph = (t / STAGES) & 1;
-        long long t0 = clock64();
-        while (!mbar_try(&s->full[st], ph) && clock64() - t0 < TIMEOUT) {
+      // drain: every issued copy has landed before the CTA may exit (the tile
+      // that shared the end slot's stage was consumed before the end was written)
+      {
+        long long c0 = clock64();
+        while (!mbar_try(&s->abar, 0) && clock64() - c0 < TIMEOUT) {
+        }
+      }
+      int first = issued - STAGES + (sent ? 1 : 0);
+      for (int tt = first < 0 ? 0 : first; tt < issued; ++tt) {
+        int st = tt % STAGES;
+        uint32_t ph = (tt / STAGES) & 1;
+        long long c0 = clock64();
+        while (!mbar_try(&s->full[st], ph) && clock64() - c0 < TIMEOUT) {
         }
       }
     }
@@ -295,14 +395,17 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (lane == 0) {
       bool ok = mbar_wait(&s->abar, 0, &s->err);
       uint32_t a_base = su32(s->A);
-      int t = 0;
-      for (; ok && t < ntiles; ++t) {
+      for (int t = 0; ok; ++t) {
         int st = t % STAGES;
         uint32_t ph = (t / STAGES) & 1;
         int ab = t & 1;
         uint32_t aph = (t >> 1) & 1;
         if (!mbar_wait(&s->tempty[ab], aph ^ 1, &s->err)) break;
         if (!mbar_wait(&s->full[st], ph, &s->err)) break;
+        if (seq_tile(s->seq, t, &s->err) == END) {
+          mbar_arrive(&s->tfull[ab]);   // the epilogue reads the end too
+          break;
+        }
         fence_after();
         uint32_t b_base = su32(s->B[st]);
         uint32_t d = tmem + (uint32_t)(ab * BN);
@@ -333,13 +436,19 @@ __global__ void __launch_bounds__(THREADS, 1)
       bidx[i] = -1;
     }
     uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
-    for (int t = 0; t < ntiles; ++t) {
+    // pruning bound of this query: threshold + |q|^2 + a margin for the FP32
+    // accumulation of the MMA (2^-15 (|q|^2 + max |p|^2), several times its bound)
+    float qn = 0.f;
+    if (coord && q < qend) qn = nrm[q] + 0x1p-15f * (nrm[q] + __uint_as_float(*pmax));
+    for (int t = 0;; ++t) {
       int ab = t & 1;
       uint32_t aph = (t >> 1) & 1;
       bool ok = mbar_wait(&s->tfull[ab], aph, &s->err);
       if (!__all_sync(0xffffffffu, ok)) break;   // warp-uniform: the TMEM loads are .aligned
       fence_after();
-      int64_t j0 = p0 + (int64_t)tile_at(t, t0, ntiles, around) * BN + half * (BN / 2);
+      const uint32_t tile = seq_tile(s->seq, t, &s->err);
+      if (__any_sync(0xffffffffu, tile == END)) break;   // warp-uniform (a timed-out lane sees END)
+      int64_t j0 = p0 + (int64_t)tile * BN + half * (BN / 2);
       uint32_t tbase = tmem + lane_off + (uint32_t)(ab * BN + half * (BN / 2));
       // two chunks per TMEM round trip: both loads are issued before one wait
 #pragma unroll 1
@@ -402,6 +511,14 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
         }
       }
+      if (coord && (t & 3) == 3) {
+        // every fourth tile; keys only fall, so a stale (larger) bound read by
+        // the producer is safe
+        float v = q < qend ? best[KH - 1] + qn : -FLT_MAX;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0) ((volatile float*)s->wmax)[ew] = v;
+      }
     }
     if (q < qend) {
       int32_t* o = cand + q * (2 * KH) + half * KH;
@@ -447,9 +564,12 @@ __global__ void k_pack_bf16(const float* __restrict__ X, int64_t n, int dp, int6
 // columns d..d+2, points carry |p|^2 split into three BF16 parts (hi, mid, lo,
 // summing to the FP32 norm of the rounded row to ~2^-24), so that the MMA yields
 // D = q.p - |p|^2/2 and the key |p|^2 - 2 q.p is -2 D.
+// With coord: also the sort coordinate (column dim) and |p|^2 of the BF16
+// operand row, and the largest |p|^2 (float bits; all values >= 0).
 __global__ void k_pack_fold(const float* __restrict__ X, int64_t n, int dp, int d,
                             __nv_bfloat16* __restrict__ Xq, __nv_bfloat16* __restrict__ Xp,
-                            const int* __restrict__ perm) {
+                            const int* __restrict__ perm, int dim, float* __restrict__ coord,
+                            float* __restrict__ nrm, unsigned* __restrict__ pmax) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     float s = 0.f;
@@ -461,6 +581,11 @@ __global__ void k_pack_fold(const float* __restrict__ X, int64_t n, int dp, int 
       Xp[i * BK + c] = b;
       float r = __bfloat162float(b);
       s = fmaf(r, r, s);
+    }
+    if (coord) {
+      coord[i] = __bfloat162float(__float2bfloat16_rn(X[src * dp + dim]));
+      nrm[i] = s;
+      atomicMax(pmax, __float_as_uint(s));
     }
     __nv_bfloat16 p1 = __float2bfloat16_rn(s);
     float r1 = s - __bfloat162float(p1);
@@ -564,7 +689,10 @@ int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unus
     // locality order: the points sorted (within each sample) along their widest
     // dimension, and every CTA visiting the tiles around its own queries first
     bool around = !getenv("SV_KNN_NOSORT") && n >= 4 * BN;
+    // tiles beyond every query's reach are skipped (locality order, folded norms)
+    const bool prune = around && fold && !getenv("SV_KNN_NOPRUNE");
     DevBuf<int> perm;
+    int dim = 0;
     if (around) {
       int nseg = segs ? (int)segs->size() - 1 : 1;
       DevBuf<double> mom(2 * dp);
@@ -573,7 +701,6 @@ int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unus
                 X32, n, dp, mom.get());
       std::vector<double> hm(2 * dp);
       sv_d2h(ctx, hm.data(), mom.get(), 2 * dp * 8);
-      int dim = 0;
       double best = -1;
       for (int c = 0; c < d; ++c) {
         double mean = hm[c] / (double)n, var = hm[dp + c] / (double)n - mean * mean;
@@ -599,10 +726,18 @@ int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unus
     const int* pm = around ? (const int*)perm.get() : (const int*)nullptr;
     DevBuf<__nv_bfloat16> Xq((size_t)n * BK), Xp;
     DevBuf<float> sq(npad);
+    DevBuf<float> coord, nrm;
+    DevBuf<unsigned> pmax;
+    if (prune) {
+      coord.alloc(n);
+      nrm.alloc(n);
+      pmax.alloc(1);
+      sv_memset(ctx, pmax.get(), 0, sizeof(unsigned));
+    }
     if (fold) {
       Xp.alloc((size_t)n * BK);
       sv_launch(ctx, "knn_pack_fold", k_pack_fold, dim3(sv_grid_for(ctx, n, 256, 8)), dim3(256), 0, X32,
-                n, dp, d, Xq.get(), Xp.get(), pm);
+                n, dp, d, Xq.get(), Xp.get(), pm, dim, coord.get(), nrm.get(), pmax.get());
     } else {
       sv_launch(ctx, "knn_pack_bf16", k_pack_bf16, dim3(sv_grid_for(ctx, npad, 256, 8)), dim3(256), 0,
                 X32, n, dp, npad, Xq.get(), sq.get(), pm);
@@ -647,12 +782,13 @@ int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unus
       SV_CUDA(cudaFuncSetAttribute(k_knn_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       sv_launch(ctx, "knn_tc_tiles", k_knn_tc<true>, dim3(nblocks), dim3(THREADS), smem, tmapA, tmapB,
                 (const float*)sq.get(), n, ntiles, cout, ctx->d_status, (const int64_t*)sched.get(),
-                (int)around);
+                (int)around, (const float*)coord.get(), (const float*)nrm.get(),
+                (const unsigned*)pmax.get());
     } else {
       SV_CUDA(cudaFuncSetAttribute(k_knn_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       sv_launch(ctx, "knn_tc_tiles", k_knn_tc<false>, dim3(nblocks), dim3(THREADS), smem, tmapA, tmapB,
                 (const float*)sq.get(), n, ntiles, cout, ctx->d_status, (const int64_t*)sched.get(),
-                (int)around);
+                (int)around, (const float*)nullptr, (const float*)nullptr, (const unsigned*)nullptr);
     }
     if (around)
       sv_launch(ctx, "knn_unperm", k_cand_unperm, dim3(sv_grid_for(ctx, n * K2, 256, 8)), dim3(256), 0,
