@@ -236,10 +236,12 @@ def timed_steps(sv, ctx, td, counts, hvf, w, init, form, steps, warmup, with_sta
             "irlba": info}
 
 
-def e2e_steps(sv, ctx, td, host, shape, hvf, w, init, form, steps):
+def e2e_steps(sv, ctx, td, host, shape, hvf, w, init, form, steps, outs=None):
     """The same pipeline through the public API with host buffers: upload of the
-    CSC counts (pinned host memory) and download of Z, nn_index and distances."""
+    CSC counts (pinned host memory) and download of Z, nn_index and distances
+    (into the pinned arrays `outs` = (Z, nn_index, distances) when given)."""
     colptr, rowval, nzval = host
+    Zo, io, do = outs if outs else (None, None, None)
     n = shape[0]
     h2d = colptr.nbytes + rowval.nbytes + nzval.nbytes
     d2h = 0
@@ -250,8 +252,9 @@ def e2e_steps(sv, ctx, td, host, shape, hvf, w, init, form, steps):
         counts = sv.CountMatrix.upload(colptr, rowval, nzval, shape, 0, ctx)
         d = sv.normalize_cells(counts, scale_factor=SCALE_FACTOR, dtype=form[0], ctx=ctx)
         S = sv.scale_features(d, scale_max=SCALE_MAX, features=hvf)
-        em = sv.pca(S, w["npcs"], tol=1e-5, init=init, download=True)
-        idx, dist = sv.ann(em, w["k"], precision=form[1], ctx=ctx)
+        em = sv.pca(S, w["npcs"], tol=1e-5, init=init, download=True, out=Zo)
+        idx, dist = sv.ann(em, w["k"], precision=form[1], ctx=ctx,
+                           out=(io, do) if io is not None else None)
         d2h = (em.coordinates.nbytes + em.stdev.nbytes + em.basis.nbytes + idx.nbytes + dist.nbytes)
         del counts, d, S, em
     ctx.sync()
@@ -443,9 +446,15 @@ def main():
             host.append(a)
             keep.append(p)
         del A
+        # results land in pinned host arrays allocated once, as the inputs do
+        outs = []
+        for shp, dt_ in (((n, w["npcs"]), np.float64), ((n, w["k"]), np.int32), ((n, w["k"]), np.float64)):
+            a, p = pinned_copy(sv, np.zeros(shp[0] * shp[1], dtype=dt_))
+            outs.append(a.reshape(shp, order="F"))
+            keep.append(p)
         ke = max(1, min(args.steps, 3))
-        e2e_steps(sv, ctx, td, host, (n, w["n_genes"]), hvf, w, init, form, 1)   # warm-up
-        dt, h2d, d2h = e2e_steps(sv, ctx, td, host, (n, w["n_genes"]), hvf, w, init, form, ke)
+        e2e_steps(sv, ctx, td, host, (n, w["n_genes"]), hvf, w, init, form, 1, outs)   # warm-up
+        dt, h2d, d2h = e2e_steps(sv, ctx, td, host, (n, w["n_genes"]), hvf, w, init, form, ke, outs)
         dt = allmax(td, dt)
         e2e = {"value": world * n * ke / dt, "unit": "cells/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": ke}

@@ -536,15 +536,27 @@ class _Embed(_Handle):
     _free = "sv_embed_free"
 
 
-def pca(S: CenteredMatrix, npcs, tol=1e-5, maxit=1000, init=None, seed=0, download=True):
-    """src/embedding.jl:46-94 with algorithm=:irlba: Z = U diag(s), stdev, loadings."""
+def _out(out, shape, dtype):
+    """A caller-provided output array (e.g. pinned host memory reused across
+    calls) checked for shape, type and column-major layout, or a new one."""
+    if out is None:
+        return np.zeros(shape, dtype=dtype, order="F")
+    if out.shape != shape or out.dtype != np.dtype(dtype) or not out.flags.f_contiguous:
+        raise ValueError(f"out must be a column-major {np.dtype(dtype)} array of shape {shape}")
+    return out
+
+
+def pca(S: CenteredMatrix, npcs, tol=1e-5, maxit=1000, init=None, seed=0, download=True, out=None):
+    """src/embedding.jl:46-94 with algorithm=:irlba: Z = U diag(s), stdev, loadings.
+    out: an optional column-major FP64 (n_cells x npcs) array that receives Z,
+    e.g. pinned host memory reused across calls."""
     ctx = S.ctx
     m, n = S.shape
     k = min(m, n, npcs)
     if init is None:
         init = np.random.default_rng(seed).standard_normal(n)
     init = np.ascontiguousarray(init, dtype=np.float64)
-    Z = np.zeros((m, k), order="F") if download else None
+    Z = _out(out, (m, k), np.float64) if download else None
     stdev = np.zeros(k)
     load = np.zeros((n, k), order="F")
     h = C.c_void_p()
@@ -652,10 +664,12 @@ _PREC = {"fp32": SV_KNN_FP32, "bf16": SV_KNN_BF16}
 
 
 def ann(X, k, metric="euclidean", include_self=True, precision="fp32", ctx: Context | None = None,
-        keep=False, download=True):
+        keep=False, download=True, out=None):
     """src/neighbours.jl:19-30: (nn_index n x k Int32 1-based, distances n x k).
     X may be a LinearEmbedding whose coordinates are still on the device;
-    download=False leaves the lists on the device (returned handle only)."""
+    download=False leaves the lists on the device (returned handle only); out
+    = (nn_index, distances) receives them in caller-provided column-major arrays
+    (device coordinates only)."""
     ctx = ctx or default_context()
     if isinstance(X, LinearEmbedding):
         h = C.c_void_p()
@@ -663,8 +677,8 @@ def ann(X, k, metric="euclidean", include_self=True, precision="fp32", ctx: Cont
         a, b = C.c_int64(), C.c_int64()
         L.check(ctx.lib.sv_embed_info(e, C.byref(a), C.byref(b)))
         n = a.value
-        idx = np.zeros((n, k), dtype=np.int32, order="F") if download else None
-        dist = np.zeros((n, k), dtype=np.float64, order="F") if download else None
+        idx = _out(out[0] if out else None, (n, k), np.int32) if download else None
+        dist = _out(out[1] if out else None, (n, k), np.float64) if download else None
         L.check(ctx.lib.sv_knn_embed(ctx.h, e, 0, k, _METRICS[metric], int(include_self),
                                       _PREC[precision], _ptr(idx), _ptr(dist), C.byref(h)))
         return (idx, dist, KNN(ctx, h)) if keep else (idx, dist)

@@ -8,6 +8,8 @@
 // within rows.
 #include "sv_internal.cuh"
 
+#include <type_traits>
+
 namespace {
 
 // ---- conversion of the uploaded arrays --------------------------------------
@@ -79,10 +81,12 @@ constexpr int TR_WARPS = 8;     // tiles (warps) per block
 constexpr int TR_MAXT = 256;    // largest tile
 
 // Checks the source invariants (indices in range, strictly increasing within a
-// segment) and writes every source segment's tile offsets.  Warp per segment.
+// segment) and writes every source segment's tile offsets, segment-major
+// (toffm[m * (n_tiles + 1) + t]: a warp's writes land next to each other).
+// Warp per segment.
 __global__ void k_tr_bounds(const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
                             int64_t n_major, int64_t n_minor, int64_t nnz, int tshift, int64_t n_tiles,
-                            int32_t* __restrict__ toff, int* status) {
+                            int32_t* __restrict__ toffm, int* status) {
   int lane = threadIdx.x & 31;
   int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -93,26 +97,62 @@ __global__ void k_tr_bounds(const int64_t* __restrict__ ptr, const int32_t* __re
       continue;
     }
     bool bad = false;
-    for (int64_t i = s + lane; i < e; i += 32) {
-      int32_t c = idx[i];
-      int32_t p = i > s ? idx[i - 1] : -1;
-      if (c < 0 || c >= n_minor) {
-        sv_flag(status, SV_STATUS_OOB);
-        bad = true;
-        continue;
+    // four entries per lane per step (16-byte loads from the aligned start);
+    // the entry before a lane's first comes from the lane below, or from the
+    // previous step's last lane
+    const int64_t a0 = s & ~3ll;
+    int32_t carry = -1;
+    for (int64_t g0 = a0; g0 < e; g0 += 128) {
+      const int64_t g = g0 + 4 * lane;
+      int4 q = g < e ? *(const int4*)(idx + g) : make_int4(-1, -1, -1, -1);
+      int32_t v[4] = {q.x, q.y, q.z, q.w};
+      int32_t before = __shfl_up_sync(0xffffffffu, v[3], 1);
+      if (lane == 0) before = carry;
+      carry = __shfl_sync(0xffffffffu, v[3], 31);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t i = g + u;
+        if (i < s || i >= e) continue;
+        const int32_t c = v[u];
+        const int32_t p = i > s ? (u ? v[u - 1] : before) : -1;
+        if (c < 0 || c >= n_minor) {
+          sv_flag(status, SV_STATUS_OOB);
+          bad = true;
+          continue;
+        }
+        if (i > s && c <= p) {
+          sv_flag(status, SV_STATUS_UNSORTED);
+          bad = true;
+          continue;
+        }
+        int64_t tc = c >> tshift;
+        int64_t tp = (p < 0 || p >= n_minor) ? -1 : (int64_t)(p >> tshift);
+        for (int64_t t = tp + 1; t <= tc; ++t) toffm[m * (n_tiles + 1) + t] = (int32_t)(i - s);
       }
-      if (i > s && c <= p) {
-        sv_flag(status, SV_STATUS_UNSORTED);
-        bad = true;
-        continue;
-      }
-      int64_t tc = c >> tshift;
-      int64_t tp = (p < 0 || p >= n_minor) ? -1 : (int64_t)(p >> tshift);
-      for (int64_t t = tp + 1; t <= tc; ++t) toff[t * n_major + m] = (int32_t)(i - s);
     }
     if (__any_sync(0xffffffffu, bad)) continue;
     int64_t last = e > s ? (int64_t)(idx[e - 1] >> tshift) : -1;
-    for (int64_t t = last + 1 + lane; t <= n_tiles; t += 32) toff[t * n_major + m] = (int32_t)(e - s);
+    for (int64_t t = last + 1 + lane; t <= n_tiles; t += 32) toffm[m * (n_tiles + 1) + t] = (int32_t)(e - s);
+  }
+}
+
+// Segment-major tile offsets -> tile-major (the walks read one tile's offsets
+// for 32 consecutive segments at a time): a 32 x 32 shared-memory transpose.
+__global__ void k_tr_swap(const int32_t* __restrict__ in, int64_t rows, int64_t cols,
+                          int32_t* __restrict__ out) {
+  __shared__ int32_t tile[32][33];
+  const int64_t r0 = (int64_t)blockIdx.x * 32;
+  for (int64_t c0 = (int64_t)blockIdx.y * 32; c0 < cols; c0 += (int64_t)gridDim.y * 32) {
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+      int64_t r = r0 + k, c = c0 + threadIdx.x;
+      if (r < rows && c < cols) tile[k][threadIdx.x] = in[r * cols + c];
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+      int64_t c = c0 + k, r = r0 + threadIdx.x;
+      if (r < rows && c < cols) out[c * rows + r] = tile[threadIdx.x][k];
+    }
+    __syncthreads();
   }
 }
 
@@ -143,51 +183,68 @@ __global__ void __launch_bounds__(TR_WARPS * 32) k_tr_count(
   for (int k = lane; k < T && c0 + k < n_minor; k += 32) seg_cnt[c0 + k] = cnt[w][k];
 }
 
-// Places every entry.  Warp per tile; per batch of 32 source segments a lane
-// mask per output segment gives each entry its rank among the batch's entries
-// of the same output segment.
+// Places every entry.  Warp per tile; per batch of 32 (or, WIDE, 64: two per
+// lane) source segments a mask per output segment gives each entry its rank
+// among the batch's entries of the same output segment.  WIDE halves the
+// batches and lengthens each output row's run per batch (faster with many
+// tiles); with few tiles the narrow form keeps a lane's load chain short.
+template <bool WIDE>
 __global__ void __launch_bounds__(TR_WARPS * 32) k_tr_write(
     const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx, const int32_t* __restrict__ val,
     int64_t n_major, int64_t n_minor, int tshift, int64_t n_tiles, const int32_t* __restrict__ toff,
     const int64_t* __restrict__ optr, int32_t* __restrict__ oidx, int32_t* __restrict__ oval) {
-  __shared__ unsigned mask[TR_WARPS][TR_MAXT];
+  using Mask = typename std::conditional<WIDE, unsigned long long, unsigned>::type;
+  constexpr int H = WIDE ? 2 : 1;
+  __shared__ Mask mask[TR_WARPS][TR_MAXT];
   __shared__ int64_t pos[TR_WARPS][TR_MAXT];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, T = 1 << tshift;
   const int64_t t = (int64_t)blockIdx.x * TR_WARPS + w;
   if (t >= n_tiles) return;
   const int64_t c0 = t << tshift;
   for (int k = lane; k < T; k += 32) {
-    mask[w][k] = 0u;
+    mask[w][k] = 0;
     pos[w][k] = c0 + k < n_minor ? optr[c0 + k] : 0;
   }
   __syncwarp();
   const int32_t* lo = toff + t * n_major;
   const int32_t* hi = lo + n_major;
-  const unsigned below = (1u << lane) - 1u;
-  for (int64_t g0 = 0; g0 < n_major; g0 += 32) {
-    int64_t g = g0 + lane;
-    int64_t a = 0, b = 0;
-    if (g < n_major) {
-      int64_t base = ptr[g];
-      a = base + lo[g];
-      b = base + hi[g];
+  for (int64_t g0 = 0; g0 < n_major; g0 += 32 * H) {
+    int64_t a[H], b[H];
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      int64_t g = g0 + 32 * h + lane;
+      a[h] = b[h] = 0;
+      if (g < n_major) {
+        int64_t base = ptr[g];
+        a[h] = base + lo[g];
+        b[h] = base + hi[g];
+      }
     }
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      const Mask bit = (Mask)1 << (32 * h + lane);
 #pragma unroll 4
-    for (int64_t j = a; j < b; ++j) atomicOr(&mask[w][idx[j] - c0], 1u << lane);
+      for (int64_t j = a[h]; j < b[h]; ++j) atomicOr(&mask[w][idx[j] - c0], bit);
+    }
     __syncwarp();
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      const Mask below = ((Mask)1 << (32 * h + lane)) - 1;
+      const int32_t g = (int32_t)(g0 + 32 * h + lane);
 #pragma unroll 4
-    for (int64_t j = a; j < b; ++j) {
-      int k = idx[j] - (int32_t)c0;
-      int64_t o = pos[w][k] + __popc(mask[w][k] & below);
-      oidx[o] = (int32_t)g;
-      oval[o] = val[j];
+      for (int64_t j = a[h]; j < b[h]; ++j) {
+        int k = idx[j] - (int32_t)c0;
+        int64_t o = pos[w][k] + __popcll((unsigned long long)(mask[w][k] & below));
+        oidx[o] = g;
+        oval[o] = val[j];
+      }
     }
     __syncwarp();
     for (int k = lane; k < T; k += 32) {
-      unsigned mk = mask[w][k];
+      Mask mk = mask[w][k];
       if (mk) {
-        pos[w][k] += __popc(mk);
-        mask[w][k] = 0u;
+        pos[w][k] += __popcll((unsigned long long)mk);
+        mask[w][k] = 0;
       }
     }
     __syncwarp();
@@ -481,9 +538,16 @@ void sv_transpose_counts(sv_context* ctx, int64_t n_major, int64_t n_minor, int6
   while (tshift < 8 && (((n_minor + (1ll << tshift) - 1) >> tshift) + 1) * n_major * 4 > (2ll << 30)) ++tshift;
   const int64_t n_tiles = (n_minor + (1ll << tshift) - 1) >> tshift;
   DevBuf<int32_t> toff((size_t)(n_tiles + 1) * (size_t)n_major);
-  sv_launch(ctx, "counts_transpose_bounds", k_tr_bounds, dim3(sv_grid_for(ctx, n_major * 32, 256)),
-            dim3(256), 0, ptr, idx, n_major, n_minor, nnz, tshift, n_tiles, toff.get(), ctx->d_status);
-  sv_check_device_status(ctx, where);
+  {
+    DevBuf<int32_t> toffm((size_t)(n_tiles + 1) * (size_t)n_major);
+    sv_launch(ctx, "counts_transpose_bounds", k_tr_bounds, dim3(sv_grid_for(ctx, n_major * 32, 256)),
+              dim3(256), 0, ptr, idx, n_major, n_minor, nnz, tshift, n_tiles, toffm.get(), ctx->d_status);
+    sv_check_device_status(ctx, where);
+    const int64_t ty = (n_tiles + 1 + 31) / 32;
+    sv_launch(ctx, "counts_transpose_bounds", k_tr_swap, dim3((unsigned)((n_major + 31) / 32),
+              (unsigned)(ty < 65535 ? ty : 65535)), dim3(32, 8), 0, (const int32_t*)toffm.get(), n_major,
+              n_tiles + 1, toff.get());
+  }
   const dim3 gt((unsigned)((n_tiles + TR_WARPS - 1) / TR_WARPS)), bt(TR_WARPS * 32);
   DevBuf<int64_t> seg(n_minor + 1);
   sv_launch(ctx, "counts_transpose_count", k_tr_count, gt, bt, 0, ptr, idx, n_major, n_minor, tshift,
@@ -492,9 +556,14 @@ void sv_transpose_counts(sv_context* ctx, int64_t n_major, int64_t n_minor, int6
   sv_scan_i64(ctx, seg.get(), optr.get(), n_minor);
   oidx.alloc(nnz);
   ocnt.alloc(nnz);
-  sv_launch(ctx, "counts_transpose_write", k_tr_write, gt, bt, 0, ptr, idx, cnt, n_major, n_minor,
-            tshift, n_tiles, (const int32_t*)toff.get(), (const int64_t*)optr.get(), oidx.get(),
-            ocnt.get());
+  if (n_tiles >= (int64_t)ctx->num_sms * 32)
+    sv_launch(ctx, "counts_transpose_write", k_tr_write<true>, gt, bt, 0, ptr, idx, cnt, n_major, n_minor,
+              tshift, n_tiles, (const int32_t*)toff.get(), (const int64_t*)optr.get(), oidx.get(),
+              ocnt.get());
+  else
+    sv_launch(ctx, "counts_transpose_write", k_tr_write<false>, gt, bt, 0, ptr, idx, cnt, n_major, n_minor,
+              tshift, n_tiles, (const int32_t*)toff.get(), (const int64_t*)optr.get(), oidx.get(),
+              ocnt.get());
   sv_sync(ctx);
 }
 

@@ -175,3 +175,24 @@ def test_feature_side_paths_agree(sv, ctx, O, monkeypatch):
         monkeypatch.setenv("SV_VSIDE", mode)
         out[mode] = sv.pca(S, 10, tol=1e-8, init=init).stdev
     assert np.max(np.abs(out["block"] - out["multi"]) / out["block"]) < 1e-7
+
+
+def test_caller_provided_outputs(sv, ctx, O):
+    """pca(out=Z) and ann(out=(idx, dist)) fill the caller's column-major arrays
+    with the same results as freshly allocated ones; wrong shapes are refused."""
+    X = O.synth_counts(2500, 1200, -1.2, 1.6, depth=0.3, seed=5, n_clusters=5)
+    d = sv.normalize_cells(X, scale_factor=1e4, dtype="float32", ctx=ctx)
+    S = sv.scale_features(d, scale_max=10.0, features=np.arange(1, 301))
+    init = np.random.default_rng(3).standard_normal(300)
+    em = sv.pca(S, 12, tol=1e-8, init=init)
+    Z = np.full((2500, 12), np.nan, order="F")
+    em2 = sv.pca(S, 12, tol=1e-8, init=init, out=Z)
+    assert em2.coordinates is Z and np.array_equal(Z, em.coordinates)
+    idx, dist = sv.ann(em, 10, ctx=ctx)
+    oi = np.zeros((2500, 10), dtype=np.int32, order="F")
+    od = np.zeros((2500, 10), dtype=np.float64, order="F")
+    i2, d2 = sv.ann(em2, 10, ctx=ctx, out=(oi, od))
+    assert i2 is oi and d2 is od
+    assert np.array_equal(oi, idx) and np.array_equal(od, dist)
+    with pytest.raises(ValueError):
+        sv.pca(S, 12, tol=1e-8, init=init, out=np.zeros((2500, 12)))   # row-major

@@ -49,14 +49,14 @@ def test_barrier_and_max_over_ranks():
     assert got == [(0, 11.0), (1, 11.0)]
 
 
-def test_reference_arm_under_torchrun():
+def test_reference_arm_under_torchrun(tmp_path):
     """`bench.py --impl reference` launched as two ranks: rank 0 alone works and
     prints one JSON line, rank 1 exits 0."""
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl",
            "reference", "--gpus", "2", "--steps", "1", "--warmup", "1", "--workload", "small"]
-    env = dict(os.environ, OMP_NUM_THREADS="2")
+    env = dict(os.environ, OMP_NUM_THREADS="2", TMPDIR=str(tmp_path))   # torchrun's scratch
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600, env=env)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
