@@ -52,6 +52,32 @@ function upload_counts(A::SparseMatrixCSC{<:Integer,Int64})
     Handle(r[], :sv_counts_free)
 end
 
+# ---- readers (src/input.jl) ------------------------------------------------------
+# readMM / the matrix of read_10X (src/input.jl:78-115,199-208): parsed on the
+# device; rows_are_features for the 10X layout (features x barcodes).
+function read_mtx(path::AbstractString; rows_are_features::Bool=true)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    svcheck(ccall((:sv_counts_read_mtx, libsv), Cint, (Ptr{Cvoid}, Cstring, Cint, Ref{Ptr{Cvoid}}),
+        ctx(), path, rows_are_features, r))
+    Handle(r[], :sv_counts_free)
+end
+
+_svtype(::Type{Int32}) = SV_I32
+_svtype(::Type{Int64}) = SV_I64
+_svtype(::Type{Float32}) = SV_F32
+_svtype(::Type{Float64}) = SV_F64
+
+# _read_10X_h5 / _read_h5 (src/input.jl:158-187,210-225): the stored features x
+# barcodes CSC (0-based indptr over barcodes) is the cells x genes CSR.
+function upload_10x_arrays(indptr::Vector, indices::Vector, data::Vector, dim)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    svcheck(ccall((:sv_counts_upload_csr, libsv), Cint,
+        (Ptr{Cvoid}, Int64, Int64, Int64, Ptr{Cvoid}, Cint, Ptr{Cvoid}, Cint, Ptr{Cvoid}, Cint, Cint, Ref{Ptr{Cvoid}}),
+        ctx(), dim[2], dim[1], length(indices), indptr, _svtype(eltype(indptr)), indices,
+        _svtype(eltype(indices)), data, _svtype(eltype(data)), 0, r))
+    Handle(r[], :sv_counts_free)
+end
+
 const DATA = WeakKeyDict{Any,Handle}()   # normalised matrix -> its device handle
 
 function normalize_cells(X::NamedArray; method=:lognormalize, scale_factor::Real=1.0,
