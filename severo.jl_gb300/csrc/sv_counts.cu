@@ -183,31 +183,34 @@ __global__ void __launch_bounds__(TR_WARPS * 32) k_tr_count(
   for (int k = lane; k < T && c0 + k < n_minor; k += 32) seg_cnt[c0 + k] = cnt[w][k];
 }
 
-// Places every entry.  Warp per tile; per batch of 32 (or, WIDE, 64: two per
-// lane) source segments a mask per output segment gives each entry its rank
-// among the batch's entries of the same output segment.  WIDE halves the
-// batches and lengthens each output row's run per batch (faster with many
-// tiles); with few tiles the narrow form keeps a lane's load chain short.
-template <bool WIDE>
+// Places every entry.  Warp per tile; per batch of 32·H source segments (H per
+// lane) an H-word mask per output segment gives each entry its rank among the
+// batch's entries of the same output segment.  Wider batches halve the batch
+// count each time and lengthen each output row's run per batch, so fewer of its
+// stores reach DRAM as partial sectors; with few tiles H = 1 keeps a lane's
+// load chain short.  Shared memory (dynamic): per warp T masks of H words and
+// T cursors.
+template <int H>
 __global__ void __launch_bounds__(TR_WARPS * 32) k_tr_write(
     const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx, const int32_t* __restrict__ val,
     int64_t n_major, int64_t n_minor, int tshift, int64_t n_tiles, const int32_t* __restrict__ toff,
     const int64_t* __restrict__ optr, int32_t* __restrict__ oidx, int32_t* __restrict__ oval) {
-  using Mask = typename std::conditional<WIDE, unsigned long long, unsigned>::type;
-  constexpr int H = WIDE ? 2 : 1;
-  __shared__ Mask mask[TR_WARPS][TR_MAXT];
-  __shared__ int64_t pos[TR_WARPS][TR_MAXT];
+  extern __shared__ __align__(16) unsigned char tr_smem[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, T = 1 << tshift;
+  int64_t* pos = (int64_t*)tr_smem + (size_t)w * T;
+  unsigned* mask = (unsigned*)((int64_t*)tr_smem + (size_t)TR_WARPS * T) + (size_t)w * T * H;
   const int64_t t = (int64_t)blockIdx.x * TR_WARPS + w;
   if (t >= n_tiles) return;
   const int64_t c0 = t << tshift;
   for (int k = lane; k < T; k += 32) {
-    mask[w][k] = 0;
-    pos[w][k] = c0 + k < n_minor ? optr[c0 + k] : 0;
+#pragma unroll
+    for (int h = 0; h < H; ++h) mask[k * H + h] = 0u;
+    pos[k] = c0 + k < n_minor ? optr[c0 + k] : 0;
   }
   __syncwarp();
   const int32_t* lo = toff + t * n_major;
   const int32_t* hi = lo + n_major;
+  const unsigned bit = 1u << lane, below = bit - 1u;
   for (int64_t g0 = 0; g0 < n_major; g0 += 32 * H) {
     int64_t a[H], b[H];
 #pragma unroll
@@ -222,30 +225,34 @@ __global__ void __launch_bounds__(TR_WARPS * 32) k_tr_write(
     }
 #pragma unroll
     for (int h = 0; h < H; ++h) {
-      const Mask bit = (Mask)1 << (32 * h + lane);
 #pragma unroll 4
-      for (int64_t j = a[h]; j < b[h]; ++j) atomicOr(&mask[w][idx[j] - c0], bit);
+      for (int64_t j = a[h]; j < b[h]; ++j) atomicOr(&mask[(idx[j] - c0) * H + h], bit);
     }
     __syncwarp();
 #pragma unroll
     for (int h = 0; h < H; ++h) {
-      const Mask below = ((Mask)1 << (32 * h + lane)) - 1;
       const int32_t g = (int32_t)(g0 + 32 * h + lane);
 #pragma unroll 4
       for (int64_t j = a[h]; j < b[h]; ++j) {
-        int k = idx[j] - (int32_t)c0;
-        int64_t o = pos[w][k] + __popcll((unsigned long long)(mask[w][k] & below));
+        const int k = idx[j] - (int32_t)c0;
+        const unsigned* mk = mask + k * H;
+        int r = __popc(mk[h] & below);
+#pragma unroll
+        for (int u = 0; u < h; ++u) r += __popc(mk[u]);
+        const int64_t o = pos[k] + r;
         oidx[o] = g;
         oval[o] = val[j];
       }
     }
     __syncwarp();
     for (int k = lane; k < T; k += 32) {
-      Mask mk = mask[w][k];
-      if (mk) {
-        pos[w][k] += __popcll((unsigned long long)mk);
-        mask[w][k] = 0;
+      int c = 0;
+#pragma unroll
+      for (int h = 0; h < H; ++h) {
+        c += __popc(mask[k * H + h]);
+        mask[k * H + h] = 0u;
       }
+      pos[k] += c;
     }
     __syncwarp();
   }
@@ -556,14 +563,21 @@ void sv_transpose_counts(sv_context* ctx, int64_t n_major, int64_t n_minor, int6
   sv_scan_i64(ctx, seg.get(), optr.get(), n_minor);
   oidx.alloc(nnz);
   ocnt.alloc(nnz);
-  if (n_tiles >= (int64_t)ctx->num_sms * 32)
-    sv_launch(ctx, "counts_transpose_write", k_tr_write<true>, gt, bt, 0, ptr, idx, cnt, n_major, n_minor,
+  // batch width: 256 source segments with many tiles, 32 with few
+  const int T = 1 << tshift;
+  const bool wide = n_tiles >= (int64_t)ctx->num_sms * 32;
+  const int H = wide ? 8 : 1;
+  const size_t smem = (size_t)TR_WARPS * T * (8 + 4 * H);
+  if (wide) {
+    SV_CUDA(cudaFuncSetAttribute(k_tr_write<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    sv_launch(ctx, "counts_transpose_write", k_tr_write<8>, gt, bt, smem, ptr, idx, cnt, n_major, n_minor,
               tshift, n_tiles, (const int32_t*)toff.get(), (const int64_t*)optr.get(), oidx.get(),
               ocnt.get());
-  else
-    sv_launch(ctx, "counts_transpose_write", k_tr_write<false>, gt, bt, 0, ptr, idx, cnt, n_major, n_minor,
+  } else {
+    sv_launch(ctx, "counts_transpose_write", k_tr_write<1>, gt, bt, smem, ptr, idx, cnt, n_major, n_minor,
               tshift, n_tiles, (const int32_t*)toff.get(), (const int64_t*)optr.get(), oidx.get(),
               ocnt.get());
+  }
   sv_sync(ctx);
 }
 
