@@ -99,12 +99,17 @@ def readMM(fname, rows_are_features=False, ctx=None):
     return _count_matrix().read_mtx(fname, rows_are_features=rows_are_features, ctx=ctx)
 
 
+def _feature_names(feature_file, gene_column=2):
+    """Column gene_column (1-based) of a tab-separated features / genes file."""
+    return [line.split("\t")[gene_column - 1] for line in _readlines(feature_file) if line != ""]
+
+
 def _read_10X(matrix_file, barcodes_file, feature_file, gene_column=2, ctx=None):
     if not (os.path.isfile(feature_file) and os.path.isfile(barcodes_file) and os.path.isfile(matrix_file)):
         raise ParseError_10X(f"Couldn't locate all components: {feature_file}, {barcodes_file}, {matrix_file}")
     X = _count_matrix().read_mtx(matrix_file, rows_are_features=True, ctx=ctx)
     barcodes = _readlines(barcodes_file)
-    features = [line.split("\t")[gene_column - 1] for line in _readlines(feature_file) if line != ""]
+    features = _feature_names(feature_file, gene_column)
     return X, features, barcodes
 
 
@@ -129,11 +134,10 @@ def read_geo(prefix, gene_column=2, unique_features=True, ctx=None):
     return convert_counts(X, features, barcodes, unique_features=unique_features)
 
 
-def read_dge(fname, unique_features=True, ctx=None):
-    """A digital gene expression file: MatrixMarket with the gene and barcode
-    names in %%GENES / %%CELL_BARCODES comment lines (_read_dge,
-    src/input.jl:131-152; the reference's read_dge passes the wrong argument to
-    it, this one reads fname)."""
+def _dge_names(fname):
+    """Gene and barcode names from the %%GENES / %%CELL_BARCODES lines among the
+    comments after the banner (parseMM_comments and the loop of _read_dge,
+    src/input.jl:66-76,140-148)."""
     genes, barcodes = [], []
     with _open_text(fname) as f:
         f.readline()
@@ -145,6 +149,15 @@ def read_dge(fname, unique_features=True, ctx=None):
                 genes.extend(line.split("\t")[1:])
             elif line.startswith("%%CELL_BARCODES"):
                 barcodes.extend(line.split("\t")[1:])
+    return genes, barcodes
+
+
+def read_dge(fname, unique_features=True, ctx=None):
+    """A digital gene expression file: MatrixMarket with the gene and barcode
+    names in %%GENES / %%CELL_BARCODES comment lines (_read_dge,
+    src/input.jl:131-152; the reference's read_dge passes the wrong argument to
+    it, this one reads fname)."""
+    genes, barcodes = _dge_names(fname)
     X = _count_matrix().read_mtx(fname, rows_are_features=True, ctx=ctx)
     return convert_counts(X, genes, barcodes, unique_features=unique_features)
 

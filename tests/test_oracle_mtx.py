@@ -131,3 +131,22 @@ def test_convert_counts_names():
     assert nc.features == ["g-1", "g-1.1", "x"]
     nc = sv.convert_counts(None, ["g_1", "g-1"], ["c1"], unique_features=False)
     assert nc.features == ["g-1", "g-1"]
+
+
+def test_reader_name_files(tmp_path):
+    """Host side of read_10X / read_dge: the feature column of a (gzip) TSV and
+    the %%GENES / %%CELL_BARCODES comment lines of a DGE file."""
+    import gzip
+    sv = ge.load_package()
+    rd = sv.readers
+    p = tmp_path / "features.tsv.gz"
+    with gzip.open(p, "wt") as f:
+        f.write("ENSG1\tA_1\tGene Expression\nENSG2\tB\tGene Expression\n\n")
+    assert rd._feature_names(str(p), 2) == ["A_1", "B"]
+    assert rd._feature_names(str(p), 1) == ["ENSG1", "ENSG2"]
+    q = tmp_path / "x.dge.txt"
+    q.write_text("%%MatrixMarket matrix coordinate integer general\n%%GENES\tg1\tg2\n\n"
+                 "%%CELL_BARCODES\tc1\n%%CELL_BARCODES\tc2\tc3\n% other\n2 3 0\n")
+    assert rd._dge_names(str(q)) == (["g1", "g2"], ["c1", "c2", "c3"])
+    nc = sv.convert_counts(None, ["A_1", "A-1", "A-1"], ["c"])
+    assert nc.features == ["A-1", "A-1.1", "A-1.2"]
