@@ -679,8 +679,13 @@ sv_counts* read_mm(sv_context* ctx, Source& src, int rows_are_features, const ch
   int64_t len = 0;
   DevBuf<unsigned char> txt = upload_text(ctx, h, len);
   const int64_t entries = m.entries;
-  DevBuf<int32_t> cell(entries), gene(entries), val(entries);
-  if (entries > 0) {
+  // the coordinates are allocated once the text is known to hold the entries
+  DevBuf<int32_t> cell, gene, val;
+  if (entries == 0) {
+    cell.alloc(0);
+    gene.alloc(0);
+    val.alloc(0);
+  } else {
     const int64_t n_tiles = std::max<int64_t>(1, (len + TILE - 1) / TILE);
     DevBuf<int64_t> tcnt(n_tiles + 1), toff(n_tiles + 1);
     dim3 gw(sv_grid_for(ctx, n_tiles * 32, 256)), bw(256);
@@ -690,6 +695,9 @@ sv_counts* read_mm(sv_context* ctx, Source& src, int rows_are_features, const ch
     SV_REQUIRE(n_nl >= entries - 1, "%s: Could not read matrix entry: the input holds fewer than %lld entry lines",
                where, (long long)entries);
     const int64_t need = std::min<int64_t>(n_nl, entries);
+    cell.alloc(entries);
+    gene.alloc(entries);
+    val.alloc(entries);
     DevBuf<int64_t> nlpos(std::max<int64_t>(1, need));
     sv_launch(ctx, "mtx_line_ends", k_nl_pos, gw, bw, 0, (const uint4*)txt.get(), n_tiles,
               (const int64_t*)toff.get(), need, nlpos.get());
