@@ -195,20 +195,24 @@ int sv_normalize_cells(sv_context* ctx, const sv_counts* counts, int method,
                        double scale_factor, int dtype, sv_data** out);
 /* normalize_cells for callers that cannot let this library allocate device
  * memory.  No counterpart in the reference: it exists for hosts that keep the
- * device memory budget in their own pool, and for work recorded inside a stream
- * capture, where cudaMalloc is not permitted and cudaFree synchronises the
- * device.  Inputs and output are device arrays owned by the caller: a 0-based
- * cells x genes CSC (colptr int64 [n_genes + 1], rowval and counts int32 [nnz])
- * and values (FP32 [nnz], CSC order, the same numbers as the SV_F32 form of
- * sv_normalize_cells).  The per-cell totals live in a file-scope device array
- * of 2,097,152 entries (16 MiB on every GPU that loads the library, until the
- * process exits); more cells are rejected with SV_ERR_ARG.  Nothing is
- * allocated: no cudaMalloc, no cudaFree.  The first call on a device looks up
- * the array's device address with that device current, so make it before any
- * stream capture.  Work is queued on `stream` (a cudaStream_t, NULL for the
- * legacy default stream) and the call returns without waiting.  Every call on a
- * device shares the array: calls that overlap on the GPU (other streams, other
- * host threads) race and corrupt each other's totals. */
+ * whole device memory budget in their own pool (a language runtime such as
+ * Julia's, which hands out device arrays from its pool and would otherwise
+ * compete with the library's cudaMalloc) and for services that must not
+ * allocate device memory once started.  Inputs and output are device arrays
+ * owned by the caller: a 0-based cells x genes CSC (colptr int64
+ * [n_genes + 1], rowval and counts int32 [nnz]) and values (FP32 [nnz], CSC
+ * order, the same numbers as the SV_F32 form of sv_normalize_cells).  The
+ * per-cell totals live in a file-scope device array of 2,097,152 entries
+ * (16 MiB on every GPU that loads the library, until the process exits); more
+ * cells are rejected with SV_ERR_ARG.  Nothing is allocated: no cudaMalloc, no
+ * cudaFree.  The first call on a device looks up the array's device address
+ * with that device current and keeps it for the life of the process (a
+ * cudaDeviceReset on that device makes the kept address stale).  Work runs on
+ * `stream` (a cudaStream_t, NULL for the legacy default stream); the call waits
+ * for it, because a row index outside [0, n_cells) -- skipped by the kernels,
+ * its value set to 0 -- is reported as SV_ERR_ARG.  Every call on a device
+ * shares the array: calls that overlap on the GPU (other streams, other host
+ * threads) race and corrupt each other's totals. */
 int sv_normalize_csc_noalloc(const int64_t* colptr, const int32_t* rowval, const int32_t* counts,
                              int64_t n_cells, int64_t n_genes, int64_t nnz, int method,
                              double scale_factor, float* values, void* stream);

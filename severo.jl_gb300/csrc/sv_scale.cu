@@ -23,14 +23,31 @@ namespace {
 
 constexpr int64_t CHUNK = 4096;   // non-zeros per warp task in the X^T u product
 
-// ---- per-feature moments (FP64) ---------------------------------------------
+// ---- per-feature moments -----------------------------------------------------
 // Mean and unbiased variance of each feature column including its implicit
-// zeros (scaling.jl:18-34): per-thread Welford over the stored values, merged
-// across the block with the pairwise (Chan) update, then merged with the group
-// of n - nnz zeros, which is the state Welford starts from in the reference.
-// With stacked samples (soff: nseg + 1 cell offsets) every (sample, feature)
-// pair is a column of its own (the sample's rows of the feature, found by
-// binary search in the sorted CSC rows); outputs at index s * nf + f.
+// zeros (scaling.jl:18-34).  The reference runs Welford over the stored values
+// from the state after the n - nnz zeros; here the same two numbers come from
+// the sums S1 = sum a and S2 = sum a^2 over the stored values (the zeros add
+// nothing): mean = S1 / n, M2 = S2 - S1 * mean, var = M2 / (n - 1).  No
+// division per element: the FP64 pipe of this GPU runs at 1/64 of the FP32
+// rate, and the former Welford form (one FP64 divide per element) ran at ~1%
+// of HBM bandwidth.
+//
+// FP32 / BF16 values are summed on the FP32 pipe in double-float form (a
+// rounded sum and its exact error, Knuth's TwoSum; x^2 exact for BF16, with
+// its FMA error term for FP32) over groups of up to 32 elements per thread,
+// and each group's (hi, lo) pairs are added into FP64 sums: relative error of
+// the sums ~2^-48 per group, of M2 ~2^-47 (1 + mean^2 / var) (3.9e-14 at
+// worst on the FP32 test data, 4e-15 for BF16, against FP64 Welford).  FP64
+// and Int32 data are summed in FP64.
+//
+// Work split: each column is cut into P equal parts (one block each, P from
+// the column length bound) so that dense features do not form a tail; the
+// per-part sums go to `part` and k_moments_finish adds them in part order, so
+// the result does not depend on scheduling.  With stacked samples (soff:
+// nseg + 1 cell offsets) every (sample, feature) pair is a column of its own
+// (the sample's rows of the feature, found by binary search in the sorted CSC
+// rows); outputs at index s * nf + f.
 __device__ __forceinline__ int64_t lower_bound_rows(const int32_t* __restrict__ r, int64_t lo,
                                                     int64_t hi, int64_t key) {
   while (lo < hi) {
@@ -41,87 +58,226 @@ __device__ __forceinline__ int64_t lower_bound_rows(const int32_t* __restrict__ 
   return lo;
 }
 
+// exact s + e = a + b (TwoSum; explicit roundings so that nothing is contracted)
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+struct DfAcc {
+  float h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
+  template <bool EXACT_SQ>
+  __device__ __forceinline__ void add(float x) {
+    float s, e;
+    two_sum_f(h1, x, s, e);
+    h1 = s;
+    l1 = __fadd_rn(l1, e);
+    float p = __fmul_rn(x, x);
+    if (!EXACT_SQ) l2 = __fadd_rn(l2, __fmaf_rn(x, x, -p));
+    two_sum_f(h2, p, s, e);
+    h2 = s;
+    l2 = __fadd_rn(l2, e);
+  }
+  __device__ __forceinline__ void flush(double& S1, double& S2) {
+    S1 += (double)h1;
+    S1 += (double)l1;
+    S2 += (double)h2;
+    S2 += (double)l2;
+    h1 = l1 = h2 = l2 = 0.f;
+  }
+};
+
+// the 16-byte vector of each storage type and how its elements are summed
+template <typename ValT> struct MomVec;
+template <> struct MomVec<__nv_bfloat16> {
+  static constexpr int N = 8;
+  static __device__ __forceinline__ void add(const uint4& w, DfAcc& acc, double&, double&) {
+    const uint32_t u[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      acc.add<true>(__uint_as_float(u[i] << 16));          // low half: the earlier element
+      acc.add<true>(__uint_as_float(u[i] & 0xffff0000u));
+    }
+  }
+  static __device__ __forceinline__ void scalar(const __nv_bfloat16* p, int64_t i, DfAcc& acc,
+                                                double&, double&) {
+    acc.add<true>(__bfloat162float(p[i]));
+  }
+  static constexpr bool DF = true;
+};
+template <> struct MomVec<float> {
+  static constexpr int N = 4;
+  static __device__ __forceinline__ void add(const uint4& w, DfAcc& acc, double&, double&) {
+    acc.add<false>(__uint_as_float(w.x));
+    acc.add<false>(__uint_as_float(w.y));
+    acc.add<false>(__uint_as_float(w.z));
+    acc.add<false>(__uint_as_float(w.w));
+  }
+  static __device__ __forceinline__ void scalar(const float* p, int64_t i, DfAcc& acc, double&,
+                                                double&) {
+    acc.add<false>(p[i]);
+  }
+  static constexpr bool DF = true;
+};
+template <> struct MomVec<double> {
+  static constexpr int N = 2;
+  static __device__ __forceinline__ void add(const uint4& w, DfAcc&, double& S1, double& S2) {
+    double a = __hiloint2double((int)w.y, (int)w.x), b = __hiloint2double((int)w.w, (int)w.z);
+    S1 += a;
+    S2 = fma(a, a, S2);
+    S1 += b;
+    S2 = fma(b, b, S2);
+  }
+  static __device__ __forceinline__ void scalar(const double* p, int64_t i, DfAcc&, double& S1,
+                                                double& S2) {
+    double a = p[i];
+    S1 += a;
+    S2 = fma(a, a, S2);
+  }
+  static constexpr bool DF = false;
+};
+template <> struct MomVec<int32_t> {
+  static constexpr int N = 4;
+  static __device__ __forceinline__ void add(const uint4& w, DfAcc&, double& S1, double& S2) {
+    const int32_t u[4] = {(int32_t)w.x, (int32_t)w.y, (int32_t)w.z, (int32_t)w.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      double a = (double)u[i];
+      S1 += a;
+      S2 = fma(a, a, S2);
+    }
+  }
+  static __device__ __forceinline__ void scalar(const int32_t* p, int64_t i, DfAcc&, double& S1,
+                                                double& S2) {
+    double a = (double)p[i];
+    S1 += a;
+    S2 = fma(a, a, S2);
+  }
+  static constexpr bool DF = false;
+};
+
+constexpr int MOM_THREADS = 256;
+constexpr int MOM_UNROLL = 4;     // 16-byte loads in flight per thread (one group)
+
 template <typename ValT>
-__global__ void k_moments(const ValT* __restrict__ val, const int64_t* __restrict__ fstart,
-                          const int64_t* __restrict__ fend, int64_t nf, int64_t n_cells,
-                          double scale_max, double* __restrict__ mean_o, double* __restrict__ std_o,
-                          double* __restrict__ mu_o, float* __restrict__ inv_f,
-                          float* __restrict__ clip_f, double* __restrict__ inv_d,
-                          double* __restrict__ clip_d, const int32_t* __restrict__ rowidx,
-                          const int64_t* __restrict__ soff, int nseg) {
-  __shared__ double sh_n[32], sh_m[32], sh_s[32];
-  for (int64_t task = blockIdx.x; task < nf * nseg; task += gridDim.x) {
-    int64_t f = task % nf;
-    int sg = (int)(task / nf);
+__global__ void __launch_bounds__(MOM_THREADS)
+k_moments_part(const ValT* __restrict__ val, const int64_t* __restrict__ fstart,
+               const int64_t* __restrict__ fend, int64_t nf, int P,
+               const int32_t* __restrict__ rowidx, const int64_t* __restrict__ soff, int nseg,
+               double2* __restrict__ part) {
+  using V = MomVec<ValT>;
+  constexpr int N = V::N;
+  __shared__ double sh1[MOM_THREADS / 32], sh2[MOM_THREADS / 32];
+  const int64_t ntask = nf * nseg * P;
+  const int tid = threadIdx.x;
+  for (int64_t task = blockIdx.x; task < ntask; task += gridDim.x) {
+    const int p = (int)(task % P);
+    const int64_t col = task / P;              // sample-major: s * nf + f
+    const int64_t f = col % nf;
+    const int sg = (int)(col / nf);
     int64_t s = fstart[f], e = fend[f];
-    int64_t ncell = n_cells;
     if (soff) {
       int64_t lo = lower_bound_rows(rowidx, s, e, soff[sg]);
       e = lower_bound_rows(rowidx, lo, e, soff[sg + 1]);
       s = lo;
-      ncell = soff[sg + 1] - soff[sg];
     }
-    const int64_t o = (int64_t)sg * nf + f;
-    double n = 0, m = 0, M2 = 0;
-    for (int64_t i = s + threadIdx.x; i < e; i += blockDim.x) {
-      double v = (double)sv_load_val(val, i);
-      n += 1;
-      double d = v - m;
-      m += d / n;
-      M2 += d * (v - m);
-    }
-    // warp merge
+    const int64_t L = e - s;
+    const int64_t a = s + L * p / P, b = s + L * (p + 1) / P;
+    double S1 = 0.0, S2 = 0.0;
+    DfAcc acc;
+    const int64_t va = (a + N - 1) / N, vb = b / N;   // whole 16-byte vectors in [a, b)
+    if (va < vb) {
+      // head [a, va*N) and tail [vb*N, b): fewer than N elements each
+      if (tid < va * N - a) V::scalar(val, a + tid, acc, S1, S2);
+      if (tid < b - vb * N) V::scalar(val, vb * N + tid, acc, S1, S2);
+      const uint4* vp = reinterpret_cast<const uint4*>(val);
+      for (int64_t v0 = va + tid; v0 < vb; v0 += (int64_t)MOM_THREADS * MOM_UNROLL) {
+        uint4 w[MOM_UNROLL];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      double n2 = __shfl_xor_sync(0xffffffffu, n, o);
-      double m2 = __shfl_xor_sync(0xffffffffu, m, o);
-      double M22 = __shfl_xor_sync(0xffffffffu, M2, o);
-      double nt = n + n2;
-      if (nt > 0) {
-        double d = m2 - m;
-        m = m + d * (n2 / nt);
-        M2 = M2 + M22 + d * d * (n * n2 / nt);
+        for (int u = 0; u < MOM_UNROLL; ++u) {
+          int64_t v = v0 + (int64_t)u * MOM_THREADS;
+          if (v < vb) w[u] = __ldg(vp + v);
+        }
+#pragma unroll
+        for (int u = 0; u < MOM_UNROLL; ++u)
+          if (v0 + (int64_t)u * MOM_THREADS < vb) V::add(w[u], acc, S1, S2);
+        if (V::DF) acc.flush(S1, S2);
       }
-      n = nt;
+    } else {
+      for (int64_t i = a + tid; i < b; i += MOM_THREADS) V::scalar(val, i, acc, S1, S2);
     }
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) {
-      sh_n[wid] = n;
-      sh_m[wid] = m;
-      sh_s[wid] = M2;
+    if (V::DF) acc.flush(S1, S2);
+    S1 = sv_warp_sum(S1);
+    S2 = sv_warp_sum(S2);
+    if ((tid & 31) == 0) {
+      sh1[tid >> 5] = S1;
+      sh2[tid >> 5] = S2;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      double N = 0, Mn = 0, S = 0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-        double n2 = sh_n[w], m2 = sh_m[w], s2 = sh_s[w];
-        double nt = N + n2;
-        if (nt > 0) {
-          double d = m2 - Mn;
-          Mn = Mn + d * (n2 / nt);
-          S = S + s2 + d * d * (N * n2 / nt);
-        }
-        N = nt;
+    if (tid == 0) {
+      double t1 = 0.0, t2 = 0.0;
+      for (int w = 0; w < MOM_THREADS / 32; ++w) {
+        t1 += sh1[w];
+        t2 += sh2[w];
       }
-      // merge the implicit zeros (count n_cells - nnz, mean 0, M2 0)
-      double nz = (double)(ncell - (e - s));
-      double nt = N + nz;
-      double d = -Mn;
-      double meanv = Mn + d * (nz / nt);
-      double M2t = S + d * d * (N * nz / nt);
-      double var = M2t / (double)(ncell - 1);
-      double sd = sqrt(var);
-      double mu = meanv / sd;                       // scaling.jl:207
-      mean_o[o] = meanv;
-      std_o[o] = sd;
-      mu_o[o] = mu;
-      inv_d[o] = 1.0 / sd;                          // a * (1/std): within 1 ulp of a/std
-      clip_d[o] = scale_max + mu;                   // scaling.jl:209
-      inv_f[o] = (float)(1.0 / sd);
-      clip_f[o] = (float)(scale_max + mu);
+      part[task] = make_double2(t1, t2);
     }
     __syncthreads();
   }
+}
+
+__global__ void k_moments_finish(const double2* __restrict__ part, int P, int64_t nf, int nseg,
+                                 const int64_t* __restrict__ soff, int64_t n_cells,
+                                 double scale_max, double* __restrict__ mean_o,
+                                 double* __restrict__ std_o, double* __restrict__ mu_o,
+                                 float* __restrict__ inv_f, float* __restrict__ clip_f,
+                                 double* __restrict__ inv_d, double* __restrict__ clip_d) {
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < nf * nseg;
+       o += (int64_t)gridDim.x * blockDim.x) {
+    double S1 = 0.0, S2 = 0.0;
+    for (int p = 0; p < P; ++p) {
+      double2 q = part[o * P + p];
+      S1 += q.x;
+      S2 += q.y;
+    }
+    const int sg = (int)(o / nf);
+    const double n = soff ? (double)(soff[sg + 1] - soff[sg]) : (double)n_cells;
+    const double meanv = S1 / n;
+    const double M2 = fmax(fma(-S1, meanv, S2), 0.0);
+    const double var = M2 / (n - 1.0);
+    const double sd = sqrt(var);
+    const double mu = meanv / sd;                   // scaling.jl:207
+    mean_o[o] = meanv;
+    std_o[o] = sd;
+    mu_o[o] = mu;
+    inv_d[o] = 1.0 / sd;                            // a * (1/std): within 1 ulp of a/std
+    clip_d[o] = scale_max + mu;                     // scaling.jl:209
+    inv_f[o] = (float)(1.0 / sd);
+    clip_f[o] = (float)(scale_max + mu);
+  }
+}
+
+// Per-column moments of a feature set (or of every (sample, feature) pair):
+// the two launches above with their partial-sum buffer.
+template <typename VT>
+void launch_moments(sv_context* ctx, const char* name, const VT* val, const int64_t* fs,
+                    const int64_t* fe, int64_t nf, int64_t n_cells, double scale_max, double* mean,
+                    double* sd, double* mu, float* invf, float* clipf, double* invd, double* clipd,
+                    const int32_t* rowidx = nullptr, const int64_t* soff = nullptr, int nseg = 1) {
+  // parts per column: a single-sample column holds at most n_cells entries;
+  // a part of at most 128 Ki entries keeps the densest features off the tail
+  const int P = soff ? 1 : (int)std::min<int64_t>(64, std::max<int64_t>(1, (n_cells + 131071) / 131072));
+  const int64_t ncol = nf * nseg;
+  DevBuf<double2> part((size_t)(ncol * P));
+  int per_sm = 0;   // one wave of resident blocks, tasks taken in order
+  SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_moments_part<VT>, MOM_THREADS, 0));
+  sv_launch(ctx, name, k_moments_part<VT>, dim3(sv_grid_for(ctx, ncol * P, 1, std::max(per_sm, 1))),
+            dim3(MOM_THREADS), 0, val, fs, fe, nf, P, rowidx, soff, nseg, part.get());
+  sv_launch(ctx, "moments_finish", k_moments_finish, dim3(sv_grid_for(ctx, ncol, 256)), dim3(256), 0,
+            (const double2*)part.get(), P, nf, nseg, soff, n_cells, scale_max, mean, sd, mu, invf,
+            clipf, invd, clipd);
+  sv_sync(ctx);
 }
 
 __global__ void k_feat_ranges(const int32_t* __restrict__ fgene, const int64_t* __restrict__ colptr,
@@ -1319,11 +1475,10 @@ static sv_centered* make_centered(sv_context* ctx, const sv_data* data, const st
     S->inv_std_d.alloc(nf);
     S->clip_d.alloc(nf);
 #define LAUNCH_MOM(VT)                                                                          \
-  sv_launch(ctx, "scale_moments", k_moments<VT>, dim3(sv_grid_for(ctx, nf, 1, 16)), dim3(256), 0, \
-            (const VT*)data->csc_val.get(), (const int64_t*)S->feat_start.get(),                 \
-            (const int64_t*)S->feat_end.get(), nf, C->n_cells, scale_max, S->mean.get(),         \
-            S->std_.get(), S->mu.get(), S->inv_std_f.get(), S->clip_f.get(), S->inv_std_d.get(), \
-            S->clip_d.get(), (const int32_t*)nullptr, (const int64_t*)nullptr, 1)
+  launch_moments<VT>(ctx, "scale_moments", (const VT*)data->csc_val.get(),                        \
+                     (const int64_t*)S->feat_start.get(), (const int64_t*)S->feat_end.get(), nf,   \
+                     C->n_cells, scale_max, S->mean.get(), S->std_.get(), S->mu.get(),             \
+                     S->inv_std_f.get(), S->clip_f.get(), S->inv_std_d.get(), S->clip_d.get())
     if (!mu_given) {
       switch (data->dtype) {
         case SV_F64: LAUNCH_MOM(double); break;
@@ -1659,14 +1814,12 @@ SV_API int sv_batch_create(sv_context* ctx, const sv_data* data, const int64_t* 
     B->clip_f.alloc(sf);
     B->mu_h.alloc(sf);
     B->mu_l.alloc(sf);
-    int mgrid = sv_grid_for(ctx, (int64_t)sf, 1, 16);
 #define LAUNCH_BMOM(VT)                                                                           \
-  sv_launch(ctx, "scale_moments", k_moments<VT>, dim3(mgrid), dim3(256), 0,                       \
-            (const VT*)data->csc_val.get(), (const int64_t*)S->feat_start.get(),                   \
-            (const int64_t*)S->feat_end.get(), nf, C->n_cells, scale_max, B->mean.get(),           \
-            B->std_.get(), B->mu.get(), B->inv_f.get(), B->clip_f.get(), B->inv_d.get(),            \
-            B->clip_d.get(), (const int32_t*)C->csc_rowidx.get(), (const int64_t*)B->off.get(),    \
-            (int)nseg)
+  launch_moments<VT>(ctx, "scale_moments", (const VT*)data->csc_val.get(),                          \
+                     (const int64_t*)S->feat_start.get(), (const int64_t*)S->feat_end.get(), nf,     \
+                     C->n_cells, scale_max, B->mean.get(), B->std_.get(), B->mu.get(),               \
+                     B->inv_f.get(), B->clip_f.get(), B->inv_d.get(), B->clip_d.get(),               \
+                     (const int32_t*)C->csc_rowidx.get(), (const int64_t*)B->off.get(), (int)nseg)
     if (data->dtype == SV_F32) LAUNCH_BMOM(float);
     else LAUNCH_BMOM(__nv_bfloat16);
 #undef LAUNCH_BMOM
@@ -1870,12 +2023,10 @@ void sv_count_moments(sv_context* ctx, const sv_counts* C, double* mean, double*
   int64_t ng = C->n_genes;
   DevBuf<double> mu(ng), invd(ng), clipd(ng);
   DevBuf<float> invf(ng), clipf(ng);
-  sv_launch(ctx, "gene_moments", k_moments<int32_t>, dim3(sv_grid_for(ctx, ng, 1, 16)), dim3(256), 0,
-            (const int32_t*)C->csc_count.get(), (const int64_t*)C->csc_colptr.get(),
-            (const int64_t*)C->csc_colptr.get() + 1, ng, C->n_cells, (double)INFINITY, mean, sd, mu.get(),
-            invf.get(), clipf.get(), invd.get(), clipd.get(), (const int32_t*)nullptr,
-            (const int64_t*)nullptr, 1);
-  sv_sync(ctx);
+  launch_moments<int32_t>(ctx, "gene_moments", (const int32_t*)C->csc_count.get(),
+                          (const int64_t*)C->csc_colptr.get(), (const int64_t*)C->csc_colptr.get() + 1,
+                          ng, C->n_cells, (double)INFINITY, mean, sd, mu.get(), invf.get(),
+                          clipf.get(), invd.get(), clipd.get());
 }
 
 SV_API int sv_gene_moments(sv_context* ctx, const sv_data* data, double* mean, double* var) {
@@ -1892,10 +2043,9 @@ SV_API int sv_gene_moments(sv_context* ctx, const sv_data* data, double* mean, d
   SV_CUDA(cudaMemcpyAsync(fe.get(), C->csc_colptr.get() + 1, ng * 8, cudaMemcpyDeviceToDevice,
                           ctx->stream));
 #define LAUNCH_MOM(VT)                                                                           \
-  sv_launch(ctx, "gene_moments", k_moments<VT>, dim3(sv_grid_for(ctx, ng, 1, 16)), dim3(256), 0, \
-            (const VT*)data->csc_val.get(), (const int64_t*)fs.get(), (const int64_t*)fe.get(), ng, \
-            C->n_cells, (double)INFINITY, m.get(), sd.get(), mu.get(), invf.get(), clipf.get(),   \
-            invd.get(), clipd.get(), (const int32_t*)nullptr, (const int64_t*)nullptr, 1)
+  launch_moments<VT>(ctx, "gene_moments", (const VT*)data->csc_val.get(), (const int64_t*)fs.get(), \
+                     (const int64_t*)fe.get(), ng, C->n_cells, (double)INFINITY, m.get(), sd.get(), \
+                     mu.get(), invf.get(), clipf.get(), invd.get(), clipd.get())
   switch (data->dtype) {
     case SV_F64: LAUNCH_MOM(double); break;
     case SV_F32: LAUNCH_MOM(float); break;
