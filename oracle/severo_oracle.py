@@ -158,21 +158,29 @@ def mean_var_column(vals, n, acc=np.float64):
 
 
 def mean_var(A, acc=np.float64):
-    """Vectorised FP64 per-column mean / unbiased variance with implicit zeros.
+    """FP64 per-column mean / unbiased variance with implicit zeros.
 
-    Mathematically the quantity of src/scaling.jl:18-34,132-142; computed here by
-    the shifted two-pass formula in FP64 (exact to a few ulps of the Welford
-    result, which is what the tests compare against)."""
+    Mathematically the quantity of src/scaling.jl:18-34,132-142, computed here
+    as an accurate reference: per column, the correctly rounded sum of the
+    stored values (math.fsum), then the corrected two-pass form
+    M2 = sum (v - m)^2 + (n - nnz) m^2 - (sum (v - m) - (n - nnz) m)^2 / n with
+    both sums correctly rounded -- within a few ulps of the exact moments even
+    for columns of 10^5 and more values."""
     A = _as_csc(A)
     n, d = A.shape
     T = np.dtype(acc)
     data = A.data.astype(np.float64)
-    nnz_col = np.diff(A.indptr)
-    col = np.repeat(np.arange(d), nnz_col)
-    sums = np.bincount(col, weights=data, minlength=d)
-    mu = sums / n
-    dev = data - mu[col]
-    m2 = np.bincount(col, weights=dev * dev, minlength=d) + (n - nnz_col) * mu * mu
+    ptr = A.indptr
+    mu = np.zeros(d)
+    m2 = np.zeros(d)
+    for j in range(d):
+        v = data[ptr[j]:ptr[j + 1]]
+        nz = n - len(v)
+        m = math.fsum(v) / n
+        dev = v - m
+        c = math.fsum(dev) - nz * m                  # sum of all n deviations (~0)
+        m2[j] = math.fsum(dev * dev) + nz * m * m - c * c / n
+        mu[j] = m
     var = m2 / (n - 1)
     return mu.astype(T), var.astype(T)
 
@@ -207,12 +215,46 @@ def mean_var_grouped(x_idx, x_val, n, lbls, nlabels, acc=np.float64):
     return mu, var, cnt
 
 
-def scale_data(A, scale_max=np.inf, dtype=np.float64):
+def mean_var_welford(A, acc=np.float32):
+    """src/scaling.jl:18-34 in the accumulation type ``acc``, vectorised across
+    columns: step t updates every column that has a t-th stored value, in the
+    column's own order, exactly as the per-column loop does.  This is the
+    reference's arithmetic for Float32 data (scaling.jl:40-44)."""
+    A = _as_csc(A)
+    n, d = A.shape
+    T = np.dtype(acc).type
+    nnz_col = np.diff(A.indptr)
+    count = (n - nnz_col).astype(acc)
+    mu = np.zeros(d, dtype=acc)
+    s = np.zeros(d, dtype=acc)
+    data = A.data.astype(acc)
+    for t in range(int(nnz_col.max()) if d else 0):
+        cols = np.nonzero(nnz_col > t)[0]
+        v = data[A.indptr[cols] + t]
+        count[cols] += T(1)
+        delta = (v - mu[cols]).astype(acc)
+        mu[cols] = (mu[cols] + delta / count[cols]).astype(acc)
+        s[cols] = (s[cols] + delta * (v - mu[cols])).astype(acc)
+    return mu, (s / T(n - 1)).astype(acc)
+
+
+def scale_data(A, scale_max=np.inf, dtype=np.float64, acc=None):
     """src/scaling.jl:199-217.  Per column: ``mu_i = mean/std``; stored values
-    ``min(a/std, scale_max + mu_i)`` (upper clip only; zeros are never clipped)."""
+    ``min(a/std, scale_max + mu_i)`` (upper clip only; zeros are never clipped).
+
+    ``acc`` is the accumulation type of the per-column moments.  None follows
+    the reference: the data eltype for floating-point data (Float32 Welford
+    for Float32 values, scaling.jl:40-44), Float64 otherwise (:39-40).  The
+    device computes the moments in FP64 for every storage type, so its parity
+    tests pass ``acc=np.float64``."""
     A = _as_csc(A)
     dt = np.dtype(dtype)
-    mean, var = mean_var(A, np.float64 if dt == np.float64 else np.float64)
+    if acc is None:
+        acc = A.data.dtype if A.data.dtype == np.float32 else np.float64
+    if np.dtype(acc) == np.float64:
+        mean, var = mean_var(A, np.float64)
+    else:
+        mean, var = mean_var_welford(A, acc)
     mean = mean.astype(dt)
     std = np.sqrt(var.astype(dt)).astype(dt)
     with np.errstate(divide="ignore", invalid="ignore"):
@@ -262,14 +304,15 @@ class CenteredMatrix:
         return out
 
 
-def scale_features(X, scale_max=np.inf, dtype=np.float64, features=None):
+def scale_features(X, scale_max=np.inf, dtype=np.float64, features=None, acc=None):
     """src/scaling.jl:335-357: optional column subset (1-based feature indices),
-    then scale_data; returns the CenteredMatrix plus the per-feature stats."""
+    then scale_data (``acc``: see scale_data); returns the CenteredMatrix plus
+    the per-feature stats."""
     X = _as_csc(X)
     if features is not None:
         X = X[:, np.asarray(features, dtype=np.int64) - 1]
         X = _as_csc(X)
-    B, mu, mean, std = scale_data(X, scale_max, dtype)
+    B, mu, mean, std = scale_data(X, scale_max, dtype, acc)
     return CenteredMatrix(B, mu), mean, std
 
 

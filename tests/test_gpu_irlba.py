@@ -118,12 +118,24 @@ def test_pca_pipeline(sv, ctx, O, dtype, tol_s):
     s = em.stdev * np.sqrt(3000 - 1)                              # embedding.jl:68
     rel = np.max(np.abs(s - sf[:20]) / sf[:20])
     assert rel < tol_s, rel
-    # subspace of the leading PCs (well separated ones)
-    gap = sf[:20] / sf[1:21] - 1
-    kk = int(np.argmax(gap > 1e-3 * 0 + 0.02)) if np.any(gap > 0.02) else 0
-    ang = O.principal_angles(em.basis[:, :10], Vtf[:10].T).max()
-    assert ang < 1e-4 or gap[9] < 0.01, (ang, gap[9])
-    # coordinates are U diag(s) (embedding.jl:67)
+    # Loadings: with tol = 1e-7 the residual of each Ritz pair is at most
+    # 1e-7 sigma_1, so a PC whose singular value lies at least 1e-3 sigma_1
+    # from its neighbours is within ~1e-4 rad of the exact one; the leading
+    # block ending at the widest gap is compared as a subspace.
+    d_next = (sf[:20] - sf[1:21]) / sf[0]                 # gap below PC i
+    d_prev = np.r_[np.inf, d_next[:-1]]                   # gap above PC i
+    sep = np.minimum(d_prev, d_next) >= 1e-3
+    assert sep.sum() >= 3, sep
+    per_pc = np.arccos(np.clip(np.abs(np.einsum("ij,ji->i", em.basis.T, Vtf[:20].T)), 0.0, 1.0))
+    assert per_pc[sep].max() < 1e-4, per_pc
+    kk = int(np.argmax(d_next[1:19])) + 2                 # leading block (>= 2 PCs), widest gap
+    assert d_next[kk - 1] >= 1e-2, (kk, d_next)
+    ang = O.principal_angles(em.basis[:, :kk], Vtf[:kk].T).max()
+    assert ang < 1e-4, (kk, ang)
+    # coordinates are U diag(s) (embedding.jl:67): Z equals X~ times the loadings
+    Z_ref = Q @ em.basis
+    zt = 1e-9 if dtype == "float64" else 1e-5
+    assert np.linalg.norm(em.coordinates - Z_ref) <= zt * np.linalg.norm(Z_ref)
     assert np.allclose(np.abs(em.coordinates.T @ em.coordinates), np.diag(s ** 2), rtol=1e-6,
                        atol=1e-6 * s[0] ** 2)
 

@@ -44,6 +44,28 @@ def test_scale_features_stats_match_oracle(sv, ctx, O):
     assert S.shape == (900, 150) and S.nnz == Sr.A.nnz
 
 
+@pytest.mark.parametrize("dtype", ["float32", "bfloat16"])
+@pytest.mark.parametrize("n_cells", [2000, 300_000])
+def test_moments_fp32_bf16_storage(sv, ctx, O, dtype, n_cells):
+    """Moments of FP32 / BF16 values (double-float sums on the device, FP64
+    merge) against the FP64 oracle on the values actually stored; 300,000
+    cells split every column into several parts.  The reference accumulates
+    Float32 data in Float32 (src/scaling.jl:40-44): the device's FP64 moments
+    differ from that by Float32 rounding only."""
+    X = O.synth_counts(n_cells, 60, -0.5, 1.5, depth=0.8, seed=24)
+    d = sv.normalize_cells(X, scale_factor=1e4, dtype=dtype, ctx=ctx)
+    ref = O.normalize_cells(X, scale_factor=1e4, dtype=np.float32)
+    ref.data = d.values_csc().astype(np.float32)          # the stored values (BF16 rounded)
+    S = sv.scale_features(d, scale_max=10.0)
+    mu, gm, gs = S.stats()
+    _, mean, std = O.scale_features(ref.astype(np.float64), 10.0, np.float64)
+    assert np.allclose(gm, mean, rtol=1e-13, atol=0)
+    assert np.allclose(gs, std, rtol=1e-13, atol=0)
+    if n_cells <= 2000 and dtype == "float32":
+        _, _, std32 = O.scale_features(ref, 10.0, np.float32)   # the reference's Float32 Welford
+        assert np.allclose(gs, std32, rtol=2e-5)
+
+
 @pytest.mark.parametrize("dtype,rtol", [("float64", 1e-12), ("float32", 2e-6), ("bfloat16", 2e-6)])
 @pytest.mark.parametrize("scale_max", [np.inf, 10.0, 0.75])
 def test_centered_products(sv, ctx, O, dtype, rtol, scale_max):

@@ -58,6 +58,28 @@ def test_mean_var_welford_matches_vectorised():
         assert abs(m - mean[j]) < 1e-14 and abs(v - var[j]) < 1e-13
 
 
+def test_float32_accumulation_follows_the_reference():
+    """For Float32 data the reference accumulates the moments in Float32
+    (src/scaling.jl:40-44); the oracle's default does the same, column by
+    column as mean_var_column, while acc=Float64 (the device's choice) gives
+    the FP64 moments of the same values."""
+    X = O.synth_counts(1500, 200, -1.0, 1.5, depth=0.5, seed=41)
+    Xn = O.normalize_cells(X, "lognormalize", 1e4, np.float32)
+    m32, v32 = O.mean_var_welford(Xn, np.float32)
+    for j in (0, 7, 123):
+        col = Xn[:, j]
+        m, v = O.mean_var_column(col.data, Xn.shape[0], acc=np.float32)
+        assert m == m32[j] and v == v32[j]
+    _, mean_ref, std_ref = O.scale_features(Xn, 10.0, np.float32)            # reference: Float32
+    _, mean_64, std_64 = O.scale_features(Xn, 10.0, np.float32, acc=np.float64)
+    assert std_ref.dtype == np.float32
+    m64, v64 = O.mean_var(Xn)
+    assert np.array_equal(std_ref, np.sqrt(v32).astype(np.float32))
+    assert np.array_equal(std_64, np.sqrt(v64.astype(np.float32)))
+    # the two differ by Float32 rounding of the running sums only
+    assert np.allclose(std_ref, std_64, rtol=2e-5)
+
+
 def test_scale_clip_upper_only():
     # scaling.jl:209-212: upper clip only; zeros never clipped
     X = sp.csc_matrix(np.array(G["scaling"]["counts"], dtype=np.float64))
