@@ -1,10 +1,19 @@
 // normalize_cells on both copies of the count matrix (src/normalize.jl:17-55).
 //
 //   K1a  csr: one warp per cell; 128-bit loads of the counts, warp-shuffle sum
-//        s_c (integer, normalize.jl:24), then the values of that row are written
-//        (the second read of the row hits L1/L2).
-//   K1b  csc: a flat map over the non-zeros: b = f(a, s[row]) with s gathered
-//        from the per-cell totals (10 MB at 1.3M cells, L2-resident).
+//        s_c (integer, normalize.jl:24).  Lane l then evaluates the value of
+//        count l + 1 in that cell, f(l + 1, s_c) -- the division and log1p
+//        once per lane instead of once per entry -- and the row's values are
+//        written with one shuffle per entry (counts above 32 are evaluated
+//        directly; the second read of the row hits L1/L2).  The first NT
+//        values of each cell (32 bytes) go to a per-cell table.
+//   K1b  csc: a flat map over the non-zeros, 8 per thread: b = table[row][a-1]
+//        for counts 1..NT (an L2-resident gather: 42 MB at 1.3M cells in BF16),
+//        f(a, s[row]) otherwise.
+//
+// Every value is the same expression f(a, s) = log1p((sf * a) / s) (or the
+// relative count) evaluated in the output type, whichever kernel and path
+// computes it.
 //
 // Algorithmic bytes (HBM): K1a nnz*(4 + v) + 8*(n_cells+1) + 8*n_cells;
 // K1b nnz*(4 + 4 + v), v = bytes of the output value type.
@@ -84,12 +93,27 @@ __device__ __forceinline__ void load4(const int32_t* p, int64_t g, int (&v)[4]) 
   v[3] = w.w;
 }
 
-// K1a: per-cell totals and the CSR values.
+// Table entries per cell: 32 bytes of values for counts 1..NT.
+template <typename OutT>
+struct NormTab {
+  static constexpr int NT = 32 / (int)sizeof(OutT);
+};
+
+__device__ __forceinline__ float shfl_out(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ double shfl_out(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ __nv_bfloat16 shfl_out(__nv_bfloat16 v, int src) {
+  unsigned short u = __bfloat16_as_ushort(v);
+  return __ushort_as_bfloat16((unsigned short)__shfl_sync(0xffffffffu, (unsigned)u, src));
+}
+
+// K1a: per-cell totals, the CSR values and the per-cell value table.
 template <typename OutT>
 __global__ void __launch_bounds__(256) k_norm_csr(const int64_t* __restrict__ rowptr,
                                                   const int32_t* __restrict__ cnt, int64_t n_rows,
                                                   NormArgs p, OutT* __restrict__ out,
-                                                  int64_t* __restrict__ totals) {
+                                                  int64_t* __restrict__ totals,
+                                                  OutT* __restrict__ table) {
+  constexpr int NT = NormTab<OutT>::NT;
   int lane = threadIdx.x & 31;
   int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -106,49 +130,69 @@ __global__ void __launch_bounds__(256) k_norm_csr(const int64_t* __restrict__ ro
     }
     sum = sv_warp_sum(sum);
     if (lane == 0) totals[r] = sum;
-    for (int64_t g = a0 + 4 * lane; g < e; g += 128) {
-      int v[4];
-      load4(cnt, g, v);
+    if (e == s) continue;
+    const OutT tv = NormOp<OutT>::apply(lane + 1, sum, p);    // the value of count lane + 1
+    if (lane < NT) table[r * NT + lane] = tv;
+    // every lane takes every pass: the shuffles need the whole warp
+    for (int64_t g0 = a0; g0 < e; g0 += 128) {
+      const int64_t g = g0 + 4 * lane;
+      int v[4] = {0, 0, 0, 0};
+      if (g < e) load4(cnt, g, v);
       OutT o[4];
 #pragma unroll
-      for (int t = 0; t < 4; ++t) o[t] = NormOp<OutT>::apply(v[t], sum, p);
-      store4(out, g, s, e, o);
+      for (int t = 0; t < 4; ++t) {
+        const bool tabbed = v[t] >= 1 && v[t] <= 32;
+        const OutT sh = shfl_out(tv, tabbed ? v[t] - 1 : 0);
+        o[t] = tabbed ? sh : NormOp<OutT>::apply(v[t], sum, p);
+      }
+      if (g < e) store4(out, g, s, e, o);
     }
   }
 }
 
-// K1b: flat map over the CSC non-zeros.
+// K1b: flat map over the CSC non-zeros, 8 per thread.
 template <typename OutT>
 __global__ void __launch_bounds__(256) k_norm_csc(const int32_t* __restrict__ rowidx,
                                                   const int32_t* __restrict__ cnt, int64_t nnz,
-                                                  const int64_t* __restrict__ totals, NormArgs p,
+                                                  const int64_t* __restrict__ totals,
+                                                  const OutT* __restrict__ table, NormArgs p,
                                                   OutT* __restrict__ out) {
-  int64_t ngroups = (nnz + 3) >> 2;
+  constexpr int NT = NormTab<OutT>::NT;
+  int64_t ngroups = (nnz + 7) >> 3;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ngroups;
        q += (int64_t)gridDim.x * blockDim.x) {
-    int64_t g = q << 2;
-    int rv[4], cv[4];
-    load4(rowidx, g, rv);
-    load4(cnt, g, cv);
-    OutT o[4];
+    int64_t g = q << 3;
+    int rv[2][4], cv[2][4];
+    load4(rowidx, g, rv[0]);
+    load4(cnt, g, cv[0]);
+    load4(rowidx, g + 4, rv[1]);
+    load4(cnt, g + 4, cv[1]);
+    OutT o[2][4];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-      if (g + t < nnz) o[t] = NormOp<OutT>::apply(cv[t], __ldg(totals + rv[t]), p);
-      else o[t] = OutT(0.0f);
-    }
-    store4(out, g, 0, nnz, o);
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int64_t i = g + 4 * h + t;
+        const int a = cv[h][t];
+        if (i >= nnz) o[h][t] = OutT(0.0f);
+        else if (a >= 1 && a <= NT) o[h][t] = table[(int64_t)rv[h][t] * NT + (a - 1)];
+        else o[h][t] = NormOp<OutT>::apply(a, __ldg(totals + rv[h][t]), p);
+      }
+    store4(out, g, 0, nnz, o[0]);
+    store4(out, g + 4, 0, nnz, o[1]);
   }
 }
 
 template <typename OutT>
 void run_normalize(sv_context* ctx, const sv_counts* c, sv_data* d, NormArgs p) {
   int64_t nnz = c->nnz;
+  OutT* table = (OutT*)d->norm_table.get();
   sv_launch(ctx, "normalize_csr", k_norm_csr<OutT>, dim3(sv_grid_for(ctx, c->n_cells * 32, 256, 8)),
             dim3(256), 0, (const int64_t*)c->csr_rowptr.get(), (const int32_t*)c->csr_count.get(),
-            c->n_cells, p, (OutT*)d->csr_val.get(), d->totals.get());
-  sv_launch(ctx, "normalize_csc", k_norm_csc<OutT>, dim3(sv_grid_for(ctx, (nnz + 3) / 4, 256, 8)),
+            c->n_cells, p, (OutT*)d->csr_val.get(), d->totals.get(), table);
+  sv_launch(ctx, "normalize_csc", k_norm_csc<OutT>, dim3(sv_grid_for(ctx, (nnz + 7) / 8, 256, 8)),
             dim3(256), 0, (const int32_t*)c->csc_rowidx.get(), (const int32_t*)c->csc_count.get(),
-            nnz, (const int64_t*)d->totals.get(), p, (OutT*)d->csc_val.get());
+            nnz, (const int64_t*)d->totals.get(), (const OutT*)table, p, (OutT*)d->csc_val.get());
 }
 
 }  // namespace
@@ -188,6 +232,7 @@ SV_API int sv_normalize_cells(sv_context* ctx, const sv_counts* counts, int meth
     d->csc_val.alloc(counts->nnz * es);
     d->csr_val.alloc(counts->nnz * es);
     d->totals.alloc(counts->n_cells);
+    d->norm_table.alloc(counts->n_cells * 32);
     sv_normalize_into(ctx, counts, d);
     sv_sync(ctx);
   } catch (...) {
