@@ -348,8 +348,13 @@ def restart_keep(nu, work, nconv):
     return max(1, min(nu, work - 1))
 
 
+def _rotate(Q, M):
+    """Q[:, :k] <- Q @ M (M: work x k), the restart rotation of a basis."""
+    Q[:, :M.shape[1]] = Q @ M
+
+
 def irlba(matvec, rmatvec, m, n, nu, work=None, maxit=1000, tol=1e-5, init=None,
-          rng=None, breakdown_tol=None):
+          rng=None, breakdown_tol=None, cgs2=None, rotate=None):
     """Augmented implicitly restarted Lanczos bidiagonalisation (FP64).
 
     ``matvec(x)`` = A x (x in R^n, result in R^m); ``rmatvec(y)`` = A^T y.
@@ -357,15 +362,19 @@ def irlba(matvec, rmatvec, m, n, nu, work=None, maxit=1000, tol=1e-5, init=None,
     maxit 1000, start vector ``init`` on the n side).  Returns
     (U (m x nu), s (nu), V (n x nu), info, iters, nmatvec), info = 0 when all
     nu residuals ||A^T u_i - s_i v_i|| are below tol * max singular value.
+    ``cgs2(x, Q)`` and ``rotate(Q, M)`` replace the basis operations (the
+    multi-threaded CPU path passes C versions); the bases are column-major.
     """
     if work is None:
         work = irlba_work_size(m, n, nu)
     rng = np.random.default_rng(0) if rng is None else rng
     if init is None:
         init = rng.standard_normal(n)
+    _cgs2_ = _cgs2 if cgs2 is None else cgs2
+    _rot = _rotate if rotate is None else rotate
     eps_b = np.sqrt(np.finfo(np.float64).eps) if breakdown_tol is None else breakdown_tol
-    V = np.zeros((n, work))
-    W = np.zeros((m, work))
+    V = np.zeros((n, work), order="F")
+    W = np.zeros((m, work), order="F")
     B = np.zeros((work, work))
     V[:, 0] = init / np.linalg.norm(init)
     k = 0
@@ -378,30 +387,30 @@ def irlba(matvec, rmatvec, m, n, nu, work=None, maxit=1000, tol=1e-5, init=None,
     while it < maxit:
         j = k
         w = matvec(V[:, j]); nmv += 1
-        w = _cgs2(w, W[:, :j])
+        w = _cgs2_(w, W[:, :j])
         S = np.linalg.norm(w)
         if S < eps_b * max(smax, 1.0):
-            w = _cgs2(rng.standard_normal(m), W[:, :j]); w /= np.linalg.norm(w); S = 0.0
+            w = _cgs2_(rng.standard_normal(m), W[:, :j]); w /= np.linalg.norm(w); S = 0.0
         else:
             w = w / S
         W[:, j] = w
         while True:
             F = rmatvec(W[:, j]) - S * V[:, j]; nmv += 1
-            F = _cgs2(F, V[:, :j + 1])
+            F = _cgs2_(F, V[:, :j + 1])
             if j + 1 < work:
                 R = np.linalg.norm(F)
                 if R < eps_b * max(smax, 1.0):
-                    F = _cgs2(rng.standard_normal(n), V[:, :j + 1]); F /= np.linalg.norm(F); R = 0.0
+                    F = _cgs2_(rng.standard_normal(n), V[:, :j + 1]); F /= np.linalg.norm(F); R = 0.0
                 else:
                     F = F / R
                 V[:, j + 1] = F
                 B[j, j] = S
                 B[j, j + 1] = R
                 w = matvec(V[:, j + 1]) - R * W[:, j]; nmv += 1
-                w = _cgs2(w, W[:, :j + 1])
+                w = _cgs2_(w, W[:, :j + 1])
                 S = np.linalg.norm(w)
                 if S < eps_b * max(smax, 1.0):
-                    w = _cgs2(rng.standard_normal(m), W[:, :j + 1]); w /= np.linalg.norm(w); S = 0.0
+                    w = _cgs2_(rng.standard_normal(m), W[:, :j + 1]); w /= np.linalg.norm(w); S = 0.0
                 else:
                     w = w / S
                 W[:, j + 1] = w
@@ -421,8 +430,8 @@ def irlba(matvec, rmatvec, m, n, nu, work=None, maxit=1000, tol=1e-5, init=None,
             break
         k = restart_keep(nu, work, nconv)
         Fh = F / RF
-        V[:, :k] = V @ Qt.T[:, :k]
-        W[:, :k] = W @ P[:, :k]
+        _rot(V, np.ascontiguousarray(Qt.T[:, :k]))
+        _rot(W, np.ascontiguousarray(P[:, :k]))
         V[:, k] = Fh
         B = np.zeros((work, work))
         B[np.arange(k), np.arange(k)] = sig[:k]

@@ -150,7 +150,10 @@ __global__ void __launch_bounds__(256) k_norm_csr(const int64_t* __restrict__ ro
   }
 }
 
-// K1b: flat map over the CSC non-zeros, 8 per thread.
+// K1b: flat map over the CSC non-zeros, 4 per thread and pass; the next
+// pass's (row, count) words are loaded before this pass's table gathers, and
+// the gathers are issued unconditionally (a clamped slot), the rare counts
+// outside 1..NT recomputed afterwards.
 template <typename OutT>
 __global__ void __launch_bounds__(256) k_norm_csc(const int32_t* __restrict__ rowidx,
                                                   const int32_t* __restrict__ cnt, int64_t nnz,
@@ -158,28 +161,38 @@ __global__ void __launch_bounds__(256) k_norm_csc(const int32_t* __restrict__ ro
                                                   const OutT* __restrict__ table, NormArgs p,
                                                   OutT* __restrict__ out) {
   constexpr int NT = NormTab<OutT>::NT;
-  int64_t ngroups = (nnz + 7) >> 3;
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ngroups;
-       q += (int64_t)gridDim.x * blockDim.x) {
-    int64_t g = q << 3;
-    int rv[2][4], cv[2][4];
-    load4(rowidx, g, rv[0]);
-    load4(cnt, g, cv[0]);
-    load4(rowidx, g + 4, rv[1]);
-    load4(cnt, g + 4, cv[1]);
-    OutT o[2][4];
+  const int64_t ngroups = (nnz + 3) >> 2;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= ngroups) return;
+  int rv[4], cv[4];
+  load4(rowidx, q << 2, rv);
+  load4(cnt, q << 2, cv);
+  for (; q < ngroups; q += stride) {
+    const int64_t g = q << 2;
+    const int64_t qn = q + stride;
+    int rn[4] = {0, 0, 0, 0}, cn[4] = {0, 0, 0, 0};
+    if (qn < ngroups) {
+      load4(rowidx, qn << 2, rn);
+      load4(cnt, qn << 2, cn);
+    }
+    OutT o[4];
 #pragma unroll
-    for (int h = 0; h < 2; ++h)
+    for (int t = 0; t < 4; ++t) {
+      const int a = cv[t];
+      const int slot = (a >= 1 && a <= NT) ? a - 1 : 0;
+      o[t] = g + t < nnz ? table[(int64_t)rv[t] * NT + slot] : OutT(0.0f);
+    }
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int64_t i = g + 4 * h + t;
-        const int a = cv[h][t];
-        if (i >= nnz) o[h][t] = OutT(0.0f);
-        else if (a >= 1 && a <= NT) o[h][t] = table[(int64_t)rv[h][t] * NT + (a - 1)];
-        else o[h][t] = NormOp<OutT>::apply(a, __ldg(totals + rv[h][t]), p);
-      }
-    store4(out, g, 0, nnz, o[0]);
-    store4(out, g + 4, 0, nnz, o[1]);
+    for (int t = 0; t < 4; ++t)
+      if (g + t < nnz && !(cv[t] >= 1 && cv[t] <= NT))
+        o[t] = NormOp<OutT>::apply(cv[t], __ldg(totals + rv[t]), p);
+    store4(out, g, 0, nnz, o);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      rv[t] = rn[t];
+      cv[t] = cn[t];
+    }
   }
 }
 
@@ -190,7 +203,7 @@ void run_normalize(sv_context* ctx, const sv_counts* c, sv_data* d, NormArgs p) 
   sv_launch(ctx, "normalize_csr", k_norm_csr<OutT>, dim3(sv_grid_for(ctx, c->n_cells * 32, 256, 8)),
             dim3(256), 0, (const int64_t*)c->csr_rowptr.get(), (const int32_t*)c->csr_count.get(),
             c->n_cells, p, (OutT*)d->csr_val.get(), d->totals.get(), table);
-  sv_launch(ctx, "normalize_csc", k_norm_csc<OutT>, dim3(sv_grid_for(ctx, (nnz + 7) / 8, 256, 8)),
+  sv_launch(ctx, "normalize_csc", k_norm_csc<OutT>, dim3(sv_grid_for(ctx, (nnz + 3) / 4, 256, 8)),
             dim3(256), 0, (const int32_t*)c->csc_rowidx.get(), (const int32_t*)c->csc_count.get(),
             nnz, (const int64_t*)d->totals.get(), (const OutT*)table, p, (OutT*)d->csc_val.get());
 }
