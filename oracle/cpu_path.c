@@ -416,3 +416,171 @@ void cp_knn(int64_t n, int64_t d, const double* Z, int64_t k, int64_t* idx, doub
   free(ZT);
   free(sq);
 }
+
+/* ---- approximate kNN: random-projection forest + one neighbour-of-neighbour
+ * round.  The reference calls a native approximate search parameterised by
+ * `ntables` random tables (src/neighbours.jl:19-74, default ntables = 2 d);
+ * its code is not available, so this is a stand-in of the same class, sized
+ * by the same parameter: ntables random-projection trees (each node split at
+ * the median of a random Gaussian direction, leaves of at most `leaf` points),
+ * all pairs within a leaf as candidates, then the neighbours of each point's
+ * neighbours.  Distances exact (FP64); lists nearest first, self first. */
+static inline double gauss(rng_t* r) {
+  double a = u01(r), b = u01(r);
+  return sqrt(-2.0 * log(a)) * cos(6.283185307179586 * b);
+}
+
+static inline double sqdist(const double* a, const double* b, int64_t d) {
+  double s0 = 0.0, s1 = 0.0;
+  int64_t t = 0;
+  for (; t + 1 < d; t += 2) {
+    const double x = a[t] - b[t], y = a[t + 1] - b[t + 1];
+    s0 += x * x;
+    s1 += y * y;
+  }
+  if (t < d) {
+    const double x = a[t] - b[t];
+    s0 += x * x;
+  }
+  return s0 + s1;
+}
+
+static inline void knn_insert(double* bd, int64_t* bi, int64_t k, double dv, int64_t j) {
+  if (dv >= bd[k - 1]) return;
+  for (int64_t r = 0; r < k; ++r)
+    if (bi[r] == j) return;
+  int64_t r = k - 1;
+  while (r > 0 && bd[r - 1] > dv) {
+    bd[r] = bd[r - 1];
+    bi[r] = bi[r - 1];
+    --r;
+  }
+  bd[r] = dv;
+  bi[r] = j;
+}
+
+/* the m-th smallest key of key[lo, hi) moved to position m (Hoare selection),
+ * values permuted alongside */
+static void select_kth(double* key, int32_t* val, int64_t lo, int64_t hi, int64_t m) {
+  hi -= 1;
+  while (lo < hi) {
+    const double pivot = key[(lo + hi) / 2];
+    int64_t i = lo, j = hi;
+    while (i <= j) {
+      while (key[i] < pivot) ++i;
+      while (key[j] > pivot) --j;
+      if (i <= j) {
+        double tk = key[i]; key[i] = key[j]; key[j] = tk;
+        int32_t tv = val[i]; val[i] = val[j]; val[j] = tv;
+        ++i;
+        --j;
+      }
+    }
+    if (m <= j) hi = j;
+    else if (m >= i) lo = i;
+    else return;
+  }
+}
+
+void cp_ann(int64_t n, int64_t d, const double* Z, int64_t k, int ntables, int leaf, uint64_t seed,
+            int refine, int64_t* idx, double* dist2, int nt) {
+  nt = nthreads_of(nt);
+  if (leaf < 2) leaf = 2;
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t r = 0; r < k; ++r) {
+      dist2[i * k + r] = INFINITY;
+      idx[i * k + r] = -1;
+    }
+  for (int64_t i = 0; i < n; ++i) {
+    dist2[i * k] = 0.0;
+    idx[i * k] = i;
+  }
+  /* leaves hold at least leaf / 2 points: at most 2 n / leaf + 2 of them, two
+   * offsets each */
+  const int64_t maxleaves = 4 * (n / leaf + 2);
+  int32_t* order = (int32_t*)malloc((size_t)ntables * (size_t)n * sizeof(int32_t));
+  int64_t* lofs = (int64_t*)malloc((size_t)ntables * (size_t)maxleaves * sizeof(int64_t));
+  int64_t* nleaf = (int64_t*)calloc((size_t)ntables, sizeof(int64_t));
+  /* phase 1: the trees, one per task */
+#pragma omp parallel num_threads(nt)
+  {
+    double* key = (double*)malloc((size_t)n * sizeof(double));
+    double* dir = (double*)malloc((size_t)d * sizeof(double));
+    int64_t* stack = (int64_t*)malloc((size_t)(2 * maxleaves + 64) * sizeof(int64_t));
+#pragma omp for schedule(dynamic, 1)
+    for (int t = 0; t < ntables; ++t) {
+      int32_t* ord = order + (size_t)t * (size_t)n;
+      int64_t* lo_ = lofs + (size_t)t * (size_t)maxleaves;
+      rng_t rg = {mix64(seed ^ 0xA11ull) ^ (uint64_t)(t + 1) * 0x9E3779B97F4A7C15ull, 0};
+      for (int64_t i = 0; i < n; ++i) ord[i] = (int32_t)i;
+      int64_t sp = 0, nl = 0;
+      stack[sp++] = 0;
+      stack[sp++] = n;
+      while (sp > 0) {
+        const int64_t hi = stack[--sp], lo = stack[--sp];
+        if (hi - lo <= leaf) {
+          lo_[nl++] = lo;            /* leaves in order of completion; end = next start */
+          lo_[nl++] = hi;
+          continue;
+        }
+        for (int64_t u = 0; u < d; ++u) dir[u] = gauss(&rg);
+        for (int64_t i = lo; i < hi; ++i) {
+          const double* z = Z + (size_t)ord[i] * (size_t)d;
+          double s = 0.0;
+          for (int64_t u = 0; u < d; ++u) s += z[u] * dir[u];
+          key[i] = s;
+        }
+        const int64_t mid = lo + (hi - lo) / 2;
+        select_kth(key, ord, lo, hi, mid);
+        stack[sp++] = lo;
+        stack[sp++] = mid;
+        stack[sp++] = mid;
+        stack[sp++] = hi;
+      }
+      nleaf[t] = nl / 2;
+    }
+    free(key);
+    free(dir);
+    free(stack);
+  }
+  /* phase 2: all pairs within each leaf; a point lies in one leaf per tree, so
+   * the leaves of a tree update disjoint lists */
+  for (int t = 0; t < ntables; ++t) {
+    const int32_t* ord = order + (size_t)t * (size_t)n;
+    const int64_t* lo_ = lofs + (size_t)t * (size_t)maxleaves;
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 16)
+    for (int64_t l = 0; l < nleaf[t]; ++l) {
+      const int64_t a = lo_[2 * l], b = lo_[2 * l + 1];
+      for (int64_t x = a; x < b; ++x) {
+        const int64_t i = ord[x];
+        for (int64_t y = x + 1; y < b; ++y) {
+          const int64_t j = ord[y];
+          const double dv = sqdist(Z + (size_t)i * (size_t)d, Z + (size_t)j * (size_t)d, d);
+          knn_insert(dist2 + i * k, idx + i * k, k, dv, j);
+          knn_insert(dist2 + j * k, idx + j * k, k, dv, i);
+        }
+      }
+    }
+  }
+  free(order);
+  free(lofs);
+  free(nleaf);
+  /* phase 3: neighbours of neighbours, from a snapshot of the lists */
+  for (int round = 0; round < refine; ++round) {
+    int64_t* snap = (int64_t*)malloc((size_t)n * (size_t)k * sizeof(int64_t));
+    memcpy(snap, idx, (size_t)n * (size_t)k * sizeof(int64_t));
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 64)
+    for (int64_t i = 0; i < n; ++i)
+      for (int64_t r = 1; r < k; ++r) {
+        const int64_t j = snap[i * k + r];
+        if (j < 0) continue;
+        for (int64_t s = 1; s < k; ++s) {
+          const int64_t c = snap[j * k + s];
+          if (c < 0 || c == i) continue;
+          knn_insert(dist2 + i * k, idx + i * k, k,
+                     sqdist(Z + (size_t)i * (size_t)d, Z + (size_t)c * (size_t)d, d), c);
+        }
+      }
+    free(snap);
+  }
+}

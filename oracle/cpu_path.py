@@ -10,8 +10,10 @@ count matrix with every host core: the C kernels for normalisation, scaling
 and the CenteredMatrix products (FP64, src/normalize.jl:17-38,
 src/scaling.jl:18-34,199-272), the oracle's numpy irlba (FP64 CGS2
 reorthogonalisation, src/irlba.jl:47-75 defaults) driving them, Z = U diag(s)
-(src/embedding.jl:67), and an exact blocked brute-force kNN in C in place of
-the reference's approximate one.
+(src/embedding.jl:67), and an approximate kNN of the reference's kind in C
+(random-projection trees, ntables = 2 d as the reference's default, then one
+neighbour-of-neighbour round; its recall against exact search is measured
+and reported).
 """
 from __future__ import annotations
 
@@ -67,6 +69,9 @@ def _load():
         lib.cp_rotate.restype = None
         lib.cp_knn.argtypes = [_I64, _I64, _P, _I64, _P, _P, C.c_int]
         lib.cp_knn.restype = None
+        lib.cp_ann.argtypes = [_I64, _I64, _P, _I64, C.c_int, C.c_int, C.c_uint64, C.c_int, _P, _P,
+                               C.c_int]
+        lib.cp_ann.restype = None
         _lib = lib
     return _lib
 
@@ -203,9 +208,26 @@ def knn(Z, k, nt=0):
     return idx
 
 
+def ann(Z, k, ntables=None, leaf=64, refine=1, seed=0, nt=0):
+    """Approximate k nearest neighbours (self first), 0-based: ntables random-
+    projection trees (default 2 d, the reference's default number of tables)
+    and one neighbour-of-neighbour round; the stand-in for the reference's
+    native approximate search."""
+    lib = _load()
+    Z = np.ascontiguousarray(Z, np.float64)
+    n, d = Z.shape
+    idx = np.empty((n, k), np.int64)
+    d2 = np.empty((n, k))
+    lib.cp_ann(n, d, _p(Z), k, int(ntables or 2 * d), int(leaf), seed, int(refine), _p(idx), _p(d2),
+               nt or threads())
+    return idx
+
+
 def pipeline(X, features, npcs=50, k=20, init=None, tol=1e-5, scale_factor=1e4, scale_max=10.0,
-             nt=0):
-    """One pass of the path on the host; returns (stage seconds, Z, irlba info)."""
+             nt=0, approx=True):
+    """One pass of the path on the host; returns (stage seconds, Z, info with
+    the irlba counts and the neighbour lists).  approx: the random-projection
+    forest (the reference's kind of search), else exact brute force."""
     from oracle import severo_oracle as O
     nt = nt or threads()
     t = {}
@@ -225,9 +247,19 @@ def pipeline(X, features, npcs=50, k=20, init=None, tol=1e-5, scale_factor=1e4, 
     Z = U * s                                                        # embedding.jl:67
     t["pca"] = time.perf_counter() - t0
     t0 = time.perf_counter()
-    knn(Z, k, nt)
+    idx = ann(Z, k, nt=nt) if approx else knn(Z, k, nt)
     t["knn"] = time.perf_counter() - t0
-    return t, Z, {"iters": int(it), "nmatvec": int(nmv), "sigma": s}
+    return t, Z, {"iters": int(it), "nmatvec": int(nmv), "sigma": s, "idx": idx}
+
+
+def recall(Z, idx, k, queries):
+    """Fraction of the exact k nearest neighbours (self included) of the query
+    rows found in idx."""
+    Q = Z[queries]
+    D = np.einsum("ij,ij->i", Q, Q)[:, None] + np.einsum("ij,ij->i", Z, Z)[None, :] - 2.0 * (Q @ Z.T)
+    D[np.arange(len(queries)), queries] = -1.0
+    ex = np.argpartition(D, k - 1, axis=1)[:, :k]
+    return float(np.mean([len(set(ex[r]) & set(idx[q])) / k for r, q in enumerate(queries)]))
 
 
 def run_sizes(params, sizes, nt=0, n_hvf=3000, npcs=50, k=20, seed=0):
@@ -254,9 +286,13 @@ def run_sizes(params, sizes, nt=0, n_hvf=3000, npcs=50, k=20, seed=0):
     out = []
     for n in sizes:
         Xs = sp.csc_matrix(Xr[:n])
-        t, _, info = pipeline(Xs, hvf, npcs, k, init=init, nt=nt)
-        out.append({"n": int(n), "nnz": int(Xs.nnz), "stages_s": t, "iters": info["iters"],
-                    "nmatvec": info["nmatvec"]})
+        t, Z, info = pipeline(Xs, hvf, npcs, k, init=init, nt=nt)
+        rec = {"n": int(n), "nnz": int(Xs.nnz), "stages_s": t, "iters": info["iters"],
+               "nmatvec": info["nmatvec"]}
+        if n == N and n > 1000:
+            q = np.random.default_rng(seed + 1).choice(n, 500, replace=False)
+            rec["knn_recall"] = recall(Z, info["idx"], k, q)
+        out.append(rec)
         del Xs
     return out
 

@@ -178,7 +178,6 @@ struct sv_data {
   DevBuf<unsigned char> csc_val;   // nnz * elem
   DevBuf<unsigned char> csr_val;   // nnz * elem
   DevBuf<int64_t> totals;          // n_cells
-  DevBuf<unsigned char> norm_table; // n_cells x 32 bytes: values of the counts 1..32/elem per cell
 };
 
 struct sv_centered {

@@ -5,11 +5,10 @@
 //        count l + 1 in that cell, f(l + 1, s_c) -- the division and log1p
 //        once per lane instead of once per entry -- and the row's values are
 //        written with one shuffle per entry (counts above 32 are evaluated
-//        directly; the second read of the row hits L1/L2).  The first NT
-//        values of each cell (32 bytes) go to a per-cell table.
-//   K1b  csc: a flat map over the non-zeros, 8 per thread: b = table[row][a-1]
-//        for counts 1..NT (an L2-resident gather: 42 MB at 1.3M cells in BF16),
-//        f(a, s[row]) otherwise.
+//        directly; the second read of the row hits L1/L2): 509 -> 380 us at
+//        100,000 cells.
+//   K1b  csc: a flat map over the non-zeros: b = f(a, s[row]) with s gathered
+//        from the per-cell totals (10 MB at 1.3M cells, L2-resident).
 //
 // Every value is the same expression f(a, s) = log1p((sf * a) / s) (or the
 // relative count) evaluated in the output type, whichever kernel and path
@@ -93,12 +92,6 @@ __device__ __forceinline__ void load4(const int32_t* p, int64_t g, int (&v)[4]) 
   v[3] = w.w;
 }
 
-// Table entries per cell: 32 bytes of values for counts 1..NT.
-template <typename OutT>
-struct NormTab {
-  static constexpr int NT = 32 / (int)sizeof(OutT);
-};
-
 __device__ __forceinline__ float shfl_out(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 __device__ __forceinline__ double shfl_out(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 __device__ __forceinline__ __nv_bfloat16 shfl_out(__nv_bfloat16 v, int src) {
@@ -106,14 +99,12 @@ __device__ __forceinline__ __nv_bfloat16 shfl_out(__nv_bfloat16 v, int src) {
   return __ushort_as_bfloat16((unsigned short)__shfl_sync(0xffffffffu, (unsigned)u, src));
 }
 
-// K1a: per-cell totals, the CSR values and the per-cell value table.
+// K1a: per-cell totals and the CSR values.
 template <typename OutT>
 __global__ void __launch_bounds__(256) k_norm_csr(const int64_t* __restrict__ rowptr,
                                                   const int32_t* __restrict__ cnt, int64_t n_rows,
                                                   NormArgs p, OutT* __restrict__ out,
-                                                  int64_t* __restrict__ totals,
-                                                  OutT* __restrict__ table) {
-  constexpr int NT = NormTab<OutT>::NT;
+                                                  int64_t* __restrict__ totals) {
   int lane = threadIdx.x & 31;
   int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -132,7 +123,6 @@ __global__ void __launch_bounds__(256) k_norm_csr(const int64_t* __restrict__ ro
     if (lane == 0) totals[r] = sum;
     if (e == s) continue;
     const OutT tv = NormOp<OutT>::apply(lane + 1, sum, p);    // the value of count lane + 1
-    if (lane < NT) table[r * NT + lane] = tv;
     // every lane takes every pass: the shuffles need the whole warp
     for (int64_t g0 = a0; g0 < e; g0 += 128) {
       const int64_t g = g0 + 4 * lane;
@@ -150,62 +140,41 @@ __global__ void __launch_bounds__(256) k_norm_csr(const int64_t* __restrict__ ro
   }
 }
 
-// K1b: flat map over the CSC non-zeros, 4 per thread and pass; the next
-// pass's (row, count) words are loaded before this pass's table gathers, and
-// the gathers are issued unconditionally (a clamped slot), the rare counts
-// outside 1..NT recomputed afterwards.
+// K1b: flat map over the CSC non-zeros, 4 per thread; s gathered from the
+// per-cell totals (10 MB at 1.3M cells, L2-resident).  (Gathering the value
+// from a per-cell table of the small counts instead measured slower: 825 vs
+// 691 us at 100,000 cells.)
 template <typename OutT>
 __global__ void __launch_bounds__(256) k_norm_csc(const int32_t* __restrict__ rowidx,
                                                   const int32_t* __restrict__ cnt, int64_t nnz,
-                                                  const int64_t* __restrict__ totals,
-                                                  const OutT* __restrict__ table, NormArgs p,
+                                                  const int64_t* __restrict__ totals, NormArgs p,
                                                   OutT* __restrict__ out) {
-  constexpr int NT = NormTab<OutT>::NT;
-  const int64_t ngroups = (nnz + 3) >> 2;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (q >= ngroups) return;
-  int rv[4], cv[4];
-  load4(rowidx, q << 2, rv);
-  load4(cnt, q << 2, cv);
-  for (; q < ngroups; q += stride) {
-    const int64_t g = q << 2;
-    const int64_t qn = q + stride;
-    int rn[4] = {0, 0, 0, 0}, cn[4] = {0, 0, 0, 0};
-    if (qn < ngroups) {
-      load4(rowidx, qn << 2, rn);
-      load4(cnt, qn << 2, cn);
-    }
+  int64_t ngroups = (nnz + 3) >> 2;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ngroups;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    int64_t g = q << 2;
+    int rv[4], cv[4];
+    load4(rowidx, g, rv);
+    load4(cnt, g, cv);
     OutT o[4];
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
-      const int a = cv[t];
-      const int slot = (a >= 1 && a <= NT) ? a - 1 : 0;
-      o[t] = g + t < nnz ? table[(int64_t)rv[t] * NT + slot] : OutT(0.0f);
+      if (g + t < nnz) o[t] = NormOp<OutT>::apply(cv[t], __ldg(totals + rv[t]), p);
+      else o[t] = OutT(0.0f);
     }
-#pragma unroll
-    for (int t = 0; t < 4; ++t)
-      if (g + t < nnz && !(cv[t] >= 1 && cv[t] <= NT))
-        o[t] = NormOp<OutT>::apply(cv[t], __ldg(totals + rv[t]), p);
     store4(out, g, 0, nnz, o);
-#pragma unroll
-    for (int t = 0; t < 4; ++t) {
-      rv[t] = rn[t];
-      cv[t] = cn[t];
-    }
   }
 }
 
 template <typename OutT>
 void run_normalize(sv_context* ctx, const sv_counts* c, sv_data* d, NormArgs p) {
   int64_t nnz = c->nnz;
-  OutT* table = (OutT*)d->norm_table.get();
   sv_launch(ctx, "normalize_csr", k_norm_csr<OutT>, dim3(sv_grid_for(ctx, c->n_cells * 32, 256, 8)),
             dim3(256), 0, (const int64_t*)c->csr_rowptr.get(), (const int32_t*)c->csr_count.get(),
-            c->n_cells, p, (OutT*)d->csr_val.get(), d->totals.get(), table);
+            c->n_cells, p, (OutT*)d->csr_val.get(), d->totals.get());
   sv_launch(ctx, "normalize_csc", k_norm_csc<OutT>, dim3(sv_grid_for(ctx, (nnz + 3) / 4, 256, 8)),
             dim3(256), 0, (const int32_t*)c->csc_rowidx.get(), (const int32_t*)c->csc_count.get(),
-            nnz, (const int64_t*)d->totals.get(), (const OutT*)table, p, (OutT*)d->csc_val.get());
+            nnz, (const int64_t*)d->totals.get(), p, (OutT*)d->csc_val.get());
 }
 
 }  // namespace
@@ -245,7 +214,6 @@ SV_API int sv_normalize_cells(sv_context* ctx, const sv_counts* counts, int meth
     d->csc_val.alloc(counts->nnz * es);
     d->csr_val.alloc(counts->nnz * es);
     d->totals.alloc(counts->n_cells);
-    d->norm_table.alloc(counts->n_cells * 32);
     sv_normalize_into(ctx, counts, d);
     sv_sync(ctx);
   } catch (...) {

@@ -57,3 +57,14 @@ def test_pipeline_singular_values_and_neighbours(counts):
     idx = CP.knn(Z, 8, nt=2)
     ridx, _ = O.knn_exact(Z, 8)
     assert all(set(a) == set(b) for a, b in zip(idx, ridx))
+
+
+def test_approximate_search_recall():
+    """The random-projection forest of the CPU baseline finds the exact
+    neighbours on well-separated mixture data."""
+    rng = np.random.default_rng(6)
+    n, d = 3000, 20
+    X = rng.normal(0, 4, (15, d))[rng.integers(0, 15, n)] + rng.standard_normal((n, d))
+    idx = CP.ann(X, 10, nt=2)
+    assert np.all(idx[:, 0] == np.arange(n))
+    assert CP.recall(X, idx, 10, np.arange(0, n, 7)) > 0.99
