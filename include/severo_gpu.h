@@ -258,6 +258,29 @@ int sv_centered_mul(sv_context* ctx, const sv_centered* s, char trans, int64_t n
                     double alpha, const double* x, int64_t ldx, double beta,
                     double* y, int64_t ldy);
 int sv_centered_free(sv_centered* s);
+/* The Gram product of two CenteredMatrix over the same cells (the Adjoint x
+ * CenteredMatrix mul! of src/scaling.jl:274-296, used by the tssvd route of
+ * src/embedding.jl:30-44): C = alpha Xl~' Xr~ + beta C, C host column-major
+ * FP64 (nf_l x nf_r, in/out), computed as Al' Ar - mu_l q_r' - (q_l - n mu_l)
+ * mu_r' with q = the column sums of the stored values. */
+int sv_centered_gram(sv_context* ctx, const sv_centered* left, const sv_centered* right, double alpha,
+                     double beta, double* C);
+
+/* ---- sparse products of src/mul.jl ------------------------------------------
+ * Host CSC arrays (Julia layout; index_base 0 or 1), FP64 values, computed on
+ * the device in the reference's order of accumulation (bit-identical results).
+ * y = alpha A x + beta y, A m x n, x a sparse vector of nnzx (index, value)
+ * pairs (mul.jl:50-77); y host FP64 (m, in/out). */
+int sv_sparse_mul_spvec(sv_context* ctx, int64_t m, int64_t n, const int64_t* colptr,
+                        const int64_t* rowval, const double* nzval, int64_t nnzx, const int64_t* xidx,
+                        const double* xval, int index_base, double alpha, double beta, double* y);
+/* C = alpha op(A) B + beta C (mul.jl:79-114), C host column-major FP64 m x n
+ * (in/out), B k x n CSC; A m x k CSC, or with transa != 0 A is k x m and
+ * op(A) = A' (the reference multiplies by copy(A'), formed here on the device). */
+int sv_sparse_mul_sparse(sv_context* ctx, int64_t m, int64_t k, int64_t n, const int64_t* acolptr,
+                         const int64_t* arowval, const double* anzval, int transa,
+                         const int64_t* bcolptr, const int64_t* browval, const double* bnzval,
+                         int index_base, double alpha, double beta, double* C);
 
 /* ---- irlba (src/irlba.jl:47-99) ---------------------------------------------
  * Truncated SVD of the implicit matrix, all Lanczos vectors in HBM.

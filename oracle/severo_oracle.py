@@ -317,6 +317,70 @@ def scale_features(X, scale_max=np.inf, dtype=np.float64, features=None, acc=Non
 
 
 # ---------------------------------------------------------------------------
+# sparse products -- src/mul.jl and the Gram product of src/scaling.jl:274-296
+# (pure-Python loops in the reference's order: small cases only)
+# ---------------------------------------------------------------------------
+
+
+def mul_spvec(A, xidx, xval, alpha=1.0, beta=0.0, y=None):
+    """src/mul.jl:50-77: y = alpha A x + beta y for a sparse vector x given by
+    its 0-based indices and values, accumulated in the reference's order."""
+    A = _as_csc(A)
+    m, n = A.shape
+    y = np.zeros(m) if y is None else np.array(y, dtype=np.float64)
+    if n == 0:
+        return y
+    if beta != 1.0:
+        y = np.zeros(m) if beta == 0.0 else y * beta
+    if alpha == 0.0:
+        return y
+    cp, rv, nz = A.indptr, A.indices, A.data.astype(np.float64)
+    for jp in range(len(xidx)):
+        nzx = float(xval[jp])
+        j = int(xidx[jp])
+        for kp in range(cp[j], cp[j + 1]):
+            i = rv[kp]
+            y[i] = y[i] + alpha * float(nz[kp]) * nzx
+    return y
+
+
+def mul_sparse(A, B, alpha=1.0, beta=0.0, C=None):
+    """src/mul.jl:82-114: C = alpha A B + beta C (dense), column by column of B
+    in the reference's order.  For A' pass the transposed matrix itself
+    (mul.jl:79-80 multiply by copy(A'))."""
+    A = _as_csc(A)
+    B = _as_csc(B)
+    m, n = A.shape[0], B.shape[1]
+    C = np.zeros((m, n)) if C is None else np.array(C, dtype=np.float64)
+    if beta != 1:
+        C = np.zeros((m, n)) if beta == 0 else C * beta
+    acp, arv, anz = A.indptr, A.indices, A.data.astype(np.float64)
+    bcp, brv, bnz = B.indptr, B.indices, B.data.astype(np.float64)
+    for col in range(n):
+        for jp in range(bcp[col], bcp[col + 1]):
+            nzb = float(bnz[jp])
+            j = brv[jp]
+            for kp in range(acp[j], acp[j + 1]):
+                C[arv[kp], col] = C[arv[kp], col] + alpha * float(anz[kp]) * nzb
+    return C
+
+
+def gram(Sl, Sr, alpha=1.0, beta=0.0, C=None):
+    """src/scaling.jl:274-296: C = alpha Xl~' Xr~ + beta C for two
+    CenteredMatrix: Al' Ar (mul.jl, A' copied), then - mu_l q_r' and
+    - (q_l - n mu_l) mu_r' with q the column sums of the stored values."""
+    Al, Ar = _as_csc(Sl.A), _as_csc(Sr.A)
+    n = Al.shape[0]
+    C = mul_sparse(_as_csc(Al.T), Ar, alpha, beta, C)
+    qr = np.asarray(Ar.sum(axis=0)).ravel()
+    C -= alpha * np.outer(Sl.mu, qr)
+    ql = qr if Sl is Sr else np.asarray(Al.sum(axis=0)).ravel()
+    ql = ql - n * Sl.mu
+    C -= alpha * np.outer(ql, Sr.mu)
+    return C
+
+
+# ---------------------------------------------------------------------------
 # irlba -- src/irlba.jl (wrapper) + the native routine restated from
 # Baglama & Reichel, "Augmented implicitly restarted Lanczos bidiagonalization
 # methods", SIAM J. Sci. Comput. 27 (2005) 19-42.
