@@ -238,6 +238,36 @@ def timed_steps(sv, ctx, td, counts, hvf, w, init, form, steps, warmup, with_sta
             "irlba": info}
 
 
+def snn_stage(sv, ctx, counts, hvf, w, init, form, reps=3):
+    """shared_nearest_neighbours timed on its own (src/neighbours.jl:76-108,
+    272-278): the Jaccard graph of the step's kNN lists (k, prune 1/15, in the
+    coordinates' FP64 type) built on the device, CUDA events around the call,
+    best of `reps`.  Bytes: the kNN lists read (4 n k), the reverse lists
+    written and read (8 n k), the graph written (12 nnz + 8 (n + 1))."""
+    import ctypes as C
+    _, _, em, kh = run_pipeline(sv, ctx, counts, hvf, w, init, form)
+    lib = sv._lib.load()
+    best, nnz = None, 0
+    for _ in range(reps):
+        h = C.c_void_p()
+        ctx.sync()
+        ctx.mark(7)
+        sv._lib.check(lib.sv_snn_knn(ctx.h, kh.h, int(w["k"]), 1.0 / 15.0, sv._lib.SV_F64, C.byref(h)))
+        ctx.mark(8)
+        ctx.sync()
+        ms = ctx.elapsed_ms(7, 8)
+        g = sv.Graph(ctx, h)
+        a, b = C.c_int64(), C.c_int64()
+        sv._lib.check(lib.sv_graph_info(h, C.byref(a), C.byref(b)))
+        nnz = b.value
+        del g
+        best = ms if best is None else min(best, ms)
+    n, k = w["n_cells"], w["k"]
+    byts = 4 * n * k + 8 * n * k + 12 * nnz + 8 * (n + 1)
+    return {"ms": round(best, 3), "nnz": int(nnz), "edges_per_cell": round(nnz / n, 2),
+            "bytes": int(byts), "gbs": round(byts / (best / 1e3) / 1e9, 1)}
+
+
 def e2e_steps(sv, ctx, td, host, shape, hvf, w, init, form, steps, outs=None):
     """The same pipeline through the public API with host buffers: upload of the
     CSC counts (pinned host memory) and download of Z, nn_index and distances
@@ -419,6 +449,7 @@ def main():
 
     # per-stage times (one extra pass with stage marks), per-kernel profile
     st = timed_steps(sv, ctx, None, counts, hvf, w, init, form, 1, 0, with_stages=True)
+    snn = snn_stage(sv, ctx, counts, hvf, w, init, form)
     rep = profile_step(sv, ctx, counts, hvf, w, init, form)
     S = sv.scale_features(sv.normalize_cells(counts, scale_factor=SCALE_FACTOR, dtype=w["dtype"],
                                              ctx=ctx), scale_max=SCALE_MAX, features=hvf)
@@ -519,6 +550,7 @@ def main():
                        "irlba": res["irlba"], "parallelism": f"replicas x{world}",
                        "l2": "inputs (tens of GB) exceed L2; no flush needed"},
             "stages_ms": st["stages_ms"],
+            "snn": snn,
             "kernels_ms": {k: {"launches": c, "ms": round(ms, 3)} for k, (c, ms) in top},
             "spmv": rl,
             "roofline": roof,
