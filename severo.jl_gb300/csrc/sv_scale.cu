@@ -670,25 +670,30 @@ __device__ __forceinline__ void dfx_fma(float& sh, float& sl, float ah, float al
   sl += err + e;
 }
 
-template <typename ValT, typename IdxT>
-__global__ void __launch_bounds__(256) k_spmv_csr_df(
-    const int64_t* __restrict__ rowptr, const IdxT* __restrict__ hcol, const ValT* __restrict__ hval,
-    int64_t n_rows, int64_t nf, const float* __restrict__ xh, const float* __restrict__ xl,
-    const float* __restrict__ inv_f, const float* __restrict__ clip_f, const float* __restrict__ mu_h,
-    const float* __restrict__ mu_l, float* __restrict__ yh, float* __restrict__ yl,
-    const double* __restrict__ csub, const float* __restrict__ zh, const float* __restrict__ zl,
-    const BlkRange* __restrict__ blk, const int* __restrict__ active) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+// Prologue shared by the double-float X v kernels: with stacked samples (blk
+// non-null) selects block b's row range and sample s = blk[b].seg (false: the
+// sample is frozen, nothing to do); builds the per-feature (inv*x, clip*x)
+// table in shared memory and returns mu.x and -csub as double-float pairs.
+struct XvDf {
+  int64_t rb0, rb1;
+  float muxh, muxl, csh, csl;
+};
+__device__ __forceinline__ bool xv_df_prologue(
+    unsigned char* smem_raw, int64_t n_rows, int64_t nf, const float* __restrict__ xh,
+    const float* __restrict__ xl, const float* __restrict__ inv_f, const float* __restrict__ clip_f,
+    const float* __restrict__ mu_h, const float* __restrict__ mu_l, const double* __restrict__ csub,
+    const BlkRange* __restrict__ blk, const int* __restrict__ active, XvDf& o) {
   __shared__ float redh[32], redl[32];
   __shared__ float sc[4];
   int sg = 0;
-  int64_t rb0 = 0, rb1 = n_rows;
+  o.rb0 = 0;
+  o.rb1 = n_rows;
   if (blk) {
     const BlkRange br = blk[blockIdx.x];
     sg = br.seg;
-    rb0 = br.r0;
-    rb1 = br.r1;
-    if (active && !active[sg]) return;
+    o.rb0 = br.r0;
+    o.rb1 = br.r1;
+    if (active && !active[sg]) return false;
     const int64_t po = (int64_t)sg * nf;
     xh += po;
     xl += po;
@@ -707,9 +712,9 @@ __global__ void __launch_bounds__(256) k_spmv_csr_df(
   }
   // mu.x: warp reduction in double-float, then warp 0 over the warps
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    float h2 = __shfl_xor_sync(0xffffffffu, mh, o);
-    float l2 = __shfl_xor_sync(0xffffffffu, ml, o);
+  for (int off = 16; off > 0; off >>= 1) {
+    float h2 = __shfl_xor_sync(0xffffffffu, mh, off);
+    float l2 = __shfl_xor_sync(0xffffffffu, ml, off);
     float t = mh + h2;
     float v = t - mh;
     float err = (mh - (t - v)) + (h2 - v);
@@ -742,7 +747,41 @@ __global__ void __launch_bounds__(256) k_spmv_csr_df(
     }
   }
   __syncthreads();
-  const float muxh = sc[0], muxl = sc[1], csh = -sc[2], csl = -sc[3];
+  o.muxh = sc[0];
+  o.muxl = sc[1];
+  o.csh = -sc[2];
+  o.csl = -sc[3];
+  return true;
+}
+
+// (acc - mu.x) - csub * z in double-float, written as (yh, yl)
+__device__ __forceinline__ void xv_df_store(float acc, const XvDf& p, bool has_z, float zhr, float zlr,
+                                            float* __restrict__ yh, float* __restrict__ yl, int64_t r) {
+  float h = acc, l = 0.f;
+  float t = h - p.muxh;
+  float v = t - h;
+  float err = (h - (t - v)) + (-p.muxh - v);
+  h = t;
+  l = err - p.muxl;
+  if (has_z) dfx_fma(h, l, p.csh, p.csl, zhr, zlr);
+  t = h + l;
+  yl[r] = l - (t - h);
+  yh[r] = t;
+}
+
+template <typename ValT, typename IdxT>
+__global__ void __launch_bounds__(256) k_spmv_csr_df(
+    const int64_t* __restrict__ rowptr, const IdxT* __restrict__ hcol, const ValT* __restrict__ hval,
+    int64_t n_rows, int64_t nf, const float* __restrict__ xh, const float* __restrict__ xl,
+    const float* __restrict__ inv_f, const float* __restrict__ clip_f, const float* __restrict__ mu_h,
+    const float* __restrict__ mu_l, float* __restrict__ yh, float* __restrict__ yl,
+    const double* __restrict__ csub, const float* __restrict__ zh, const float* __restrict__ zl,
+    const BlkRange* __restrict__ blk, const int* __restrict__ active) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  XvDf pr;
+  if (!xv_df_prologue(smem_raw, n_rows, nf, xh, xl, inv_f, clip_f, mu_h, mu_l, csub, blk, active, pr))
+    return;
+  const int64_t rb0 = pr.rb0, rb1 = pr.rb1;
 
   int lane = threadIdx.x & 31;
   int64_t warp, nwarps;
@@ -824,19 +863,7 @@ __global__ void __launch_bounds__(256) k_spmv_csr_df(
       }
     }
     acc = sv_warp_sum(acc);
-    if (lane == 0) {
-      // (acc - mu.x) - csub * z in double-float
-      float h = acc, l = 0.f;
-      float t = h - muxh;
-      float v = t - h;
-      float err = (h - (t - v)) + (-muxh - v);
-      h = t;
-      l = err - muxl;
-      if (zh) dfx_fma(h, l, csh, csl, zh[r], zl[r]);
-      t = h + l;
-      yl[r] = l - (t - h);
-      yh[r] = t;
-    }
+    if (lane == 0) xv_df_store(acc, pr, zh != nullptr, zh ? zh[r] : 0.f, zh ? zl[r] : 0.f, yh, yl, r);
   }
 }
 
