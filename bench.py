@@ -386,7 +386,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-knn-stress", action="store_true")
-    ap.add_argument("--kernel-case", choices=["irlba", "knn"], default=None,
+    ap.add_argument("--kernel-case", choices=["irlba", "knn", "prep"], default=None,
                     help="run one small case of a kernel family (for profiler captures) and exit")
     ap.add_argument("--reader", action="store_true",
                     help="MatrixMarket reader: 10X-layout text in host memory to the device count matrix")
@@ -812,7 +812,9 @@ def kernel_case(args):
       irlba: a random sparse 600,000 x 3,000 CenteredMatrix (40 non-zeros per
              cell, FP32) and 3 restart cycles of irlba 50 -- the Lanczos kernels
              on a 274 MB cell-side basis;
-      knn:   400,000 x 50 mixture points, k = 20, BF16 tensor-core path."""
+      knn:   400,000 x 50 mixture points, k = 20, BF16 tensor-core path;
+      prep:  filter_counts and find_variable_features(:vst) on 200,000 atlas
+             cells generated on the device."""
     import __graft_entry__ as ge
     import scipy.sparse as sp
     ge._build_module().build()
@@ -835,6 +837,21 @@ def kernel_case(args):
         ctx.sync()
         out = {"kernel_case": "irlba", "n_cells": n, "features": nf, "nnz": int(X.nnz),
                "cycles": 3, "s": round(time.perf_counter() - t0, 4)}
+    elif args.kernel_case == "prep":
+        # the steps before the path: filter_counts and find_variable_features(:vst)
+        w = dict(WORKLOADS["atlas"])
+        n = args.cells or 200_000
+        mu_g, s_c, cl, lfc = gen_params(w, n, SEED)
+        D = calibrate_depth(mu_g, s_c, cl, lfc, w["nnz_per_cell"])
+        counts = sv.CountMatrix.generate(n, w["n_genes"], mu_g, s_c, cl, lfc, depth=D,
+                                         dispersion=DISPERSION, seed=SEED, ctx=ctx)
+        t0 = time.perf_counter()
+        F, ci, fi = sv.filter_counts(counts, min_cells=3, min_features=200)
+        t1 = time.perf_counter()
+        feats, _ = sv.find_variable_features(F, w["n_hvf"])
+        ctx.sync()
+        out = {"kernel_case": "prep", "n_cells": n, "kept_cells": int(ci.sum()), "kept_genes": int(fi.sum()),
+               "filter_s": round(t1 - t0, 4), "vst_s": round(time.perf_counter() - t1, 4)}
     else:
         n, d = args.cells or 400_000, 50
         means = rng.normal(0, 4, (60, d))

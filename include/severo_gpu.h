@@ -95,6 +95,12 @@ int  sv_profile_query(sv_context* ctx, const char* name_substring, double* total
 /* Writes "name launches total_ms" lines for every kernel seen into buf. */
 int  sv_profile_report(sv_context* ctx, char* buf, size_t len);
 int  sv_device_memory(sv_context* ctx, size_t* free_bytes, size_t* total_bytes);
+/* Self-test of the bounded waits of the tensor-core kNN kernel: one warp waits
+ * on an mbarrier that nothing completes, with a limit of `cycles` (1 .. 2^32)
+ * clock cycles; the wait runs out and the call returns SV_ERR_DEVICE through
+ * the context's status word, the context staying usable (no reference
+ * counterpart: it exercises this library's failure path without a fault). */
+int  sv_selftest_wait_timeout(sv_context* ctx, long long cycles);
 
 /* ---- count matrix ------------------------------------------------------------
  * sv_counts_upload_csc replaces holding the CountMatrix of src/Severo.jl:26-27

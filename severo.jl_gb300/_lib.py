@@ -84,6 +84,7 @@ SIGNATURES = {
     "sv_counts_select_cells": (i32, [vp, vp, i64, i64, P(vp)]),
     "sv_find_variable_features_vst": (i32, [vp, vp, i64, C.c_double, vp, vp]),
     "sv_normalize_cells": (i32, [vp, vp, i32, dbl, i32, P(vp)]),
+    "sv_selftest_wait_timeout": (i32, [vp, C.c_longlong]),
     "sv_centered_gram": (i32, [vp, vp, vp, dbl, dbl, vp]),
     "sv_sparse_mul_spvec": (i32, [vp, i64, i64, vp, vp, vp, i64, vp, vp, i32, dbl, dbl, vp]),
     "sv_sparse_mul_sparse": (i32, [vp, i64, i64, i64, vp, vp, vp, i32, vp, vp, vp, i32, dbl, dbl, vp]),

@@ -95,17 +95,38 @@ __device__ __forceinline__ uint32_t seq_tile(unsigned long long* seq, int t, int
 }
 
 // Bounded wait.  Returns false when the CTA is aborting (timeout here or elsewhere).
-__device__ __forceinline__ bool mbar_wait(unsigned long long* b, uint32_t parity, int* err) {
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, uint32_t parity, int* err,
+                                          long long limit = TIMEOUT) {
   if (mbar_try(b, parity)) return true;
   long long t0 = clock64();
   while (!mbar_try(b, parity)) {
     if (*(volatile int*)err) return false;
-    if (clock64() - t0 > TIMEOUT) {
+    if (clock64() - t0 > limit) {
       atomicOr(err, 1);
       return false;
     }
   }
   return true;
+}
+
+// The bounded wait on its own: one warp waits on a barrier that nothing
+// arrives at, with a limit of `limit` cycles; the wait runs out, the kernel
+// records SV_STATUS_LIMIT in *status and returns.  No copy or MMA is in
+// flight, so nothing needs draining.
+__global__ void k_wait_timeout_selftest(long long limit, int* status) {
+  __shared__ unsigned long long bar;
+  __shared__ int err;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    err = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  if (!mbar_wait(&bar, 0, &err, limit)) {
+    if (threadIdx.x == 0) atomicOr(status, SV_STATUS_LIMIT);
+    return;
+  }
+  // unreachable: nothing arrives at the barrier
 }
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
@@ -798,4 +819,19 @@ int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unus
     return e.code;
   }
   return SV_OK;
+}
+
+// Runs the bounded mbarrier wait of the tensor-core kNN kernel against a
+// barrier that never completes, with a limit of `cycles` clock cycles
+// (1 .. 2^32); returns SV_ERR_DEVICE (the wait ran out, recorded through the
+// context's status word) with the context still usable.  A self-test of the
+// timeout path that needs no fault: no copy or MMA is involved.
+SV_API int sv_selftest_wait_timeout(sv_context* ctx, long long cycles) {
+  SV_TRY
+  sv_ctx_check(ctx);
+  SV_REQUIRE(cycles >= 1 && cycles <= (1ll << 32), "cycles out of range");
+  sv_launch(ctx, "selftest_wait_timeout", k_wait_timeout_selftest, dim3(1), dim3(32), 0, cycles,
+            ctx->d_status);
+  sv_check_device_status(ctx, "sv_selftest_wait_timeout");
+  SV_CATCH
 }

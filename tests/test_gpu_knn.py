@@ -154,3 +154,16 @@ def test_knn_stress_2m_bf16_recall(sv, ctx, O):
     assert hits / ref.size >= 0.999, hits / ref.size
     assert np.all(idx[q, 0] == q + 1)
     assert np.all(np.diff(dist[q], axis=1) >= 0)
+
+
+def test_bounded_wait_runs_out_and_context_survives(sv, ctx, O):
+    """The bounded mbarrier wait of the tensor-core kernel, made to run out on
+    a barrier that nothing completes (a limit of 10^5 cycles): the call reports
+    SV_ERR_DEVICE through the status word, and the context keeps working."""
+    lib = sv._lib.load()
+    st = lib.sv_selftest_wait_timeout(ctx.h, 100000)
+    assert st == sv._lib.SV_ERR_DEVICE
+    assert "iteration limit" in sv._lib.last_error()
+    X = np.random.default_rng(9).standard_normal((2000, 16))
+    idx, _ = sv.ann(X, 5, precision="bf16", ctx=ctx)
+    assert _check_sets(idx, X, 5, True, "euclidean", O=O) == 0
