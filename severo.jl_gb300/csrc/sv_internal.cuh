@@ -212,6 +212,7 @@ struct sv_centered {
   DevBuf<double> scal;                // small device scalars
   // row-blocked CSC copy of the subset for X^T u (FP32 / BF16 storage)
   int64_t rb_rows = 0, n_rb = 0;      // rows per block, number of row blocks
+  int rb_per_sm = 3;                  // resident blocks per SM of the X^T u kernel
   DevBuf<int64_t> rb_ptr;             // n_rb * nf + 1 entry offsets, ordered (block, feature)
   DevBuf<uint16_t> rb_idx;            // local row within the block
   DevBuf<unsigned char> rb_val;       // value (storage type)

@@ -1113,6 +1113,93 @@ __global__ void __launch_bounds__(RB_THREADS) k_spmv_rb(
   }
 }
 
+// The same product for one sample, as a single wave of resident blocks: tasks
+// (row block b, feature group g) taken round-robin (b-major), the features of
+// a task (g, g + fg, ...) handed to the warps one at a time through a shared
+// counter, so that dense and sparse features even out within the block and no
+// partial last wave is left (the grid form above ran 3.2 waves of blocks with
+// 43% of its warps active).  Same loop and partials as k_spmv_rb.
+template <typename ValT>
+__global__ void __launch_bounds__(RB_THREADS) k_spmv_rb_waves(
+    const int64_t* __restrict__ rb_ptr, const uint16_t* __restrict__ rb_idx,
+    const ValT* __restrict__ rb_val, int64_t nf, int64_t n_cells, int64_t n_rb, int fg,
+    const float* __restrict__ inv_f, const float* __restrict__ clip_f, const float* __restrict__ uf,
+    float* __restrict__ partial) {
+  extern __shared__ __align__(16) float us[];
+  __shared__ int next_f;
+  const int lane = threadIdx.x & 31;
+  const int64_t ntask = n_rb * fg;
+  for (int64_t task = blockIdx.x; task < ntask; task += gridDim.x) {
+    const int64_t b = task / fg;
+    const int g = (int)(task % fg);
+    const int64_t r0 = b * RB_ROWS;
+    const int64_t nr = n_cells - r0 < RB_ROWS ? n_cells - r0 : RB_ROWS;
+    __syncthreads();                        // the previous task is done with us and next_f
+    for (int64_t i = threadIdx.x; i < RB_ROWS; i += blockDim.x) us[i] = i < nr ? uf[r0 + i] : 0.f;
+    if (threadIdx.x == 0) next_f = 0;
+    __syncthreads();
+    while (true) {
+      int fi = 0;
+      if (lane == 0) fi = atomicAdd(&next_f, 1);
+      fi = __shfl_sync(0xffffffffu, fi, 0);
+      const int64_t f = g + (int64_t)fi * fg;
+      if (f >= nf) break;
+      const int64_t s = rb_ptr[b * nf + f], e = rb_ptr[b * nf + f + 1];
+      const float inv = inv_f[f], clip = clip_f[f];
+      float acc = 0.f;
+      const int64_t a0 = s & ~3ll;
+      if constexpr (sizeof(ValT) == 2) {
+        const uint16_t* pi = rb_idx + a0;
+        const uint16_t* pv = (const uint16_t*)rb_val + a0;
+        const int ls = (int)(s - a0), le = (int)(e - a0);
+        for (int q = 4 * lane; q < le; q += 512) {
+          uint2 ri[4], rv[4];
+#pragma unroll
+          for (int h = 0; h < 4; ++h)
+            if (q + 128 * h < le) {
+              ri[h] = __ldg((const uint2*)(pi + q + 128 * h));
+              rv[h] = __ldg((const uint2*)(pv + q + 128 * h));
+            }
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            const int qh = q + 128 * h;
+            if (qh >= le) break;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+              const unsigned wi = t < 2 ? ri[h].x : ri[h].y;
+              const unsigned wv = t < 2 ? rv[h].x : rv[h].y;
+              const int ci = (t & 1) ? (int)(wi >> 16) : (int)(wi & 0xffffu);
+              const float av = __uint_as_float((t & 1) ? (wv & 0xffff0000u) : (wv << 16));
+              if (qh + t >= ls && qh + t < le) acc += fminf(av * inv, clip) * us[ci];
+            }
+          }
+        }
+      } else {
+        for (int64_t gg = a0 + 4 * lane; gg < e; gg += 256) {
+          int ci[2][4];
+          float av[2][4];
+#pragma unroll
+          for (int h = 0; h < 2; ++h)
+            if (gg + 128 * h < e) {
+              ld4(rb_idx, gg + 128 * h, ci[h]);
+              ld4v(rb_val, gg + 128 * h, av[h]);
+            }
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            if (gg + 128 * h >= e) break;
+            const int64_t gh = gg + 128 * h;
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+              if (gh + t >= s && gh + t < e) acc += fminf(av[h][t] * inv, clip) * us[ci[h][t]];
+          }
+        }
+      }
+      acc = sv_warp_sum(acc);
+      if (lane == 0) partial[b * nf + f] = acc;
+    }
+  }
+}
+
 // y_f = alpha * (sum_b partial[b][f] - mu_f * sum(u)) + beta*y_f - csub*z_f
 __global__ void k_rb_finish(const float* __restrict__ partial, int64_t n_rb, int64_t nf,
                             const double* __restrict__ mu, const double* __restrict__ upart,
@@ -1332,23 +1419,23 @@ void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const 
     sv_centered* Sm = const_cast<sv_centered*>(S);
     sv_launch(ctx, "spmv_csc_uprep", k_u_prep, dim3(UPREP_BLOCKS), dim3(256), 0, x, S->n_cells,
               Sm->u_f32.get(), Sm->red_partial.get());
-    int resident = ctx->num_sms * 3;
-    int fg = (int)std::max<int64_t>(1, std::min<int64_t>(S->nf, (3 * resident + S->n_rb - 1) / S->n_rb));
-    dim3 grid((unsigned)S->n_rb, (unsigned)fg);
+    // one wave of resident blocks, ~6 tasks (row block, feature group) each
+    const int resident = ctx->num_sms * S->rb_per_sm;
+    const int fg = (int)std::max<int64_t>(1, std::min<int64_t>(S->nf, (6 * resident + S->n_rb - 1) / S->n_rb));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(resident, S->n_rb * fg));
     size_t smem = RB_ROWS * sizeof(float);
     if (S->dtype == SV_F32)
-      sv_launch(ctx, "spmv_rb", k_spmv_rb<float>, grid, dim3(RB_THREADS), smem,
+      sv_launch(ctx, "spmv_rb", k_spmv_rb_waves<float>, dim3(grid), dim3(RB_THREADS), smem,
                 (const int64_t*)S->rb_ptr.get(), (const uint16_t*)S->rb_idx.get(),
-                (const float*)S->rb_val.get(), S->nf, S->n_cells, (const float*)S->inv_std_f.get(),
-                (const float*)S->clip_f.get(), (const float*)Sm->u_f32.get(), Sm->rb_partial.get(),
-                (const int64_t*)nullptr, (const int*)nullptr, (const int*)nullptr);
-    else
-      sv_launch(ctx, "spmv_rb", k_spmv_rb<__nv_bfloat16>, grid, dim3(RB_THREADS), smem,
-                (const int64_t*)S->rb_ptr.get(), (const uint16_t*)S->rb_idx.get(),
-                (const __nv_bfloat16*)S->rb_val.get(), S->nf, S->n_cells,
+                (const float*)S->rb_val.get(), S->nf, S->n_cells, S->n_rb, fg,
                 (const float*)S->inv_std_f.get(), (const float*)S->clip_f.get(),
-                (const float*)Sm->u_f32.get(), Sm->rb_partial.get(), (const int64_t*)nullptr,
-                (const int*)nullptr, (const int*)nullptr);
+                (const float*)Sm->u_f32.get(), Sm->rb_partial.get());
+    else
+      sv_launch(ctx, "spmv_rb", k_spmv_rb_waves<__nv_bfloat16>, dim3(grid), dim3(RB_THREADS), smem,
+                (const int64_t*)S->rb_ptr.get(), (const uint16_t*)S->rb_idx.get(),
+                (const __nv_bfloat16*)S->rb_val.get(), S->nf, S->n_cells, S->n_rb, fg,
+                (const float*)S->inv_std_f.get(), (const float*)S->clip_f.get(),
+                (const float*)Sm->u_f32.get(), Sm->rb_partial.get());
     sv_launch(ctx, "spmv_rb_finish", k_rb_finish, dim3(sv_grid_for(ctx, S->nf, 256, 4)), dim3(256), 0,
               (const float*)Sm->rb_partial.get(), S->n_rb, S->nf, (const double*)S->mu.get(),
               (const double*)Sm->red_partial.get(), UPREP_BLOCKS, alpha, beta, y, csub, z);
@@ -1669,6 +1756,21 @@ static sv_centered* make_centered(sv_context* ctx, const sv_data* data, const st
         SV_CUDA(cudaFuncSetAttribute(k_spmv_rb<float>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         SV_CUDA(cudaFuncSetAttribute(k_spmv_rb<__nv_bfloat16>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                      100));
+        SV_CUDA(cudaFuncSetAttribute(k_spmv_rb_waves<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(RB_ROWS * sizeof(float))));
+        SV_CUDA(cudaFuncSetAttribute(k_spmv_rb_waves<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(RB_ROWS * sizeof(float))));
+        SV_CUDA(cudaFuncSetAttribute(k_spmv_rb_waves<float>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        SV_CUDA(cudaFuncSetAttribute(k_spmv_rb_waves<__nv_bfloat16>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     100));
+        int per = 0;
+        if (data->dtype == SV_F32)
+          SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmv_rb_waves<float>, RB_THREADS,
+                                                                RB_ROWS * sizeof(float)));
+        else
+          SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmv_rb_waves<__nv_bfloat16>, RB_THREADS,
+                                                                RB_ROWS * sizeof(float)));
+        S->rb_per_sm = std::max(1, per);
         sv_sync(ctx);
       }
     }
