@@ -145,20 +145,23 @@ __global__ void __launch_bounds__(KNN_THREADS) k_knn_fp32(const float* __restric
   }
 }
 
-// Exact FP32 re-rank: one warp per query; K2 candidates sorted by (d2, index).
+// Exact FP32 re-rank: one warp per query; K2 candidates sorted by (d2, index)
+// (a bitonic sort over the next power of two, P2, padded with the largest key).
 template <int DP>
 __global__ void k_rerank(const float* __restrict__ X, int64_t n, const int32_t* __restrict__ cand,
                          int K2, int k, int include_self, int cosine, int32_t* __restrict__ out_idx,
                          float* __restrict__ out_dist) {
   extern __shared__ unsigned long long keys_all[];
+  int P2 = 32;
+  while (P2 < K2) P2 <<= 1;
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  unsigned long long* keys = keys_all + wid * K2;
+  unsigned long long* keys = keys_all + wid * P2;
   int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t qi = warp; qi < n; qi += nwarps) {
     const float* q = X + qi * DP;
-    for (int t = lane; t < K2; t += 32) {
-      int c = cand[qi * K2 + t];
+    for (int t = lane; t < P2; t += 32) {
+      int c = t < K2 ? cand[qi * K2 + t] : -1;
       unsigned long long key = ~0ull;
       if (c >= 0 && c != qi) {
         const float* p = X + (int64_t)c * DP;
@@ -176,10 +179,10 @@ __global__ void k_rerank(const float* __restrict__ X, int64_t n, const int32_t* 
       keys[t] = key;
     }
     __syncwarp();
-    // bitonic sort of K2 (power of two) keys by the warp
-    for (int kk = 2; kk <= K2; kk <<= 1) {
+    // bitonic sort of the P2 keys by the warp
+    for (int kk = 2; kk <= P2; kk <<= 1) {
       for (int j = kk >> 1; j > 0; j >>= 1) {
-        for (int i = lane; i < K2; i += 32) {
+        for (int i = lane; i < P2; i += 32) {
           int ixj = i ^ j;
           if (ixj > i) {
             unsigned long long a = keys[i], b = keys[ixj];
@@ -226,8 +229,10 @@ void launch_fp32(sv_context* ctx, const float* X, const float* sq, int64_t n, in
 template <int DP>
 void launch_rerank(sv_context* ctx, const float* X, int64_t n, const int32_t* cand, int K2, int k,
                    int inc, int cosine, int32_t* idx, float* dist) {
+  int P2 = 32;
+  while (P2 < K2) P2 <<= 1;
   sv_launch(ctx, "knn_rerank", k_rerank<DP>, dim3(sv_grid_for(ctx, n * 32, 256, 8)), dim3(256),
-            (size_t)8 * K2 * 8, X, n, cand, K2, k, inc, cosine, idx, dist);
+            (size_t)8 * P2 * 8, X, n, cand, K2, k, inc, cosine, idx, dist);
 }
 
 // candidate indices of one sample (local, >= 0) -> stacked rows
@@ -259,7 +264,9 @@ static void knn_core(sv_context* ctx, const float* X32, const float* sq, int64_t
                      int include_self, int cosine, int precision, sv_knn* out,
                      const std::vector<int64_t>* segs = nullptr) {
   // candidates per query: at least 2k; the tensor-core stage always keeps 64
-  int K2 = (2 * k <= 32 && precision != SV_KNN_BF16) ? 32 : 64;
+  // candidates per query: 32 or 64 from the FP32 tiles, 40 (k <= 20) or 64 from
+  // the tensor-core tiles
+  int K2 = precision == SV_KNN_BF16 ? (2 * k <= 40 ? 40 : 64) : (2 * k <= 32 ? 32 : 64);
   if (2 * k > 64) sv_throw(SV_ERR_UNSUPPORTED, "k = %d exceeds the supported maximum of 32", k);
   DevBuf<int32_t> cand((size_t)n * K2);
   bool done = false;

@@ -10,8 +10,9 @@
 //               per tile into one of two 256-column TMEM accumulators;
 //   warps 2..9  epilogue: tcgen05.ld of their lane quarter (= 32 queries) and
 //               column half (128 points), key = |p|^2 - 2 acc, and a register
-//               top-32 per (query, half).
-// The 64 candidates per query then go through the exact FP32 re-rank
+//               top-KH per (query, half): KH = 20 for k <= 20 (the 40
+//               candidates of the atlas's k = 20), 32 up to k = 32.
+// The 2 KH candidates per query then go through the exact FP32 re-rank
 // (sv_knn.cu).  Every mbarrier wait is bounded: on a timeout the kernel records
 // an error, drains its own outstanding copies and MMAs (bounded as well),
 // releases its tensor memory and returns.
@@ -27,7 +28,7 @@ constexpr int BK = 64;             // padded dimension (BF16 elements, 128 bytes
 constexpr int STAGES = 4;
 constexpr int EPI_WARPS = 8;
 constexpr int THREADS = (2 + EPI_WARPS) * 32;
-constexpr int KH = 32;             // candidates kept per (query, column half)
+constexpr int KH_MAX = 32;         // most candidates kept per (query, column half)
 constexpr long long TIMEOUT = 4000000000ll;   // cycles (~2 s) per wait
 constexpr int RING = 16;           // tile-sequence slots (> STAGES + 2 tiles in flight)
 constexpr uint32_t END = 0xffffffffu;   // tile id of the end-of-sequence slot
@@ -256,7 +257,7 @@ __device__ __forceinline__ int tile_at(int j, int t0, int ntiles, bool around) {
 // FOLD: |p|^2 is part of the MMA (see k_pack_fold): the accumulator is
 // D = q.p - |p|^2 / 2 and key = -2 D, so no norm is loaded in the epilogue and a
 // 32-candidate chunk is rejected by one compare of its maximum D.
-template <bool FOLD>
+template <bool FOLD, int KH>
 __global__ void __launch_bounds__(THREADS, 1)
     k_knn_tc(const __grid_constant__ CUtensorMap tmapA, const __grid_constant__ CUtensorMap tmapB,
              const float* __restrict__ sqpad, int64_t n, int ntiles, int32_t* __restrict__ cand,
@@ -701,7 +702,8 @@ int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unus
   (void)include_self;   // the re-rank places or removes the point itself
   try {
     if (dp > BK) sv_throw(SV_ERR_UNSUPPORTED, "tensor-core kNN handles up to %d dimensions", BK);
-    if (K2 != 2 * KH) sv_throw(SV_ERR_UNSUPPORTED, "tensor-core kNN keeps %d candidates", 2 * KH);
+    if (K2 != 40 && K2 != 2 * KH_MAX)
+      sv_throw(SV_ERR_UNSUPPORTED, "tensor-core kNN keeps 40 or %d candidates", 2 * KH_MAX);
     if (n >= (1ll << 31) - BN) sv_throw(SV_ERR_UNSUPPORTED, "too many points");
     int ntiles = (int)((n + BN - 1) / BN);
     // one spare tile of padding: a sample's last tile may start anywhere
@@ -799,18 +801,27 @@ int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unus
       sched.alloc(hs.size());
       sv_h2d(ctx, sched.get(), hs.data(), hs.size() * 8);
     }
+#define KNN_TC(FOLD, KHV, CO, NR, PM)                                                                \
+  do {                                                                                              \
+    SV_CUDA(cudaFuncSetAttribute(k_knn_tc<FOLD, KHV>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                                 (int)smem));                                                       \
+    sv_launch(ctx, "knn_tc_tiles", k_knn_tc<FOLD, KHV>, dim3(nblocks), dim3(THREADS), smem, tmapA,   \
+              tmapB, (const float*)sq.get(), n, ntiles, cout, ctx->d_status,                        \
+              (const int64_t*)sched.get(), (int)around, CO, NR, PM);                               \
+  } while (0)
+    // 20 candidates per column half (40 per query) for k <= 20, else 32
     if (fold) {
-      SV_CUDA(cudaFuncSetAttribute(k_knn_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      sv_launch(ctx, "knn_tc_tiles", k_knn_tc<true>, dim3(nblocks), dim3(THREADS), smem, tmapA, tmapB,
-                (const float*)sq.get(), n, ntiles, cout, ctx->d_status, (const int64_t*)sched.get(),
-                (int)around, (const float*)coord.get(), (const float*)nrm.get(),
-                (const unsigned*)pmax.get());
+      if (K2 == 40)
+        KNN_TC(true, 20, (const float*)coord.get(), (const float*)nrm.get(), (const unsigned*)pmax.get());
+      else
+        KNN_TC(true, 32, (const float*)coord.get(), (const float*)nrm.get(), (const unsigned*)pmax.get());
     } else {
-      SV_CUDA(cudaFuncSetAttribute(k_knn_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      sv_launch(ctx, "knn_tc_tiles", k_knn_tc<false>, dim3(nblocks), dim3(THREADS), smem, tmapA, tmapB,
-                (const float*)sq.get(), n, ntiles, cout, ctx->d_status, (const int64_t*)sched.get(),
-                (int)around, (const float*)nullptr, (const float*)nullptr, (const unsigned*)nullptr);
+      if (K2 == 40)
+        KNN_TC(false, 20, (const float*)nullptr, (const float*)nullptr, (const unsigned*)nullptr);
+      else
+        KNN_TC(false, 32, (const float*)nullptr, (const float*)nullptr, (const unsigned*)nullptr);
     }
+#undef KNN_TC
     if (around)
       sv_launch(ctx, "knn_unperm", k_cand_unperm, dim3(sv_grid_for(ctx, n * K2, 256, 8)), dim3(256), 0,
                 (const int32_t*)cand_sorted.get(), pm, n, K2, cand);

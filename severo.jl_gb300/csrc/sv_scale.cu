@@ -1120,7 +1120,7 @@ __global__ void __launch_bounds__(RB_THREADS) k_spmv_rb(
 // partial last wave is left (the grid form above ran 3.2 waves of blocks with
 // 43% of its warps active).  Same loop and partials as k_spmv_rb.
 template <typename ValT>
-__global__ void __launch_bounds__(RB_THREADS) k_spmv_rb_waves(
+__global__ void __launch_bounds__(RB_THREADS, 3) k_spmv_rb_waves(
     const int64_t* __restrict__ rb_ptr, const uint16_t* __restrict__ rb_idx,
     const ValT* __restrict__ rb_val, int64_t nf, int64_t n_cells, int64_t n_rb, int fg,
     const float* __restrict__ inv_f, const float* __restrict__ clip_f, const float* __restrict__ uf,
@@ -1419,9 +1419,11 @@ void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const 
     sv_centered* Sm = const_cast<sv_centered*>(S);
     sv_launch(ctx, "spmv_csc_uprep", k_u_prep, dim3(UPREP_BLOCKS), dim3(256), 0, x, S->n_cells,
               Sm->u_f32.get(), Sm->red_partial.get());
-    // one wave of resident blocks, ~6 tasks (row block, feature group) each
+    // one wave of resident blocks, ~6 tasks (row block, feature group) each,
+    // at least 32 features per task
     const int resident = ctx->num_sms * S->rb_per_sm;
-    const int fg = (int)std::max<int64_t>(1, std::min<int64_t>(S->nf, (6 * resident + S->n_rb - 1) / S->n_rb));
+    const int fg = (int)std::max<int64_t>(
+        1, std::min<int64_t>(std::max<int64_t>(1, S->nf / 32), (6 * resident + S->n_rb - 1) / S->n_rb));
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(resident, S->n_rb * fg));
     size_t smem = RB_ROWS * sizeof(float);
     if (S->dtype == SV_F32)
