@@ -825,14 +825,26 @@ __global__ void __launch_bounds__(256) k_spmv_csr_df(
           const int qh = q + 32 * E * h;
           const unsigned wi[4] = {ri[h].x, ri[h].y, ri[h].z, ri[h].w};
           const unsigned wv[4] = {rv[h].x, rv[h].y, rv[h].z, rv[h].w};
+          if (qh >= ls && qh + E <= le) {
+            // a group inside the row (all but a row's first and last): no guards
 #pragma unroll
-          for (int t = 0; t < E; ++t) {
-            if (qh + t >= ls && qh + t < le) {
+            for (int t = 0; t < E; ++t) {
               const int ci = (t & 1) ? (int)(wi[t >> 1] >> 16) : (int)(wi[t >> 1] & 0xffffu);
               const float av = __uint_as_float((t & 1) ? (wv[t >> 1] & 0xffff0000u) : (wv[t >> 1] << 16));
               const float2 pq = ((const float2*)smem_raw)[ci];
               const float rr = av * pq.x;
               acc += pq.x >= 0.f ? fminf(rr, pq.y) : fmaxf(rr, pq.y);
+            }
+          } else {
+#pragma unroll
+            for (int t = 0; t < E; ++t) {
+              if (qh + t >= ls && qh + t < le) {
+                const int ci = (t & 1) ? (int)(wi[t >> 1] >> 16) : (int)(wi[t >> 1] & 0xffffu);
+                const float av = __uint_as_float((t & 1) ? (wv[t >> 1] & 0xffff0000u) : (wv[t >> 1] << 16));
+                const float2 pq = ((const float2*)smem_raw)[ci];
+                const float rr = av * pq.x;
+                acc += pq.x >= 0.f ? fminf(rr, pq.y) : fmaxf(rr, pq.y);
+              }
             }
           }
         }
@@ -1164,13 +1176,25 @@ __global__ void __launch_bounds__(RB_THREADS, 3) k_spmv_rb_waves(
           for (int h = 0; h < 4; ++h) {
             const int qh = q + 128 * h;
             if (qh >= le) break;
+            if (qh >= ls && qh + 4 <= le) {
+              // a group inside the run: no guards
 #pragma unroll
-            for (int t = 0; t < 4; ++t) {
-              const unsigned wi = t < 2 ? ri[h].x : ri[h].y;
-              const unsigned wv = t < 2 ? rv[h].x : rv[h].y;
-              const int ci = (t & 1) ? (int)(wi >> 16) : (int)(wi & 0xffffu);
-              const float av = __uint_as_float((t & 1) ? (wv & 0xffff0000u) : (wv << 16));
-              if (qh + t >= ls && qh + t < le) acc += fminf(av * inv, clip) * us[ci];
+              for (int t = 0; t < 4; ++t) {
+                const unsigned wi = t < 2 ? ri[h].x : ri[h].y;
+                const unsigned wv = t < 2 ? rv[h].x : rv[h].y;
+                const int ci = (t & 1) ? (int)(wi >> 16) : (int)(wi & 0xffffu);
+                const float av = __uint_as_float((t & 1) ? (wv & 0xffff0000u) : (wv << 16));
+                acc += fminf(av * inv, clip) * us[ci];
+              }
+            } else {
+#pragma unroll
+              for (int t = 0; t < 4; ++t) {
+                const unsigned wi = t < 2 ? ri[h].x : ri[h].y;
+                const unsigned wv = t < 2 ? rv[h].x : rv[h].y;
+                const int ci = (t & 1) ? (int)(wi >> 16) : (int)(wi & 0xffffu);
+                const float av = __uint_as_float((t & 1) ? (wv & 0xffff0000u) : (wv << 16));
+                if (qh + t >= ls && qh + t < le) acc += fminf(av * inv, clip) * us[ci];
+              }
             }
           }
         }
