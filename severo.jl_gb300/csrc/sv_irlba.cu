@@ -743,11 +743,67 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(const double* __restrict__ 
   }
 }
 
+// ---- packed double-float arithmetic -----------------------------------------
+// Two independent FP32 lanes per instruction (the f32x2 forms of sm_100 and
+// later): each lane is the IEEE FP32 operation of its scalar counterpart, so a
+// packed sequence gives bit for bit what the same scalar sequence gives for each
+// of the two values, in half the issue slots.
+typedef unsigned long long f2_t;
+__device__ __forceinline__ f2_t f2_pack(float a, float b) {
+  f2_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(f2_t r, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f2_t f2_add(f2_t a, f2_t b) {
+  f2_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2_t f2_sub(f2_t a, f2_t b) {
+  f2_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b) {
+  f2_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c) {
+  f2_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+// df_fma on two accumulator pairs at once with one shared multiplicand a:
+// ah, nah = -ah and al broadcast to both lanes.  The product is formed negated
+// (pn = -ah*bh, exact negation of the rounded product), which turns df_fma's
+// sh + p and p - v into subtractions without a negation instruction.
+__device__ __forceinline__ void df_fma2(f2_t& sh, f2_t& sl, f2_t ah, f2_t nah, f2_t al, f2_t bh,
+                                        f2_t bl) {
+  f2_t pn = f2_mul(nah, bh);
+  f2_t e = f2_fma(ah, bh, pn);   // ah*bh - p, exact
+  e = f2_fma(ah, bl, e);
+  e = f2_fma(al, bh, e);
+  f2_t t = f2_sub(sh, pn);       // sh + p
+  f2_t v = f2_sub(t, sh);
+  f2_t err = f2_sub(sh, f2_sub(t, v));
+  err = f2_sub(err, f2_add(pn, v));   // + (p - v)
+  sh = t;
+  sl = f2_add(sl, f2_add(err, e));
+}
+
 // Out[:, c] = sum_r In[:, r] * M[r + c*nin] for c < nout (tall x small), In
 // double-float; Out double-float (outh/outl) or FP64 (outd).  KB output columns
-// per pass; EXACT when KB divides nout (no column guards).  M sits in shared
-// memory as (hi, lo) pairs read with one broadcast 8-byte load per term.
-template <int KB, bool EXACT>
+// per pass over a row (KB even; the columns are taken in pairs, one packed
+// f32x2 double-float multiply-add per pair and term); gridDim.y blocks share
+// the passes of a row range (the short feature side).  M sits in shared memory
+// as one float4 (hi c, hi c+1, lo c, lo c+1) per term and column pair, zero
+// beyond nout, read with one broadcast 16-byte load.
+template <int KB>
 __global__ void __launch_bounds__(256) k_rotate_df(const float* __restrict__ Inh,
                                                    const float* __restrict__ Inl, int64_t ld_in,
                                                    const BlkRange* __restrict__ blk,
@@ -756,40 +812,60 @@ __global__ void __launch_bounds__(256) k_rotate_df(const float* __restrict__ Inh
                                                    int nout, float* __restrict__ outh,
                                                    float* __restrict__ outl, double* __restrict__ outd,
                                                    int64_t ld_out) {
-  extern __shared__ float2 Ms[];   // nin*nout pairs (hi, lo)
+  static_assert(KB % 2 == 0, "column pairs");
+  constexpr int NP = KB / 2;
+  extern __shared__ float4 Ms4[];   // nin * (npass * NP)
   const BlkRange br = blk[blockIdx.x];
   if (sel && !sel[br.seg]) return;   // samples not selected keep their rows
   const double* M = M0 + br.seg * mstride;
-  for (int i = threadIdx.x; i < nin * nout; i += blockDim.x) df_split(M[i], Ms[i].x, Ms[i].y);
+  const int npass = (nout + KB - 1) / KB;
+  const int npair = npass * NP;
+  for (int idx = threadIdx.x; idx < nin * npair; idx += blockDim.x) {
+    int r = idx % nin, q = idx / nin, c = 2 * q;
+    float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
+    if (c < nout) df_split(M[r + (int64_t)c * nin], h0, l0);
+    if (c + 1 < nout) df_split(M[r + (int64_t)(c + 1) * nin], h1, l1);
+    Ms4[idx] = make_float4(h0, h1, l0, l1);
+  }
   __syncthreads();
   for (int64_t i = br.r0 + threadIdx.x; i < br.r1; i += blockDim.x) {
-    for (int c0 = 0; c0 < nout; c0 += KB) {
-      float ah[KB], al[KB];
+    for (int ps = blockIdx.y; ps < npass; ps += gridDim.y) {
+      f2_t sh[NP], sl[NP];
 #pragma unroll
-      for (int t = 0; t < KB; ++t) ah[t] = al[t] = 0.f;
+      for (int q = 0; q < NP; ++q) sh[q] = sl[q] = 0ull;
+      const float4* mrow = Ms4 + (int64_t)ps * NP * nin;
       for (int r = 0; r < nin; ++r) {
         int64_t o = (int64_t)r * ld_in + i;
         float wh = Inh[o], wl = Inl[o];
+        f2_t ah = f2_pack(wh, wh), nah = f2_pack(-wh, -wh), al = f2_pack(wl, wl);
 #pragma unroll
-        for (int t = 0; t < KB; ++t)
-          if (EXACT || c0 + t < nout) {
-            float2 m = Ms[r + (c0 + t) * nin];
-            df_fma(ah[t], al[t], wh, wl, m.x, m.y);
-          }
+        for (int q = 0; q < NP; ++q) {
+          float4 m = mrow[r + q * nin];
+          df_fma2(sh[q], sl[q], ah, nah, al, f2_pack(m.x, m.y), f2_pack(m.z, m.w));
+        }
       }
 #pragma unroll
-      for (int t = 0; t < KB; ++t)
-        if (EXACT || c0 + t < nout) {
-          int64_t o = (int64_t)(c0 + t) * ld_out + i;
-          if (outd) {
-            outd[o] = df_val(ah[t], al[t]);
-          } else {
-            // renormalise the pair
-            float h = ah[t] + al[t];
-            outh[o] = h;
-            outl[o] = al[t] - (h - ah[t]);
+      for (int q = 0; q < NP; ++q) {
+        // renormalise the pairs
+        f2_t h2 = f2_add(sh[q], sl[q]);
+        f2_t l2 = f2_sub(sl[q], f2_sub(h2, sh[q]));
+        float hv[2], lv[2];
+        f2_unpack(h2, hv[0], hv[1]);
+        f2_unpack(l2, lv[0], lv[1]);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          int c = ps * KB + 2 * q + u;
+          if (c < nout) {
+            int64_t o = (int64_t)c * ld_out + i;
+            if (outd) {
+              outd[o] = df_val(hv[u], lv[u]);
+            } else {
+              outh[o] = hv[u];
+              outl[o] = lv[u];
+            }
           }
         }
+      }
     }
   }
 }
@@ -1117,12 +1193,9 @@ struct Lanczos {
     op->bind_active(active.get());
     SV_CUDA(cudaFuncSetAttribute(k_jacobi_svd, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  4 * MAX_WORK * MAX_WORK * 4));
-    SV_CUDA(cudaFuncSetAttribute(k_rotate_df<10, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 MAX_WORK * MAX_WORK * 8));
-    SV_CUDA(cudaFuncSetAttribute(k_rotate_df<8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 MAX_WORK * MAX_WORK * 8));
-    SV_CUDA(cudaFuncSetAttribute(k_rotate_df<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 MAX_WORK * MAX_WORK * 8));
+    for (auto kern : {k_rotate_df<10>, k_rotate_df<16>, k_rotate_df<26>})
+      SV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   MAX_WORK * (MAX_WORK / 2 + 13) * 16));
   }
   ~Lanczos() {
     for (auto& g : graphs)
@@ -1213,12 +1286,20 @@ struct Lanczos {
   // out = basis * M_s[:, :nout] per sample: into the other basis set (outd null)
   // or FP64 outd (ld = the side's length); only the samples with sel[s] != 0
   void rotate(Side& s, const double* M, int nout, double* outd, const int* sel) {
-    auto kern = nout % 10 == 0 ? k_rotate_df<10, true> : nout % 8 == 0 ? k_rotate_df<8, true>
-                                                                       : k_rotate_df<16, false>;
-    sv_launch(ctx, "irlba_rotate", kern, dim3(s.rows.nblk), dim3(256), (size_t)work * nout * 8,
-              (const float*)s.bh(), (const float*)s.bl(), s.len, (const BlkRange*)s.rows.blk.get(), sel,
-              work, M, (int64_t)work * work, nout, outd ? (float*)nullptr : s.th(),
-              outd ? (float*)nullptr : s.tl(), outd, s.len);
+    // columns per pass: the fewest padded columns, then the fewest passes (at
+    // 50 columns 10 per pass measured 1.65 ms per cell-side rotation at the
+    // atlas size, 16 and 26 per pass 1.96 and 1.94 ms)
+    int kb = 10;
+    for (int c : {16, 26})
+      if ((nout + c - 1) / c * c <= (nout + kb - 1) / kb * kb) kb = c;
+    auto kern = kb == 26 ? k_rotate_df<26> : kb == 16 ? k_rotate_df<16> : k_rotate_df<10>;
+    int npass = (nout + kb - 1) / kb;
+    // a short side (the features) spreads the passes of its rows over blocks
+    int gy = s.rows.nblk < ctx->num_sms ? npass : 1;
+    sv_launch(ctx, "irlba_rotate", kern, dim3(s.rows.nblk, gy), dim3(256),
+              (size_t)work * npass * (kb / 2) * 16, (const float*)s.bh(), (const float*)s.bl(), s.len,
+              (const BlkRange*)s.rows.blk.get(), sel, work, M, (int64_t)work * work, nout,
+              outd ? (float*)nullptr : s.th(), outd ? (float*)nullptr : s.tl(), outd, s.len);
   }
 
   // One cycle, enqueued on the context stream without any host round trip:
