@@ -87,6 +87,19 @@ void sv_memset(sv_context* ctx, void* p, int v, size_t bytes) {
   if (bytes) SV_CUDA(cudaMemsetAsync(p, v, bytes, ctx->stream));
 }
 
+sv_encode_tiled_fn sv_encode_tiled() {
+  static sv_encode_tiled_fn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    SV_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p)
+      sv_throw(SV_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available from the driver");
+    fn = (sv_encode_tiled_fn)p;
+  }
+  return fn;
+}
+
 void sv_parallel_memcpy(void* dst, const void* src, size_t n) {
   const size_t PART = (size_t)4 << 20;
   int t = (int)std::min<size_t>(std::min<size_t>(8, std::max(1u, std::thread::hardware_concurrency())),

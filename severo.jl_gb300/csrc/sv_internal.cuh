@@ -1,6 +1,7 @@
 // Internal definitions shared by the translation units of libseverogpu.so.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
@@ -329,6 +330,13 @@ __device__ __forceinline__ double sv_load_val(const int32_t* p, int64_t i) { ret
 void sv_scan_i64(sv_context* ctx, const int64_t* in, int64_t* out, int64_t n);
 int64_t sv_read_i64(sv_context* ctx, const int64_t* dptr);
 void sv_memset(sv_context* ctx, void* p, int v, size_t bytes);
+// cuTensorMapEncodeTiled, obtained from the driver through the runtime (no
+// link against libcuda)
+typedef CUresult (*sv_encode_tiled_fn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                       const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                       const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                       CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+sv_encode_tiled_fn sv_encode_tiled();
 // host <-> device copies on the context stream; sv_d2h returns when the data
 // are on the host.  Copies of 32 MB or more to or from pageable memory are
 // staged through the context's pinned buffers with several host threads.

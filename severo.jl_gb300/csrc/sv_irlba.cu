@@ -303,6 +303,620 @@ __global__ void __launch_bounds__(256) k_cgs_df(const float* __restrict__ Qh,
   }
 }
 
+// ---- packed double-float arithmetic -----------------------------------------
+// Two independent FP32 lanes per instruction (the f32x2 forms of sm_100 and
+// later): each lane is the IEEE FP32 operation of its scalar counterpart, so a
+// packed sequence gives bit for bit what the same scalar sequence gives for each
+// of the two values, in half the issue slots.
+typedef unsigned long long f2_t;
+__device__ __forceinline__ f2_t f2_pack(float a, float b) {
+  f2_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(f2_t r, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f2_t f2_add(f2_t a, f2_t b) {
+  f2_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2_t f2_sub(f2_t a, f2_t b) {
+  f2_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b) {
+  f2_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c) {
+  f2_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+// df_fma on two accumulator pairs at once with one shared multiplicand a:
+// ah, nah = -ah and al broadcast to both lanes.  The product is formed negated
+// (pn = -ah*bh, exact negation of the rounded product), which turns df_fma's
+// sh + p and p - v into subtractions without a negation instruction.
+__device__ __forceinline__ void df_fma2(f2_t& sh, f2_t& sl, f2_t ah, f2_t nah, f2_t al, f2_t bh,
+                                        f2_t bl) {
+  f2_t pn = f2_mul(nah, bh);
+  f2_t e = f2_fma(ah, bh, pn);   // ah*bh - p, exact
+  e = f2_fma(ah, bl, e);
+  e = f2_fma(al, bh, e);
+  f2_t t = f2_sub(sh, pn);       // sh + p
+  f2_t v = f2_sub(t, sh);
+  f2_t err = f2_sub(sh, f2_sub(t, v));
+  err = f2_sub(err, f2_add(pn, v));   // + (p - v)
+  sh = t;
+  sl = f2_add(sl, f2_add(err, e));
+}
+
+// The cell-side step of the lagged CGS2 in one pass over the basis Q (double-
+// float, columns 0..ncols-1).  The second projection of a step's new vector is
+// carried to the next step's pass, which reads the basis anyway:
+//   * column pend (pend >= 0) holds w' = w + Q[:, :pend] cp, the previous
+//     step's vector before its second projection; it is corrected in place,
+//     w = w' - Q[:, :pend] cp, and used corrected below;
+//   * x = y - Q c0, with the first projection's coefficients c0 formed on the
+//     feature side (c0 = G^T v - beta (cp, 1), G = A^T Q; k_gdots) instead of a
+//     pass over Q;
+//   * c1 = Q^T x (the second projection) and |x|^2.
+// The last block forms per sample nrm = sqrt(|x|^2 - |c1|^2) -- the norm of
+// x - Q c1, by Pythagoras, since x is orthogonal to Q up to c1 -- and
+// cp := c1 / nrm, the pending correction of the new basis vector x / nrm.  The
+// vector that becomes the basis column is the CGS2 vector (x - Q c1) / nrm;
+// only where it is materialised moves.  Layout and reductions as k_cgs_df: 8
+// warps, warp w owning columns w + 8t, 64 rows per iteration, per-block FP64
+// partials reduced in block order by the last block.
+template <int NJ>
+__global__ void __launch_bounds__(256) k_cgs_lag(float* __restrict__ Qh, float* __restrict__ Ql,
+                                                 int64_t ld, int ncols, int pend,
+                                                 float* __restrict__ xh, float* __restrict__ xl,
+                                                 const double* __restrict__ y,
+                                                 const BlkRange* __restrict__ blk,
+                                                 const int* __restrict__ seg_blk, int nseg,
+                                                 const int* __restrict__ active,
+                                                 const double* __restrict__ c0, double* __restrict__ cp,
+                                                 double* __restrict__ part, double* __restrict__ npart,
+                                                 double* __restrict__ nrm, unsigned int* __restrict__ counter) {
+  // coefficients as packed pairs (both lanes the same value): hi, -hi, lo
+  __shared__ f2_t ck[MAX_WORK][3], pk[MAX_WORK][3];
+  __shared__ float redh[8][64], redl[8][64], rch[8][64], rcl[8][64];
+  __shared__ float xsh[64], xsl[64], wsh[64], wsl[64];
+  __shared__ double nsh[32];
+  __shared__ bool last;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const BlkRange br = blk[blockIdx.x];
+  const int sg = br.seg;
+  for (int j = tid; j < ncols; j += blockDim.x) {
+    float h, l;
+    df_split(c0[sg * MAX_WORK + j], h, l);
+    ck[j][0] = f2_pack(h, h);
+    ck[j][1] = f2_pack(-h, -h);
+    ck[j][2] = f2_pack(l, l);
+  }
+  for (int j = tid; j < pend; j += blockDim.x) {
+    float h, l;
+    df_split(cp[sg * MAX_WORK + j], h, l);
+    pk[j][0] = f2_pack(h, h);
+    pk[j][1] = f2_pack(-h, -h);
+    pk[j][2] = f2_pack(l, l);
+  }
+  __syncthreads();
+  const int64_t r0 = br.r0, r1 = (active == nullptr || active[sg]) ? br.r1 : br.r0;
+  const int pw = pend >= 0 ? (pend & 7) : -1, pt = pend >= 0 ? (pend >> 3) : -1;
+  // dot accumulators: one packed pair per column, lanes = the thread's two rows
+  f2_t dh[NJ], dl[NJ];
+#pragma unroll
+  for (int t = 0; t < NJ; ++t) dh[t] = dl[t] = 0ull;
+  float nah = 0.f, nal = 0.f;   // |x|^2, double-float
+  for (int64_t i0 = r0; i0 < r1; i0 += 64) {
+    const int64_t ia = i0 + lane, ib = ia + 32;
+    const bool va = ia < r1, vb = ib < r1;
+    // the row of the product this thread finishes below, loaded ahead
+    float yh = 0.f, yl = 0.f;
+    if (tid < 64 && i0 + tid < r1) {
+      if (y) {
+        df_split(y[i0 + tid], yh, yl);
+      } else {
+        yh = xh[i0 + tid];
+        yl = xl[i0 + tid];
+      }
+    }
+    f2_t qh[NJ], ql[NJ];
+#pragma unroll
+    for (int t = 0; t < NJ; ++t) {
+      const int j = w + 8 * t;
+      const int64_t o = (int64_t)j * ld + ia;
+      float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
+      if (j < ncols) {
+        if (va) {
+          a0 = Qh[o];
+          b0 = Ql[o];
+        }
+        if (vb) {
+          a1 = Qh[o + 32];
+          b1 = Ql[o + 32];
+        }
+      }
+      qh[t] = f2_pack(a0, a1);
+      ql[t] = f2_pack(b0, b1);
+    }
+    f2_t sh = 0ull, sl = 0ull;   // Q c0 (but the pending column)
+    f2_t ph = 0ull, pl = 0ull;   // Q[:, :pend] cp
+#pragma unroll
+    for (int t = 0; t < NJ; ++t) {
+      const int j = w + 8 * t;
+      if (j < ncols && j != pend) df_fma2(sh, sl, ck[j][0], ck[j][1], ck[j][2], qh[t], ql[t]);
+      if (j < pend) df_fma2(ph, pl, pk[j][0], pk[j][1], pk[j][2], qh[t], ql[t]);
+      if (t == pt && w == pw) {
+        f2_unpack(qh[t], wsh[lane], wsh[lane + 32]);
+        f2_unpack(ql[t], wsl[lane], wsl[lane + 32]);
+      }
+    }
+    f2_unpack(sh, redh[w][lane], redh[w][lane + 32]);
+    f2_unpack(sl, redl[w][lane], redl[w][lane + 32]);
+    f2_unpack(ph, rch[w][lane], rch[w][lane + 32]);
+    f2_unpack(pl, rcl[w][lane], rcl[w][lane + 32]);
+    __syncthreads();
+    if (tid < 64) {
+      const int64_t i = i0 + tid;
+      float h = 0.f, l = 0.f, wh = 0.f, wl = 0.f;
+      if (i < r1) {
+        float uh = 0.f, ul = 0.f;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) df_acc(uh, ul, redh[u][tid], redl[u][tid]);
+        if (pend >= 0) {
+          float qh2 = 0.f, ql2 = 0.f;
+#pragma unroll
+          for (int u = 0; u < 8; ++u) df_acc(qh2, ql2, rch[u][tid], rcl[u][tid]);
+          wh = wsh[tid];
+          wl = wsl[tid];
+          df_sub(wh, wl, qh2, ql2);
+          Qh[(int64_t)pend * ld + i] = wh;
+          Ql[(int64_t)pend * ld + i] = wl;
+          float c0h, c0l, nc0h;
+          f2_unpack(ck[pend][0], c0h, nc0h);
+          f2_unpack(ck[pend][2], c0l, nc0h);
+          df_fma(uh, ul, wh, wl, c0h, c0l);
+        }
+        h = yh;
+        l = yl;
+        df_sub(h, l, uh, ul);
+        xh[i] = h;
+        xl[i] = l;
+        df_fma(nah, nal, h, l, h, l);
+      }
+      xsh[tid] = h;
+      xsl[tid] = l;
+      wsh[tid] = wh;
+      wsl[tid] = wl;
+    }
+    __syncthreads();
+    const float x0h = xsh[lane], x1h = xsh[lane + 32];
+    const f2_t xh2 = f2_pack(x0h, x1h), nxh2 = f2_pack(-x0h, -x1h), xl2 = f2_pack(xsl[lane], xsl[lane + 32]);
+#pragma unroll
+    for (int t = 0; t < NJ; ++t) {
+      if (t == pt && w == pw) {
+        qh[t] = f2_pack(wsh[lane], wsh[lane + 32]);
+        ql[t] = f2_pack(wsl[lane], wsl[lane + 32]);
+      }
+      if (w + 8 * t < ncols) df_fma2(dh[t], dl[t], xh2, nxh2, xl2, qh[t], ql[t]);
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < NJ; ++t) {
+    const int j = w + 8 * t;
+    if (j < ncols) {
+      // the two rows' sums, then across the warp (double-float, FP32 shuffles)
+      float h, l, h2, l2;
+      f2_unpack(dh[t], h, h2);
+      f2_unpack(dl[t], l, l2);
+      df_acc(h, l, h2, l2);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        float hs = __shfl_xor_sync(0xffffffffu, h, o);
+        float ls = __shfl_xor_sync(0xffffffffu, l, o);
+        float s = h + hs;
+        float v = s - h;
+        float err = (h - (s - v)) + (hs - v);
+        float lo = err + l + ls;
+        h = s + lo;
+        l = lo - (h - s);
+      }
+      if (lane == 0) part[(int64_t)blockIdx.x * ncols + j] = df_val(h, l);
+    }
+  }
+  const double nacc = block_sum(df_val(nah, nal), nsh);
+  if (tid == 0) npart[blockIdx.x] = nacc;
+  if (last_block(counter, &last)) {
+    // c1 per (sample, column), in block order
+    for (int pq = w; pq < nseg * ncols; pq += 8) {
+      const int s2 = pq / ncols, j = pq - s2 * ncols;
+      double sacc = 0;
+      for (int b = seg_blk[s2] + lane; b < seg_blk[s2 + 1]; b += 32) sacc += part[(int64_t)b * ncols + j];
+      sacc = sv_warp_sum(sacc);
+      if (lane == 0) cp[s2 * MAX_WORK + j] = sacc;
+    }
+    __syncthreads();
+    for (int s2 = tid; s2 < nseg; s2 += blockDim.x) {
+      double nsq = 0, csq = 0;
+      for (int b = seg_blk[s2]; b < seg_blk[s2 + 1]; ++b) nsq += npart[b];
+      for (int j = 0; j < ncols; ++j) csq += cp[s2 * MAX_WORK + j] * cp[s2 * MAX_WORK + j];
+      const double r = sqrt(fmax(nsq - csq, 0.0));
+      nrm[s2] = r;
+      const double inv = r > 0 ? 1.0 / r : 0.0;
+      for (int j = 0; j < ncols; ++j) cp[s2 * MAX_WORK + j] *= inv;
+    }
+    if (tid == 0) *counter = 0;
+  }
+}
+
+// ---- the same pass with the basis tiles brought in by the tensor-memory
+// accelerator ---------------------------------------------------------------
+// Per block a ring of LT_STAGES tiles of LT_ROWS rows x ncols columns: one 2D
+// tensor copy per 8-column group and array (hi, lo), box 64 rows x 8 columns,
+// landing column-major ([column][row]) so that a lane reads its two adjacent
+// rows of a column as one packed pair.  A stage is refilled by thread 0 right
+// after the block barrier that follows its last read, so LT_STAGES tiles stay in
+// flight whatever the arithmetic does.  Rows outside the block's range (the
+// 4-row alignment of the copy start) are read but carry x = 0 and are not
+// written; columns at or beyond ncols and rows beyond the basis are filled with
+// zeros by the copy.  Every wait is bounded: on a timeout the block records
+// SV_STATUS_LIMIT, drains its copies (bounded) and contributes nothing.
+// (sh, sl) += (bh, bl) on packed pairs, unnormalised (df_acc per lane)
+__device__ __forceinline__ void df_acc2(f2_t& sh, f2_t& sl, f2_t bh, f2_t bl) {
+  f2_t t = f2_add(sh, bh);
+  f2_t v = f2_sub(t, sh);
+  f2_t err = f2_add(f2_sub(sh, f2_sub(t, v)), f2_sub(bh, v));
+  sh = t;
+  sl = f2_add(sl, f2_add(err, bl));
+}
+// sum of the 8 per-warp partials of row r, as a tree (depth 3)
+__device__ __forceinline__ void df_tree8(const float (*ph)[64], const float (*pl)[64], int r, float& h,
+                                         float& l) {
+  float ah[8], al[8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    ah[u] = ph[u][r];
+    al[u] = pl[u][r];
+  }
+#pragma unroll
+  for (int st = 1; st < 8; st <<= 1)
+#pragma unroll
+    for (int u = 0; u < 8; u += 2 * st) df_acc(ah[u], al[u], ah[u + st], al[u + st]);
+  h = ah[0];
+  l = al[0];
+}
+
+constexpr int LT_ROWS = 64;
+constexpr int LT_STAGES = 3;
+constexpr int LT_GC = 8;
+constexpr long long LT_TIMEOUT = 4000000000ll;   // cycles (~2 s) per wait
+
+__device__ __forceinline__ uint32_t lt_su32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ bool lt_try(unsigned long long* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(lt_su32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool lt_wait(unsigned long long* b, uint32_t parity) {
+  if (lt_try(b, parity)) return true;
+  const long long t0 = clock64();
+  while (!lt_try(b, parity))
+    if (clock64() - t0 > LT_TIMEOUT) return false;
+  return true;
+}
+
+template <int NJ>
+__global__ void __launch_bounds__(256) k_cgs_lag_tma(const __grid_constant__ CUtensorMap mh,
+                                                     const __grid_constant__ CUtensorMap ml,
+                                                     float* __restrict__ Qh, float* __restrict__ Ql,
+                                                     int64_t ld, int ncols, int pend,
+                                                     float* __restrict__ xh, float* __restrict__ xl,
+                                                     const double* __restrict__ y,
+                                                     const BlkRange* __restrict__ blk,
+                                                     const int* __restrict__ seg_blk, int nseg,
+                                                     const int* __restrict__ active,
+                                                     const double* __restrict__ c0, double* __restrict__ cp,
+                                                     double* __restrict__ part, double* __restrict__ npart,
+                                                     double* __restrict__ nrm, unsigned int* __restrict__ counter,
+                                                     int* __restrict__ status) {
+  static_assert(NJ * 8 <= 64 && NJ <= LT_GC, "one 8-column group per warp slot");
+  extern __shared__ unsigned char lt_dyn[];
+  float* tiles = (float*)(((uintptr_t)lt_dyn + 1023) & ~(uintptr_t)1023);
+  __shared__ f2_t ck[MAX_WORK][3], pk[MAX_WORK][3];
+  __shared__ float redh[8][64], redl[8][64], rch[8][64], rcl[8][64];
+  __shared__ float xsh[64], xsl[64], wsh[64], wsl[64];
+  __shared__ double nsh[32];
+  __shared__ unsigned long long full[LT_STAGES];
+  __shared__ int err;
+  __shared__ bool last;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const BlkRange br = blk[blockIdx.x];
+  const int sg = br.seg;
+  for (int j = tid; j < ncols; j += blockDim.x) {
+    float h, l;
+    df_split(c0[sg * MAX_WORK + j], h, l);
+    ck[j][0] = f2_pack(h, h);
+    ck[j][1] = f2_pack(-h, -h);
+    ck[j][2] = f2_pack(l, l);
+  }
+  for (int j = tid; j < pend; j += blockDim.x) {
+    float h, l;
+    df_split(cp[sg * MAX_WORK + j], h, l);
+    pk[j][0] = f2_pack(h, h);
+    pk[j][1] = f2_pack(-h, -h);
+    pk[j][2] = f2_pack(l, l);
+  }
+  const int ngroups = (ncols + LT_GC - 1) / LT_GC;
+  const int gfl = 2 * LT_GC * LT_ROWS;   // floats per group: the hi box, then the lo box
+  const int sfl = ngroups * gfl;         // floats per stage
+  const int64_t r0 = br.r0, r1 = (active == nullptr || active[sg]) ? br.r1 : br.r0;
+  const int64_t xs = r0 & ~(int64_t)3;   // copy start: 16-byte aligned row
+  const int ntiles = r1 > r0 ? (int)((r1 - xs + LT_ROWS - 1) / LT_ROWS) : 0;
+  if (tid == 0) {
+    for (int st = 0; st < LT_STAGES; ++st)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(lt_su32(&full[st])) : "memory");
+    err = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  int issued = 0;   // thread 0: tiles whose copies were issued
+  auto issue = [&](int t) {
+    const int st = t % LT_STAGES;
+    float* dst = tiles + st * sfl;
+    const int x = (int)(xs + (int64_t)t * LT_ROWS);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(lt_su32(&full[st])),
+                 "r"((uint32_t)sfl * 4u)
+                 : "memory");
+    for (int g = 0; g < ngroups; ++g) {
+      asm volatile(
+          "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+              lt_su32(dst + g * gfl)),
+          "l"(&mh), "r"(x), "r"(g * LT_GC), "r"(lt_su32(&full[st]))
+          : "memory");
+      asm volatile(
+          "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+              lt_su32(dst + g * gfl + LT_GC * LT_ROWS)),
+          "l"(&ml), "r"(x), "r"(g * LT_GC), "r"(lt_su32(&full[st]))
+          : "memory");
+    }
+    ++issued;
+  };
+  if (tid == 0)
+    for (int t = 0; t < LT_STAGES && t < ntiles; ++t) issue(t);
+  const int pw = pend >= 0 ? (pend & 7) : -1, pt = pend >= 0 ? (pend >> 3) : -1;
+  f2_t dh[NJ], dl[NJ];
+#pragma unroll
+  for (int t = 0; t < NJ; ++t) dh[t] = dl[t] = 0ull;
+  float nah = 0.f, nal = 0.f;   // |x|^2, double-float
+  int it = 0;
+  for (; it < ntiles; ++it) {
+    const int st = it % LT_STAGES;
+    const int64_t i0 = xs + (int64_t)it * LT_ROWS;
+    float yh = 0.f, yl = 0.f;
+    if (tid < 64) {
+      const int64_t i = i0 + tid;
+      if (i >= r0 && i < r1) {
+        if (y) {
+          df_split(y[i], yh, yl);
+        } else {
+          yh = xh[i];
+          yl = xl[i];
+        }
+      }
+    }
+    if (!lt_wait(&full[st], (uint32_t)((it / LT_STAGES) & 1))) atomicOr(&err, 1);
+    const float* T = tiles + st * sfl + w * LT_ROWS + 2 * lane;
+    f2_t qh[NJ], ql[NJ];
+#pragma unroll
+    for (int t = 0; t < NJ; ++t) {
+      qh[t] = ql[t] = 0ull;
+      if (t < ngroups) {
+        qh[t] = *(const f2_t*)(T + t * gfl);
+        ql[t] = *(const f2_t*)(T + t * gfl + LT_GC * LT_ROWS);
+      }
+    }
+    // two accumulators per sum (even and odd column slots): shorter chains
+    f2_t sh = 0ull, sl = 0ull, ph = 0ull, pl = 0ull;
+    f2_t sh2 = 0ull, sl2 = 0ull, ph2 = 0ull, pl2 = 0ull;
+#pragma unroll
+    for (int t = 0; t < NJ; ++t) {
+      const int j = w + 8 * t;
+      if (j < ncols && j != pend) {
+        if (t & 1) df_fma2(sh2, sl2, ck[j][0], ck[j][1], ck[j][2], qh[t], ql[t]);
+        else df_fma2(sh, sl, ck[j][0], ck[j][1], ck[j][2], qh[t], ql[t]);
+      }
+      if (j < pend) {
+        if (t & 1) df_fma2(ph2, pl2, pk[j][0], pk[j][1], pk[j][2], qh[t], ql[t]);
+        else df_fma2(ph, pl, pk[j][0], pk[j][1], pk[j][2], qh[t], ql[t]);
+      }
+      if (t == pt && w == pw) {
+        f2_unpack(qh[t], wsh[2 * lane], wsh[2 * lane + 1]);
+        f2_unpack(ql[t], wsl[2 * lane], wsl[2 * lane + 1]);
+      }
+    }
+    df_acc2(sh, sl, sh2, sl2);
+    df_acc2(ph, pl, ph2, pl2);
+    f2_unpack(sh, redh[w][2 * lane], redh[w][2 * lane + 1]);
+    f2_unpack(sl, redl[w][2 * lane], redl[w][2 * lane + 1]);
+    f2_unpack(ph, rch[w][2 * lane], rch[w][2 * lane + 1]);
+    f2_unpack(pl, rcl[w][2 * lane], rcl[w][2 * lane + 1]);
+    __syncthreads();
+    if (err) break;
+    // every warp is past its reads of the previous tile's stage: refill it
+    if (tid == 0 && it >= 1 && it - 1 + LT_STAGES < ntiles) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(it - 1 + LT_STAGES);
+    }
+    if (tid < 64) {
+      const int64_t i = i0 + tid;
+      float h = 0.f, l = 0.f, wh = 0.f, wl = 0.f;
+      if (i >= r0 && i < r1) {
+        float uh, ul;
+        df_tree8(redh, redl, tid, uh, ul);
+        if (pend >= 0) {
+          float qh2, ql2;
+          df_tree8(rch, rcl, tid, qh2, ql2);
+          wh = wsh[tid];
+          wl = wsl[tid];
+          df_sub(wh, wl, qh2, ql2);
+          Qh[(int64_t)pend * ld + i] = wh;
+          Ql[(int64_t)pend * ld + i] = wl;
+          float c0h, c0l, dummy;
+          f2_unpack(ck[pend][0], c0h, dummy);
+          f2_unpack(ck[pend][2], c0l, dummy);
+          df_fma(uh, ul, wh, wl, c0h, c0l);
+        }
+        h = yh;
+        l = yl;
+        df_sub(h, l, uh, ul);
+        xh[i] = h;
+        xl[i] = l;
+        df_fma(nah, nal, h, l, h, l);
+      }
+      xsh[tid] = h;
+      xsl[tid] = l;
+      wsh[tid] = wh;
+      wsl[tid] = wl;
+    }
+    __syncthreads();
+    const float x0h = xsh[2 * lane], x1h = xsh[2 * lane + 1];
+    const f2_t xh2 = f2_pack(x0h, x1h), nxh2 = f2_pack(-x0h, -x1h),
+               xl2 = f2_pack(xsl[2 * lane], xsl[2 * lane + 1]);
+#pragma unroll
+    for (int t = 0; t < NJ; ++t) {
+      if (t == pt && w == pw) {
+        qh[t] = f2_pack(wsh[2 * lane], wsh[2 * lane + 1]);
+        ql[t] = f2_pack(wsl[2 * lane], wsl[2 * lane + 1]);
+      }
+      if (w + 8 * t < ncols) df_fma2(dh[t], dl[t], xh2, nxh2, xl2, qh[t], ql[t]);
+    }
+  }
+  if (err) {
+    // a copy did not arrive in time: drain the ones in flight (bounded), report,
+    // and contribute nothing
+    if (tid == 0) {
+      for (int t = it; t < issued; ++t) lt_wait(&full[t % LT_STAGES], (uint32_t)((t / LT_STAGES) & 1));
+      atomicOr(status, SV_STATUS_LIMIT);
+    }
+#pragma unroll
+    for (int t = 0; t < NJ; ++t) dh[t] = dl[t] = 0ull;
+    nah = nal = 0.f;
+  }
+#pragma unroll
+  for (int t = 0; t < NJ; ++t) {
+    const int j = w + 8 * t;
+    if (j < ncols) {
+      float h, l, h2, l2;
+      f2_unpack(dh[t], h, h2);
+      f2_unpack(dl[t], l, l2);
+      df_acc(h, l, h2, l2);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        float hs = __shfl_xor_sync(0xffffffffu, h, o);
+        float ls = __shfl_xor_sync(0xffffffffu, l, o);
+        float s = h + hs;
+        float v = s - h;
+        float e2 = (h - (s - v)) + (hs - v);
+        float lo = e2 + l + ls;
+        h = s + lo;
+        l = lo - (h - s);
+      }
+      if (lane == 0) part[(int64_t)blockIdx.x * ncols + j] = df_val(h, l);
+    }
+  }
+  const double nacc = block_sum(df_val(nah, nal), nsh);
+  if (tid == 0) npart[blockIdx.x] = nacc;
+  if (last_block(counter, &last)) {
+    for (int pq = w; pq < nseg * ncols; pq += 8) {
+      const int s2 = pq / ncols, j = pq - s2 * ncols;
+      double sacc = 0;
+      for (int b = seg_blk[s2] + lane; b < seg_blk[s2 + 1]; b += 32) sacc += part[(int64_t)b * ncols + j];
+      sacc = sv_warp_sum(sacc);
+      if (lane == 0) cp[s2 * MAX_WORK + j] = sacc;
+    }
+    __syncthreads();
+    for (int s2 = tid; s2 < nseg; s2 += blockDim.x) {
+      double nsq = 0, csq = 0;
+      for (int b = seg_blk[s2]; b < seg_blk[s2 + 1]; ++b) nsq += npart[b];
+      for (int j = 0; j < ncols; ++j) csq += cp[s2 * MAX_WORK + j] * cp[s2 * MAX_WORK + j];
+      const double r = sqrt(fmax(nsq - csq, 0.0));
+      nrm[s2] = r;
+      const double inv = r > 0 ? 1.0 / r : 0.0;
+      for (int j = 0; j < ncols; ++j) cp[s2 * MAX_WORK + j] *= inv;
+    }
+    if (tid == 0) *counter = 0;
+  }
+}
+
+// First projection coefficients of a cell-side step from the feature side: the
+// new vector is y = A v - beta w' (w' the stored, not yet corrected column pend;
+// no subtraction when pend < 0), so Q^T y = G^T v - beta Q^T w' with G = A^T Q
+// and Q^T w' = (cp, 1, 0...) (w' = w + Q[:, :pend] cp, w a unit vector
+// orthogonal to Q[:, :pend]).  Block (column l, sample s); FP64 sums over the
+// sample's feature rows.
+__global__ void __launch_bounds__(256) k_gdots(const float* __restrict__ Gh, const float* __restrict__ Gl,
+                                               int64_t ld, const int64_t* __restrict__ off,
+                                               const double* __restrict__ v, int pend,
+                                               const double* __restrict__ beta,
+                                               const double* __restrict__ cp, const int* __restrict__ active,
+                                               double* __restrict__ c0) {
+  __shared__ double sh[32];
+  const int l = blockIdx.x, sg = blockIdx.y;
+  if (active && !active[sg]) return;
+  double acc = 0;
+  for (int64_t i = off[sg] + threadIdx.x; i < off[sg + 1]; i += blockDim.x) {
+    const int64_t o = (int64_t)l * ld + i;
+    acc += df_val(Gh[o], Gl[o]) * v[i];
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) {
+    if (pend >= 0) acc -= beta[sg] * (l < pend ? cp[sg * MAX_WORK + l] : l == pend ? 1.0 : 0.0);
+    c0[sg * MAX_WORK + l] = acc;
+  }
+}
+
+// After the feature-side product of a cell-side column jn, F = A^T w' - alpha v
+// with w' = w + Q[:, :jn] cp not yet corrected: F -= G[:, :jn] cp makes it the
+// product of the corrected w, and G[:, jn] := F + alpha v = A^T w.
+__global__ void __launch_bounds__(256) k_gcol(float* __restrict__ Gh, float* __restrict__ Gl, int64_t ld,
+                                              const BlkRange* __restrict__ blk, const int* __restrict__ active,
+                                              int jn, const double* __restrict__ cp,
+                                              const double* __restrict__ alpha, const double* __restrict__ v,
+                                              double* __restrict__ F) {
+  __shared__ double cs[MAX_WORK];
+  const BlkRange br = blk[blockIdx.x];
+  const int sg = br.seg;
+  if (active && !active[sg]) return;
+  for (int j = threadIdx.x; j < jn; j += blockDim.x) cs[j] = cp[sg * MAX_WORK + j];
+  __syncthreads();
+  const double a = alpha[sg];
+  for (int64_t i = br.r0 + threadIdx.x; i < br.r1; i += blockDim.x) {
+    double corr = 0;
+    for (int j = 0; j < jn; ++j) {
+      const int64_t o = (int64_t)j * ld + i;
+      corr += df_val(Gh[o], Gl[o]) * cs[j];
+    }
+    const double f = F[i] - corr;
+    F[i] = f;
+    df_split(f + a * v[i], Gh[(int64_t)jn * ld + i], Gl[(int64_t)jn * ld + i]);
+  }
+}
+
 // FP64 vector -> double-float working vector
 __global__ void k_to_df(const double* __restrict__ y, int64_t len, float* __restrict__ xh,
                         float* __restrict__ xl) {
@@ -373,11 +987,16 @@ __global__ void k_scal_df(const float* __restrict__ xh, const float* __restrict_
 }
 
 // zero the norm slot (the sub-diagonal scalar the next product uses) of every
-// sample whose breakdown was flagged; separate launch so every k_scal_df block
-// has read it
-__global__ void k_scal_post(double* nrm, const int* flag, int nseg) {
+// sample whose breakdown was flagged, and its pending correction (cp, cell
+// side); separate launch so every k_scal_df block has read it
+__global__ void k_scal_post(double* nrm, const int* flag, int nseg, double* cp) {
   for (int s = threadIdx.x; s < nseg; s += blockDim.x)
-    if (flag[s]) nrm[s] = 0.0;
+    if (flag[s]) {
+      nrm[s] = 0.0;
+      // the replacement vector is orthonormalised in full: nothing pending
+      if (cp)
+        for (int j = 0; j < MAX_WORK; ++j) cp[s * MAX_WORK + j] = 0.0;
+    }
 }
 
 // One block per sample: if flag[s], cur <- CGS2(cur, Q[:, :ncols]) normalised
@@ -622,6 +1241,11 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(const double* __restrict__ 
   __shared__ int rotated;
   __shared__ int order[MAX_WORK];
   __shared__ double nrm[MAX_WORK];
+  // squared column norms (double-float): computed at the start of a sweep and
+  // carried through its rotations by alpha' = alpha - t gamma, beta' = beta +
+  // t gamma (exact for the diagonalising angle); they only steer the angles and
+  // the convergence test -- the singular values come from the final columns
+  __shared__ float cnh[MAX_WORK], cnl[MAX_WORK];
   int tid = threadIdx.x;
   for (int idx = tid; idx < m * m; idx += blockDim.x) {
     int r = idx % m, c = idx / m;
@@ -637,6 +1261,15 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(const double* __restrict__ 
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     if (tid == 0) rotated = 0;
+    for (int c = wid; c < m; c += nw) {
+      float h = 0.f, l = 0.f;
+      for (int r = lane; r < m; r += 32) df_fma(h, l, Ah[c * m + r], Al[c * m + r], Ah[c * m + r], Al[c * m + r]);
+      df_warp_sum(h, l);
+      if (lane == 0) {
+        cnh[c] = h;
+        cnl[c] = l;
+      }
+    }
     __syncthreads();
     for (int round = 0; round < mp - 1; ++round) {
       for (int pi = wid; pi < npairs; pi += nw) {
@@ -648,15 +1281,9 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(const double* __restrict__ 
         float* apl = Al + p * m;
         float* aqh = Ah + q * m;
         float* aql = Al + q * m;
-        float alh = 0.f, all = 0.f, beh = 0.f, bel = 0.f, gah = 0.f, gal = 0.f;
-        for (int r = lane; r < m; r += 32) {
-          float xh = aph[r], xl = apl[r], yh = aqh[r], yl = aql[r];
-          df_fma(alh, all, xh, xl, xh, xl);
-          df_fma(beh, bel, yh, yl, yh, yl);
-          df_fma(gah, gal, xh, xl, yh, yl);
-        }
-        df_warp_sum(alh, all);
-        df_warp_sum(beh, bel);
+        const float alh = cnh[p], all = cnl[p], beh = cnh[q], bel = cnl[q];
+        float gah = 0.f, gal = 0.f;
+        for (int r = lane; r < m; r += 32) df_fma(gah, gal, aph[r], apl[r], aqh[r], aql[r]);
         df_warp_sum(gah, gal);
         // every lane holds the sums; the test and the angle are FP32 (from
         // double-float sums): the angle only steers convergence, while the
@@ -685,7 +1312,16 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(const double* __restrict__ 
             df_rot(aph[r], apl[r], aqh[r], aql[r], ch, cl, sh, sl);
             df_rot(Jh[p * m + r], Jl[p * m + r], Jh[q * m + r], Jl[q * m + r], ch, cl, sh, sl);
           }
-          if (lane == 0) rotated = 1;
+          if (lane == 0) {
+            rotated = 1;
+            float ah2 = alh, al2 = all, bh2 = beh, bl2 = bel;
+            df_fma(ah2, al2, -t, 0.f, gah, gal);
+            df_fma(bh2, bl2, t, 0.f, gah, gal);
+            cnh[p] = ah2;
+            cnl[p] = al2;
+            cnh[q] = bh2;
+            cnl[q] = bl2;
+          }
         }
       }
       __syncthreads();
@@ -741,59 +1377,6 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(const double* __restrict__ 
     ctl[CTL_THRESH] = eps_b * fmax(smax, 1.0);
     ctl[CTL_CYCLE] += 1.0;
   }
-}
-
-// ---- packed double-float arithmetic -----------------------------------------
-// Two independent FP32 lanes per instruction (the f32x2 forms of sm_100 and
-// later): each lane is the IEEE FP32 operation of its scalar counterpart, so a
-// packed sequence gives bit for bit what the same scalar sequence gives for each
-// of the two values, in half the issue slots.
-typedef unsigned long long f2_t;
-__device__ __forceinline__ f2_t f2_pack(float a, float b) {
-  f2_t r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-  return r;
-}
-__device__ __forceinline__ void f2_unpack(f2_t r, float& a, float& b) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
-}
-__device__ __forceinline__ f2_t f2_add(f2_t a, f2_t b) {
-  f2_t d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2_t f2_sub(f2_t a, f2_t b) {
-  f2_t d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b) {
-  f2_t d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c) {
-  f2_t d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-
-// df_fma on two accumulator pairs at once with one shared multiplicand a:
-// ah, nah = -ah and al broadcast to both lanes.  The product is formed negated
-// (pn = -ah*bh, exact negation of the rounded product), which turns df_fma's
-// sh + p and p - v into subtractions without a negation instruction.
-__device__ __forceinline__ void df_fma2(f2_t& sh, f2_t& sl, f2_t ah, f2_t nah, f2_t al, f2_t bh,
-                                        f2_t bl) {
-  f2_t pn = f2_mul(nah, bh);
-  f2_t e = f2_fma(ah, bh, pn);   // ah*bh - p, exact
-  e = f2_fma(ah, bl, e);
-  e = f2_fma(al, bh, e);
-  f2_t t = f2_sub(sh, pn);       // sh + p
-  f2_t v = f2_sub(t, sh);
-  f2_t err = f2_sub(sh, f2_sub(t, v));
-  err = f2_sub(err, f2_add(pn, v));   // + (p - v)
-  sh = t;
-  sl = f2_add(sl, f2_add(err, e));
 }
 
 // Out[:, c] = sum_r In[:, r] * M[r + c*nin] for c < nout (tall x small), In
@@ -1068,6 +1651,8 @@ struct Sched {
 // row-parallel kernels.
 struct Side {
   int64_t len = 0;
+  int64_t ld = 0;                // leading dimension of the bases: len rounded up to 4
+                                 // rows (16-byte column strides for the tensor copies)
   int nseg = 1;
   int64_t max_seg = 0;           // longest sample
   std::vector<int64_t> hoff;     // nseg + 1 row offsets
@@ -1082,14 +1667,15 @@ struct Side {
     hoff = offsets;
     nseg = (int)hoff.size() - 1;
     len = hoff[nseg];
+    ld = (len + 3) & ~(int64_t)3;
     for (int s = 0; s < nseg; ++s) max_seg = std::max(max_seg, hoff[s + 1] - hoff[s]);
     off.alloc(nseg + 1);
     sv_h2d(ctx, off.get(), hoff.data(), (nseg + 1) * 8);
     red.build(ctx, hoff, red_target);
     rows.build(ctx, hoff, rows_target);
     for (int t = 0; t < 2; ++t) {
-      h[t].alloc(len * work);
-      l[t].alloc(len * work);
+      h[t].alloc(ld * work);
+      l[t].alloc(ld * work);
     }
     xh.alloc(len);
     xl.alloc(len);
@@ -1097,8 +1683,8 @@ struct Side {
   }
   float* bh() { return h[set].get(); }
   float* bl() { return l[set].get(); }
-  float* ch(int j) { return bh() + (int64_t)j * len; }
-  float* cl(int j) { return bl() + (int64_t)j * len; }
+  float* ch(int j) { return bh() + (int64_t)j * ld; }
+  float* cl(int j) { return bl() + (int64_t)j * ld; }
   float* th() { return h[1 - set].get(); }
   float* tl() { return l[1 - set].get(); }
   void flip() { set = 1 - set; }
@@ -1129,6 +1715,9 @@ struct Lanczos {
   int nu, work, nseg;
   Side Ws, Vs;
   DevBuf<double> ytmp, F, B, P, Q, sig, summary, scal, part, cvec, Ufin, Vfin;
+  // G = A^T W (feature rows x work, double-float), two sets that follow the
+  // cell-side basis sets through the restart rotations
+  DevBuf<float> gh[2], gl[2];
   DevBuf<unsigned int> counter;
   DevBuf<int> flag, active, finsel;
   double* hsum = nullptr;       // pinned copy of the cycle summaries
@@ -1136,6 +1725,7 @@ struct Lanczos {
   double eps_b = 0;
   int cgs_blocks = RED_BLOCKS;  // resident blocks of the CGS kernels (one wave)
   bool vside_multi = false;     // feature side through the multi-block kernels
+  bool lag_tma = false;         // the cell-side pass with TMA-fed basis tiles
   // graphs of the first cycle and of restart cycles from basis set 0 / set 1
   CycleGraph graphs[3];
 
@@ -1146,10 +1736,18 @@ struct Lanczos {
     m = woff[nseg];
     n = voff[nseg];
     int per_sm = 0;
-    if (work <= 64)
-      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_df<8, true, true, false>, 256, 0));
-    else
-      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_df<12, true, true, false>, 256, 0));
+    // one wave of the cell-side pass (the heaviest of the kernels that share
+    // this schedule): the TMA-fed form up to 64 basis columns
+    lag_tma = work <= 64 && !getenv("SV_NO_LAG_TMA");
+    if (lag_tma) {
+      const size_t dyn = lag_smem(work - 1);
+      SV_CUDA(cudaFuncSetAttribute(k_cgs_lag_tma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_lag_tma<8>, 256, dyn));
+    } else if (work <= 64) {
+      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_lag<8>, 256, 0));
+    } else {
+      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_lag<12>, 256, 0));
+    }
     cgs_blocks = std::max(1, std::min(RED_BLOCKS, per_sm * ctx->num_sms));
     auto red_target = [&](int64_t len) {
       return (int)std::max<int64_t>(1, std::min<int64_t>(cgs_blocks, (len + 63) / 64));
@@ -1178,7 +1776,11 @@ struct Lanczos {
     scal.alloc((size_t)nseg * (2 + 2 * CTL_N));
     int maxblk = std::max(Ws.red.nblk, Vs.red.nblk);
     part.alloc((size_t)maxblk * (work + 1));
-    cvec.alloc((size_t)2 * nseg * MAX_WORK);
+    cvec.alloc((size_t)5 * nseg * MAX_WORK);
+    for (int t = 0; t < 2; ++t) {
+      gh[t].alloc(n * work);
+      gl[t].alloc(n * work);
+    }
     counter.alloc(4);
     flag.alloc(nseg);
     active.alloc(nseg);
@@ -1210,6 +1812,11 @@ struct Lanczos {
   double* sR() { return scal.get() + nseg; }               // V-side norms (beta), per sample
   double* ctl() { return scal.get() + 2 * nseg; }          // cycle control blocks
   double* ctl0() { return scal.get() + 2 * nseg + CTL_N * nseg; }   // start-vector control blocks
+  double* c0v() { return cvec.get() + (size_t)2 * nseg * MAX_WORK; }  // first-projection coefficients
+  double* cpv() { return cvec.get() + (size_t)3 * nseg * MAX_WORK; }  // pending correction, cell side
+  double* scratch() { return cvec.get() + (size_t)4 * nseg * MAX_WORK; }
+  float* Gh() { return gh[Ws.set].get(); }
+  float* Gl() { return gl[Ws.set].get(); }
 
   // working vector <- CGS2(y, basis[:, :ncols]) (y FP64; null: the working
   // vector already holds it); nrm[s] = its norm per sample
@@ -1225,20 +1832,20 @@ struct Lanczos {
     if (ncols == 0) {
       if (y) to_working(s, y);
       sv_launch(ctx, "irlba_upd_norm", k_cgs_df<NJ, true, false, true>, dim3(g), dim3(256), 0,
-                (const float*)s.bh(), (const float*)s.bl(), s.len, 0, s.xh.get(), s.xl.get(),
+                (const float*)s.bh(), (const float*)s.bl(), s.ld, 0, s.xh.get(), s.xl.get(),
                 (const double*)nullptr, bk, sb, nseg, act, (const double*)c1, part.get(), np, c2, nrm,
                 counter.get());
       return;
     }
     sv_launch(ctx, "irlba_dots", k_cgs_df<NJ, false, true, false>, dim3(g), dim3(256), 0,
-              (const float*)s.bh(), (const float*)s.bl(), s.len, ncols, s.xh.get(), s.xl.get(), y, bk, sb,
+              (const float*)s.bh(), (const float*)s.bl(), s.ld, ncols, s.xh.get(), s.xl.get(), y, bk, sb,
               nseg, act, (const double*)nullptr, part.get(), np, c1, (double*)nullptr, counter.get());
     sv_launch(ctx, "irlba_upd_dots", k_cgs_df<NJ, true, true, false>, dim3(g), dim3(256), 0,
-              (const float*)s.bh(), (const float*)s.bl(), s.len, ncols, s.xh.get(), s.xl.get(),
+              (const float*)s.bh(), (const float*)s.bl(), s.ld, ncols, s.xh.get(), s.xl.get(),
               (const double*)nullptr, bk, sb, nseg, act, (const double*)c1, part.get(), np, c2,
               (double*)nullptr, counter.get());
     sv_launch(ctx, "irlba_upd_norm", k_cgs_df<NJ, true, false, true>, dim3(g), dim3(256), 0,
-              (const float*)s.bh(), (const float*)s.bl(), s.len, ncols, s.xh.get(), s.xl.get(),
+              (const float*)s.bh(), (const float*)s.bl(), s.ld, ncols, s.xh.get(), s.xl.get(),
               (const double*)nullptr, bk, sb, nseg, act, (const double*)c2, part.get(), np, c1, nrm,
               counter.get());
   }
@@ -1257,10 +1864,10 @@ struct Lanczos {
               s.cl(j), s.cur.get(), boff >= 0 ? B.get() : (double*)nullptr, boff,
               (int64_t)work * work, flag.get(), (unsigned long long)seed, step);
     sv_launch(ctx, "irlba_scal_post", k_scal_post, dim3(1), dim3(64), 0, nrm, (const int*)flag.get(),
-              nseg);
+              nseg, &s == &Ws ? cpv() : (double*)nullptr);
     sv_launch(ctx, "irlba_fix", k_fix_df, dim3(nseg), dim3(1024), 0, s.cur.get(),
-              (const int64_t*)s.off.get(), (const float*)s.bh(), (const float*)s.bl(), s.len, j, s.bh() + (int64_t)j * s.len,
-              s.bl() + (int64_t)j * s.len, flag.get());
+              (const int64_t*)s.off.get(), (const float*)s.bh(), (const float*)s.bl(), s.ld, j, s.ch(j),
+              s.cl(j), flag.get());
   }
 
   // the feature-side step: one block per sample (k_vside), or the multi-block
@@ -1273,7 +1880,7 @@ struct Lanczos {
       return;
     }
     sv_launch(ctx, "irlba_vside", k_vside, dim3(nseg), dim3(1024), 0, (const double*)F.get(),
-              (const int64_t*)Vs.off.get(), Vs.len, Vs.bh(), Vs.bl(), ncols, write_col, nrm, c,
+              (const int64_t*)Vs.off.get(), Vs.ld, Vs.bh(), Vs.bl(), ncols, write_col, nrm, c,
               boff >= 0 ? B.get() : (double*)nullptr, boff, (int64_t)work * work, Vs.cur.get(),
               Vs.xh.get(), Vs.xl.get(), (const int*)active.get(), (unsigned long long)seed, step);
   }
@@ -1286,6 +1893,12 @@ struct Lanczos {
   // out = basis * M_s[:, :nout] per sample: into the other basis set (outd null)
   // or FP64 outd (ld = the side's length); only the samples with sel[s] != 0
   void rotate(Side& s, const double* M, int nout, double* outd, const int* sel) {
+    // into the other basis set (leading dimension ld) or FP64 outd (len)
+    rotate_raw(s.bh(), s.bl(), s.ld, s.rows, M, nout, outd ? (float*)nullptr : s.th(),
+               outd ? (float*)nullptr : s.tl(), outd, outd ? s.len : s.ld, sel);
+  }
+  void rotate_raw(const float* inh, const float* inl, int64_t ld_in, const Sched& rows, const double* M,
+                  int nout, float* outh, float* outl, double* outd, int64_t ld_out, const int* sel) {
     // columns per pass: the fewest padded columns, then the fewest passes (at
     // 50 columns 10 per pass measured 1.65 ms per cell-side rotation at the
     // atlas size, 16 and 26 per pass 1.96 and 1.94 ms)
@@ -1295,11 +1908,78 @@ struct Lanczos {
     auto kern = kb == 26 ? k_rotate_df<26> : kb == 16 ? k_rotate_df<16> : k_rotate_df<10>;
     int npass = (nout + kb - 1) / kb;
     // a short side (the features) spreads the passes of its rows over blocks
-    int gy = s.rows.nblk < ctx->num_sms ? npass : 1;
-    sv_launch(ctx, "irlba_rotate", kern, dim3(s.rows.nblk, gy), dim3(256),
-              (size_t)work * npass * (kb / 2) * 16, (const float*)s.bh(), (const float*)s.bl(), s.len,
-              (const BlkRange*)s.rows.blk.get(), sel, work, M, (int64_t)work * work, nout,
-              outd ? (float*)nullptr : s.th(), outd ? (float*)nullptr : s.tl(), outd, s.len);
+    int gy = rows.nblk < ctx->num_sms ? npass : 1;
+    sv_launch(ctx, "irlba_rotate", kern, dim3(rows.nblk, gy), dim3(256),
+              (size_t)work * npass * (kb / 2) * 16, inh, inl, ld_in, (const BlkRange*)rows.blk.get(), sel,
+              work, M, (int64_t)work * work, nout, outh, outl, outd, ld_out);
+  }
+
+  // The cell-side CGS2 step of column jn in one pass over the basis (k_cgs_lag):
+  // first-projection coefficients from G (k_gdots), the pending column pend
+  // (the previous step's, or -1) corrected on the way; y: the FP64 product, or
+  // null when the product is in the working vector.  s0 = the norm per sample,
+  // cp = the new column's pending correction.
+  template <int NJ>
+  void w_step_nj(int jn, int pend, const double* y) {
+    const int g = Ws.red.nblk;
+    sv_launch(ctx, "irlba_gdots", k_gdots, dim3(jn, nseg), dim3(256), 0, (const float*)Gh(),
+              (const float*)Gl(), n, (const int64_t*)Vs.off.get(), (const double*)Vs.cur.get(), pend,
+              (const double*)sR(), (const double*)cpv(), (const int*)active.get(), c0v());
+    if (NJ == 8 && lag_tma) {
+      // the basis columns 0..jn-1 as two 2D tensors (rows x jn columns, 16-byte
+      // column stride), boxes of 64 rows x 8 columns
+      CUtensorMap mh, ml;
+      cuuint64_t gdim[2] = {(cuuint64_t)Ws.len, (cuuint64_t)jn};
+      cuuint64_t gstride[1] = {(cuuint64_t)Ws.ld * 4};
+      cuuint32_t box[2] = {(cuuint32_t)LT_ROWS, (cuuint32_t)LT_GC};
+      cuuint32_t estr[2] = {1, 1};
+      for (int a = 0; a < 2; ++a) {
+        CUresult r = sv_encode_tiled()(a ? &ml : &mh, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, a ? Ws.bl() : Ws.bh(),
+                                       gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) sv_throw(SV_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+      }
+      sv_launch(ctx, "irlba_cgs_lag", k_cgs_lag_tma<8>, dim3(g), dim3(256), lag_smem(jn), mh, ml, Ws.bh(),
+                Ws.bl(), Ws.ld, jn, pend, Ws.xh.get(), Ws.xl.get(), y, (const BlkRange*)Ws.red.blk.get(),
+                (const int*)Ws.red.seg_blk.get(), nseg, (const int*)active.get(), (const double*)c0v(),
+                cpv(), part.get(), part.get() + (size_t)g * work, sS(), counter.get(), ctx->d_status);
+      return;
+    }
+    sv_launch(ctx, "irlba_cgs_lag", k_cgs_lag<NJ>, dim3(g), dim3(256), 0, Ws.bh(), Ws.bl(), Ws.ld, jn,
+              pend, Ws.xh.get(), Ws.xl.get(), y, (const BlkRange*)Ws.red.blk.get(),
+              (const int*)Ws.red.seg_blk.get(), nseg, (const int*)active.get(), (const double*)c0v(),
+              cpv(), part.get(), part.get() + (size_t)g * work, sS(), counter.get());
+  }
+  void w_step(int jn, int pend, const double* y) {
+    if (work <= 64) w_step_nj<8>(jn, pend, y);
+    else w_step_nj<12>(jn, pend, y);
+  }
+  // dynamic shared memory of the TMA pass over ncols columns (the ring + 1 KB
+  // alignment slack)
+  static size_t lag_smem(int ncols) {
+    return (size_t)LT_STAGES * ((ncols + LT_GC - 1) / LT_GC) * 2 * LT_GC * LT_ROWS * 4 + 1024;
+  }
+  // F = A^T w' - alpha v of cell-side column jn: corrected for the pending
+  // part of w', and G[:, jn] = A^T w
+  void g_col(int jn) {
+    sv_launch(ctx, "irlba_gcol", k_gcol, dim3(Vs.rows.nblk), dim3(256), 0, Gh(), Gl(), n,
+              (const BlkRange*)Vs.rows.blk.get(), (const int*)active.get(), jn, (const double*)cpv(),
+              (const double*)sS(), (const double*)Vs.cur.get(), F.get());
+  }
+  // the pending correction of the last cell-side column, applied in place
+  template <int NJ>
+  void w_settle_nj(int col) {
+    const int g = Ws.red.nblk;
+    sv_launch(ctx, "irlba_settle", k_cgs_df<NJ, true, false, true>, dim3(g), dim3(256), 0,
+              (const float*)Ws.bh(), (const float*)Ws.bl(), Ws.ld, col, Ws.ch(col), Ws.cl(col),
+              (const double*)nullptr, (const BlkRange*)Ws.red.blk.get(), (const int*)Ws.red.seg_blk.get(),
+              nseg, (const int*)active.get(), (const double*)cpv(), part.get(),
+              part.get() + (size_t)g * work, scratch(), scratch(), counter.get());
+  }
+  void w_settle(int col) {
+    if (work <= 64) w_settle_nj<8>(col);
+    else w_settle_nj<12>(col);
   }
 
   // One cycle, enqueued on the context stream without any host round trip:
@@ -1316,6 +1996,9 @@ struct Lanczos {
     if (restart) {
       rotate(Vs, Q.get(), k, nullptr, act);
       rotate(Ws, P.get(), k, nullptr, act);
+      // G follows W: A^T (W P) = G P
+      rotate_raw(Gh(), Gl(), n, Vs.rows, P.get(), k, gh[1 - Ws.set].get(), gl[1 - Ws.set].get(), nullptr, n,
+                 act);
       Vs.flip();
       Ws.flip();
       df_residual_to_fp64();
@@ -1326,28 +2009,35 @@ struct Lanczos {
     }
     unsigned step = 1;
     int j = k;
-    // W[:, j] = A V[:, j]; CGS2 against W[:, :j]
+    // W[:, j] = A V[:, j]; CGS2 against W[:, :j] (the first column of a run:
+    // its norm only)
+    bool pending = false;
     if (op->N_df(Vs.ch(j), Vs.cl(j), Ws.xh.get(), Ws.xl.get(), nullptr, nullptr, nullptr)) {
-      orth_norm(Ws, nullptr, j, s0);
+      if (j == 0) orth_norm(Ws, nullptr, 0, s0);
+      else w_step(j, -1, nullptr);
     } else {
       op->N(Vs.cur.get(), ytmp.get(), nullptr, nullptr);
-      orth_norm(Ws, ytmp.get(), j, s0);
+      if (j == 0) orth_norm(Ws, ytmp.get(), 0, s0);
+      else w_step(j, -1, ytmp.get());
     }
+    pending = j > 0;
     nmv++;
     scal_fix(Ws, j, s0, c, (int64_t)j * work + j, seed, step++);
     while (true) {
       // F = A^T W[:, j] - S V[:, j]; CGS2 against V[:, :j+1]
       op->T(Ws.cur.get(), F.get(), s0, Vs.cur.get());
       nmv++;
+      g_col(j);
       if (j + 1 < work) {
         vside(j + 1, j + 1, s1, c, (int64_t)j * work + j + 1, seed, step++);
         // W[:, j+1] = A V[:, j+1] - R W[:, j]
         if (op->N_df(Vs.ch(j + 1), Vs.cl(j + 1), Ws.xh.get(), Ws.xl.get(), s1, Ws.ch(j), Ws.cl(j))) {
-          orth_norm(Ws, nullptr, j + 1, s0);
+          w_step(j + 1, j, nullptr);
         } else {
           op->N(Vs.cur.get(), ytmp.get(), s1, Ws.cur.get());
-          orth_norm(Ws, ytmp.get(), j + 1, s0);
+          w_step(j + 1, j, ytmp.get());
         }
+        pending = true;
         nmv++;
         scal_fix(Ws, j + 1, s0, c, (int64_t)(j + 1) * work + j + 1, seed, step++);
         ++j;
@@ -1356,6 +2046,9 @@ struct Lanczos {
         break;
       }
     }
+    // the last cell-side column's second projection: W is complete for the
+    // restart rotation and the final U
+    if (pending) w_settle(j);
     sv_launch(ctx, "irlba_svd", k_jacobi_svd, dim3(nseg), dim3(1024), (size_t)4 * work * work * 4,
               (const double*)B.get(), work, P.get(), sig.get(), Q.get(), summary.get(),
               (const double*)s1, 60, ctx->d_status, ctl(), eps_b, act);

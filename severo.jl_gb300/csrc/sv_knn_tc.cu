@@ -676,24 +676,6 @@ __global__ void k_cand_unperm(const int32_t* __restrict__ cs, const int* __restr
   }
 }
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
-                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
-                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    SV_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
-    if (q != cudaDriverEntryPointSuccess || !p)
-      sv_throw(SV_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available from the driver");
-    fn = (EncodeTiledFn)p;
-  }
-  return fn;
-}
-
 }  // namespace
 
 int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unused, int64_t n, int dp,
@@ -775,11 +757,11 @@ int sv_knn_tc_candidates(sv_context* ctx, const float* X32, const float* sq_unus
     cuuint32_t boxA[2] = {(cuuint32_t)BK, (cuuint32_t)BM};
     cuuint32_t boxB[2] = {(cuuint32_t)BK, (cuuint32_t)BN};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = encode_fn()(&tmapA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, Xq.get(), gdim, gstride,
+    CUresult r = sv_encode_tiled()(&tmapA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, Xq.get(), gdim, gstride,
                              boxA, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) sv_throw(SV_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
-    r = encode_fn()(&tmapB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, fold ? Xp.get() : Xq.get(), gdim,
+    r = sv_encode_tiled()(&tmapB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, fold ? Xp.get() : Xq.get(), gdim,
                     gstride, boxB, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) sv_throw(SV_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
