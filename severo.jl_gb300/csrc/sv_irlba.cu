@@ -14,7 +14,15 @@
 // the norms and the small matrix B are FP64; the SVD of B is double-float.
 //
 // Every new vector is reorthogonalised against its basis by classical
-// Gram-Schmidt applied twice (CGS2).  After `work` steps B (work x work, upper
+// Gram-Schmidt applied twice (CGS2).  On the cell side (the long one) both
+// projections share one pass over the basis per step: the first projection's
+// coefficients Q^T (A v) = G^T v come from G = A^T W, kept on the feature side
+// from the feature-side products (and rotated with W at a restart); the second
+// projection of a step's vector is applied, in place, during the next step's
+// pass, which reads the basis anyway, and the products that used the vector in
+// between are corrected through G (see k_cgs_lag).  The vector each step adds
+// is the CGS2 vector; the pass count drops from three to one.  The feature side
+// (a few thousand rows) runs CGS2 directly.  After `work` steps B (work x work, upper
 // triangular) is decomposed by a one-block one-sided Jacobi SVD; the nu
 // leading Ritz vectors are kept (thick restart):
 //   V <- [V Q_k, f/|f|],  W <- W P_k,  B <- [diag(s_k) rho; 0 ...],
@@ -559,16 +567,13 @@ __global__ void __launch_bounds__(256) k_cgs_lag(float* __restrict__ Qh, float* 
 
 // ---- the same pass with the basis tiles brought in by the tensor-memory
 // accelerator ---------------------------------------------------------------
-// Per block a ring of LT_STAGES tiles of LT_ROWS rows x ncols columns: one 2D
-// tensor copy per 8-column group and array (hi, lo), box 64 rows x 8 columns,
-// landing column-major ([column][row]) so that a lane reads its two adjacent
-// rows of a column as one packed pair.  A stage is refilled by thread 0 right
-// after the block barrier that follows its last read, so LT_STAGES tiles stay in
-// flight whatever the arithmetic does.  Rows outside the block's range (the
-// 4-row alignment of the copy start) are read but carry x = 0 and are not
-// written; columns at or beyond ncols and rows beyond the basis are filled with
-// zeros by the copy.  Every wait is bounded: on a timeout the block records
-// SV_STATUS_LIMIT, drains its copies (bounded) and contributes nothing.
+// The basis columns 0..ncols-1 are two 2D tensors (rows x ncols, hi and lo);
+// one tensor copy per 8-column group and array lands a box of rows x 8 columns
+// column-major ([column][row]).  Rows outside the block's range (the 4-row
+// alignment of the copy start) are read but carry x = 0 and are not written;
+// columns at or beyond ncols and rows beyond the basis are filled with zeros
+// by the copy.  Every wait is bounded: on a timeout the block records
+// SV_STATUS_LIMIT, lets its copies land (bounded) and contributes nothing.
 // (sh, sl) += (bh, bl) on packed pairs, unnormalised (df_acc per lane)
 __device__ __forceinline__ void df_acc2(f2_t& sh, f2_t& sl, f2_t bh, f2_t bl) {
   f2_t t = f2_add(sh, bh);
@@ -577,26 +582,7 @@ __device__ __forceinline__ void df_acc2(f2_t& sh, f2_t& sl, f2_t bh, f2_t bl) {
   sh = t;
   sl = f2_add(sl, f2_add(err, bl));
 }
-// sum of the 8 per-warp partials of row r, as a tree (depth 3)
-__device__ __forceinline__ void df_tree8(const float (*ph)[64], const float (*pl)[64], int r, float& h,
-                                         float& l) {
-  float ah[8], al[8];
-#pragma unroll
-  for (int u = 0; u < 8; ++u) {
-    ah[u] = ph[u][r];
-    al[u] = pl[u][r];
-  }
-#pragma unroll
-  for (int st = 1; st < 8; st <<= 1)
-#pragma unroll
-    for (int u = 0; u < 8; u += 2 * st) df_acc(ah[u], al[u], ah[u + st], al[u + st]);
-  h = ah[0];
-  l = al[0];
-}
-
-constexpr int LT_ROWS = 64;
-constexpr int LT_STAGES = 3;
-constexpr int LT_GC = 8;
+constexpr int LT_GC = 8;   // columns per tensor box
 constexpr long long LT_TIMEOUT = 4000000000ll;   // cycles (~2 s) per wait
 
 __device__ __forceinline__ uint32_t lt_su32(const void* p) {
@@ -620,97 +606,127 @@ __device__ __forceinline__ bool lt_wait(unsigned long long* b, uint32_t parity) 
   return true;
 }
 
-template <int NJ>
-__global__ void __launch_bounds__(256) k_cgs_lag_tma(const __grid_constant__ CUtensorMap mh,
-                                                     const __grid_constant__ CUtensorMap ml,
-                                                     float* __restrict__ Qh, float* __restrict__ Ql,
-                                                     int64_t ld, int ncols, int pend,
-                                                     float* __restrict__ xh, float* __restrict__ xl,
-                                                     const double* __restrict__ y,
-                                                     const BlkRange* __restrict__ blk,
-                                                     const int* __restrict__ seg_blk, int nseg,
-                                                     const int* __restrict__ active,
-                                                     const double* __restrict__ c0, double* __restrict__ cp,
-                                                     double* __restrict__ part, double* __restrict__ npart,
-                                                     double* __restrict__ nrm, unsigned int* __restrict__ counter,
-                                                     int* __restrict__ status) {
-  static_assert(NJ * 8 <= 64 && NJ <= LT_GC, "one 8-column group per warp slot");
+// The TMA-fed pass.  Eight compute warps in two groups of four and one copy
+// warp per block; a tile is 128 rows (32 per warp of a group) x ncols columns;
+// the groups take alternate tiles from a ring of NST stages, which the copy warp
+// refills as soon as the four warps of the consuming group have released a
+// stage (empty barriers).  No block barrier in the main loop:
+//   phase 1, lane = row: the lane sums Q c0 and Q[:, :pend] cp over every column
+//     of its row (column pairs in packed double-float), corrects the pending
+//     column (global and in the tile) and forms x;
+//   phase 2, lane = column pair: the lane walks the warp's 32 rows diagonally
+//     (row (lane + k) mod 32, so that the 32 lanes read 32 different banks) and
+//     accumulates its two dot products in registers across all tiles.
+// Per-warp dot products are combined per block in fixed warp order.
+constexpr int LR_GROUP = 4;                 // compute warps per tile
+constexpr int LR_WARPS = 2 * LR_GROUP;      // compute warps per block
+constexpr int LR_ROWS = 32 * LR_GROUP;      // rows per tile
+constexpr int LR_STAGES = 3;
+
+template <int NST>
+__global__ void __launch_bounds__(32 * (LR_WARPS + 1)) k_cgs_lag_tma(
+    const __grid_constant__ CUtensorMap mh, const __grid_constant__ CUtensorMap ml, float* __restrict__ Qh,
+    float* __restrict__ Ql, int64_t ld, int ncols, int pend, float* __restrict__ xh, float* __restrict__ xl,
+    const double* __restrict__ y, const BlkRange* __restrict__ blk, const int* __restrict__ seg_blk, int nseg,
+    const int* __restrict__ active, const double* __restrict__ c0, double* __restrict__ cp,
+    double* __restrict__ part, double* __restrict__ npart, double* __restrict__ nrm,
+    unsigned int* __restrict__ counter, int* __restrict__ status) {
   extern __shared__ unsigned char lt_dyn[];
   float* tiles = (float*)(((uintptr_t)lt_dyn + 1023) & ~(uintptr_t)1023);
-  __shared__ f2_t ck[MAX_WORK][3], pk[MAX_WORK][3];
-  __shared__ float redh[8][64], redl[8][64], rch[8][64], rcl[8][64];
-  __shared__ float xsh[64], xsl[64], wsh[64], wsl[64];
+  // coefficients of the column pairs (2q, 2q+1), packed: hi, -hi, lo
+  __shared__ f2_t ck[MAX_WORK / 2][3], pk[MAX_WORK / 2][3];
+  __shared__ float c0p[2];   // c0 of the pending column (hi, lo)
+  __shared__ float xsh[LR_WARPS][32], xsl[LR_WARPS][32];
+  __shared__ double wred[LR_WARPS][MAX_WORK];
   __shared__ double nsh[32];
-  __shared__ unsigned long long full[LT_STAGES];
+  __shared__ unsigned long long full[NST], empty[NST];
   __shared__ int err;
   __shared__ bool last;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const BlkRange br = blk[blockIdx.x];
   const int sg = br.seg;
-  for (int j = tid; j < ncols; j += blockDim.x) {
-    float h, l;
-    df_split(c0[sg * MAX_WORK + j], h, l);
-    ck[j][0] = f2_pack(h, h);
-    ck[j][1] = f2_pack(-h, -h);
-    ck[j][2] = f2_pack(l, l);
+  const int npairs = (ncols + 1) >> 1;
+  for (int q = tid; q < npairs; q += blockDim.x) {
+    float h[2], l[2], ph[2], pl[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int j = 2 * q + u;
+      h[u] = l[u] = ph[u] = pl[u] = 0.f;
+      // the pending column enters corrected, separately
+      if (j < ncols && j != pend) df_split(c0[sg * MAX_WORK + j], h[u], l[u]);
+      if (j < pend) df_split(cp[sg * MAX_WORK + j], ph[u], pl[u]);
+    }
+    ck[q][0] = f2_pack(h[0], h[1]);
+    ck[q][1] = f2_pack(-h[0], -h[1]);
+    ck[q][2] = f2_pack(l[0], l[1]);
+    pk[q][0] = f2_pack(ph[0], ph[1]);
+    pk[q][1] = f2_pack(-ph[0], -ph[1]);
+    pk[q][2] = f2_pack(pl[0], pl[1]);
   }
-  for (int j = tid; j < pend; j += blockDim.x) {
-    float h, l;
-    df_split(cp[sg * MAX_WORK + j], h, l);
-    pk[j][0] = f2_pack(h, h);
-    pk[j][1] = f2_pack(-h, -h);
-    pk[j][2] = f2_pack(l, l);
+  if (tid == 0) {
+    c0p[0] = c0p[1] = 0.f;
+    if (pend >= 0) df_split(c0[sg * MAX_WORK + pend], c0p[0], c0p[1]);
   }
   const int ngroups = (ncols + LT_GC - 1) / LT_GC;
-  const int gfl = 2 * LT_GC * LT_ROWS;   // floats per group: the hi box, then the lo box
-  const int sfl = ngroups * gfl;         // floats per stage
+  const int gfl = 2 * LT_GC * LR_ROWS;   // floats per column group: the hi box, then the lo box
+  const int sfl = ngroups * gfl;
   const int64_t r0 = br.r0, r1 = (active == nullptr || active[sg]) ? br.r1 : br.r0;
-  const int64_t xs = r0 & ~(int64_t)3;   // copy start: 16-byte aligned row
-  const int ntiles = r1 > r0 ? (int)((r1 - xs + LT_ROWS - 1) / LT_ROWS) : 0;
+  const int64_t xs = r0 & ~(int64_t)3;
+  const int ntiles = r1 > r0 ? (int)((r1 - xs + LR_ROWS - 1) / LR_ROWS) : 0;
   if (tid == 0) {
-    for (int st = 0; st < LT_STAGES; ++st)
+    for (int st = 0; st < NST; ++st) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(lt_su32(&full[st])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(lt_su32(&empty[st])), "r"(LR_GROUP)
+                   : "memory");
+    }
     err = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  int issued = 0;   // thread 0: tiles whose copies were issued
-  auto issue = [&](int t) {
-    const int st = t % LT_STAGES;
-    float* dst = tiles + st * sfl;
-    const int x = (int)(xs + (int64_t)t * LT_ROWS);
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(lt_su32(&full[st])),
-                 "r"((uint32_t)sfl * 4u)
-                 : "memory");
-    for (int g = 0; g < ngroups; ++g) {
-      asm volatile(
-          "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-              lt_su32(dst + g * gfl)),
-          "l"(&mh), "r"(x), "r"(g * LT_GC), "r"(lt_su32(&full[st]))
-          : "memory");
-      asm volatile(
-          "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-              lt_su32(dst + g * gfl + LT_GC * LT_ROWS)),
-          "l"(&ml), "r"(x), "r"(g * LT_GC), "r"(lt_su32(&full[st]))
-          : "memory");
+  float nah = 0.f, nal = 0.f;
+  if (w == LR_WARPS) {
+    // the copy warp
+    if (lane == 0) {
+      int t = 0;
+      for (; t < ntiles; ++t) {
+        const int st = t % NST;
+        if (t >= NST && !lt_wait(&empty[st], (uint32_t)(((t / NST) - 1) & 1))) {
+          atomicOr(&err, 1);
+          break;
+        }
+        float* dst = tiles + st * sfl;
+        const int x = (int)(xs + (int64_t)t * LR_ROWS);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(lt_su32(&full[st])),
+                     "r"((uint32_t)sfl * 4u)
+                     : "memory");
+        for (int g = 0; g < ngroups; ++g) {
+          asm volatile(
+              "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+                  lt_su32(dst + g * gfl)),
+              "l"(&mh), "r"(x), "r"(g * LT_GC), "r"(lt_su32(&full[st]))
+              : "memory");
+          asm volatile(
+              "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+                  lt_su32(dst + g * gfl + LT_GC * LR_ROWS)),
+              "l"(&ml), "r"(x), "r"(g * LT_GC), "r"(lt_su32(&full[st]))
+              : "memory");
+        }
+      }
+      // the copies in flight land before the block moves on (bounded)
+      for (int u = t - NST; u < t; ++u)
+        if (u >= 0) lt_wait(&full[u % NST], (uint32_t)((u / NST) & 1));
     }
-    ++issued;
-  };
-  if (tid == 0)
-    for (int t = 0; t < LT_STAGES && t < ntiles; ++t) issue(t);
-  const int pw = pend >= 0 ? (pend & 7) : -1, pt = pend >= 0 ? (pend >> 3) : -1;
-  f2_t dh[NJ], dl[NJ];
-#pragma unroll
-  for (int t = 0; t < NJ; ++t) dh[t] = dl[t] = 0ull;
-  float nah = 0.f, nal = 0.f;   // |x|^2, double-float
-  int it = 0;
-  for (; it < ntiles; ++it) {
-    const int st = it % LT_STAGES;
-    const int64_t i0 = xs + (int64_t)it * LT_ROWS;
+    __syncwarp();
+  } else {
+    const int grp = w / LR_GROUP, wi = w % LR_GROUP;
+    const int rl = 32 * wi + lane;   // the lane's row within a tile
+    // the lane's column pair, four accumulators (row k mod 4)
+    f2_t dh = 0ull, dl = 0ull, dh2 = 0ull, dl2 = 0ull, dh3 = 0ull, dl3 = 0ull, dh4 = 0ull, dl4 = 0ull;
     float yh = 0.f, yl = 0.f;
-    if (tid < 64) {
-      const int64_t i = i0 + tid;
-      if (i >= r0 && i < r1) {
+    auto load_y = [&](int t) {
+      const int64_t i = xs + (int64_t)t * LR_ROWS + rl;
+      yh = yl = 0.f;
+      if (t < ntiles && i >= r0 && i < r1) {
         if (y) {
           df_split(y[i], yh, yl);
         } else {
@@ -718,131 +734,118 @@ __global__ void __launch_bounds__(256) k_cgs_lag_tma(const __grid_constant__ CUt
           yl = xl[i];
         }
       }
-    }
-    if (!lt_wait(&full[st], (uint32_t)((it / LT_STAGES) & 1))) atomicOr(&err, 1);
-    const float* T = tiles + st * sfl + w * LT_ROWS + 2 * lane;
-    f2_t qh[NJ], ql[NJ];
-#pragma unroll
-    for (int t = 0; t < NJ; ++t) {
-      qh[t] = ql[t] = 0ull;
-      if (t < ngroups) {
-        qh[t] = *(const f2_t*)(T + t * gfl);
-        ql[t] = *(const f2_t*)(T + t * gfl + LT_GC * LT_ROWS);
+    };
+    load_y(grp);
+    for (int t = grp; t < ntiles; t += 2) {
+      const int st = t % NST;
+      const int64_t i = xs + (int64_t)t * LR_ROWS + rl;
+      const bool valid = i >= r0 && i < r1;
+      const float cyh = yh, cyl = yl;
+      load_y(t + 2);
+      if (!lt_wait(&full[st], (uint32_t)((t / NST) & 1))) {
+        atomicOr(&err, 1);
+        break;
       }
-    }
-    // two accumulators per sum (even and odd column slots): shorter chains
-    f2_t sh = 0ull, sl = 0ull, ph = 0ull, pl = 0ull;
-    f2_t sh2 = 0ull, sl2 = 0ull, ph2 = 0ull, pl2 = 0ull;
-#pragma unroll
-    for (int t = 0; t < NJ; ++t) {
-      const int j = w + 8 * t;
-      if (j < ncols && j != pend) {
-        if (t & 1) df_fma2(sh2, sl2, ck[j][0], ck[j][1], ck[j][2], qh[t], ql[t]);
-        else df_fma2(sh, sl, ck[j][0], ck[j][1], ck[j][2], qh[t], ql[t]);
+      float* T = tiles + st * sfl;
+      // phase 1: the lane's row (two accumulators per sum: even and odd pairs)
+      f2_t uh = 0ull, ul = 0ull, ph = 0ull, pl = 0ull;
+      f2_t uh2 = 0ull, ul2 = 0ull, ph2 = 0ull, pl2 = 0ull;
+      for (int q = 0; q < npairs; ++q) {
+        const int c = 2 * q;
+        const float* ch = T + (c >> 3) * gfl + (c & 7) * LR_ROWS + rl;
+        const f2_t qh = f2_pack(ch[0], ch[LR_ROWS]);
+        const f2_t ql = f2_pack(ch[LT_GC * LR_ROWS], ch[LT_GC * LR_ROWS + LR_ROWS]);
+        if (q & 1) {
+          df_fma2(uh2, ul2, ck[q][0], ck[q][1], ck[q][2], qh, ql);
+          if (c < pend) df_fma2(ph2, pl2, pk[q][0], pk[q][1], pk[q][2], qh, ql);
+        } else {
+          df_fma2(uh, ul, ck[q][0], ck[q][1], ck[q][2], qh, ql);
+          if (c < pend) df_fma2(ph, pl, pk[q][0], pk[q][1], pk[q][2], qh, ql);
+        }
       }
-      if (j < pend) {
-        if (t & 1) df_fma2(ph2, pl2, pk[j][0], pk[j][1], pk[j][2], qh[t], ql[t]);
-        else df_fma2(ph, pl, pk[j][0], pk[j][1], pk[j][2], qh[t], ql[t]);
-      }
-      if (t == pt && w == pw) {
-        f2_unpack(qh[t], wsh[2 * lane], wsh[2 * lane + 1]);
-        f2_unpack(ql[t], wsl[2 * lane], wsl[2 * lane + 1]);
-      }
-    }
-    df_acc2(sh, sl, sh2, sl2);
-    df_acc2(ph, pl, ph2, pl2);
-    f2_unpack(sh, redh[w][2 * lane], redh[w][2 * lane + 1]);
-    f2_unpack(sl, redl[w][2 * lane], redl[w][2 * lane + 1]);
-    f2_unpack(ph, rch[w][2 * lane], rch[w][2 * lane + 1]);
-    f2_unpack(pl, rcl[w][2 * lane], rcl[w][2 * lane + 1]);
-    __syncthreads();
-    if (err) break;
-    // every warp is past its reads of the previous tile's stage: refill it
-    if (tid == 0 && it >= 1 && it - 1 + LT_STAGES < ntiles) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue(it - 1 + LT_STAGES);
-    }
-    if (tid < 64) {
-      const int64_t i = i0 + tid;
-      float h = 0.f, l = 0.f, wh = 0.f, wl = 0.f;
-      if (i >= r0 && i < r1) {
-        float uh, ul;
-        df_tree8(redh, redl, tid, uh, ul);
-        if (pend >= 0) {
-          float qh2, ql2;
-          df_tree8(rch, rcl, tid, qh2, ql2);
-          wh = wsh[tid];
-          wl = wsl[tid];
-          df_sub(wh, wl, qh2, ql2);
+      df_acc2(uh, ul, uh2, ul2);
+      df_acc2(ph, pl, ph2, pl2);
+      float sh, sl, s2h, s2l;
+      f2_unpack(uh, sh, s2h);
+      f2_unpack(ul, sl, s2l);
+      df_acc(sh, sl, s2h, s2l);
+      if (pend >= 0) {
+        float p1h, p1l, p2h, p2l;
+        f2_unpack(ph, p1h, p2h);
+        f2_unpack(pl, p1l, p2l);
+        df_acc(p1h, p1l, p2h, p2l);
+        float* cw = T + (pend >> 3) * gfl + (pend & 7) * LR_ROWS + rl;
+        float wh = cw[0], wl = cw[LT_GC * LR_ROWS];
+        df_sub(wh, wl, p1h, p1l);
+        cw[0] = wh;
+        cw[LT_GC * LR_ROWS] = wl;
+        if (valid) {
           Qh[(int64_t)pend * ld + i] = wh;
           Ql[(int64_t)pend * ld + i] = wl;
-          float c0h, c0l, dummy;
-          f2_unpack(ck[pend][0], c0h, dummy);
-          f2_unpack(ck[pend][2], c0l, dummy);
-          df_fma(uh, ul, wh, wl, c0h, c0l);
         }
-        h = yh;
-        l = yl;
-        df_sub(h, l, uh, ul);
-        xh[i] = h;
-        xl[i] = l;
-        df_fma(nah, nal, h, l, h, l);
+        df_fma(sh, sl, wh, wl, c0p[0], c0p[1]);
       }
-      xsh[tid] = h;
-      xsl[tid] = l;
-      wsh[tid] = wh;
-      wsl[tid] = wl;
-    }
-    __syncthreads();
-    const float x0h = xsh[2 * lane], x1h = xsh[2 * lane + 1];
-    const f2_t xh2 = f2_pack(x0h, x1h), nxh2 = f2_pack(-x0h, -x1h),
-               xl2 = f2_pack(xsl[2 * lane], xsl[2 * lane + 1]);
+      float x_h = 0.f, x_l = 0.f;
+      if (valid) {
+        x_h = cyh;
+        x_l = cyl;
+        df_sub(x_h, x_l, sh, sl);
+        xh[i] = x_h;
+        xl[i] = x_l;
+        df_fma(nah, nal, x_h, x_l, x_h, x_l);
+      }
+      xsh[w][lane] = x_h;
+      xsl[w][lane] = x_l;
+      __syncwarp();
+      // phase 2: the lane's column pair over the warp's 32 rows
+      if (lane < npairs) {
+        const float* ch = T + ((2 * lane) >> 3) * gfl + ((2 * lane) & 7) * LR_ROWS + 32 * wi;
+        for (int k = 0; k < 32; k += 4) {
+          f2_t qh[4], ql[4];
+          float a[4], b[4];
 #pragma unroll
-    for (int t = 0; t < NJ; ++t) {
-      if (t == pt && w == pw) {
-        qh[t] = f2_pack(wsh[2 * lane], wsh[2 * lane + 1]);
-        ql[t] = f2_pack(wsl[2 * lane], wsl[2 * lane + 1]);
+          for (int u = 0; u < 4; ++u) {
+            const int r = (lane + k + u) & 31;
+            qh[u] = f2_pack(ch[r], ch[LR_ROWS + r]);
+            ql[u] = f2_pack(ch[LT_GC * LR_ROWS + r], ch[LT_GC * LR_ROWS + LR_ROWS + r]);
+            a[u] = xsh[w][r];
+            b[u] = xsl[w][r];
+          }
+          df_fma2(dh, dl, f2_pack(a[0], a[0]), f2_pack(-a[0], -a[0]), f2_pack(b[0], b[0]), qh[0], ql[0]);
+          df_fma2(dh2, dl2, f2_pack(a[1], a[1]), f2_pack(-a[1], -a[1]), f2_pack(b[1], b[1]), qh[1], ql[1]);
+          df_fma2(dh3, dl3, f2_pack(a[2], a[2]), f2_pack(-a[2], -a[2]), f2_pack(b[2], b[2]), qh[2], ql[2]);
+          df_fma2(dh4, dl4, f2_pack(a[3], a[3]), f2_pack(-a[3], -a[3]), f2_pack(b[3], b[3]), qh[3], ql[3]);
+        }
       }
-      if (w + 8 * t < ncols) df_fma2(dh[t], dl[t], xh2, nxh2, xl2, qh[t], ql[t]);
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(lt_su32(&empty[st])) : "memory");
+    }
+    df_acc2(dh, dl, dh2, dl2);
+    df_acc2(dh3, dl3, dh4, dl4);
+    df_acc2(dh, dl, dh3, dl3);
+    if (lane < npairs) {
+      float h0, h1, l0, l1;
+      f2_unpack(dh, h0, h1);
+      f2_unpack(dl, l0, l1);
+      wred[w][2 * lane] = df_val(h0, l0);
+      if (2 * lane + 1 < ncols) wred[w][2 * lane + 1] = df_val(h1, l1);
     }
   }
+  __syncthreads();
   if (err) {
-    // a copy did not arrive in time: drain the ones in flight (bounded), report,
-    // and contribute nothing
-    if (tid == 0) {
-      for (int t = it; t < issued; ++t) lt_wait(&full[t % LT_STAGES], (uint32_t)((t / LT_STAGES) & 1));
-      atomicOr(status, SV_STATUS_LIMIT);
-    }
-#pragma unroll
-    for (int t = 0; t < NJ; ++t) dh[t] = dl[t] = 0ull;
+    if (tid == 0) atomicOr(status, SV_STATUS_LIMIT);
     nah = nal = 0.f;
   }
-#pragma unroll
-  for (int t = 0; t < NJ; ++t) {
-    const int j = w + 8 * t;
-    if (j < ncols) {
-      float h, l, h2, l2;
-      f2_unpack(dh[t], h, h2);
-      f2_unpack(dl[t], l, l2);
-      df_acc(h, l, h2, l2);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        float hs = __shfl_xor_sync(0xffffffffu, h, o);
-        float ls = __shfl_xor_sync(0xffffffffu, l, o);
-        float s = h + hs;
-        float v = s - h;
-        float e2 = (h - (s - v)) + (hs - v);
-        float lo = e2 + l + ls;
-        h = s + lo;
-        l = lo - (h - s);
-      }
-      if (lane == 0) part[(int64_t)blockIdx.x * ncols + j] = df_val(h, l);
-    }
+  for (int j = tid; j < ncols; j += blockDim.x) {
+    double v = 0;
+    if (!err)
+      for (int u = 0; u < LR_WARPS; ++u) v += wred[u][j];
+    part[(int64_t)blockIdx.x * ncols + j] = v;
   }
   const double nacc = block_sum(df_val(nah, nal), nsh);
   if (tid == 0) npart[blockIdx.x] = nacc;
   if (last_block(counter, &last)) {
-    for (int pq = w; pq < nseg * ncols; pq += 8) {
+    for (int pq = w; pq < nseg * ncols; pq += LR_WARPS + 1) {
       const int s2 = pq / ncols, j = pq - s2 * ncols;
       double sacc = 0;
       for (int b = seg_blk[s2] + lane; b < seg_blk[s2 + 1]; b += 32) sacc += part[(int64_t)b * ncols + j];
@@ -1741,8 +1744,9 @@ struct Lanczos {
     lag_tma = work <= 64 && !getenv("SV_NO_LAG_TMA");
     if (lag_tma) {
       const size_t dyn = lag_smem(work - 1);
-      SV_CUDA(cudaFuncSetAttribute(k_cgs_lag_tma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_lag_tma<8>, 256, dyn));
+      SV_CUDA(cudaFuncSetAttribute(k_cgs_lag_tma<LR_STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_lag_tma<LR_STAGES>,
+                                                            32 * (LR_WARPS + 1), dyn));
     } else if (work <= 64) {
       SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_lag<8>, 256, 0));
     } else {
@@ -1931,7 +1935,7 @@ struct Lanczos {
       CUtensorMap mh, ml;
       cuuint64_t gdim[2] = {(cuuint64_t)Ws.len, (cuuint64_t)jn};
       cuuint64_t gstride[1] = {(cuuint64_t)Ws.ld * 4};
-      cuuint32_t box[2] = {(cuuint32_t)LT_ROWS, (cuuint32_t)LT_GC};
+      cuuint32_t box[2] = {(cuuint32_t)LR_ROWS, (cuuint32_t)LT_GC};
       cuuint32_t estr[2] = {1, 1};
       for (int a = 0; a < 2; ++a) {
         CUresult r = sv_encode_tiled()(a ? &ml : &mh, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, a ? Ws.bl() : Ws.bh(),
@@ -1940,7 +1944,8 @@ struct Lanczos {
                                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) sv_throw(SV_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
       }
-      sv_launch(ctx, "irlba_cgs_lag", k_cgs_lag_tma<8>, dim3(g), dim3(256), lag_smem(jn), mh, ml, Ws.bh(),
+      sv_launch(ctx, "irlba_cgs_lag", k_cgs_lag_tma<LR_STAGES>, dim3(g), dim3(32 * (LR_WARPS + 1)), lag_smem(jn),
+                mh, ml, Ws.bh(),
                 Ws.bl(), Ws.ld, jn, pend, Ws.xh.get(), Ws.xl.get(), y, (const BlkRange*)Ws.red.blk.get(),
                 (const int*)Ws.red.seg_blk.get(), nseg, (const int*)active.get(), (const double*)c0v(),
                 cpv(), part.get(), part.get() + (size_t)g * work, sS(), counter.get(), ctx->d_status);
@@ -1958,7 +1963,7 @@ struct Lanczos {
   // dynamic shared memory of the TMA pass over ncols columns (the ring + 1 KB
   // alignment slack)
   static size_t lag_smem(int ncols) {
-    return (size_t)LT_STAGES * ((ncols + LT_GC - 1) / LT_GC) * 2 * LT_GC * LT_ROWS * 4 + 1024;
+    return (size_t)LR_STAGES * ((ncols + LT_GC - 1) / LT_GC) * 2 * LT_GC * LR_ROWS * 4 + 1024;
   }
   // F = A^T w' - alpha v of cell-side column jn: corrected for the pending
   // part of w', and G[:, jn] = A^T w
