@@ -8,12 +8,17 @@
 // (droptol!, :92).  Output: CSC, rows sorted per column.
 //
 // Per column j the candidate rows are the reverse neighbours of its neighbours,
-// cand(j) = concat_{r in N(j)} R(r) with R(r) = {i : r in N(i)}; sorting cand(j)
-// turns the intersection counts into run lengths (each i appears once per shared
-// neighbour).  Columns are processed by one warp (<= 1024 candidates, shared
-// memory), one block (<= 16384, shared memory) or one block over a global
-// scratch buffer (larger hubs).  Two passes: count the kept entries, scan,
-// write.  All integer work; the one division is IEEE-correctly rounded.
+// cand(j) = concat_{r in N(j)} R(r) with R(r) = {i : r in N(i)}; each i appears
+// once per shared neighbour, so its count is its multiplicity in cand(j).
+// Columns are processed by one warp (<= 1024 candidates), one block (<= 16384)
+// or one block over a global scratch buffer (larger hubs).  The warp and block
+// forms count the candidates in a shared-memory hash table (row and count
+// packed in one 32-bit word, open addressing, at least twice as many slots as
+// candidates), keep the entries whose weight passes the prune threshold, and
+// sort only those by row; the hub form (and rows or k too large for the
+// packing) sorts all candidates and reads the counts as run lengths.  Two
+// passes: count the kept entries, scan, write.  All integer work; the one
+// division is IEEE-correctly rounded.
 #include "sv_internal.cuh"
 #include <limits.h>
 
@@ -22,6 +27,8 @@ namespace {
 constexpr int CAP_WARP = 1024;
 constexpr int CAP_BLOCK = 16384;
 constexpr int SNN_BLOCK = 256;
+constexpr int SLOTS_WARP = 3 * CAP_WARP / 2;     // hash slots per warp (load <= 2/3)
+constexpr int SLOTS_BLOCK = 3 * CAP_BLOCK / 2;   // hash slots per block
 
 // nn (n x k row-major 0-based) -> G (n x k row-major, sorted unique, -1 padded), gcnt
 __global__ void k_snn_graph(const int32_t* __restrict__ nn, int64_t n, int k,
@@ -121,6 +128,27 @@ __device__ void group_bitonic(int32_t* buf, int n2, const Grp& g) {
   }
 }
 
+// bitonic sort of n2 (a power of two) unsigned words, ascending
+template <typename Grp>
+__device__ void group_bitonic_u32(uint32_t* buf, int n2, const Grp& g) {
+  for (int kk = 2; kk <= n2; kk <<= 1) {
+    for (int j = kk >> 1; j > 0; j >>= 1) {
+      for (int i = g.rank(); i < n2; i += g.size()) {
+        int ixj = i ^ j;
+        if (ixj > i) {
+          uint32_t a = buf[i], b = buf[ixj];
+          bool up = (i & kk) == 0;
+          if ((a > b) == up) {
+            buf[i] = b;
+            buf[ixj] = a;
+          }
+        }
+      }
+      g.sync();
+    }
+  }
+}
+
 template <typename T>
 struct Wt {
   __device__ static T w(int c, int kk) {
@@ -196,23 +224,129 @@ __device__ int64_t snn_column(int64_t j, const int32_t* __restrict__ G, const in
   return kept_total;
 }
 
+// group-wide exclusive prefix of a flag: (before, total)
+template <typename Grp>
+__device__ __forceinline__ void group_prefix(bool flag, int* wsum, const Grp& g, int& before, int& chunk) {
+  unsigned msk = __ballot_sync(0xffffffffu, flag);
+  if (g.size() == 32) {
+    before = __popc(msk & ((1u << (threadIdx.x & 31)) - 1));
+    chunk = __popc(msk);
+    return;
+  }
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) wsum[wid] = __popc(msk);
+  __syncthreads();
+  before = __popc(msk & ((1u << lane) - 1));
+  chunk = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+    if (w < wid) before += wsum[w];
+    chunk += wsum[w];
+  }
+  __syncthreads();
+}
+
+// Column j counted in a hash table `tab` of 1.5 * (candidates) slots or more:
+// word = (row + 1) << cb | count (cb bits hold any count <= k; 0 = empty).
+// WRITE=false: the kept count; WRITE=true: the kept entries written at `base`
+// in row order.  Same weights and threshold as snn_column.
+template <typename T, bool WRITE, typename Grp>
+__device__ int64_t snn_column_hash(int64_t j, const int32_t* __restrict__ G, const int32_t* __restrict__ gcnt,
+                                   const int64_t* __restrict__ rptr, const int32_t* __restrict__ rlist, int k,
+                                   int kparam, T prune, int cb, uint32_t* tab, int* wsum, const Grp& g,
+                                   int64_t base, int32_t* __restrict__ orow, T* __restrict__ oval,
+                                   int* status) {
+  const int m = gcnt[j];
+  int tot = 0;
+  for (int t = 0; t < m; ++t) {
+    const int32_t r = G[j * k + t];
+    tot += (int)(rptr[r + 1] - rptr[r]);
+  }
+  // a multiple of 32, load at most 2/3; never above the table (tot <= CAP)
+  const int S = max(32, (3 * tot / 2 + 31) / 32 * 32);
+  const uint32_t cmask = (1u << cb) - 1u;
+  for (int i = g.rank(); i < S; i += g.size()) tab[i] = 0u;
+  g.sync();
+  for (int t = 0; t < m; ++t) {
+    const int32_t r = G[j * k + t];
+    const int64_t s0 = rptr[r], e0 = rptr[r + 1];
+    for (int64_t q = s0 + g.rank(); q < e0; q += g.size()) {
+      const uint32_t key = (uint32_t)rlist[q] + 1u;
+      uint32_t h = __umulhi(key * 2654435761u, (uint32_t)S);
+      int probes = 0;
+      while (true) {
+        uint32_t cur = tab[h];
+        if (cur == 0u) {
+          cur = atomicCAS(&tab[h], 0u, (key << cb) | 1u);
+          if (cur == 0u) break;
+        }
+        if ((cur >> cb) == key) {
+          atomicAdd(&tab[h], 1u);
+          break;
+        }
+        h = h + 1 == (uint32_t)S ? 0u : h + 1;
+        if (++probes >= S) {   // cannot happen with S > candidates
+          sv_flag(status, SV_STATUS_LIMIT);
+          break;
+        }
+      }
+    }
+  }
+  g.sync();
+  const int kk = kparam >= 0 ? kparam : m;
+  // compact the kept entries to the front, in place (each chunk is read before
+  // it is written, and writes land at or before the slots already read)
+  int nk = 0;
+  for (int c0 = 0; c0 < S; c0 += g.size()) {
+    const int i = c0 + g.rank();
+    const uint32_t v = i < S ? tab[i] : 0u;
+    bool keep = false;
+    if (v != 0u) keep = Wt<T>::w((int)(v & cmask), kk) > prune;   // droptol!: |w| > prune kept
+    int before, chunk;
+    group_prefix(keep, wsum, g, before, chunk);
+    if (WRITE) {
+      g.sync();   // every read of this chunk before any write
+      if (keep) tab[nk + before] = v;
+    }
+    nk += chunk;
+  }
+  if (!WRITE) {
+    g.sync();
+    return nk;
+  }
+  int n2 = 1;
+  while (n2 < nk) n2 <<= 1;
+  for (int i = nk + g.rank(); i < n2; i += g.size()) tab[i] = 0xFFFFFFFFu;
+  g.sync();
+  group_bitonic_u32(tab, n2, g);
+  for (int p = g.rank(); p < nk; p += g.size()) {
+    const uint32_t v = tab[p];
+    orow[base + p] = (int32_t)((v >> cb) - 1u);
+    oval[base + p] = Wt<T>::w((int)(v & cmask), kk);
+  }
+  g.sync();
+  return nk;
+}
+
 template <typename T, bool WRITE>
 __global__ void __launch_bounds__(SNN_BLOCK) k_snn_warp(
     const int32_t* __restrict__ list, int64_t nlist, const int32_t* __restrict__ G,
     const int32_t* __restrict__ gcnt, const int64_t* __restrict__ rptr,
     const int32_t* __restrict__ rlist, int k, int kparam, T prune, int64_t* __restrict__ kept,
-    const int64_t* __restrict__ colptr, int32_t* __restrict__ orow, T* __restrict__ oval) {
-  __shared__ int32_t sbuf[(SNN_BLOCK / 32) * CAP_WARP];
+    const int64_t* __restrict__ colptr, int32_t* __restrict__ orow, T* __restrict__ oval, int cb,
+    int* status) {
+  extern __shared__ int32_t sbuf[];   // SLOTS_WARP words per warp
   int wid = threadIdx.x >> 5;
-  int32_t* buf = sbuf + wid * CAP_WARP;
+  int32_t* buf = sbuf + wid * SLOTS_WARP;
   int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   WarpG g;
   for (int64_t t = warp; t < nlist; t += nwarps) {
     int64_t j = list[t];
     int64_t base = WRITE ? colptr[j] : 0;
-    int64_t c = snn_column<T, WRITE>(j, G, gcnt, rptr, rlist, k, kparam, prune, buf, nullptr, g,
-                                     base, orow, oval);
+    int64_t c = cb > 0 ? snn_column_hash<T, WRITE>(j, G, gcnt, rptr, rlist, k, kparam, prune, cb,
+                                                   (uint32_t*)buf, nullptr, g, base, orow, oval, status)
+                       : snn_column<T, WRITE>(j, G, gcnt, rptr, rlist, k, kparam, prune, buf, nullptr, g,
+                                              base, orow, oval);
     if (!WRITE && g.rank() == 0) kept[j] = c;
   }
 }
@@ -223,7 +357,7 @@ __global__ void __launch_bounds__(1024) k_snn_block(
     const int32_t* __restrict__ gcnt, const int64_t* __restrict__ rptr,
     const int32_t* __restrict__ rlist, int k, int kparam, T prune, int64_t* __restrict__ kept,
     const int64_t* __restrict__ colptr, int32_t* __restrict__ orow, T* __restrict__ oval,
-    int32_t* __restrict__ gscratch, int64_t scratch_per_block) {
+    int32_t* __restrict__ gscratch, int64_t scratch_per_block, int cb, int* status) {
   extern __shared__ int32_t dbuf[];
   __shared__ int wsum[32];
   int32_t* buf = gscratch ? gscratch + blockIdx.x * scratch_per_block : dbuf;
@@ -231,8 +365,10 @@ __global__ void __launch_bounds__(1024) k_snn_block(
   for (int64_t t = blockIdx.x; t < nlist; t += gridDim.x) {
     int64_t j = list[t];
     int64_t base = WRITE ? colptr[j] : 0;
-    int64_t c = snn_column<T, WRITE>(j, G, gcnt, rptr, rlist, k, kparam, prune, buf, wsum, g, base,
-                                     orow, oval);
+    int64_t c = cb > 0 ? snn_column_hash<T, WRITE>(j, G, gcnt, rptr, rlist, k, kparam, prune, cb,
+                                                   (uint32_t*)buf, wsum, g, base, orow, oval, status)
+                       : snn_column<T, WRITE>(j, G, gcnt, rptr, rlist, k, kparam, prune, buf, wsum, g,
+                                              base, orow, oval);
     if (!WRITE && threadIdx.x == 0) kept[j] = c;
     __syncthreads();
   }
@@ -276,10 +412,15 @@ void snn_run(sv_context* ctx, const int32_t* nn, int64_t n, int k, int64_t kpara
   DevBuf<int64_t> kept(n + 1);
   out->colptr.alloc(n + 1);
   size_t es = sizeof(T);
-  SV_CUDA(cudaFuncSetAttribute(k_snn_block<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               CAP_BLOCK * 4));
-  SV_CUDA(cudaFuncSetAttribute(k_snn_block<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               CAP_BLOCK * 4));
+  // count bits of the hash words: any count <= k; rows + 1 in the remaining bits
+  int cb = 32 - __builtin_clz((unsigned)k);
+  if ((uint64_t)(n + 1) >= (1ull << (32 - cb))) cb = 0;   // does not fit: the sorting form
+  const size_t warp_smem = (size_t)(SNN_BLOCK / 32) * SLOTS_WARP * 4;
+  const size_t block_smem = (size_t)(cb > 0 ? SLOTS_BLOCK : CAP_BLOCK) * 4;
+  for (auto kern : {k_snn_warp<T, false>, k_snn_warp<T, true>})
+    SV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warp_smem));
+  for (auto kern : {k_snn_block<T, false>, k_snn_block<T, true>})
+    SV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)block_smem));
   for (int pass = 0; pass < 2; ++pass) {
     bool W = pass == 1;
     int32_t* orow = W ? out->rowidx.get() : nullptr;
@@ -288,31 +429,33 @@ void snn_run(sv_context* ctx, const int32_t* nn, int64_t n, int k, int64_t kpara
     int gw = sv_grid_for(ctx, nl[0] * 32, SNN_BLOCK, 4);
     int gb = (int)std::min<int64_t>(std::max<int64_t>(nl[1], 1), (int64_t)ctx->num_sms * 2);
     if (W) {
-      sv_launch(ctx, "snn_columns_warp", k_snn_warp<T, true>, dim3(nl[0] ? gw : 0), dim3(SNN_BLOCK), 0,
-                (const int32_t*)lists.get(), nl[0], (const int32_t*)G.get(), (const int32_t*)gcnt.get(),
-                (const int64_t*)rptr.get(), (const int32_t*)rlist.get(), k, (int)kparam, prune,
-                kept.get(), cp, orow, oval);
-      sv_launch(ctx, "snn_columns_block", k_snn_block<T, true>, dim3(nl[1] ? gb : 0), dim3(1024),
-                (size_t)CAP_BLOCK * 4, (const int32_t*)lists.get() + n, nl[1], (const int32_t*)G.get(),
+      sv_launch(ctx, "snn_columns_warp", k_snn_warp<T, true>, dim3(nl[0] ? gw : 0), dim3(SNN_BLOCK),
+                warp_smem, (const int32_t*)lists.get(), nl[0], (const int32_t*)G.get(),
                 (const int32_t*)gcnt.get(), (const int64_t*)rptr.get(), (const int32_t*)rlist.get(), k,
-                (int)kparam, prune, kept.get(), cp, orow, oval, (int32_t*)nullptr, (int64_t)0);
+                (int)kparam, prune, kept.get(), cp, orow, oval, cb, ctx->d_status);
+      sv_launch(ctx, "snn_columns_block", k_snn_block<T, true>, dim3(nl[1] ? gb : 0), dim3(1024),
+                block_smem, (const int32_t*)lists.get() + n, nl[1], (const int32_t*)G.get(),
+                (const int32_t*)gcnt.get(), (const int64_t*)rptr.get(), (const int32_t*)rlist.get(), k,
+                (int)kparam, prune, kept.get(), cp, orow, oval, (int32_t*)nullptr, (int64_t)0, cb,
+                ctx->d_status);
       sv_launch(ctx, "snn_columns_big", k_snn_block<T, true>, dim3(nl[2] ? big_blocks : 0), dim3(1024),
                 (size_t)0, (const int32_t*)lists.get() + 2 * n, nl[2], (const int32_t*)G.get(),
                 (const int32_t*)gcnt.get(), (const int64_t*)rptr.get(), (const int32_t*)rlist.get(), k,
-                (int)kparam, prune, kept.get(), cp, orow, oval, gscratch.get(), big_n2);
+                (int)kparam, prune, kept.get(), cp, orow, oval, gscratch.get(), big_n2, 0, ctx->d_status);
     } else {
-      sv_launch(ctx, "snn_columns_warp", k_snn_warp<T, false>, dim3(nl[0] ? gw : 0), dim3(SNN_BLOCK), 0,
-                (const int32_t*)lists.get(), nl[0], (const int32_t*)G.get(), (const int32_t*)gcnt.get(),
-                (const int64_t*)rptr.get(), (const int32_t*)rlist.get(), k, (int)kparam, prune,
-                kept.get(), cp, orow, oval);
-      sv_launch(ctx, "snn_columns_block", k_snn_block<T, false>, dim3(nl[1] ? gb : 0), dim3(1024),
-                (size_t)CAP_BLOCK * 4, (const int32_t*)lists.get() + n, nl[1], (const int32_t*)G.get(),
+      sv_launch(ctx, "snn_columns_warp", k_snn_warp<T, false>, dim3(nl[0] ? gw : 0), dim3(SNN_BLOCK),
+                warp_smem, (const int32_t*)lists.get(), nl[0], (const int32_t*)G.get(),
                 (const int32_t*)gcnt.get(), (const int64_t*)rptr.get(), (const int32_t*)rlist.get(), k,
-                (int)kparam, prune, kept.get(), cp, orow, oval, (int32_t*)nullptr, (int64_t)0);
+                (int)kparam, prune, kept.get(), cp, orow, oval, cb, ctx->d_status);
+      sv_launch(ctx, "snn_columns_block", k_snn_block<T, false>, dim3(nl[1] ? gb : 0), dim3(1024),
+                block_smem, (const int32_t*)lists.get() + n, nl[1], (const int32_t*)G.get(),
+                (const int32_t*)gcnt.get(), (const int64_t*)rptr.get(), (const int32_t*)rlist.get(), k,
+                (int)kparam, prune, kept.get(), cp, orow, oval, (int32_t*)nullptr, (int64_t)0, cb,
+                ctx->d_status);
       sv_launch(ctx, "snn_columns_big", k_snn_block<T, false>, dim3(nl[2] ? big_blocks : 0), dim3(1024),
                 (size_t)0, (const int32_t*)lists.get() + 2 * n, nl[2], (const int32_t*)G.get(),
                 (const int32_t*)gcnt.get(), (const int64_t*)rptr.get(), (const int32_t*)rlist.get(), k,
-                (int)kparam, prune, kept.get(), cp, orow, oval, gscratch.get(), big_n2);
+                (int)kparam, prune, kept.get(), cp, orow, oval, gscratch.get(), big_n2, 0, ctx->d_status);
       sv_scan_i64(ctx, kept.get(), out->colptr.get(), n);
       out->nnz = sv_read_i64(ctx, out->colptr.get() + n);
       out->rowidx.alloc(std::max<int64_t>(1, out->nnz));
@@ -320,6 +463,7 @@ void snn_run(sv_context* ctx, const int32_t* nn, int64_t n, int k, int64_t kpara
     }
   }
   sv_sync(ctx);
+  sv_check_device_status(ctx, "snn");
 }
 
 __global__ void k_nn_from_host_layout(const int32_t* __restrict__ in, int64_t n, int k,
