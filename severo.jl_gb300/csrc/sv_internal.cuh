@@ -215,7 +215,7 @@ struct sv_centered {
   int64_t rb_rows = 0, n_rb = 0;      // rows per block, number of row blocks
   int rb_per_sm = 3;                  // resident blocks per SM of the X^T u kernel
   DevBuf<int64_t> rb_ptr;             // n_rb * nf + 1 entry offsets, ordered (block, feature)
-  DevBuf<uint16_t> rb_idx;            // local row within the block
+  DevBuf<unsigned long long> rb_idx;  // rows within the block, one coded word per 8 entries
   DevBuf<unsigned char> rb_val;       // value (storage type)
   DevBuf<float> rb_partial;           // n_rb x nf partial sums
   int t_blocks = 0;                   // > 0: X^T u over CSR_h with this many blocks
@@ -257,7 +257,7 @@ struct sv_batch {
   DevBuf<int> rb_seg;                 // n_rb
   DevBuf<int64_t> rb_first;           // nseg + 1
   DevBuf<int64_t> rb_ptr;             // n_rb * nf + 1
-  DevBuf<uint16_t> rb_idx;
+  DevBuf<unsigned long long> rb_idx;
   DevBuf<unsigned char> rb_val;
   DevBuf<float> rb_partial;           // n_rb x nf
   DevBuf<double> upart;               // n_rb sums of u

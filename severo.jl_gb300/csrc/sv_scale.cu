@@ -1006,42 +1006,148 @@ __device__ __forceinline__ int64_t rb_first_row(const int64_t* row0, int64_t b) 
   return row0 ? row0[b] : b * RB_ROWS;
 }
 
+// The row-blocked copy codes a segment's rows in groups of 8 entries, one
+// 64-bit word per group: bits 0-15 the row (within the block) of the group's
+// first entry, bits 16 + 6 (t - 1) .. the 6-bit step from entry t - 1 to entry
+// t (t = 1..7).  A step longer than 63 between consecutive entries is bridged
+// by padding entries (rows r + 63, r + 126, ... and value 0), and every segment
+// is padded with value-0 entries to a whole number of groups, so segments
+// start on group boundaries.  Padding adds exactly 0 to the product:
+// min(0 * (1/sigma), clip) = 0 with clip > 0.
+constexpr int RB_GROUP = 8;
+__device__ __forceinline__ int rb_pads(int64_t step) { return step > 63 ? (int)((step - 1) / 63) : 0; }
+
+// per (row block, feature), one warp: entries + padding (whole groups), first source entry
 __global__ void k_rb_count(const int64_t* __restrict__ fstart, const int64_t* __restrict__ fend,
                            const int32_t* __restrict__ rowidx, int64_t nf, int64_t n_rb,
                            int64_t* __restrict__ cnt, int64_t* __restrict__ src,
                            const int64_t* __restrict__ row0) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n_rb * nf;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    int64_t b = p / nf, f = p % nf;
-    int64_t s = fstart[f], e = fend[f];
-    int64_t lo = lower_bound_rows(rowidx, s, e, rb_first_row(row0, b));
-    int64_t hi = lower_bound_rows(rowidx, lo, e, rb_first_row(row0, b + 1));
-    cnt[p] = hi - lo;
-    src[p] = lo;
-  }
-}
-
-template <typename ValT>
-__global__ void k_rb_copy(const int64_t* __restrict__ src, const int64_t* __restrict__ dst,
-                          const int32_t* __restrict__ rowidx, const ValT* __restrict__ val,
-                          int64_t npairs, int64_t nf, uint16_t* __restrict__ oidx,
-                          ValT* __restrict__ oval, const int64_t* __restrict__ row0) {
-  int lane = threadIdx.x & 31;
-  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t p = warp; p < npairs; p += nwarps) {
-    int64_t b = p / nf;
-    int64_t s = src[p], d = dst[p], n = dst[p + 1] - d;
-    for (int64_t i = lane; i < n; i += 32) {
-      oidx[d + i] = (uint16_t)(rowidx[s + i] - rb_first_row(row0, b));
-      oval[d + i] = val[s + i];
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t p = warp; p < n_rb * nf; p += nwarps) {
+    const int64_t b = p / nf, f = p % nf;
+    const int64_t s = fstart[f], e = fend[f];
+    const int64_t lo = lower_bound_rows(rowidx, s, e, rb_first_row(row0, b));
+    const int64_t hi = lower_bound_rows(rowidx, lo, e, rb_first_row(row0, b + 1));
+    int64_t pads = 0;
+    for (int64_t t = lo + 1 + lane; t < hi; t += 32) pads += rb_pads((int64_t)rowidx[t] - rowidx[t - 1]);
+    pads = sv_warp_sum(pads);
+    if (lane == 0) {
+      const int64_t n = hi - lo + pads;
+      cnt[p] = (n + RB_GROUP - 1) / RB_GROUP * RB_GROUP;
+      src[p] = lo;
     }
   }
 }
 
+// one warp per (row block, feature): the coded rows (ocode zeroed beforehand,
+// bit fields or-ed in) and the values, padding included
+template <typename ValT>
+__global__ void k_rb_copy(const int64_t* __restrict__ src, const int64_t* __restrict__ dst,
+                          const int64_t* __restrict__ fend, const int32_t* __restrict__ rowidx,
+                          const ValT* __restrict__ val, int64_t npairs, int64_t nf,
+                          unsigned long long* __restrict__ ocode, ValT* __restrict__ oval,
+                          const int64_t* __restrict__ row0) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t p = warp; p < npairs; p += nwarps) {
+    const int64_t b = p / nf;
+    const int64_t first = rb_first_row(row0, b);
+    const int64_t s = src[p], d = dst[p], dend = dst[p + 1];
+    const int64_t hi = lower_bound_rows(rowidx, s, fend[p % nf], rb_first_row(row0, b + 1));
+    // entry q (from d) at row r; the previous entry at row rp
+    auto put = [&](int64_t q, int64_t r, int64_t rp, ValT v) {
+      const int64_t rel = q - d;
+      const int slot = (int)(rel % RB_GROUP);
+      const unsigned long long field =
+          slot == 0 ? (unsigned long long)r : (unsigned long long)(r - rp) << (16 + 6 * (slot - 1));
+      if (field) atomicOr(&ocode[q / RB_GROUP], field);
+      oval[q] = v;
+    };
+    int64_t o = d;
+    int64_t last_row = 0;
+    for (int64_t t0 = s; t0 < hi; t0 += 32) {
+      const int64_t t = t0 + lane;
+      int64_t r = 0, rp = 0;
+      int k = 0;
+      if (t < hi) {
+        r = (int64_t)rowidx[t] - first;
+        rp = t > s ? (int64_t)rowidx[t - 1] - first : r;
+        k = t > s ? rb_pads(r - rp) : 0;
+      }
+      int incl = t < hi ? k + 1 : 0;
+#pragma unroll
+      for (int sh = 1; sh < 32; sh <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, sh);
+        if (lane >= sh) incl += y;
+      }
+      const int tot = __shfl_sync(0xffffffffu, incl, 31);
+      if (t < hi) {
+        int64_t q = o + incl - (k + 1);
+        int64_t prev = rp;
+        for (int u = 1; u <= k; ++u, ++q) {
+          put(q, rp + 63 * u, prev, ValT(0.f));
+          prev = rp + 63 * u;
+        }
+        put(q, r, prev, val[t]);
+      }
+      const int64_t lr = __shfl_sync(0xffffffffu, r, (tot > 0 ? min(31, (int)(hi - 1 - t0)) : 0));
+      if (hi > t0) last_row = lr;
+      o += tot;
+    }
+    // value-0 entries up to the group boundary, at the last row
+    for (int64_t q = o + lane; q < dend; q += 32) put(q, last_row, last_row, ValT(0.f));
+  }
+}
+
+// sum over a segment of whole groups (g0 .. g1) of min(a (1/sigma), clip) u[row];
+// two groups per lane in flight, lane-local decoding
+template <typename ValT>
+__device__ __forceinline__ float rb_seg_dot(const unsigned long long* __restrict__ code,
+                                           const ValT* __restrict__ pv, int64_t g0, int64_t g1,
+                                           float inv, float clip, const float* us, int lane) {
+  float acc = 0.f;
+  for (int64_t g = g0 + lane; g < g1; g += 64) {
+    unsigned long long c[2];
+    uint4 rv[2][sizeof(ValT) == 2 ? 1 : 2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+      if (g + 32 * h < g1) {
+        c[h] = __ldg(code + g + 32 * h);
+        const uint4* vp = (const uint4*)(pv + (g + 32 * h) * RB_GROUP);
+        rv[h][0] = __ldg(vp);
+        if constexpr (sizeof(ValT) == 4) rv[h][1] = __ldg(vp + 1);
+      }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (g + 32 * h >= g1) break;
+      int r = (int)(c[h] & 0xffffu);
+      unsigned long long st = c[h] >> 16;
+#pragma unroll
+      for (int t = 0; t < RB_GROUP; ++t) {
+        if (t > 0) {
+          r += (int)(st & 63u);
+          st >>= 6;
+        }
+        float a;
+        if constexpr (sizeof(ValT) == 2) {
+          const unsigned w = (&rv[h][0].x)[t >> 1];
+          a = __uint_as_float((t & 1) ? (w & 0xffff0000u) : (w << 16));
+        } else {
+          a = __uint_as_float((&rv[h][t >> 2].x)[t & 3]);
+        }
+        acc += fminf(a * inv, clip) * us[r];
+      }
+    }
+  }
+  return acc;
+}
+
 template <typename ValT>
 __global__ void __launch_bounds__(RB_THREADS) k_spmv_rb(
-    const int64_t* __restrict__ rb_ptr, const uint16_t* __restrict__ rb_idx,
+    const int64_t* __restrict__ rb_ptr, const unsigned long long* __restrict__ rb_code,
     const ValT* __restrict__ rb_val, int64_t nf, int64_t n_cells, const float* __restrict__ inv_f,
     const float* __restrict__ clip_f, const float* __restrict__ uf, float* __restrict__ partial,
     const int64_t* __restrict__ row0, const int* __restrict__ rb_seg,
@@ -1068,58 +1174,7 @@ __global__ void __launch_bounds__(RB_THREADS) k_spmv_rb(
   for (int64_t f = g + (int64_t)fg * w; f < nf; f += (int64_t)fg * nw) {
     int64_t s = rb_ptr[b * nf + f], e = rb_ptr[b * nf + f + 1];
     float inv = inv_f[f], clip = clip_f[f];
-    float acc = 0.f;
-    int64_t a0 = s & ~3ll;
-    // guarded loads for both groups: measured faster here than the
-    // unconditional-first form (1.37 vs 1.72 ms at 1.3M cells), the opposite of
-    // k_spmv_csr
-    if constexpr (sizeof(ValT) == 2) {
-      // 32-bit offsets relative to the feature's aligned start, raw packed loads
-      const uint16_t* pi = rb_idx + a0;
-      const uint16_t* pv = (const uint16_t*)rb_val + a0;
-      const int ls = (int)(s - a0), le = (int)(e - a0);
-      for (int q = 4 * lane; q < le; q += 512) {
-        uint2 ri[4], rv[4];
-#pragma unroll
-        for (int h = 0; h < 4; ++h)
-          if (q + 128 * h < le) {
-            ri[h] = __ldg((const uint2*)(pi + q + 128 * h));
-            rv[h] = __ldg((const uint2*)(pv + q + 128 * h));
-          }
-#pragma unroll
-        for (int h = 0; h < 4; ++h) {
-          int qh = q + 128 * h;
-          if (qh >= le) break;
-#pragma unroll
-          for (int t = 0; t < 4; ++t) {
-            unsigned wi = t < 2 ? ri[h].x : ri[h].y;
-            unsigned wv = t < 2 ? rv[h].x : rv[h].y;
-            int ci = (t & 1) ? (int)(wi >> 16) : (int)(wi & 0xffffu);
-            float av = __uint_as_float((t & 1) ? (wv & 0xffff0000u) : (wv << 16));
-            if (qh + t >= ls && qh + t < le) acc += fminf(av * inv, clip) * us[ci];
-          }
-        }
-      }
-    } else {
-    for (int64_t gg = a0 + 4 * lane; gg < e; gg += 256) {
-      int ci[2][4];
-      float av[2][4];
-#pragma unroll
-      for (int h = 0; h < 2; ++h)
-        if (gg + 128 * h < e) {
-          ld4(rb_idx, gg + 128 * h, ci[h]);
-          ld4v(rb_val, gg + 128 * h, av[h]);
-        }
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        if (gg + 128 * h >= e) break;
-        int64_t gh = gg + 128 * h;
-#pragma unroll
-        for (int t = 0; t < 4; ++t)
-          if (gh + t >= s && gh + t < e) acc += fminf(av[h][t] * inv, clip) * us[ci[h][t]];
-      }
-    }
-    }
+    float acc = rb_seg_dot<ValT>(rb_code, rb_val, s / RB_GROUP, e / RB_GROUP, inv, clip, us, lane);
     acc = sv_warp_sum(acc);
     if (lane == 0) partial[b * nf + f] = acc;
   }
@@ -1132,8 +1187,8 @@ __global__ void __launch_bounds__(RB_THREADS) k_spmv_rb(
 // partial last wave is left (the grid form above ran 3.2 waves of blocks with
 // 43% of its warps active).  Same loop and partials as k_spmv_rb.
 template <typename ValT>
-__global__ void __launch_bounds__(RB_THREADS, 3) k_spmv_rb_waves(
-    const int64_t* __restrict__ rb_ptr, const uint16_t* __restrict__ rb_idx,
+__global__ void __launch_bounds__(RB_THREADS, 2) k_spmv_rb_waves(
+    const int64_t* __restrict__ rb_ptr, const unsigned long long* __restrict__ rb_code,
     const ValT* __restrict__ rb_val, int64_t nf, int64_t n_cells, int64_t n_rb, int fg,
     const float* __restrict__ inv_f, const float* __restrict__ clip_f, const float* __restrict__ uf,
     float* __restrict__ partial) {
@@ -1158,66 +1213,7 @@ __global__ void __launch_bounds__(RB_THREADS, 3) k_spmv_rb_waves(
       if (f >= nf) break;
       const int64_t s = rb_ptr[b * nf + f], e = rb_ptr[b * nf + f + 1];
       const float inv = inv_f[f], clip = clip_f[f];
-      float acc = 0.f;
-      const int64_t a0 = s & ~3ll;
-      if constexpr (sizeof(ValT) == 2) {
-        const uint16_t* pi = rb_idx + a0;
-        const uint16_t* pv = (const uint16_t*)rb_val + a0;
-        const int ls = (int)(s - a0), le = (int)(e - a0);
-        for (int q = 4 * lane; q < le; q += 512) {
-          uint2 ri[4], rv[4];
-#pragma unroll
-          for (int h = 0; h < 4; ++h)
-            if (q + 128 * h < le) {
-              ri[h] = __ldg((const uint2*)(pi + q + 128 * h));
-              rv[h] = __ldg((const uint2*)(pv + q + 128 * h));
-            }
-#pragma unroll
-          for (int h = 0; h < 4; ++h) {
-            const int qh = q + 128 * h;
-            if (qh >= le) break;
-            if (qh >= ls && qh + 4 <= le) {
-              // a group inside the run: no guards
-#pragma unroll
-              for (int t = 0; t < 4; ++t) {
-                const unsigned wi = t < 2 ? ri[h].x : ri[h].y;
-                const unsigned wv = t < 2 ? rv[h].x : rv[h].y;
-                const int ci = (t & 1) ? (int)(wi >> 16) : (int)(wi & 0xffffu);
-                const float av = __uint_as_float((t & 1) ? (wv & 0xffff0000u) : (wv << 16));
-                acc += fminf(av * inv, clip) * us[ci];
-              }
-            } else {
-#pragma unroll
-              for (int t = 0; t < 4; ++t) {
-                const unsigned wi = t < 2 ? ri[h].x : ri[h].y;
-                const unsigned wv = t < 2 ? rv[h].x : rv[h].y;
-                const int ci = (t & 1) ? (int)(wi >> 16) : (int)(wi & 0xffffu);
-                const float av = __uint_as_float((t & 1) ? (wv & 0xffff0000u) : (wv << 16));
-                if (qh + t >= ls && qh + t < le) acc += fminf(av * inv, clip) * us[ci];
-              }
-            }
-          }
-        }
-      } else {
-        for (int64_t gg = a0 + 4 * lane; gg < e; gg += 256) {
-          int ci[2][4];
-          float av[2][4];
-#pragma unroll
-          for (int h = 0; h < 2; ++h)
-            if (gg + 128 * h < e) {
-              ld4(rb_idx, gg + 128 * h, ci[h]);
-              ld4v(rb_val, gg + 128 * h, av[h]);
-            }
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            if (gg + 128 * h >= e) break;
-            const int64_t gh = gg + 128 * h;
-#pragma unroll
-            for (int t = 0; t < 4; ++t)
-              if (gh + t >= s && gh + t < e) acc += fminf(av[h][t] * inv, clip) * us[ci[h][t]];
-          }
-        }
-      }
+      float acc = rb_seg_dot<ValT>(rb_code, rb_val, s / RB_GROUP, e / RB_GROUP, inv, clip, us, lane);
       acc = sv_warp_sum(acc);
       if (lane == 0) partial[b * nf + f] = acc;
     }
@@ -1452,13 +1448,13 @@ void sv_centered_apply(sv_context* ctx, const sv_centered* S, char trans, const 
     size_t smem = RB_ROWS * sizeof(float);
     if (S->dtype == SV_F32)
       sv_launch(ctx, "spmv_rb", k_spmv_rb_waves<float>, dim3(grid), dim3(RB_THREADS), smem,
-                (const int64_t*)S->rb_ptr.get(), (const uint16_t*)S->rb_idx.get(),
+                (const int64_t*)S->rb_ptr.get(), (const unsigned long long*)S->rb_idx.get(),
                 (const float*)S->rb_val.get(), S->nf, S->n_cells, S->n_rb, fg,
                 (const float*)S->inv_std_f.get(), (const float*)S->clip_f.get(),
                 (const float*)Sm->u_f32.get(), Sm->rb_partial.get());
     else
       sv_launch(ctx, "spmv_rb", k_spmv_rb_waves<__nv_bfloat16>, dim3(grid), dim3(RB_THREADS), smem,
-                (const int64_t*)S->rb_ptr.get(), (const uint16_t*)S->rb_idx.get(),
+                (const int64_t*)S->rb_ptr.get(), (const unsigned long long*)S->rb_idx.get(),
                 (const __nv_bfloat16*)S->rb_val.get(), S->nf, S->n_cells, S->n_rb, fg,
                 (const float*)S->inv_std_f.get(), (const float*)S->clip_f.get(),
                 (const float*)Sm->u_f32.get(), Sm->rb_partial.get());
@@ -1577,37 +1573,38 @@ static std::vector<int32_t> feature_genes(const sv_counts* C, const int64_t* fea
 }
 
 // Row-blocked CSC copy of the feature subset (the X^T u layout): for every
-// (row block, feature) the block's entries of the feature, each as its row
-// within the block (uint16) and its value.  Row blocks of RB_ROWS rows, or with
+// (row block, feature) the block's entries of the feature, their rows within
+// the block coded in groups of 8 (see k_rb_count) and their values.  Row blocks of RB_ROWS rows, or with
 // first rows row0 (n_rb + 1 entries, device) when aligned to samples.
 static void rb_build(sv_context* ctx, const sv_counts* C, const sv_data* data, const int64_t* fstart,
                      const int64_t* fend, int64_t nf, int64_t nnz_h, int64_t n_rb, const int64_t* row0,
-                     DevBuf<int64_t>& rb_ptr, DevBuf<uint16_t>& rb_idx, DevBuf<unsigned char>& rb_val,
+                     DevBuf<int64_t>& rb_ptr, DevBuf<unsigned long long>& rb_idx, DevBuf<unsigned char>& rb_val,
                      DevBuf<float>& rb_partial) {
   int64_t np = n_rb * nf;
   DevBuf<int64_t> cnt(np + 1), src(np + 1);
-  sv_launch(ctx, "scale_rb_count", k_rb_count, dim3(sv_grid_for(ctx, np, 256, 8)), dim3(256), 0, fstart,
+  sv_launch(ctx, "scale_rb_count", k_rb_count, dim3(sv_grid_for(ctx, np * 32, 256, 8)), dim3(256), 0, fstart,
             fend, (const int32_t*)C->csc_rowidx.get(), nf, n_rb, cnt.get(), src.get(), row0);
   rb_ptr.alloc(np + 1);
   sv_scan_i64(ctx, cnt.get(), rb_ptr.get(), np);
-  int64_t tot = sv_read_i64(ctx, rb_ptr.get() + np);
-  if (tot != nnz_h)
+  const int64_t tot = sv_read_i64(ctx, rb_ptr.get() + np);   // entries + padding
+  if (tot < nnz_h)
     sv_throw(SV_ERR_DEVICE, "row-blocked copy size mismatch (%lld vs %lld)", (long long)tot,
              (long long)nnz_h);
   size_t es2 = sv_elem_size(data->dtype);
-  rb_idx.alloc(std::max<int64_t>(1, nnz_h));
-  rb_val.alloc(std::max<int64_t>(1, nnz_h) * es2);
+  rb_idx.alloc(std::max<int64_t>(1, tot / RB_GROUP));
+  sv_memset(ctx, rb_idx.get(), 0, std::max<int64_t>(1, tot / RB_GROUP) * 8);
+  rb_val.alloc(std::max<int64_t>(1, tot) * es2);
   rb_partial.alloc(std::max<int64_t>(1, np));
   int gridc = sv_grid_for(ctx, np * 32, 256, 8);
   if (data->dtype == SV_F32)
     sv_launch(ctx, "scale_rb_copy", k_rb_copy<float>, dim3(gridc), dim3(256), 0, (const int64_t*)src.get(),
-              (const int64_t*)rb_ptr.get(), (const int32_t*)C->csc_rowidx.get(),
+              (const int64_t*)rb_ptr.get(), fend, (const int32_t*)C->csc_rowidx.get(),
               (const float*)data->csc_val.get(), np, nf, rb_idx.get(), (float*)rb_val.get(), row0);
   else
     sv_launch(ctx, "scale_rb_copy", k_rb_copy<__nv_bfloat16>, dim3(gridc), dim3(256), 0,
-              (const int64_t*)src.get(), (const int64_t*)rb_ptr.get(), (const int32_t*)C->csc_rowidx.get(),
-              (const __nv_bfloat16*)data->csc_val.get(), np, nf, rb_idx.get(),
-              (__nv_bfloat16*)rb_val.get(), row0);
+              (const int64_t*)src.get(), (const int64_t*)rb_ptr.get(), fend,
+              (const int32_t*)C->csc_rowidx.get(), (const __nv_bfloat16*)data->csc_val.get(), np, nf,
+              rb_idx.get(), (__nv_bfloat16*)rb_val.get(), row0);
   sv_sync(ctx);
 }
 
@@ -2129,13 +2126,13 @@ void sv_batch_apply_T(sv_context* ctx, const sv_batch* b, const double* u, doubl
   size_t smem = RB_ROWS * sizeof(float);
   if (b->data->dtype == SV_F32)
     sv_launch(ctx, "spmv_rb", k_spmv_rb<float>, grid, dim3(RB_THREADS), smem,
-              (const int64_t*)b->rb_ptr.get(), (const uint16_t*)b->rb_idx.get(), (const float*)b->rb_val.get(),
+              (const int64_t*)b->rb_ptr.get(), (const unsigned long long*)b->rb_idx.get(), (const float*)b->rb_val.get(),
               b->nf, b->n_cells, (const float*)b->inv_f.get(), (const float*)b->clip_f.get(),
               (const float*)S->u_f32.get(), bm->rb_partial.get(), (const int64_t*)b->rb_row0.get(),
               (const int*)b->rb_seg.get(), active);
   else
     sv_launch(ctx, "spmv_rb", k_spmv_rb<__nv_bfloat16>, grid, dim3(RB_THREADS), smem,
-              (const int64_t*)b->rb_ptr.get(), (const uint16_t*)b->rb_idx.get(),
+              (const int64_t*)b->rb_ptr.get(), (const unsigned long long*)b->rb_idx.get(),
               (const __nv_bfloat16*)b->rb_val.get(), b->nf, b->n_cells, (const float*)b->inv_f.get(),
               (const float*)b->clip_f.get(), (const float*)S->u_f32.get(), bm->rb_partial.get(),
               (const int64_t*)b->rb_row0.get(), (const int*)b->rb_seg.get(), active);
