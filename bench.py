@@ -57,8 +57,8 @@ BATCHED = dict(n_samples=64, n_genes=20_000, cells_min=500, cells_max=50_000, de
                k=15, dtype="bfloat16", knn="bf16")
 SEED = 20261203
 # DRAM bytes per algorithmic byte of the X v product kernel, from an ncu capture
-# of the 100,000-cell case (425.4 + 4.1 MB read + written for 425.7 MB algorithmic)
-SPMV_TRAFFIC_PER_BYTE = 429.4 / 425.7
+# of the 100,000-cell case (425.1 + 4.1 MB read + written for 425.7 MB algorithmic)
+SPMV_TRAFFIC_PER_BYTE = 429.2 / 425.7
 SCALE_FACTOR = 1e4
 SCALE_MAX = 10.0
 DISPERSION = 0.2
