@@ -337,6 +337,11 @@ typedef CUresult (*sv_encode_tiled_fn)(CUtensorMap*, CUtensorMapDataType, cuuint
                                        const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
                                        CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 sv_encode_tiled_fn sv_encode_tiled();
+// the cell-side restart rotation on the tensor cores (sv_rotate_tc.cu)
+bool sv_rotate_tc_supported(int nin, int nout, int64_t ld_in);
+void sv_rotate_tc(sv_context* ctx, const float* inh, const float* inl, int64_t ld_in, int64_t len, int nin,
+                  const double* M, int nout, float* outh, float* outl, int64_t ld_out, unsigned char* bsl,
+                  int* fexp);
 // host <-> device copies on the context stream; sv_d2h returns when the data
 // are on the host.  Copies of 32 MB or more to or from pageable memory are
 // staged through the context's pinned buffers with several host threads.

@@ -1660,7 +1660,7 @@ struct Side {
   int64_t max_seg = 0;           // longest sample
   std::vector<int64_t> hoff;     // nseg + 1 row offsets
   DevBuf<int64_t> off;
-  Sched red, rows;
+  Sched red, rows, lag;   // lag: the cell-side lagged CGS2 pass (cell side only)
   DevBuf<float> h[2], l[2];     // basis sets
   int set = 0;                  // the current set
   DevBuf<float> xh, xl;         // working vector
@@ -1721,6 +1721,9 @@ struct Lanczos {
   // G = A^T W (feature rows x work, double-float), two sets that follow the
   // cell-side basis sets through the restart rotations
   DevBuf<float> gh[2], gl[2];
+  // scratch of the tensor-core rotation: the slices of M and their exponents
+  DevBuf<unsigned char> rot_b;
+  DevBuf<int> rot_f;
   DevBuf<unsigned int> counter;
   DevBuf<int> flag, active, finsel;
   double* hsum = nullptr;       // pinned copy of the cycle summaries
@@ -1739,28 +1742,37 @@ struct Lanczos {
     m = woff[nseg];
     n = voff[nseg];
     int per_sm = 0;
-    // one wave of the cell-side pass (the heaviest of the kernels that share
-    // this schedule): the TMA-fed form up to 64 basis columns
-    lag_tma = work <= 64 && !getenv("SV_NO_LAG_TMA");
-    if (lag_tma) {
-      const size_t dyn = lag_smem(work - 1);
-      SV_CUDA(cudaFuncSetAttribute(k_cgs_lag_tma<LR_STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_lag_tma<LR_STAGES>,
-                                                            32 * (LR_WARPS + 1), dyn));
-    } else if (work <= 64) {
-      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_lag<8>, 256, 0));
-    } else {
-      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_lag<12>, 256, 0));
-    }
+    // one wave of the CGS passes (k_cgs_df; the scaling and fix kernels share
+    // the schedule)
+    if (work <= 64)
+      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_df<8, true, true, false>, 256, 0));
+    else
+      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgs_df<12, true, true, false>, 256, 0));
     cgs_blocks = std::max(1, std::min(RED_BLOCKS, per_sm * ctx->num_sms));
     auto red_target = [&](int64_t len) {
       return (int)std::max<int64_t>(1, std::min<int64_t>(cgs_blocks, (len + 63) / 64));
     };
+    // its own one-wave schedule for the cell-side lagged pass: the TMA-fed form
+    // (one block per SM, its ring takes the shared memory) up to 64 basis columns
+    int lag_per_sm = 0;
+    lag_tma = work <= 64 && !getenv("SV_NO_LAG_TMA");
+    if (lag_tma) {
+      const size_t dyn = lag_smem(work - 1);
+      SV_CUDA(cudaFuncSetAttribute(k_cgs_lag_tma<LR_STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lag_per_sm, k_cgs_lag_tma<LR_STAGES>,
+                                                            32 * (LR_WARPS + 1), dyn));
+    } else if (work <= 64) {
+      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lag_per_sm, k_cgs_lag<8>, 256, 0));
+    } else {
+      SV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lag_per_sm, k_cgs_lag<12>, 256, 0));
+    }
+    const int lag_blocks = std::max(1, std::min(RED_BLOCKS, lag_per_sm * ctx->num_sms));
     auto rows_target = [&](int64_t len) {
       return (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->num_sms * 8, (len + 255) / 256));
     };
     Ws.alloc(ctx, woff, work, red_target(m), rows_target(m));
     Vs.alloc(ctx, voff, work, red_target(n), rows_target(n));
+    Ws.lag.build(ctx, woff, (int)std::max<int64_t>(1, std::min<int64_t>(lag_blocks, (m + 63) / 64)));
     {
       const char* mode = getenv("SV_VSIDE");
       // one sample: the multi-block kernels (one 1024-thread block per step
@@ -1778,13 +1790,15 @@ struct Lanczos {
     sig.alloc((size_t)nseg * work);
     summary.alloc((size_t)nseg * (2 * work + 2));
     scal.alloc((size_t)nseg * (2 + 2 * CTL_N));
-    int maxblk = std::max(Ws.red.nblk, Vs.red.nblk);
+    int maxblk = std::max(std::max(Ws.red.nblk, Vs.red.nblk), Ws.lag.nblk);
     part.alloc((size_t)maxblk * (work + 1));
     cvec.alloc((size_t)5 * nseg * MAX_WORK);
     for (int t = 0; t < 2; ++t) {
       gh[t].alloc(n * work);
       gl[t].alloc(n * work);
     }
+    rot_b.alloc(6 * 64 * 64 * 2);
+    rot_f.alloc(64);
     counter.alloc(4);
     flag.alloc(nseg);
     active.alloc(nseg);
@@ -1897,6 +1911,12 @@ struct Lanczos {
   // out = basis * M_s[:, :nout] per sample: into the other basis set (outd null)
   // or FP64 outd (ld = the side's length); only the samples with sel[s] != 0
   void rotate(Side& s, const double* M, int nout, double* outd, const int* sel) {
+    // the cell side of one sample into the other basis set: on the tensor cores
+    if (&s == &Ws && !outd && nseg == 1 && sv_rotate_tc_supported(work, nout, s.ld)) {
+      sv_rotate_tc(ctx, s.bh(), s.bl(), s.ld, s.len, work, M, nout, s.th(), s.tl(), s.ld, rot_b.get(),
+                   rot_f.get());
+      return;
+    }
     // into the other basis set (leading dimension ld) or FP64 outd (len)
     rotate_raw(s.bh(), s.bl(), s.ld, s.rows, M, nout, outd ? (float*)nullptr : s.th(),
                outd ? (float*)nullptr : s.tl(), outd, outd ? s.len : s.ld, sel);
@@ -1925,7 +1945,7 @@ struct Lanczos {
   // cp = the new column's pending correction.
   template <int NJ>
   void w_step_nj(int jn, int pend, const double* y) {
-    const int g = Ws.red.nblk;
+    const int g = Ws.lag.nblk;
     sv_launch(ctx, "irlba_gdots", k_gdots, dim3(jn, nseg), dim3(256), 0, (const float*)Gh(),
               (const float*)Gl(), n, (const int64_t*)Vs.off.get(), (const double*)Vs.cur.get(), pend,
               (const double*)sR(), (const double*)cpv(), (const int*)active.get(), c0v());
@@ -1946,14 +1966,14 @@ struct Lanczos {
       }
       sv_launch(ctx, "irlba_cgs_lag", k_cgs_lag_tma<LR_STAGES>, dim3(g), dim3(32 * (LR_WARPS + 1)), lag_smem(jn),
                 mh, ml, Ws.bh(),
-                Ws.bl(), Ws.ld, jn, pend, Ws.xh.get(), Ws.xl.get(), y, (const BlkRange*)Ws.red.blk.get(),
-                (const int*)Ws.red.seg_blk.get(), nseg, (const int*)active.get(), (const double*)c0v(),
+                Ws.bl(), Ws.ld, jn, pend, Ws.xh.get(), Ws.xl.get(), y, (const BlkRange*)Ws.lag.blk.get(),
+                (const int*)Ws.lag.seg_blk.get(), nseg, (const int*)active.get(), (const double*)c0v(),
                 cpv(), part.get(), part.get() + (size_t)g * work, sS(), counter.get(), ctx->d_status);
       return;
     }
     sv_launch(ctx, "irlba_cgs_lag", k_cgs_lag<NJ>, dim3(g), dim3(256), 0, Ws.bh(), Ws.bl(), Ws.ld, jn,
-              pend, Ws.xh.get(), Ws.xl.get(), y, (const BlkRange*)Ws.red.blk.get(),
-              (const int*)Ws.red.seg_blk.get(), nseg, (const int*)active.get(), (const double*)c0v(),
+              pend, Ws.xh.get(), Ws.xl.get(), y, (const BlkRange*)Ws.lag.blk.get(),
+              (const int*)Ws.lag.seg_blk.get(), nseg, (const int*)active.get(), (const double*)c0v(),
               cpv(), part.get(), part.get() + (size_t)g * work, sS(), counter.get());
   }
   void w_step(int jn, int pend, const double* y) {
