@@ -15,12 +15,14 @@
 // and scales by 2^(e_i + f_c - 14).
 //
 // One CTA per SM, persistent over tiles of 128 rows (MMA M = 128, N = 64
-// output columns, K = 64 basis columns); 4 warps, one thread per row.  Per
-// tile: the raw double-float rows (boxes of 128 rows x 8 columns, hi and lo)
-// arrive by TMA during the previous tile's MMAs and epilogue; each thread cuts
-// its row into slices, written in the 128-byte-swizzled K-major layout; one
-// thread issues the 21 x 4 MMAs (K = 16 each) and commits; the threads read
-// the six accumulators back, combine and store.  Every wait is bounded; on a
+// output columns, K = 64 basis columns); 16 warps, four threads per row (thread
+// t: row t mod 128, quarter q = t / 128, which is also the warp's TMEM lane
+// quarter and column group).  Per tile: the raw double-float rows (boxes of
+// 128 rows x 8 columns, hi and lo) arrive by TMA during the previous tile's
+// MMAs and epilogue; each thread cuts 16 columns of its row into slices,
+// written in the 128-byte-swizzled K-major layout; one thread issues the
+// 21 x 4 MMAs (K = 16 each) and commits; each thread reads 16 output columns
+// of its row from the six accumulators, combines and stores them.  Every wait is bounded; on a
 // timeout the CTA records SV_STATUS_LIMIT, lets its copies and MMAs land
 // (bounded), frees its tensor memory and returns.
 #include "sv_internal.cuh"
@@ -34,7 +36,7 @@ constexpr int RT_ROWS = 128;          // rows per tile (MMA M)
 constexpr int RT_K = 64;              // basis columns, padded (MMA K)
 constexpr int RT_N = 64;              // output columns, padded (MMA N)
 constexpr int RT_SLICES = 6;
-constexpr int RT_THREADS = 128;
+constexpr int RT_THREADS = 512;
 constexpr int RT_GC = 8;              // columns per tensor box
 constexpr long long RT_TIMEOUT = 4000000000ll;   // cycles (~2 s) per wait
 constexpr uint32_t RT_IDESC = idesc_bf16(RT_ROWS, RT_N);
@@ -99,7 +101,10 @@ __global__ void __launch_bounds__(RT_THREADS, 1) k_rotate_tc(
   __shared__ uint32_t tbase;
   __shared__ int err;
   __shared__ int fx[RT_N];
+  __shared__ float rmx[RT_THREADS / RT_ROWS][RT_ROWS];
   const int tid = threadIdx.x, warp = tid >> 5;
+  const int r = tid & (RT_ROWS - 1);    // the thread's row in a tile
+  const int qq = tid / RT_ROWS;         // its column quarter (cutting and output)
   const int ngroups = (nin + RT_GC - 1) / RT_GC;
   const uint32_t raw_bytes = (uint32_t)ngroups * 2u * RT_GC * RT_ROWS * 4u;
   const int64_t ntiles = (len + RT_ROWS - 1) / RT_ROWS;
@@ -143,15 +148,18 @@ __global__ void __launch_bounds__(RT_THREADS, 1) k_rotate_tc(
     __syncthreads();
     if (err) break;
     if (tid == 0) raw_pending = false;
-    // this thread's row: exponent, then six digit slices per basis column
-    const int r = tid;
+    // this thread's row: exponent (the largest entry, over the row's four
+    // threads), then six digit slices of its 16 basis columns
     float mx = 0.f;
-    for (int c = 0; c < nin; ++c)
+    for (int c = 16 * qq; c < 16 * qq + 16 && c < nin; ++c)
       mx = fmaxf(mx, fabsf(raw[(size_t)(c >> 3) * 2 * RT_GC * RT_ROWS + (c & 7) * RT_ROWS + r]));
+    rmx[qq][r] = mx;
+    __syncthreads();
+    mx = fmaxf(fmaxf(rmx[0][r], rmx[1][r]), fmaxf(rmx[2][r], rmx[3][r]));
     const int e = mx > 0.f ? max(-100, min(100, ilogbf(mx) + 1)) : 0;
     const float sc = pow2f(-e) * 128.f;
 #pragma unroll 1
-    for (int ch = 0; ch < RT_K / 8; ++ch) {
+    for (int ch = 2 * qq; ch < 2 * qq + 2; ++ch) {
       uint32_t w[RT_SLICES][4];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
@@ -218,24 +226,25 @@ __global__ void __launch_bounds__(RT_THREADS, 1) k_rotate_tc(
     if (err) break;
     if (tid == 0) mma_pending = false;
     fence_after();
-    // epilogue: the six levels of this thread's row, 32 columns at a time
+    // epilogue: the six levels of this thread's 16 output columns (its warp's
+    // lane quarter is its row block, its column group is qq)
     const int64_t row = t * RT_ROWS + r;
-    const uint32_t tl = tmem + ((uint32_t)(32 * warp) << 16);
-    for (int q = 0; q < RT_N / 32 && 32 * q < nout; ++q) {
-      float h[32], l[32];
-      uint32_t v[32];
-      tmem_ld32(tl + (uint32_t)((RT_SLICES - 1) * RT_N + 32 * q), v);
+    const uint32_t tl = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+    if (16 * qq < nout) {
+      float h[16], l[16];
+      uint32_t v[16];
+      tmem_ld16(tl + (uint32_t)((RT_SLICES - 1) * RT_N + 16 * qq), v);
       tmem_ld_wait();
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
+      for (int i = 0; i < 16; ++i) {
         h[i] = __uint_as_float(v[i]);
         l[i] = 0.f;
       }
       for (int L = RT_SLICES - 2; L >= 0; --L) {
-        tmem_ld32(tl + (uint32_t)(L * RT_N + 32 * q), v);
+        tmem_ld16(tl + (uint32_t)(L * RT_N + 16 * qq), v);
         tmem_ld_wait();
 #pragma unroll
-        for (int i = 0; i < 32; ++i) {
+        for (int i = 0; i < 16; ++i) {
           float s2, e2;
           two_sum(h[i] * 0x1p-8f, __uint_as_float(v[i]), s2, e2);
           h[i] = s2;
@@ -244,8 +253,8 @@ __global__ void __launch_bounds__(RT_THREADS, 1) k_rotate_tc(
       }
       if (row < len) {
 #pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          const int c = 32 * q + i;
+        for (int i = 0; i < 16; ++i) {
+          const int c = 16 * qq + i;
           if (c < nout) {
             const float sc2 = pow2f(max(-126, min(127, e + fx[c] - 14)));
             const float hh = h[i] * sc2, ll = l[i] * sc2;
