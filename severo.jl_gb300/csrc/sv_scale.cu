@@ -378,39 +378,11 @@ template <int NC, int EPL>
 __device__ __forceinline__ int bo_class(int64_t p) {
   return (int)(((p / EPL) + (NC / EPL) * (p % EPL)) & (NC - 1));
 }
-// slots p < X of class c: EPL per period of EPL NC slots, at offsets
-// EPL ((c - (NC/EPL) t) mod NC) + t
-template <int NC, int EPL>
-__device__ __forceinline__ int64_t bo_count(int c, int64_t X) {
-  int64_t n = EPL * (X / (EPL * NC));
-  int r = (int)(X % (EPL * NC));
-#pragma unroll
-  for (int t = 0; t < EPL; ++t) n += (EPL * ((c - (NC / EPL) * t) & (NC - 1)) + t) < r;
-  return n;
-}
-// the idx-th slot (from 0) of class c
-template <int NC, int EPL>
-__device__ __forceinline__ int64_t bo_slot(int c, int64_t idx) {
-  int o[EPL];
-#pragma unroll
-  for (int t = 0; t < EPL; ++t) o[t] = EPL * ((c - (NC / EPL) * t) & (NC - 1)) + t;
-#pragma unroll
-  for (int i = 0; i < EPL; ++i)
-#pragma unroll
-    for (int j = 0; j < EPL - 1 - i; ++j)
-      if (o[j] > o[j + 1]) {
-        int tmp = o[j];
-        o[j] = o[j + 1];
-        o[j + 1] = tmp;
-      }
-  const int k = (int)(idx % EPL);
-  int ok = o[0];
-#pragma unroll
-  for (int t = 1; t < EPL; ++t)
-    if (k == t) ok = o[t];
-  return (int64_t)(EPL * NC) * (idx / EPL) + ok;
-}
-
+// The slots of class c repeat with period EPL NC: EPL of them per period, at
+// the offsets EPL ((c - (NC/EPL) t) mod NC) + t (t < EPL).  The kernel keeps
+// per class the sorted offsets (the idx-th slot of the class) and, for every
+// position x within a period, the number of the class's offsets below x (the
+// slots before a position), so that both are table lookups.
 // One warp per segment, three passes (class counts; the empty slots; ranks and
 // placement), the result written to a second copy (segments with more than
 // BO_EMPTY empty slots are copied unchanged).
@@ -421,10 +393,35 @@ __global__ void __launch_bounds__(BO_WARPS * 32) k_bankorder(const int64_t* __re
                                                              const VT* __restrict__ ival,
                                                              uint16_t* __restrict__ ocol,
                                                              VT* __restrict__ oval) {
+  constexpr int PER = EPL * NC;
   __shared__ uint16_t sempty[BO_WARPS][BO_EMPTY];
   __shared__ int cnt[BO_WARPS][NC], run[BO_WARPS][NC];
+  __shared__ uint8_t soff[NC][EPL], sbelow[NC][PER + 1];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
+  for (int i = threadIdx.x; i < NC * (PER + 1); i += blockDim.x) {
+    const int c = i / (PER + 1), x = i % (PER + 1);
+    int k = 0;
+#pragma unroll
+    for (int t = 0; t < EPL; ++t) k += (EPL * ((c - (NC / EPL) * t) & (NC - 1)) + t) < x;
+    sbelow[c][x] = (uint8_t)k;
+  }
+  for (int c = threadIdx.x; c < NC; c += blockDim.x) {
+    int o[EPL];
+#pragma unroll
+    for (int t = 0; t < EPL; ++t) o[t] = EPL * ((c - (NC / EPL) * t) & (NC - 1)) + t;
+    for (int i = 1; i < EPL; ++i)
+      for (int j = i; j > 0 && o[j - 1] > o[j]; --j) {
+        const int tmp = o[j];
+        o[j] = o[j - 1];
+        o[j - 1] = tmp;
+      }
+    for (int t = 0; t < EPL; ++t) soff[c][t] = (uint8_t)o[t];
+  }
+  __syncthreads();
+  // slots of class c before position X; the idx-th slot of class c
+  auto bo_count = [&](int c, int64_t X) -> int64_t { return EPL * (X / PER) + sbelow[c][X % PER]; };
+  auto bo_slot = [&](int c, int64_t idx) -> int64_t { return (int64_t)PER * (idx / EPL) + soff[c][idx % EPL]; };
   for (int64_t r = (int64_t)blockIdx.x * BO_WARPS + w; r < nseg; r += (int64_t)gridDim.x * BO_WARPS) {
     const int64_t s = ptr[r], e = ptr[r + 1];
     const int64_t L = e - s;
@@ -450,7 +447,7 @@ __global__ void __launch_bounds__(BO_WARPS * 32) k_bankorder(const int64_t* __re
       bool emp = false;
       if (p < P1) {
         int c = bo_class<NC, EPL>(p);
-        emp = bo_count<NC, EPL>(c, p) - bo_count<NC, EPL>(c, P0) >= cnt[w][c];
+        emp = bo_count(c, p) - bo_count(c, P0) >= cnt[w][c];
       }
       unsigned m = __ballot_sync(0xffffffffu, emp);
       int64_t at = nempty + __popc(m & lt);
@@ -468,7 +465,7 @@ __global__ void __launch_bounds__(BO_WARPS * 32) k_bankorder(const int64_t* __re
     // surplus entries of the classes before c (prefix over the classes)
     int sur = 0;
     if (lane < NC) {
-      int64_t slots = bo_count<NC, EPL>(lane, P1) - bo_count<NC, EPL>(lane, P0);
+      int64_t slots = bo_count(lane, P1) - bo_count(lane, P0);
       sur = (int)max((int64_t)0, (int64_t)cnt[w][lane] - slots);
     }
     int incl = sur;
@@ -491,8 +488,8 @@ __global__ void __launch_bounds__(BO_WARPS * 32) k_bankorder(const int64_t* __re
       if (v) {
         int rk = base_c + __popc(same & lt);
         if ((same & lt) == 0) run[w][c] = base_c + __popc(same);
-        int64_t slots = bo_count<NC, EPL>(c, P1) - bo_count<NC, EPL>(c, P0);
-        int64_t q = rk < slots ? bo_slot<NC, EPL>(c, bo_count<NC, EPL>(c, P0) + rk) - P0
+        int64_t slots = bo_count(c, P1) - bo_count(c, P0);
+        int64_t q = rk < slots ? bo_slot(c, bo_count(c, P0) + rk) - P0
                                : (int64_t)sempty[w][pre + (rk - slots)];
         ocol[s + q] = f;
         oval[s + q] = ival[s + i];
