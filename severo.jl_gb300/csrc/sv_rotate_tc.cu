@@ -295,11 +295,8 @@ bool sv_rotate_tc_supported(int nin, int nout, int64_t ld_in) {
 void sv_rotate_tc(sv_context* ctx, const float* inh, const float* inl, int64_t ld_in, int64_t len, int nin,
                   const double* M, int nout, float* outh, float* outl, int64_t ld_out, unsigned char* bsl,
                   int* fexp) {
-  static bool attr = false;
-  if (!attr) {
-    SV_CUDA(cudaFuncSetAttribute(k_rotate_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RT_SMEM));
-    attr = true;
-  }
+  // per call: the attribute belongs to the current device
+  SV_CUDA(cudaFuncSetAttribute(k_rotate_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RT_SMEM));
   sv_launch(ctx, "irlba_rotate_tc_b", k_rotate_tc_bslices, dim3(RT_N), dim3(RT_K), 0, M, nin, nout, bsl, fexp);
   CUtensorMap mh, ml;
   cuuint64_t gdim[2] = {(cuuint64_t)len, (cuuint64_t)nin};
