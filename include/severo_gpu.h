@@ -181,15 +181,33 @@ int sv_counts_select_cells(sv_context* ctx, const sv_counts* counts, int64_t r0,
 
 /* ---- find_variable_features(:vst) (src/variablefeatures.jl:19-50,128-160) ----
  * Per-gene mean and std (n - 1) of the counts; over the genes with std > 0 a
- * local quadratic regression (loess, span loess_span, tricube weights,
- * evaluated directly at every gene) of log10(std) on log10(mean); expected std
- * 10^fit (NaN -> 0); metric = variance of min((x - mean)/expected std,
- * sqrt(n_cells)) over all cells (implicit zeros included).  features receives
- * the nfeatures genes of largest metric (1-based, largest first, ties by
- * index); metric (n_genes) may be NULL.  The reference's Loess.jl interpolates
- * the same fit between kd-tree vertices; that interpolation is not restated. */
+ * local quadratic regression (loess, span loess_span, tricube weights) of
+ * log10(std) on log10(mean); expected std 10^fit (NaN -> 0); metric = variance
+ * of min((x - mean)/expected std, sqrt(n_cells)) over all cells (implicit
+ * zeros included).  features receives the nfeatures genes of largest metric
+ * (1-based, largest first, ties by index); metric (n_genes) may be NULL.
+ * surface selects how the fit is evaluated at the genes:
+ *   SV_LOESS_INTERPOLATE  fits at the vertices of the kd-tree that Loess.jl's
+ *                         loess builds (cells of at most ceil(0.2 span n)
+ *                         genes), blended linearly inside each cell: the
+ *                         loess / predict calls of variablefeatures.jl:41-42
+ *   SV_LOESS_HERMITE      the same vertices, cubic Hermite blend of the
+ *                         vertex fits' values and slopes
+ *   SV_LOESS_DIRECT       the local fit evaluated at every gene
+ * sv_find_variable_features_vst is the call with SV_LOESS_INTERPOLATE. */
+#define SV_LOESS_INTERPOLATE 0
+#define SV_LOESS_HERMITE     1
+#define SV_LOESS_DIRECT      2
 int sv_find_variable_features_vst(sv_context* ctx, const sv_counts* counts, int64_t nfeatures,
                                   double loess_span, int64_t* features, double* metric);
+int sv_find_variable_features_vst_surface(sv_context* ctx, const sv_counts* counts, int64_t nfeatures,
+                                          double loess_span, int surface, int64_t* features,
+                                          double* metric);
+/* The leaf bounds b_0 <= b_1 <= ... of that kd-tree over n sorted values xs
+ * (leaf i is [b_i, b_i+1]; b_0 and the last are the extremes): writes
+ * min(count, cap) of them and returns the count, or SV_ERR_ARG (xs unsorted,
+ * n < 1, span <= 0).  Host only: needs no device. */
+int64_t sv_loess_vertices(const double* xs, int64_t n, double loess_span, double* bounds, int64_t cap);
 
 /* ---- normalize_cells (src/normalize.jl:17-55,76-79) -------------------------
  * method SV_LOGNORMALIZE or SV_RELATIVECOUNTS; value dtype SV_F64 (the

@@ -744,61 +744,171 @@ def synth_counts(n_cells, n_genes, mu_mean=-1.0, mu_sd=1.5, depth=1.0, size_sd=0
     return X
 
 
+def _loess_window(xs, q, x0):
+    """First a with x0 - xs[a] <= xs[a + q] - x0 over sorted xs: [a, a + q) are
+    the q nearest points to x0 (ties in distance toward the lower index)."""
+    lo, hi = 0, len(xs) - q
+    while lo < hi:
+        mid = (lo + hi) >> 1
+        if (x0 - xs[mid]) > (xs[mid + q] - x0):
+            lo = mid + 1
+        else:
+            hi = mid
+    return lo
+
+
+def loess_fit_at(xs, ys, q, x0, flat="ones"):
+    """The local quadratic fit of loess at x0 (any point, not only a data
+    point): the q nearest of the sorted xs, tricube weights (1 - (d / d_q)^3)^3
+    with d_q the largest distance among them, weighted least squares in the
+    centred x - x0.  Returns (value, slope) of the fitted polynomial at x0.
+    flat: what a window of zero width (d_q = 0) gives -- "ones" (unit weights)
+    or "nan" (the 0/0 of the weight formula, as Loess.jl computes it)."""
+    a = _loess_window(xs, q, x0)
+    win = slice(a, a + q)
+    t = xs[win] - x0
+    d = np.abs(t)
+    dq = max(x0 - xs[a], xs[a + q - 1] - x0)
+    if dq > 0:
+        w = (1.0 - (d / dq) ** 3) ** 3
+    elif flat == "nan":
+        return math.nan, math.nan
+    else:
+        w = np.ones(q)
+    s0, s1, s2, s3, s4 = (np.sum(w * t ** k) for k in range(5))
+    r0, r1, r2 = (np.sum(w * t ** k * ys[win]) for k in range(3))
+    M = np.array([[s0, s1, s2], [s1, s2, s3], [s2, s3, s4]])
+    try:
+        beta = np.linalg.solve(M, [r0, r1, r2])
+    except np.linalg.LinAlgError:
+        beta = np.linalg.lstsq(M, [r0, r1, r2], rcond=None)[0]
+    return float(beta[0]), float(beta[1])
+
+
+def _loess_q(n, span):
+    return max(3, min(n, int(np.floor(n * span))))
+
+
 def loess_direct(x, y, span=0.5):
     """Local quadratic regression (Cleveland 1979; Cleveland & Grosse 1991),
-    evaluated directly at every x: the q = floor(n * span) nearest x (a
-    contiguous window of the sorted x; ties in distance resolved toward the
-    lower index), tricube weights (1 - (d / d_q)^3)^3 with d_q the largest
-    distance in the window, weighted least squares in the centred x - x0.
-    Returns the fitted values at x (in the input order).  The reference calls
-    Loess.jl (loess(xs, ys, span), degree 2, src/variablefeatures.jl:41), whose
-    default evaluates this fit at kd-tree vertices and interpolates between
-    them; this direct form is the fit itself, not that interpolation."""
+    evaluated directly at every x (loess_fit_at with q = floor(n * span)).
+    Returns the fitted values at x (in the input order)."""
     x = np.asarray(x, dtype=np.float64)
     y = np.asarray(y, dtype=np.float64)
     n = len(x)
-    q = max(3, min(n, int(np.floor(n * span))))
+    q = _loess_q(n, span)
     order = np.argsort(x, kind="stable")
     xs, ys = x[order], y[order]
     out = np.empty(n)
-    a = 0
     for i in range(n):
-        x0 = xs[i]
-        # slide the window [a, a + q) while the next point is strictly closer
-        while a + q < n and (x0 - xs[a]) > (xs[a + q] - x0):
-            a += 1
-        win = slice(a, a + q)
-        d = np.abs(xs[win] - x0)
-        dq = d.max()
-        if dq > 0:
-            w = (1.0 - (d / dq) ** 3) ** 3
-        else:
-            w = np.ones(q)
-        t = xs[win] - x0
-        s0, s1, s2, s3, s4 = (np.sum(w * t ** k) for k in range(5))
-        r0, r1, r2 = (np.sum(w * t ** k * ys[win]) for k in range(3))
-        M = np.array([[s0, s1, s2], [s1, s2, s3], [s2, s3, s4]])
-        try:
-            beta = np.linalg.solve(M, [r0, r1, r2])
-        except np.linalg.LinAlgError:
-            beta = np.linalg.lstsq(M, [r0, r1, r2], rcond=None)[0]
-        out[order[i]] = beta[0]
+        out[order[i]] = loess_fit_at(xs, ys, q, xs[i])[0]
     return out
 
 
-def vst_metric(A, loess_span=0.5):
+LOESS_CELL = 0.2
+
+
+def loess_kdtree_cells(xs, span, cell=LOESS_CELL):
+    """The one-dimensional kd-tree over which Loess.jl (the package the
+    reference calls, src/variablefeatures.jl:15,41; Cleveland & Grosse 1991)
+    interpolates its fit, over sorted xs.  A cell holding L points is split
+    when L > ceil(cell * span * n) and it has a positive width: at the
+    (L div 2)-th smallest of its points for odd L, at the mean of the
+    (L/2)-th and (L/2 + 1)-th for even L; the smaller half goes left.  The
+    vertices are the extremes of xs and every split value.  Returns the leaf
+    boundaries b_0 <= b_1 <= ... <= b_L in order (leaf i is [b_i, b_i+1])."""
+    n = len(xs)
+    cutoff = math.ceil((cell * span) * n)
+    bounds = [xs[0]]
+    stack = [(0, n, xs[0], xs[-1])]
+    while stack:                      # depth first, left before right
+        s, e, lo, hi = stack.pop()
+        L = e - s
+        if L <= cutoff or hi - lo <= 0:
+            bounds.append(hi)
+            continue
+        mid = L // 2
+        med = xs[s + mid - 1] if L % 2 else (xs[s + mid - 1] + xs[s + mid]) / 2
+        stack.append((s + mid, e, med, hi))
+        stack.append((s, s + mid, lo, med))
+    return np.array(bounds)
+
+
+def loess_kdtree(x, y, span=0.5, blend="linear", cell=LOESS_CELL):
+    """loess(xs, ys, span) then predict(model, xs) as the reference calls them
+    (src/variablefeatures.jl:40-42): the local fit (loess_fit_at, zero-width
+    windows giving NaN) at every vertex of the kd-tree (loess_kdtree_cells);
+    a point z takes the first leaf in order whose upper bound is >= z (the
+    leaf that the tree's descent, left when z <= split, reaches) and blends
+    the two vertex fits of that leaf:
+      "linear"  (1 - u) f(lo) + u f(hi), u = (z - lo) / (hi - lo) -- NaN in a
+                zero-width leaf, which the reference's nan2zero! turns into an
+                expected std of 0 (src/variablefeatures.jl:46-47);
+      "hermite" cubic Hermite with the fits' values and slopes at lo and hi,
+                a vertex's own value at z = lo or z = hi.
+    Returns the values at x (in the input order)."""
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    n = len(x)
+    q = _loess_q(n, span)
+    order = np.argsort(x, kind="stable")
+    xs, ys = x[order], y[order]
+    b = loess_kdtree_cells(xs, span, cell)
+    fits = {}
+    for v in b:
+        if v not in fits:
+            fits[v] = loess_fit_at(xs, ys, q, v, flat="nan")
+    out = np.empty(n)
+    for i in range(n):
+        z = x[i]
+        k = int(np.searchsorted(b[1:], z, side="left"))   # first upper bound >= z
+        lo, hi = b[k], b[k + 1]
+        (f0, d0), (f1, d1) = fits[lo], fits[hi]
+        h = hi - lo
+        if blend == "linear":
+            u = (z - lo) / h if h != 0 else math.nan
+            out[i] = (1.0 - u) * f0 + u * f1
+        elif z == lo:
+            out[i] = f0
+        elif z == hi:
+            out[i] = f1
+        else:
+            t = (z - lo) / h
+            t2, t3 = t * t, t * t * t
+            out[i] = ((2 * t3 - 3 * t2 + 1) * f0 + (t3 - 2 * t2 + t) * h * d0
+                      + (-2 * t3 + 3 * t2) * f1 + (t3 - t2) * h * d1)
+    return out
+
+
+LOESS_SURFACES = ("interpolate", "hermite", "direct")
+
+
+def loess_surface(x, y, span=0.5, surface="interpolate"):
+    """The fitted log10 std per gene for the three surfaces the device offers."""
+    if surface == "direct":
+        return loess_direct(x, y, span)
+    if surface == "interpolate":
+        return loess_kdtree(x, y, span, "linear")
+    if surface == "hermite":
+        return loess_kdtree(x, y, span, "hermite")
+    raise ValueError(f"unknown loess surface: {surface}")
+
+
+def vst_metric(A, loess_span=0.5, surface="interpolate"):
     """src/variablefeatures.jl:19-50: per-gene mean and std of the counts (n - 1),
-    loess of log10(std) on log10(mean) over the non-constant genes, expected
-    std = 10^fit (NaN -> 0), then the variance of the standardised values
-    clipped at sqrt(n_cells) (implicit zeros included).  A: cells x genes CSC."""
+    loess of log10(std) on log10(mean) over the non-constant genes (surface:
+    loess_surface), expected std = 10^fit (NaN -> 0), then the variance of the
+    standardised values clipped at sqrt(n_cells) (implicit zeros included).
+    A: cells x genes CSC."""
     A = _as_csc(A)
     n = A.shape[0]
     mu, var = mean_var(A.astype(np.float64))
     sd = np.sqrt(var)
     nc = sd > 0
     exp_sd = sd.copy()
-    fit = loess_direct(np.log10(mu[nc]), np.log10(sd[nc]), loess_span)
-    exp_sd[nc] = 10.0 ** fit
+    fit = loess_surface(np.log10(mu[nc]), np.log10(sd[nc]), loess_span, surface)
+    with np.errstate(invalid="ignore"):
+        exp_sd[nc] = 10.0 ** fit
     exp_sd[np.isnan(exp_sd)] = 0.0
     vmax = math.sqrt(n)
     out = np.zeros(A.shape[1])
@@ -812,10 +922,10 @@ def vst_metric(A, loess_span=0.5):
     return out
 
 
-def find_variable_features_vst(A, nfeatures=2000, loess_span=0.5):
+def find_variable_features_vst(A, nfeatures=2000, loess_span=0.5, surface="interpolate"):
     """src/variablefeatures.jl:128-160 with method=:vst: the nfeatures genes of
     largest vst metric, 1-based, in decreasing metric order (ties by index)."""
-    m = vst_metric(A, loess_span)
+    m = vst_metric(A, loess_span, surface)
     order = np.lexsort((np.arange(len(m)), -m))[:nfeatures]
     return order + 1, m
 

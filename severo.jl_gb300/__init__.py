@@ -349,17 +349,28 @@ def filter_features(X: CountMatrix, min_cells=0):
     return A, fi
 
 
-def find_variable_features(X: CountMatrix, nfeatures=2000, method="vst", loess_span=0.5):
+LOESS_SURFACES = {"interpolate": 0, "hermite": 1, "direct": 2}
+
+
+def find_variable_features(X: CountMatrix, nfeatures=2000, method="vst", loess_span=0.5,
+                           loess_surface="interpolate"):
     """src/variablefeatures.jl:128-160 with method=:vst on the device counts:
-    (features 1-based, largest metric first; metric per gene)."""
+    (features 1-based, largest metric first; metric per gene).  loess_surface:
+    "interpolate" (the kd-tree vertex fits blended linearly, as the reference's
+    loess / predict calls evaluate them), "hermite" (the same vertices, cubic
+    Hermite blend) or "direct" (the local fit at every gene)."""
     if str(method).lstrip(":") != "vst":
         raise ValueError("only method=:vst runs on the device")
+    surface = str(loess_surface).lstrip(":")
+    if surface not in LOESS_SURFACES:
+        raise ValueError(f"unknown loess surface: {loess_surface}")
     ctx = X.ctx
     n_genes = X.shape[1]
     feats = np.zeros(nfeatures, np.int64)
     metric = np.zeros(n_genes)
-    L.check(ctx.lib.sv_find_variable_features_vst(ctx.h, X.h, int(nfeatures), float(loess_span),
-                                                  _ptr(feats), _ptr(metric)))
+    L.check(ctx.lib.sv_find_variable_features_vst_surface(ctx.h, X.h, int(nfeatures), float(loess_span),
+                                                          LOESS_SURFACES[surface], _ptr(feats),
+                                                          _ptr(metric)))
     return feats, metric
 
 

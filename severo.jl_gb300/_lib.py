@@ -83,6 +83,8 @@ SIGNATURES = {
     "sv_filter_counts": (i32, [vp, vp, i64, i64, i64, i64, vp, vp, P(vp)]),
     "sv_counts_select_cells": (i32, [vp, vp, i64, i64, P(vp)]),
     "sv_find_variable_features_vst": (i32, [vp, vp, i64, C.c_double, vp, vp]),
+    "sv_find_variable_features_vst_surface": (i32, [vp, vp, i64, C.c_double, i32, vp, vp]),
+    "sv_loess_vertices": (i64, [vp, i64, C.c_double, vp, i64]),
     "sv_normalize_cells": (i32, [vp, vp, i32, dbl, i32, P(vp)]),
     "sv_selftest_wait_timeout": (i32, [vp, C.c_longlong]),
     "sv_centered_gram": (i32, [vp, vp, vp, dbl, dbl, vp]),
@@ -135,7 +137,7 @@ def header_symbols():
     """Function names declared in include/severo_gpu.h."""
     text = HEADER.read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    names = re.findall(r"^\s*(?:int|void)\s+\**\s*([A-Za-z_]\w*)\s*\(", text, flags=re.M)
+    names = re.findall(r"^\s*(?:int64_t|int|void)\s+\**\s*([A-Za-z_]\w*)\s*\(", text, flags=re.M)
     return sorted(set(names))
 
 

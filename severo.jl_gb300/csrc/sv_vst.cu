@@ -4,12 +4,22 @@
 // genes, the expected std 10^fit, and the variance of the standardised counts
 // clipped at sqrt(n_cells); the nfeatures genes of largest variance.
 //
-// The regression is loess (Cleveland 1979; Cleveland & Grosse 1991) evaluated
-// directly at every gene: the q = floor(span * n) nearest genes in log10(mean)
-// (a contiguous window of the sorted values), tricube weights, weighted least
-// squares in x - x0, FP64.  The reference calls Loess.jl, whose default
-// interpolates this fit between kd-tree vertices; that interpolation is not
-// restated, so the metric agrees with the reference to the interpolation error.
+// The regression is loess (Cleveland 1979; Cleveland & Grosse 1991): the local
+// fit at a point x0 takes the q = floor(span * n) nearest genes in log10(mean)
+// (a contiguous window of the sorted values), tricube weights and weighted
+// least squares in x - x0, FP64.  The reference calls Loess.jl's
+// loess(xs, ys, span) and predict (variablefeatures.jl:41-42), which fits at
+// the vertices of a kd-tree over xs and blends the two vertex fits of the
+// cell holding each gene.  Three surfaces:
+//   SV_LOESS_INTERPOLATE  kd-tree vertices, linear blend (NaN in a cell of
+//                         zero width, or at a vertex whose q nearest genes
+//                         all share its x: the reference's nan2zero! makes
+//                         the expected std 0 and the metric 0 there)
+//   SV_LOESS_HERMITE      kd-tree vertices, cubic Hermite blend of the fits'
+//                         values and slopes
+//   SV_LOESS_DIRECT       the local fit evaluated at every gene
+// The kd-tree (a few dozen vertices) is built on the host from the sorted x;
+// the fits and the blend run on the device.
 #include "sv_internal.cuh"
 #include <math.h>
 
@@ -17,14 +27,18 @@ void sv_count_moments(sv_context* ctx, const sv_counts* C, double* mean, double*
 
 namespace {
 
-// One thread per evaluation point (sorted x): the window [a, a + q) is the
-// first a with x0 - x[a] <= x[a + q] - x0 (binary search: the difference falls
-// with a), then the weighted normal equations of the quadratic.
+// One thread per evaluation point x0 (any value in [x[0], x[n-1]]): the window
+// [a, a + q) is the first a with x0 - x[a] <= x[a + q] - x0 (binary search:
+// the difference falls with a), then the weighted normal equations of the
+// quadratic in x - x0.  val = its value at x0, slope (may be null) = its
+// derivative.  A window of zero width gives unit weights, or NaN when
+// flat_nan is set (the 0/0 of the weight formula).
 __global__ void k_loess(const double* __restrict__ xs, const double* __restrict__ ys, int64_t n, int64_t q,
-                        double* __restrict__ fit) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+                        const double* __restrict__ x0s, int64_t m, int flat_nan, double* __restrict__ val,
+                        double* __restrict__ slope) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
        i += (int64_t)gridDim.x * blockDim.x) {
-    double x0 = xs[i];
+    double x0 = x0s[i];
     int64_t lo = 0, hi = n - q;   // answer in [0, n - q]
     while (lo < hi) {
       int64_t mid = (lo + hi) >> 1;
@@ -33,6 +47,11 @@ __global__ void k_loess(const double* __restrict__ xs, const double* __restrict_
     }
     int64_t a = lo;
     double dq = fmax(x0 - xs[a], xs[a + q - 1] - x0);
+    if (dq <= 0 && flat_nan) {
+      val[i] = nan("");
+      if (slope) slope[i] = nan("");
+      continue;
+    }
     double s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, r0 = 0, r1 = 0, r2 = 0;
     for (int64_t j = a; j < a + q; ++j) {
       double t = xs[j] - x0;
@@ -72,8 +91,75 @@ __global__ void k_loess(const double* __restrict__ xs, const double* __restrict_
     double b2 = M[2][2] != 0.0 ? M[2][3] / M[2][2] : 0.0;
     double b1 = M[1][1] != 0.0 ? (M[1][3] - M[1][2] * b2) / M[1][1] : 0.0;
     double b0 = M[0][0] != 0.0 ? (M[0][3] - M[0][1] * b1 - M[0][2] * b2) / M[0][0] : 0.0;
-    fit[i] = b0;
+    val[i] = b0;
+    if (slope) slope[i] = b1;
   }
+}
+
+// One thread per point z of xs: the first leaf k whose upper bound bnd[k + 1]
+// is >= z (the leaf the tree's descent reaches, left when z <= split), then the
+// blend of the fits at its bounds (vval / vslope indexed like bnd).
+__global__ void k_loess_blend(const double* __restrict__ xs, int64_t n, const double* __restrict__ bnd,
+                              int64_t nb, const double* __restrict__ vval, const double* __restrict__ vslope,
+                              int hermite, double* __restrict__ fit) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double z = xs[i];
+    int64_t lo = 1, hi = nb - 1;   // first index in [1, nb - 1] with bnd >= z
+    while (lo < hi) {
+      int64_t mid = (lo + hi) >> 1;
+      if (bnd[mid] < z) lo = mid + 1;
+      else hi = mid;
+    }
+    int64_t k = lo - 1;
+    double x0 = bnd[k], x1 = bnd[k + 1], f0 = vval[k], f1 = vval[k + 1];
+    double h = x1 - x0;
+    double y;
+    if (!hermite) {
+      double u = (z - x0) / h;     // 0/0 = NaN in a cell of zero width
+      y = (1.0 - u) * f0 + u * f1;
+    } else if (z == x0) {
+      y = f0;
+    } else if (z == x1) {
+      y = f1;
+    } else {
+      double t = (z - x0) / h, t2 = t * t, t3 = t2 * t;
+      y = (2 * t3 - 3 * t2 + 1) * f0 + (t3 - 2 * t2 + t) * h * vslope[k] + (-2 * t3 + 3 * t2) * f1 +
+          (t3 - t2) * h * vslope[k + 1];
+    }
+    fit[i] = y;
+  }
+}
+
+// The leaf bounds b_0 <= ... <= b_L of the kd-tree over the sorted xs (leaf i
+// is [b_i, b_i+1]): a cell of L points is split when L > ceil(cell * span * n)
+// and it has a positive width, at the (L div 2)-th smallest of its points for
+// odd L, at the mean of the (L/2)-th and (L/2 + 1)-th for even L, the smaller
+// half going left.
+std::vector<double> loess_kdtree_bounds(const std::vector<double>& xs, double span) {
+  const int64_t n = (int64_t)xs.size();
+  const double cell = 0.2;
+  const int64_t cutoff = (int64_t)ceil((cell * span) * (double)n);
+  std::vector<double> b{xs[0]};
+  struct Node {
+    int64_t s, e;
+    double lo, hi;
+  };
+  std::vector<Node> stack{{0, n, xs[0], xs[n - 1]}};
+  while (!stack.empty()) {
+    Node c = stack.back();
+    stack.pop_back();
+    const int64_t L = c.e - c.s;
+    if (L <= cutoff || c.hi - c.lo <= 0) {
+      b.push_back(c.hi);
+      continue;
+    }
+    const int64_t mid = L / 2;
+    const double med = (L & 1) ? xs[c.s + mid - 1] : (xs[c.s + mid - 1] + xs[c.s + mid]) / 2;
+    stack.push_back({c.s + mid, c.e, med, c.hi});
+    stack.push_back({c.s, c.s + mid, c.lo, med});
+  }
+  return b;
 }
 
 // one warp per gene: sum of min((x - mu) / esd, vmax)^2 over the stored
@@ -107,14 +193,17 @@ __global__ void k_vst_var(const int64_t* __restrict__ colptr, const int32_t* __r
 
 }  // namespace
 
-SV_API int sv_find_variable_features_vst(sv_context* ctx, const sv_counts* C, int64_t nfeatures,
-                                         double loess_span, int64_t* features, double* metric) {
+SV_API int sv_find_variable_features_vst_surface(sv_context* ctx, const sv_counts* C, int64_t nfeatures,
+                                                 double loess_span, int surface, int64_t* features,
+                                                 double* metric) {
   SV_TRY
   sv_ctx_check(ctx);
   SV_REQUIRE(C && C->ctx == ctx, "bad count-matrix handle");
   SV_REQUIRE(C->n_cells >= 2, "need at least two cells for a variance");
   SV_REQUIRE(nfeatures >= 0 && nfeatures <= C->n_genes, "nfeatures must be in 0..n_genes");
   SV_REQUIRE(loess_span > 0, "loess span must be positive");
+  SV_REQUIRE(surface == SV_LOESS_INTERPOLATE || surface == SV_LOESS_HERMITE || surface == SV_LOESS_DIRECT,
+             "unknown loess surface");
   const int64_t ng = C->n_genes;
   DevBuf<double> mean(ng), sd(ng);
   sv_count_moments(ctx, C, mean.get(), sd.get());
@@ -146,8 +235,22 @@ SV_API int sv_find_variable_features_vst(sv_context* ctx, const sv_counts* C, in
     DevBuf<double> dx(n), dy(n), df(n);
     sv_h2d(ctx, dx.get(), xs.data(), n * 8);
     sv_h2d(ctx, dy.get(), ys.data(), n * 8);
-    sv_launch(ctx, "vst_loess", k_loess, dim3(sv_grid_for(ctx, n, 128, 4)), dim3(128), 0,
-              (const double*)dx.get(), (const double*)dy.get(), n, q, df.get());
+    if (surface == SV_LOESS_DIRECT) {
+      sv_launch(ctx, "vst_loess", k_loess, dim3(sv_grid_for(ctx, n, 128, 4)), dim3(128), 0,
+                (const double*)dx.get(), (const double*)dy.get(), n, q, (const double*)dx.get(), n, 0,
+                df.get(), (double*)nullptr);
+    } else {
+      std::vector<double> bnd = loess_kdtree_bounds(xs, loess_span);
+      const int64_t nb = (int64_t)bnd.size();   // >= 2: the extremes
+      DevBuf<double> db(nb), dv(nb), ds(nb);
+      sv_h2d(ctx, db.get(), bnd.data(), nb * 8);
+      sv_launch(ctx, "vst_loess_vertices", k_loess, dim3(sv_grid_for(ctx, nb, 128, 4)), dim3(128), 0,
+                (const double*)dx.get(), (const double*)dy.get(), n, q, (const double*)db.get(), nb, 1,
+                dv.get(), ds.get());
+      sv_launch(ctx, "vst_loess_blend", k_loess_blend, dim3(sv_grid_for(ctx, n, 128, 4)), dim3(128), 0,
+                (const double*)dx.get(), n, (const double*)db.get(), nb, (const double*)dv.get(),
+                (const double*)ds.get(), surface == SV_LOESS_HERMITE ? 1 : 0, df.get());
+    }
     sv_d2h(ctx, fit.data(), df.get(), n * 8);
     for (int64_t i = 0; i < n; ++i) {
       double e = pow(10.0, fit[i]);
@@ -172,4 +275,20 @@ SV_API int sv_find_variable_features_vst(sv_context* ctx, const sv_counts* C, in
     for (int64_t i = 0; i < nfeatures; ++i) features[i] = idx[i] + 1;
   }
   SV_CATCH
+}
+
+SV_API int sv_find_variable_features_vst(sv_context* ctx, const sv_counts* C, int64_t nfeatures,
+                                         double loess_span, int64_t* features, double* metric) {
+  return sv_find_variable_features_vst_surface(ctx, C, nfeatures, loess_span, SV_LOESS_INTERPOLATE, features,
+                                               metric);
+}
+
+SV_API int64_t sv_loess_vertices(const double* xs, int64_t n, double loess_span, double* bounds, int64_t cap) {
+  if (!xs || n < 1 || !(loess_span > 0) || (cap > 0 && !bounds)) return SV_ERR_ARG;
+  for (int64_t i = 1; i < n; ++i)
+    if (!(xs[i - 1] <= xs[i])) return SV_ERR_ARG;
+  std::vector<double> v(xs, xs + n);
+  std::vector<double> b = loess_kdtree_bounds(v, loess_span);
+  for (int64_t i = 0; i < (int64_t)b.size() && i < cap; ++i) bounds[i] = b[i];
+  return (int64_t)b.size();
 }

@@ -1,5 +1,7 @@
 """GPU parity: find_variable_features(:vst) (src/variablefeatures.jl:19-50,128-160)
-against the oracle's restatement (direct loess)."""
+against the oracle's restatement, for each loess surface: the kd-tree vertex fits
+blended linearly (the reference's loess / predict), blended by cubic Hermite, and
+the fit evaluated directly at every gene."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -7,15 +9,16 @@ import scipy.sparse as sp
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("surface", ["interpolate", "hermite", "direct"])
 @pytest.mark.parametrize("span", [0.5, 0.3])
-def test_vst_matches_oracle(sv, ctx, O, span):
+def test_vst_matches_oracle(sv, ctx, O, span, surface):
     X = O.synth_counts(4000, 3000, -1.2, 1.6, depth=0.4, seed=71, n_clusters=6)
     X = sp.csc_matrix(X)
     X[:, 5] = 0                       # constant genes: metric 0
     X.eliminate_zeros()
     C = sv.CountMatrix.from_csc(X, ctx=ctx)
-    feats, metric = sv.find_variable_features(C, 500, loess_span=span)
-    rf, rm = O.find_variable_features_vst(X, 500, loess_span=span)
+    feats, metric = sv.find_variable_features(C, 500, loess_span=span, loess_surface=surface)
+    rf, rm = O.find_variable_features_vst(X, 500, loess_span=span, surface=surface)
     assert metric[5] == 0.0 and rm[5] == 0.0
     assert np.allclose(metric, rm, rtol=1e-9, atol=1e-12)
     # the selection agrees except where two metrics tie within the tolerance
@@ -29,3 +32,38 @@ def test_vst_selection_order(sv, ctx, O):
     feats, metric = sv.find_variable_features(C, 100)
     assert np.all(np.diff(metric[feats - 1]) <= 0)
     assert len(np.unique(feats)) == 100
+
+
+def _singles_and_rich(single, rich, n_cells=400, seed=5):
+    import scipy.sparse as sp
+    rng = np.random.default_rng(seed)
+    cols = []
+    for g in range(single):
+        c = np.zeros(n_cells, np.int64)
+        c[rng.integers(n_cells)] = 1
+        cols.append(c)
+    for g in range(rich):
+        cols.append(rng.poisson(0.2 + 0.1 * g, n_cells))
+    return sp.csc_matrix(np.stack(cols, axis=1).astype(np.int32))
+
+
+@pytest.mark.parametrize("single,rich", [(36, 84), (70, 50)])
+def test_vst_zero_width_cells(sv, ctx, O, single, rich):
+    """Genes at the lowest mean filling a zero-width first cell (36 of 120) or the
+    whole window of the vertex there (70 of 120): the device gives the oracle's
+    metric 0 to exactly the same genes under every surface."""
+    X = _singles_and_rich(single, rich)
+    C = sv.CountMatrix.from_csc(X, ctx=ctx)
+    for surf in ("interpolate", "hermite", "direct"):
+        _, metric = sv.find_variable_features(C, 10, loess_surface=surf)
+        rm = O.vst_metric(X, 0.5, surf)
+        assert np.array_equal(metric == 0.0, rm == 0.0), surf
+        assert np.allclose(metric, rm, rtol=1e-9, atol=1e-12), surf
+
+
+def test_vst_unknown_surface_raises(sv, ctx, O):
+    X = O.synth_counts(200, 50, seed=3)
+    C = sv.CountMatrix.from_csc(X, ctx=ctx)
+    with pytest.raises(ValueError):
+        sv.find_variable_features(C, 5, loess_surface="cubic")
+
