@@ -887,6 +887,20 @@ def kernel_case(args):
         ctx.sync()
         out = {"kernel_case": "prep", "n_cells": n, "kept_cells": int(ci.sum()), "kept_genes": int(fi.sum()),
                "filter_s": round(t1 - t0, 4), "vst_s": round(time.perf_counter() - t1, 4)}
+        # per-kernel device times (CUDA events) of vst under each loess surface
+        sel = {}
+        for surf in ("interpolate", "hermite", "direct"):
+            ctx.profile(True)
+            ctx.profile_reset()
+            t2 = time.perf_counter()
+            f2, _ = sv.find_variable_features(F, w["n_hvf"], loess_surface=surf)
+            ctx.sync()
+            out[f"vst_{surf}"] = {"s": round(time.perf_counter() - t2, 4),
+                                  "kernels_ms": {k: round(v[1], 3) for k, v in ctx.profile_report().items()}}
+            ctx.profile(False)
+            sel[surf] = set(f2.tolist())
+        out["vst_selection_overlap_vs_direct"] = {
+            s: round(len(sel[s] & sel["direct"]) / max(1, len(sel["direct"])), 4) for s in ("interpolate", "hermite")}
     else:
         n, d = args.cells or 400_000, 50
         means = rng.normal(0, 4, (60, d))

@@ -27,33 +27,39 @@ void sv_count_moments(sv_context* ctx, const sv_counts* C, double* mean, double*
 
 namespace {
 
-// One thread per evaluation point x0 (any value in [x[0], x[n-1]]): the window
+// One block per evaluation point x0 (any value in [x[0], x[n-1]]): the window
 // [a, a + q) is the first a with x0 - x[a] <= x[a + q] - x0 (binary search:
-// the difference falls with a), then the weighted normal equations of the
-// quadratic in x - x0.  val = its value at x0, slope (may be null) = its
+// the difference falls with a); the block's threads stride over the window
+// summing the weighted moments, then one thread solves the normal equations of
+// the quadratic in x - x0.  val = its value at x0, slope (may be null) = its
 // derivative.  A window of zero width gives unit weights, or NaN when
 // flat_nan is set (the 0/0 of the weight formula).
-__global__ void k_loess(const double* __restrict__ xs, const double* __restrict__ ys, int64_t n, int64_t q,
-                        const double* __restrict__ x0s, int64_t m, int flat_nan, double* __restrict__ val,
-                        double* __restrict__ slope) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    double x0 = x0s[i];
+constexpr int LOESS_THREADS = 256;
+__global__ void __launch_bounds__(LOESS_THREADS)
+    k_loess(const double* __restrict__ xs, const double* __restrict__ ys, int64_t n, int64_t q,
+            const double* __restrict__ x0s, int64_t m, int flat_nan, double* __restrict__ val,
+            double* __restrict__ slope) {
+  __shared__ double part[LOESS_THREADS / 32][8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t i = blockIdx.x; i < m; i += gridDim.x) {
+    const double x0 = x0s[i];
     int64_t lo = 0, hi = n - q;   // answer in [0, n - q]
     while (lo < hi) {
       int64_t mid = (lo + hi) >> 1;
       if ((x0 - xs[mid]) > (xs[mid + q] - x0)) lo = mid + 1;
       else hi = mid;
     }
-    int64_t a = lo;
-    double dq = fmax(x0 - xs[a], xs[a + q - 1] - x0);
+    const int64_t a = lo;
+    const double dq = fmax(x0 - xs[a], xs[a + q - 1] - x0);
     if (dq <= 0 && flat_nan) {
-      val[i] = nan("");
-      if (slope) slope[i] = nan("");
+      if (threadIdx.x == 0) {
+        val[i] = nan("");
+        if (slope) slope[i] = nan("");
+      }
       continue;
     }
-    double s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, r0 = 0, r1 = 0, r2 = 0;
-    for (int64_t j = a; j < a + q; ++j) {
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // s0..s4, r0..r2
+    for (int64_t j = a + threadIdx.x; j < a + q; j += LOESS_THREADS) {
       double t = xs[j] - x0;
       double w = 1.0;
       if (dq > 0) {
@@ -61,38 +67,52 @@ __global__ void k_loess(const double* __restrict__ xs, const double* __restrict_
         double c = 1.0 - u * u * u;
         w = c * c * c;
       }
-      double wt = w * t, wt2 = wt * t;
-      s0 += w;
-      s1 += wt;
-      s2 += wt2;
-      s3 += wt2 * t;
-      s4 += wt2 * t * t;
-      r0 += w * ys[j];
-      r1 += wt * ys[j];
-      r2 += wt2 * ys[j];
+      double wt = w * t, wt2 = wt * t, y = ys[j];
+      acc[0] += w;
+      acc[1] += wt;
+      acc[2] += wt2;
+      acc[3] += wt2 * t;
+      acc[4] += wt2 * t * t;
+      acc[5] += w * y;
+      acc[6] += wt * y;
+      acc[7] += wt2 * y;
     }
-    // [s0 s1 s2; s1 s2 s3; s2 s3 s4] b = r: Gaussian elimination, partial pivoting
-    double M[3][4] = {{s0, s1, s2, r0}, {s1, s2, s3, r1}, {s2, s3, s4, r2}};
-    for (int c = 0; c < 3; ++c) {
-      int p = c;
-      for (int r = c + 1; r < 3; ++r)
-        if (fabs(M[r][c]) > fabs(M[p][c])) p = r;
-      if (p != c)
-        for (int k = 0; k < 4; ++k) {
-          double tmp = M[c][k];
-          M[c][k] = M[p][k];
-          M[p][k] = tmp;
-        }
-      for (int r = c + 1; r < 3; ++r) {
-        double f = M[c][c] != 0.0 ? M[r][c] / M[c][c] : 0.0;
-        for (int k = c; k < 4; ++k) M[r][k] -= f * M[c][k];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc[k] = sv_warp_sum(acc[k]);
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < 8; ++k) part[warp][k] = acc[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double S[8];
+      for (int k = 0; k < 8; ++k) {
+        S[k] = 0;
+        for (int w = 0; w < LOESS_THREADS / 32; ++w) S[k] += part[w][k];
       }
+      // [s0 s1 s2; s1 s2 s3; s2 s3 s4] b = r: Gaussian elimination, partial pivoting
+      double M[3][4] = {{S[0], S[1], S[2], S[5]}, {S[1], S[2], S[3], S[6]}, {S[2], S[3], S[4], S[7]}};
+      for (int c = 0; c < 3; ++c) {
+        int p = c;
+        for (int r = c + 1; r < 3; ++r)
+          if (fabs(M[r][c]) > fabs(M[p][c])) p = r;
+        if (p != c)
+          for (int k = 0; k < 4; ++k) {
+            double tmp = M[c][k];
+            M[c][k] = M[p][k];
+            M[p][k] = tmp;
+          }
+        for (int r = c + 1; r < 3; ++r) {
+          double f = M[c][c] != 0.0 ? M[r][c] / M[c][c] : 0.0;
+          for (int k = c; k < 4; ++k) M[r][k] -= f * M[c][k];
+        }
+      }
+      double b2 = M[2][2] != 0.0 ? M[2][3] / M[2][2] : 0.0;
+      double b1 = M[1][1] != 0.0 ? (M[1][3] - M[1][2] * b2) / M[1][1] : 0.0;
+      double b0 = M[0][0] != 0.0 ? (M[0][3] - M[0][1] * b1 - M[0][2] * b2) / M[0][0] : 0.0;
+      val[i] = b0;
+      if (slope) slope[i] = b1;
     }
-    double b2 = M[2][2] != 0.0 ? M[2][3] / M[2][2] : 0.0;
-    double b1 = M[1][1] != 0.0 ? (M[1][3] - M[1][2] * b2) / M[1][1] : 0.0;
-    double b0 = M[0][0] != 0.0 ? (M[0][3] - M[0][1] * b1 - M[0][2] * b2) / M[0][0] : 0.0;
-    val[i] = b0;
-    if (slope) slope[i] = b1;
+    __syncthreads();   // part is reused by the next point
   }
 }
 
@@ -163,7 +183,9 @@ std::vector<double> loess_kdtree_bounds(const std::vector<double>& xs, double sp
 }
 
 // one warp per gene: sum of min((x - mu) / esd, vmax)^2 over the stored
-// counts plus the implicit zeros' share, / (n - 1)
+// counts plus the implicit zeros' share, / (n - 1).  The square depends on the
+// count only: lane l holds it for the count l + 1, and a stored count in
+// 1..32 (nearly all of them) reads it from that lane instead of dividing.
 __global__ void k_vst_var(const int64_t* __restrict__ colptr, const int32_t* __restrict__ cnt,
                           int64_t n_genes, int64_t n_cells, const double* __restrict__ mu,
                           const double* __restrict__ esd, double vmax, double* __restrict__ out) {
@@ -177,11 +199,19 @@ __global__ void k_vst_var(const int64_t* __restrict__ colptr, const int32_t* __r
       continue;
     }
     double m = mu[g];
+    double zl = fmin(((double)(lane + 1) - m) / e, vmax);
+    double tab = zl * zl;
     int64_t s = colptr[g], t = colptr[g + 1];
     double acc = 0;
-    for (int64_t i = s + lane; i < t; i += 32) {
-      double z = fmin(((double)cnt[i] - m) / e, vmax);
-      acc += z * z;
+    for (int64_t b = s; b < t; b += 32) {   // every lane runs every round (the shuffle)
+      int64_t i = b + lane;
+      int c = i < t ? cnt[i] : 1;
+      double z2 = __shfl_sync(0xffffffffu, tab, (int)(((unsigned)c - 1u) & 31u));
+      if (c < 1 || c > 32) {
+        double z = fmin(((double)c - m) / e, vmax);
+        z2 = z * z;
+      }
+      if (i < t) acc += z2;
     }
     acc = sv_warp_sum(acc);
     if (lane == 0) {
@@ -236,7 +266,7 @@ SV_API int sv_find_variable_features_vst_surface(sv_context* ctx, const sv_count
     sv_h2d(ctx, dx.get(), xs.data(), n * 8);
     sv_h2d(ctx, dy.get(), ys.data(), n * 8);
     if (surface == SV_LOESS_DIRECT) {
-      sv_launch(ctx, "vst_loess", k_loess, dim3(sv_grid_for(ctx, n, 128, 4)), dim3(128), 0,
+      sv_launch(ctx, "vst_loess", k_loess, dim3(sv_grid_for(ctx, n, 1, 8)), dim3(LOESS_THREADS), 0,
                 (const double*)dx.get(), (const double*)dy.get(), n, q, (const double*)dx.get(), n, 0,
                 df.get(), (double*)nullptr);
     } else {
@@ -244,7 +274,7 @@ SV_API int sv_find_variable_features_vst_surface(sv_context* ctx, const sv_count
       const int64_t nb = (int64_t)bnd.size();   // >= 2: the extremes
       DevBuf<double> db(nb), dv(nb), ds(nb);
       sv_h2d(ctx, db.get(), bnd.data(), nb * 8);
-      sv_launch(ctx, "vst_loess_vertices", k_loess, dim3(sv_grid_for(ctx, nb, 128, 4)), dim3(128), 0,
+      sv_launch(ctx, "vst_loess_vertices", k_loess, dim3(sv_grid_for(ctx, nb, 1, 8)), dim3(LOESS_THREADS), 0,
                 (const double*)dx.get(), (const double*)dy.get(), n, q, (const double*)db.get(), nb, 1,
                 dv.get(), ds.get());
       sv_launch(ctx, "vst_loess_blend", k_loess_blend, dim3(sv_grid_for(ctx, n, 128, 4)), dim3(128), 0,
