@@ -16,7 +16,10 @@ test/test_scaling.jl:20-131, test/test_irlba.jl:24-116, test/test_nn.jl:21-96)
 through the committed fixtures in ``tests/golden``; irlba, kNN and SNN have no
 stored expected outputs in the reference, so they are pinned by the reference
 tests' properties (singular values vs LAPACK, residual bound, brute-force
-neighbour sets) and, for SNN, by hand-computed graphs.
+neighbour sets) and, for SNN, by hand-computed graphs.  The vst loess is the
+third-party Loess.jl package (absent here, no version pinned by the reference);
+its kd-tree and vertex blending are restated from the package's published method
+and pinned only by hand-worked trees and properties.
 """
 from __future__ import annotations
 
