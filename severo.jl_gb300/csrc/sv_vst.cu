@@ -317,8 +317,12 @@ SV_API int64_t sv_loess_vertices(const double* xs, int64_t n, double loess_span,
   if (!xs || n < 1 || !(loess_span > 0) || (cap > 0 && !bounds)) return SV_ERR_ARG;
   for (int64_t i = 1; i < n; ++i)
     if (!(xs[i - 1] <= xs[i])) return SV_ERR_ARG;
-  std::vector<double> v(xs, xs + n);
-  std::vector<double> b = loess_kdtree_bounds(v, loess_span);
-  for (int64_t i = 0; i < (int64_t)b.size() && i < cap; ++i) bounds[i] = b[i];
-  return (int64_t)b.size();
+  try {
+    std::vector<double> v(xs, xs + n);
+    std::vector<double> b = loess_kdtree_bounds(v, loess_span);
+    for (int64_t i = 0; i < (int64_t)b.size() && i < cap; ++i) bounds[i] = b[i];
+    return (int64_t)b.size();
+  } catch (const std::bad_alloc&) {
+    return SV_ERR_OOM;
+  }
 }
