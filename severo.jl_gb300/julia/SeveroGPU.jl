@@ -98,6 +98,46 @@ function normalize_cells(X::NamedArray; method=:lognormalize, scale_factor::Real
     N
 end
 
+# ---- filter_counts (src/filtering.jl:15-35,98-103) ------------------------------
+# Cells, then genes, on the device; the kept matrix comes back as a labelled
+# SparseMatrixCSC like the reference's X[CI, FI].
+function filter_counts(A::NamedArray; min_cells=0, min_features=0, min_feature_count=0, min_umi=0)
+    counts = upload_counts(A.array)
+    CI = Vector{UInt8}(undef, size(A, 1)); FI = Vector{UInt8}(undef, size(A, 2))
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    svcheck(ccall((:sv_filter_counts, libsv), Cint,
+        (Ptr{Cvoid}, Ptr{Cvoid}, Int64, Int64, Int64, Int64, Ptr{UInt8}, Ptr{UInt8}, Ref{Ptr{Cvoid}}),
+        ctx(), counts.h, min_cells, min_features, min_feature_count, min_umi, CI, FI, r))
+    kept = Handle(r[], :sv_counts_free)
+    ci, fi = CI .!= 0, FI .!= 0
+    m, n = count(ci), count(fi)
+    nz = Ref{Int64}(0)
+    svcheck(ccall((:sv_counts_info, libsv), Cint, (Ptr{Cvoid}, Ptr{Int64}, Ptr{Int64}, Ref{Int64}),
+        kept.h, C_NULL, C_NULL, nz))
+    colptr = Vector{Int64}(undef, n + 1); rowval = Vector{Int32}(undef, nz[]); nzval = Vector{Int32}(undef, nz[])
+    svcheck(ccall((:sv_counts_download_csc, libsv), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Int64}, Ptr{Int32}, Ptr{Int32}),
+        ctx(), kept.h, colptr, rowval, nzval))
+    X = SparseMatrixCSC(m, n, colptr .+ 1, Int64.(rowval) .+ 1, eltype(A.array).(nzval))
+    barcodes, features = names(A)
+    NamedArray(X, (barcodes[ci], features[fi]), A.dimnames)
+end
+
+# ---- find_variable_features(:vst) (src/variablefeatures.jl:19-50,128-160) -------
+# loess_surface: :interpolate (Loess.jl's kd-tree vertex fits blended linearly,
+# what the reference's loess / predict give), :hermite, :direct.
+const LOESS_SURFACE = Dict(:interpolate => Cint(0), :hermite => Cint(1), :direct => Cint(2))
+function find_variable_features(X::NamedArray, nfeatures=2000; method=:vst, loess_span::Real=0.5,
+                                loess_surface::Symbol=:interpolate)
+    method isa AbstractString && (method = Symbol(method))
+    method == :vst || error("unknown selection method: $method")
+    counts = upload_counts(X.array)
+    selected = Vector{Int64}(undef, nfeatures); metric = Vector{Float64}(undef, size(X, 2))
+    svcheck(ccall((:sv_find_variable_features_vst_surface, libsv), Cint,
+        (Ptr{Cvoid}, Ptr{Cvoid}, Int64, Cdouble, Cint, Ptr{Int64}, Ptr{Float64}),
+        ctx(), counts.h, nfeatures, loess_span, LOESS_SURFACE[loess_surface], selected, metric))
+    NamedArray(selected, (names(X, 2)[selected],), (dimnames(X, 2),))
+end
+
 # ---- scale_features / CenteredMatrix (src/scaling.jl:219-357) ------------------
 struct GPUCenteredMatrix{T} <: AbstractMatrix{T}
     h::Handle
