@@ -13,8 +13,8 @@
 // Columns are processed by one warp (<= 1024 candidates), one block (<= 16384)
 // or one block over a global scratch buffer (larger hubs).  The warp and block
 // forms count the candidates in a shared-memory hash table (row and count
-// packed in one 32-bit word, open addressing, at least twice as many slots as
-// candidates), keep the entries whose weight passes the prune threshold, and
+// packed in one 32-bit word, open addressing, at least 1.5 times as many slots
+// as candidates), keep the entries whose weight passes the prune threshold, and
 // sort only those by row; the hub form (and rows or k too large for the
 // packing) sorts all candidates and reads the counts as run lengths.  Two
 // passes: count the kept entries, scan, write.  All integer work; the one
