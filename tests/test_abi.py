@@ -67,3 +67,10 @@ def test_python_api_validates_method(lib):
     pkg = ge.load_package()
     with pytest.raises(ValueError, match="unknown normalization method"):
         pkg.normalize_cells(None, method="bogus")
+
+
+def test_missing_library_fails_loudly(lib, monkeypatch, tmp_path):
+    """Without the built library there is no fallback: loading raises."""
+    monkeypatch.setattr(lib, "_lib", None)
+    with pytest.raises(lib.SeveroGPUError, match="is missing"):
+        lib.load(tmp_path / "libseverogpu.so")
